@@ -1,0 +1,263 @@
+"""ctypes mirrors of the C-ABI structures (include/dmrg_gb300_types.h, dmrg_gb300_ed.h,
+dmrg_gb300.h) and helpers that wrap numpy arrays into them.
+
+The layouts are those of the reference's include/SML.h, include/dmrg.h and include/exact.h,
+so a structure built here can be handed to libdmrg_gb300 or to any library compiled against
+the reference headers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+c_double_p = C.POINTER(C.c_double)
+c_int_p = C.POINTER(C.c_int)
+c_long_p = C.POINTER(C.c_long)
+c_short_p = C.POINTER(C.c_short)
+
+
+class CRS1(C.Structure):
+    """include/SML.h:17-28"""
+    _fields_ = [("max_val", C.c_long), ("max_row", C.c_int), ("row_dim", C.c_int), ("col_dim", C.c_int),
+                ("Col", c_int_p), ("Row", c_long_p), ("Val", c_double_p)]
+
+
+class BOX_CG(C.Structure):
+    """include/SML.h:56-65"""
+    _fields_ = [("M", C.POINTER(CRS1)), ("acc", C.c_double), ("Vec", c_double_p), ("Out_Vec", c_double_p),
+                ("max_step", C.c_int), ("p_threads", C.c_int)]
+
+
+class BOX_II(C.Structure):
+    """include/SML.h:67-86"""
+    _fields_ = [("M", C.POINTER(CRS1)), ("ii_acc", C.c_double), ("ii_diag_add", C.c_double), ("ii_max_step", C.c_int),
+                ("cg_acc", C.c_double), ("cg_max_step", C.c_int), ("error", C.c_double), ("Eig_Vec", c_double_p),
+                ("Eig_Val", c_double_p), ("p_threads", C.c_int), ("Type", C.c_char * 100)]
+
+
+class BOX_LAN(C.Structure):
+    """include/SML.h:122-135"""
+    _fields_ = [("M", C.POINTER(CRS1)), ("Eig_Vec", c_double_p), ("eig_val", c_double_p), ("acc", C.c_double),
+                ("min_step", C.c_int), ("max_step", C.c_int), ("max_block_step", C.c_int), ("p_threads", C.c_int),
+                ("Guess", C.c_char * 100), ("Type", C.c_char * 100)]
+
+
+class DMRG_PARAMETER(C.Structure):
+    """include/dmrg.h:6-38"""
+    _fields_ = [("Initial_Guess", C.c_char * 1000), ("Enviro_Copy", C.c_char * 1000), ("II_Type", C.c_char * 1000),
+                ("Lan_Con", C.c_char * 1000), ("max_dim_system", C.c_int), ("sweep", C.c_int),
+                ("Diag_Method", C.c_char * 1000), ("diag_acc", C.c_double), ("diag_min_step", C.c_int),
+                ("diag_max_step", C.c_int), ("cg_acc", C.c_double), ("cg_max_step", C.c_int),
+                ("inv_iter_acc", C.c_double), ("inv_iter_diag_add", C.c_double), ("inv_iter_max_step", C.c_int),
+                ("sp_LL", C.c_double), ("param_iter", C.c_int), ("param_iter_now", C.c_int),
+                ("dim_LLLRRRRL_limit", C.c_int)]
+
+
+class DMRG_TIME(C.Structure):
+    """include/dmrg.h:40-51"""
+    _fields_ = [(n, C.c_double) for n in ("diag", "inv_iter", "make_ham", "make_basis", "make_dens_mat", "trans_main",
+                                          "trans_exp", "total")]
+
+
+class DMRG_BASIS(C.Structure):
+    """include/dmrg.h:54-99"""
+    _fields_ = [("LL_LLLRRRRL", c_short_p), ("LR_LLLRRRRL", c_short_p), ("RL_LLLRRRRL", c_short_p),
+                ("RR_LLLRRRRL", c_short_p), ("Inv_LLLRRRRL", c_int_p), ("dim_LLLRRRRL", C.c_int), ("dim_LL", C.c_int),
+                ("dim_RR", C.c_int), ("dim_onsite", C.c_int), ("tot_sz_LLLRRRRL", C.c_int),
+                ("tot_ele_LLLRRRRL", C.c_int), ("tot_ele_1_LLLRRRRL", C.c_int), ("tot_ele_2_LLLRRRRL", C.c_int),
+                ("tot_parity_LLLRRRRL", C.c_int), ("LL_LLLR", c_short_p), ("LR_LLLR", c_short_p),
+                ("Inv_LLLR", C.POINTER(c_int_p)), ("dim_LLLR", C.c_int), ("LR_LRRL", c_short_p), ("RL_LRRL", c_short_p),
+                ("Inv_LRRL", C.POINTER(c_int_p)), ("dim_LRRL", C.c_int), ("RR_RRRL", c_short_p), ("RL_RRRL", c_short_p),
+                ("Inv_RRRL", C.POINTER(c_int_p)), ("dim_RRRL", C.c_int), ("Sum_LLLR", c_int_p), ("Tot_Sz_LLLR", c_int_p),
+                ("Tot_Ele_LLLR", c_int_p), ("Tot_Ele_1_LLLR", c_int_p), ("Tot_Ele_2_LLLR", c_int_p),
+                ("Tot_Parity_LLLR", c_int_p)]
+
+
+class DMRG_STATUS(C.Structure):
+    """include/dmrg.h:236-267"""
+    _fields_ = [("BC", C.c_char * 1000), ("Enviro_Copy", C.c_char * 100), ("LL_site", C.c_int), ("RR_site", C.c_int),
+                ("max_dim_system", C.c_int), ("dim_LLLRRRRL", C.c_int), ("dim_LL", C.c_int), ("dim_onsite", C.c_int),
+                ("dim_RR", C.c_int), ("spin", C.c_int), ("tot_sz", C.c_int), ("tot_ele", C.c_int), ("tot_ele_1", C.c_int),
+                ("tot_ele_2", C.c_int), ("tot_parity", C.c_int), ("GS_Vec", c_double_p), ("gs_val", C.c_double),
+                ("gs_error", C.c_double), ("percent_LL", C.c_double), ("sweep_now", C.c_int),
+                ("param_iter_now", C.c_int), ("tot_iter_now", C.c_int), ("sweep", C.c_int), ("param_iter", C.c_int),
+                ("tot_iter", C.c_int)]
+
+
+class DMRG_BOX_LAN(C.Structure):
+    """include/dmrg.h:269-286"""
+    _fields_ = [("Eig_Vec", c_double_p), ("eig_val", c_double_p), ("acc", C.c_double), ("min_step", C.c_int),
+                ("max_step", C.c_int), ("p_threads", C.c_int), ("Guess", C.c_char * 100), ("Type", C.c_char * 100),
+                ("M_LLLR", C.POINTER(CRS1)), ("M_LRRL", C.POINTER(CRS1)), ("M_LRRL_Sign", C.POINTER(CRS1)),
+                ("M_RRRL", C.POINTER(CRS1)), ("Ele_RR", c_int_p), ("Dmrg_Basis", C.POINTER(DMRG_BASIS))]
+
+
+class DMRG_BOX_CG(C.Structure):
+    """include/dmrg.h:288-303"""
+    _fields_ = [("acc", C.c_double), ("diag_val", C.c_double), ("Vec", c_double_p), ("Out_Vec", c_double_p),
+                ("max_step", C.c_int), ("p_threads", C.c_int), ("M_LLLR", C.POINTER(CRS1)),
+                ("M_LRRL", C.POINTER(CRS1)), ("M_LRRL_Sign", C.POINTER(CRS1)), ("M_RRRL", C.POINTER(CRS1)),
+                ("Ele_RR", c_int_p), ("Dmrg_Basis", C.POINTER(DMRG_BASIS))]
+
+
+class DMRG_BOX_II(C.Structure):
+    """include/dmrg.h:305-328"""
+    _fields_ = [("ii_acc", C.c_double), ("ii_diag_add", C.c_double), ("ii_max_step", C.c_int), ("cg_acc", C.c_double),
+                ("cg_max_step", C.c_int), ("Eig_Vec", c_double_p), ("eig_val", c_double_p), ("error", C.c_double),
+                ("p_threads", C.c_int), ("M_LLLR", C.POINTER(CRS1)), ("M_LRRL", C.POINTER(CRS1)),
+                ("M_LRRL_Sign", C.POINTER(CRS1)), ("M_RRRL", C.POINTER(CRS1)), ("Ele_RR", c_int_p),
+                ("Dmrg_Basis", C.POINTER(DMRG_BASIS))]
+
+
+class EXACT_PARAMETER(C.Structure):
+    """include/exact.h:14-37"""
+    _fields_ = [("diag_num", C.c_int), ("est_max_row_elem_num", C.c_int), ("Diag_Method", C.c_char * 1000),
+                ("diag_acc", C.c_double), ("diag_min_step", C.c_int), ("diag_max_step", C.c_int), ("cg_acc", C.c_double),
+                ("cg_max_step", C.c_int), ("inv_iter_acc", C.c_double), ("inv_iter_diag_add", C.c_double),
+                ("inv_iter_max_step", C.c_int), ("param_iter", C.c_int), ("param_iter_now", C.c_int)]
+
+
+class EXACT_TIME(C.Structure):
+    """include/exact.h:39-51"""
+    _fields_ = [(n, C.c_double) for n in ("diag", "inv_iter", "make_ham", "find_dim", "make_basis", "exp_values", "cf",
+                                          "sc", "total")]
+
+
+class EXACT_HAM_INFO(C.Structure):
+    """include/exact.h:54-64"""
+    _fields_ = [("dim", C.c_int), ("diag_num", C.c_int), ("Vector", C.POINTER(c_double_p)), ("Value", c_double_p),
+                ("Error", c_double_p), ("mem_ham", C.c_double), ("Ham", C.POINTER(CRS1))]
+
+
+class EXACT_BASIS_INFO(C.Structure):
+    """include/exact.h:66-74"""
+    _fields_ = [("dim", C.c_int), ("Basis", c_long_p), ("tot_sz", C.c_int), ("tot_ele", C.c_int),
+                ("tot_parity", C.c_int)]
+
+
+class EXACT_WHOLE_BASIS_Q1(C.Structure):
+    """include/exact.h:89-95"""
+    _fields_ = [("Dim", c_int_p), ("Basis", C.POINTER(c_long_p)), ("max_dim", C.c_int)]
+
+
+class EXACT_WHOLE_BASIS_Q2(C.Structure):
+    """include/exact.h:97-103"""
+    _fields_ = [("Dim", C.POINTER(c_int_p)), ("Basis", C.POINTER(C.POINTER(c_long_p))), ("max_dim", C.c_int)]
+
+
+class EXACT_WHOLE_BASIS_Q3(C.Structure):
+    """include/exact.h:105-111"""
+    _fields_ = [("Dim", C.POINTER(C.POINTER(c_int_p))), ("Basis", C.POINTER(C.POINTER(C.POINTER(c_long_p)))),
+                ("max_dim", C.c_int)]
+
+
+class MODEL_1DKLM_VF(C.Structure):
+    """include/model.h:23-45"""
+    _fields_ = [("BC", C.c_char * 1000), ("p_threads", C.c_int), ("spin_loc", C.c_int), ("tot_site", C.c_int),
+                ("tot_sz", C.c_int), ("tot_ele", C.c_int), ("dim_onsite", C.c_int), ("dim_lspin", C.c_int),
+                ("dim_charge", C.c_int), ("cf_origin", C.c_int), ("avg_range", C.c_double), ("t", C.c_double),
+                ("J", C.c_double), ("D_z", C.c_double), ("I_xy", C.c_double), ("I_z", C.c_double), ("h_z", C.c_double),
+                ("mu", C.c_double)]
+
+
+class dg_solver_params(C.Structure):
+    """include/dmrg_gb300.h: dg_solver_params"""
+    _fields_ = [("lanczos_acc", C.c_double), ("lanczos_min_step", C.c_int), ("lanczos_max_step", C.c_int),
+                ("lanczos_block_step", C.c_int), ("lanczos_tight", C.c_int), ("lanczos_slow", C.c_int),
+                ("dense_below", C.c_int), ("ii_acc", C.c_double), ("ii_diag_add", C.c_double), ("ii_max_step", C.c_int),
+                ("cg_acc", C.c_double), ("cg_max_step", C.c_int), ("ii_minres", C.c_int), ("mixed", C.c_int),
+                ("seed", C.c_uint64), ("lookahead", C.c_int)]
+
+
+class dg_solve_info(C.Structure):
+    """include/dmrg_gb300.h: dg_solve_info"""
+    _fields_ = [("eig_val", C.c_double), ("error", C.c_double), ("lanczos_steps", C.c_int), ("ii_steps", C.c_int),
+                ("cg_steps", C.c_int), ("spmv_count", C.c_int), ("converged", C.c_int), ("ii_converged", C.c_int),
+                ("dense", C.c_int), ("ms_lanczos", C.c_double), ("ms_ii", C.c_double)]
+
+
+class dg_ed_term(C.Structure):
+    """include/dmrg_gb300_ed.h"""
+    _fields_ = [("kind", C.c_int), ("site1", C.c_int), ("site2", C.c_int), ("op1", C.c_int), ("op2", C.c_int),
+                ("coef", C.c_double), ("sign_mode", C.c_int)]
+
+
+class dg_ed_model(C.Structure):
+    """include/dmrg_gb300_ed.h"""
+    _fields_ = [("n_sites", C.c_int), ("dim_onsite", C.c_int), ("qn1", c_int_p), ("qn2", c_int_p), ("use_qn1", C.c_int),
+                ("use_qn2", C.c_int), ("target_qn1", C.c_int), ("target_qn2", C.c_int), ("n_ops", C.c_int),
+                ("ops", C.POINTER(CRS1)), ("n_terms", C.c_int), ("terms", C.POINTER(dg_ed_term)), ("n_ele", c_int_p)]
+
+
+# ---------------------------------------------------------------------------------------
+# numpy <-> struct helpers
+# ---------------------------------------------------------------------------------------
+def ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Crs:
+    """A CRS1 structure viewing numpy arrays (row int64, col int32, val float64).
+
+    The arrays are kept alive by this object; ``.struct`` is the CRS1 and ``.ref`` a
+    pointer to it."""
+
+    def __init__(self, row, col, val, n=None, ncol=None):
+        self.row = np.ascontiguousarray(row, dtype=np.int64)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        self.val = np.ascontiguousarray(val, dtype=np.float64)
+        n = len(self.row) - 1 if n is None else n
+        if len(self.col) == 0:          # keep valid pointers for empty matrices
+            self.col = np.zeros(1, np.int32)
+            self.val = np.zeros(1, np.float64)
+        self.struct = CRS1(max_val=max(len(self.val), 1), max_row=n + 1, row_dim=n, col_dim=n if ncol is None else ncol,
+                           Col=ptr(self.col, C.c_int), Row=ptr(self.row, C.c_long), Val=ptr(self.val, C.c_double))
+        self.ref = C.pointer(self.struct)
+
+    @property
+    def n(self) -> int:
+        return self.struct.row_dim
+
+    @property
+    def nnz(self) -> int:
+        return int(self.row[self.n])
+
+    @classmethod
+    def from_scipy(cls, A):
+        A = A.tocsr()
+        A.sort_indices()
+        return cls(A.indptr, A.indices, A.data, n=A.shape[0], ncol=A.shape[1])
+
+
+def lower_diag_last(A) -> Crs:
+    """Symmetric matrix -> the *_SYM layout: lower triangle, columns ascending, diagonal
+    stored last in every row (explicitly, even when zero)."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix(A)
+    n = A.shape[0]
+    L = sp.tril(A, k=-1).tocsr()
+    L.sort_indices()
+    d = A.diagonal()
+    rows, cols, vals = [0], [], []
+    for i in range(n):
+        b, e = L.indptr[i], L.indptr[i + 1]
+        cols.extend(L.indices[b:e].tolist())
+        vals.extend(L.data[b:e].tolist())
+        cols.append(i)
+        vals.append(d[i])
+        rows.append(len(cols))
+    return Crs(np.array(rows), np.array(cols), np.array(vals), n=n)
+
+
+def full_from_lower(c: Crs):
+    """Full scipy CSR from a lower-triangle-diagonal-last Crs."""
+    import scipy.sparse as sp
+    n = c.n
+    L = sp.csr_matrix((c.val[:c.nnz], c.col[:c.nnz], c.row), shape=(n, n))
+    D = sp.diags(L.diagonal())
+    return (L + L.T - D).tocsr()
+
+
+def cstr(s: str) -> bytes:
+    return s.encode()

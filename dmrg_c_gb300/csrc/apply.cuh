@@ -1,0 +1,128 @@
+// apply.cuh -- the fused operator-application kernel.
+//
+// One launch computes y = (H + sigma I) (s x) for every row, where s is an optional scale
+// read from a device scalar (the lazily applied normalisation of a Krylov vector), and
+// hands each finished row to an epilogue that may store outputs and contribute to one
+// grid-wide deterministic reduction (a dot product, a residual norm, ...).  The epilogue's
+// finalize() runs once, in the last block, with the reduced total.
+//
+// Rows are processed by groups of L lanes (L = 1, 2, ..., 32 lanes of one warp); a warp
+// handles 32/L consecutive rows per trip and warps stride over the row range, so loads of
+// a row's column indices and values are coalesced across the group's lanes.  Each lane
+// accumulates its strided share of the row in order and the L partials are combined with
+// a fixed xor-shuffle tree, so every y_i is bitwise reproducible run to run.
+//
+// Operators (Op) provide
+//   __device__ double row_partial<L>(int i, int lane, const XT *x, double s) const;
+// returning the lane's partial sum of H[i][:] . (s x).
+#pragma once
+
+#include "common.cuh"
+
+namespace dg {
+
+// How the input scale s is derived from a device scalar.
+enum ScaleMode : int { SCALE_ONE = 0, SCALE_RSQRT = 1, SCALE_RECIP = 2 };
+
+__device__ __forceinline__ double load_scale(const double *sp, int mode) {
+  if (mode == SCALE_RSQRT) return 1.0 / sqrt(*sp);   // NORMALIZE: norm = 1.0/sqrt(sum)
+  if (mode == SCALE_RECIP) return 1.0 / (*sp);      // MINIMUM_RESIDUAL: temp = 1.0/gamma0
+  return 1.0;
+}
+
+template <class T>
+__device__ __forceinline__ double to_d(T v) { return (double)v; }
+
+// Full CRS row operator; VT is the stored value type (double, or float for the mixed form).
+template <class VT>
+struct CrsOp {
+  const int64_t *__restrict__ row;
+  const int *__restrict__ col;
+  const VT *__restrict__ val;
+
+  template <int L, class XT>
+  __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double s) const {
+    const int64_t b = row[i], e = row[i + 1];
+    double sum = 0.0;
+    if (s == 1.0) {
+      for (int64_t k = b + lane; k < e; k += L) sum += to_d(val[k]) * to_d(x[col[k]]);
+    } else {
+      for (int64_t k = b + lane; k < e; k += L) sum += to_d(val[k]) * (to_d(x[col[k]]) * s);
+    }
+    return sum;
+  }
+};
+
+template <int L>
+__device__ __forceinline__ double lanes_sum(double v) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, L);
+  return v;
+}
+
+// Generic fused apply.  gate: when non-null and *gate != 0 the whole launch is a no-op
+// (speculatively enqueued iterations after an iterative solver has converged).
+template <int L, class Op, class XT, class Epi>
+__global__ void __launch_bounds__(kThreads)
+k_apply(Op op, int n, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma,
+        const int *gate, Epi epi, RedSlot slot) {
+  if (gate && *((volatile const int *)gate)) return;
+  const double s = load_scale(scale_src, scale_mode);
+  constexpr int RPW = 32 / L;   // rows per warp trip
+  const int lane_w = threadIdx.x & 31;
+  const int sub = lane_w / L, lane = lane_w % L;
+  const int warp_global = (blockIdx.x * kThreads + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * kThreads) >> 5;
+  double acc = 0.0;
+  for (long base = (long)warp_global * RPW; base < n; base += (long)nwarps * RPW) {
+    const int i = (int)(base + sub);
+    const bool valid = i < n;
+    double part = valid ? op.template row_partial<L>(i, lane, x, s) : 0.0;
+    part = lanes_sum<L>(part);
+    if (valid && lane == 0) {
+      const double xi = (s == 1.0) ? to_d(x[i]) : to_d(x[i]) * s;
+      const double yi = (sigma == 0.0) ? part : part + sigma * xi;
+      epi.row(i, xi, yi, acc);
+    }
+  }
+  if (Epi::kReduce) {
+    grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Epilogues.  row(i, xi, yi, acc): xi = scaled input element, yi = ((H + sigma) s x)_i.
+// ---------------------------------------------------------------------------------
+
+// y = H x (plain product, optionally in FP32 output).
+template <class YT>
+struct EpiStore {
+  static constexpr bool kReduce = false;
+  YT *y;
+  __device__ void row(int i, double, double yi, double &) const { y[i] = (YT)yi; }
+  __device__ void finalize(double) const {}
+};
+
+// y = H x, *out = sum_i x_i y_i.
+template <class YT>
+struct EpiDot {
+  static constexpr bool kReduce = true;
+  YT *y;
+  double *out;
+  __device__ void row(int i, double xi, double yi, double &acc) const {
+    y[i] = (YT)yi;
+    acc += yi * xi;
+  }
+  __device__ void finalize(double t) const { *out = t; }
+};
+
+// *out = sum_i |lambda x_i - y_i| (CONVERGE_CHECK, sml/CONVERGE_CHECK.c:18-20).
+struct EpiResidualL1 {
+  static constexpr bool kReduce = true;
+  double lambda;
+  double *out;
+  __device__ void row(int, double xi, double yi, double &acc) const { acc += fabs(lambda * xi - yi); }
+  __device__ void finalize(double t) const { *out = t; }
+};
+
+}  // namespace dg

@@ -1,0 +1,196 @@
+// common.cuh -- shared infrastructure of libdmrg_gb300: error reporting, device buffers,
+// deterministic block reductions with last-block finalisation, launch geometry.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dmrg_gb300.h"
+
+namespace dg {
+
+// ---------------------------------------------------------------------------------
+// Error reporting (thread-local last error; dg_* return codes).
+// ---------------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+const char *last_error();
+
+struct Error {
+  int code;
+};
+
+#define DG_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      ::dg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      throw ::dg::Error{e_ == cudaErrorMemoryAllocation ? DG_ERR_NOMEM : DG_ERR_CUDA}; \
+    }                                                                                  \
+  } while (0)
+
+#define DG_REQUIRE(cond, code, ...)       \
+  do {                                    \
+    if (!(cond)) {                        \
+      ::dg::set_error(__VA_ARGS__);       \
+      throw ::dg::Error{code};            \
+    }                                     \
+  } while (0)
+
+// Run f, translating thrown dg::Error into a status code.
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    return DG_OK;
+  } catch (const Error &e) {
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    set_error("host allocation failed");
+    return DG_ERR_NOMEM;
+  }
+}
+
+// Process-wide count of kernel launches issued by this library (bench evidence).
+void count_launch(long k = 1);
+
+// Ensure a device exists and the runtime is usable; throws DG_ERR_NODEVICE otherwise.
+void require_device();
+// Per-thread library stream (non-blocking with respect to the legacy stream).
+cudaStream_t stream();
+int sm_count();
+
+// ---------------------------------------------------------------------------------
+// RAII device / pinned buffers.
+// ---------------------------------------------------------------------------------
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    DG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  T *get() const { return p; }
+};
+
+// Mapped, pinned host memory that the device writes progress into and the host polls.
+template <class T>
+struct Mapped {
+  T *h = nullptr;
+  T *d = nullptr;
+  Mapped() = default;
+  explicit Mapped(size_t count) { alloc(count); }
+  Mapped(const Mapped &) = delete;
+  Mapped &operator=(const Mapped &) = delete;
+  ~Mapped() { release(); }
+  void alloc(size_t count) {
+    release();
+    DG_CUDA(cudaHostAlloc((void **)&h, count * sizeof(T), cudaHostAllocMapped));
+    std::memset((void *)h, 0, count * sizeof(T));
+    DG_CUDA(cudaHostGetDevicePointer((void **)&d, (void *)h, 0));
+  }
+  void release() {
+    if (h) cudaFreeHost(h);
+    h = d = nullptr;
+  }
+};
+
+// Is p a device (or managed) pointer?  Plain host memory (malloc) is "unregistered".
+bool is_device_ptr(const void *p);
+
+// ---------------------------------------------------------------------------------
+// Launch geometry.
+// ---------------------------------------------------------------------------------
+constexpr int kThreads = 256;   // threads per block for every kernel here
+constexpr int kWarps = kThreads / 32;
+
+// Grid for grid-stride vector kernels over n elements: at most 4 blocks per SM.
+int vector_grid(long n);
+
+// ---------------------------------------------------------------------------------
+// Deterministic reductions.  Every reduction sums per-thread partials in a fixed
+// order (xor-shuffle tree inside a warp, warps in index order, blocks in index order),
+// so results are bitwise reproducible for a fixed grid.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of v over the block; valid in thread 0.
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double sm[kWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sm[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (lane < kWarps) ? sm[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+
+// Reduction slot used by one kernel at a time on a stream.
+struct RedSlot {
+  double *partials;   // >= gridDim.x entries
+  unsigned *ticket;   // zero between uses
+};
+
+// Reduce v over the grid.  The last block to finish sums the per-block partials in block
+// order and calls fin(total) from thread 0, then re-arms the ticket.
+template <class Fin>
+__device__ __forceinline__ void grid_reduce(double v, RedSlot slot, Fin fin) {
+  __shared__ bool s_last;
+  double b = block_sum(v);
+  if (threadIdx.x == 0) {
+    slot.partials[blockIdx.x] = b;
+    __threadfence();
+    unsigned t = atomicAdd(slot.ticket, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += __ldcg(slot.partials + i);
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+      fin(s);
+      *slot.ticket = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Host-side helpers.
+// ---------------------------------------------------------------------------------
+double now_ms();
+uint64_t splitmix64(uint64_t x);
+
+}  // namespace dg

@@ -1,0 +1,180 @@
+// ed_vm.cu -- single-site operator application on an exact-diagonalisation basis,
+// Out = O_site Vec  (exact/EXACT_V_M_Q0.c:14-37, EXACT_V_M_Q1.c:8-38, EXACT_V_M_Q2.c:10-63,
+// EXACT_V_M_Q3.c).
+//
+// A basis state is an integer code whose base-dim_onsite digit s is the local state of site
+// s (exact/EXACT_FIND_SITE_STATE.c:3-15); basis tables are sorted ascending.  For output row
+// i with local state l at the operator's site, every stored element O[l][c] contributes
+// Vec[j] * O[l][c] where j is the position of code_i - (l - c) dim_onsite^site in the input
+// table (binary search; absent codes contribute nothing).  With Sign_Flag "Yes" the row is
+// multiplied by (-1)^(electrons on sites < op_site) (Jordan-Wigner string, EXACT_V_M_Q2.c:31-44).
+#include <cmath>
+#include <cstring>
+#include <sys/stat.h>
+
+#include "common.cuh"
+
+namespace dg {
+
+// Position of key in the ascending table a[0..n) or -1 (search confined to the table).
+__device__ __forceinline__ long find_code(const int64_t *__restrict__ a, long n, int64_t key) {
+  long lo = 0, hi = n - 1;
+  while (lo <= hi) {
+    const long mid = lo + ((hi - lo) >> 1);
+    const int64_t v = a[mid];
+    if (v < key)
+      lo = mid + 1;
+    else if (v > key)
+      hi = mid - 1;
+    else
+      return mid;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ int digit_of(int64_t code, int site, int d) {
+  for (int s = 0; s < site; ++s) code /= d;
+  return (int)(code % d);
+}
+
+struct SiteOp {
+  const int64_t *row;
+  const int *col;
+  const double *val;
+};
+
+__global__ void k_site_apply(const int64_t *__restrict__ out_basis, long dim_out, const int64_t *__restrict__ in_basis, long dim_in,
+                             SiteOp op, int d, int site, int64_t dim_site, const int *__restrict__ n_ele, int use_sign,
+                             const double *__restrict__ vec, double *__restrict__ out) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < dim_out; i += (long)gridDim.x * blockDim.x) {
+    const int64_t code = out_basis[i];
+    const int local = digit_of(code, site, d);
+    int sign = 1;
+    if (use_sign) {
+      int ne = 0;
+      int64_t c = code;
+      for (int s = 0; s < site; ++s) {
+        ne += n_ele[(int)(c % d)];
+        c /= d;
+      }
+      sign = (ne % 2 == 0) ? 1 : -1;
+    }
+    double v = 0.0;
+    for (int64_t k = op.row[local]; k < op.row[local + 1]; ++k) {
+      const int64_t target = code - (int64_t)(local - op.col[k]) * dim_site;
+      const long j = find_code(in_basis, dim_in, target);
+      if (j >= 0) v = v + vec[j] * op.val[k];
+    }
+    out[i] = (use_sign ? v * sign : v);
+  }
+}
+
+// Host driver: uploads the tables and runs the kernel.
+void site_apply(const CRS1 *M_On, const long *out_basis, long dim_out, const long *in_basis, long dim_in, int d, int site,
+                const int *n_ele, bool use_sign, const double *vec, double *out) {
+  require_device();
+  DG_REQUIRE(M_On && out_basis && in_basis && vec && out, DG_ERR_ARG, "null argument");
+  DG_REQUIRE(d >= 2 && site >= 0, DG_ERR_ARG, "bad dim_onsite=%d / site=%d", d, site);
+  DG_REQUIRE(M_On->row_dim <= d || M_On->row_dim == 0, DG_ERR_ARG, "site operator larger than dim_onsite");
+  cudaStream_t st = stream();
+  int64_t dim_site = 1;
+  for (int s = 0; s < site; ++s) dim_site *= d;
+  const long nnz = M_On->Row[d];
+  DevBuf<int64_t> ob(dim_out), ib(dim_in), r(d + 1);
+  DevBuf<int> c(nnz), ne(d);
+  DevBuf<double> v(nnz), x(dim_in), y(dim_out);
+  DG_CUDA(cudaMemcpyAsync(ob.get(), out_basis, sizeof(int64_t) * dim_out, cudaMemcpyHostToDevice, st));
+  DG_CUDA(cudaMemcpyAsync(ib.get(), in_basis, sizeof(int64_t) * dim_in, cudaMemcpyHostToDevice, st));
+  DG_CUDA(cudaMemcpyAsync(r.get(), M_On->Row, sizeof(int64_t) * (d + 1), cudaMemcpyHostToDevice, st));
+  if (nnz) {
+    DG_CUDA(cudaMemcpyAsync(c.get(), M_On->Col, sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(v.get(), M_On->Val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+  }
+  if (use_sign) DG_CUDA(cudaMemcpyAsync(ne.get(), n_ele, sizeof(int) * d, cudaMemcpyHostToDevice, st));
+  DG_CUDA(cudaMemcpyAsync(x.get(), vec, sizeof(double) * dim_in, cudaMemcpyHostToDevice, st));
+  k_site_apply<<<vector_grid(dim_out), kThreads, 0, st>>>(ob.get(), dim_out, ib.get(), dim_in, SiteOp{r.get(), c.get(), v.get()}, d,
+                                                          site, dim_site, ne.get(), use_sign ? 1 : 0, x.get(), y.get()); ::dg::count_launch();
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(cudaMemcpyAsync(out, y.get(), sizeof(double) * dim_out, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+namespace {
+
+[[noreturn]] void vm_fatal(const char *who, const char *msg) {
+  printf("Error in %s\n%s\n", who, msg);
+  fflush(stdout);
+  exit(1);
+}
+
+void vm_must(int rc, const char *who) {
+  if (rc != DG_OK) {
+    char msg[1100];
+    snprintf(msg, sizeof(msg), "GPU path failed (status %d): %s", rc, dg_last_error());
+    vm_fatal(who, msg);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void EXACT_V_M_Q0(CRS1 *M_On, double *Vec, double *Out_Vec, int dim_onsite, int site, int, EXACT_BASIS_INFO *Basis_Info) {
+  vm_must(guarded([&] {
+            site_apply(M_On, Basis_Info->Basis, Basis_Info->dim, Basis_Info->Basis, Basis_Info->dim, dim_onsite, site, nullptr, false,
+                       Vec, Out_Vec);
+          }),
+          "EXACT_V_M_Q0");
+}
+
+void EXACT_V_M_Q1(CRS1 *M_On, int qn_out, double *Vec, int qn_in, double *Out_Vec, int dim_onsite, int site, int,
+                  EXACT_WHOLE_BASIS_Q1 *W_Basis) {
+  if (qn_out < 0 || qn_in < 0) {
+    char msg[128];
+    snprintf(msg, sizeof(msg), "qn_out=%d,qn_in=%d", qn_out, qn_in);
+    vm_fatal("EXACT_V_M_Q1", msg);
+  }
+  vm_must(guarded([&] {
+            site_apply(M_On, W_Basis->Basis[qn_out], W_Basis->Dim[qn_out], W_Basis->Basis[qn_in], W_Basis->Dim[qn_in], dim_onsite, site,
+                       nullptr, false, Vec, Out_Vec);
+          }),
+          "EXACT_V_M_Q1");
+}
+
+void EXACT_V_M_Q2(CRS1 *M_On, int qn1_out, int qn2_out, double *Vec, int qn1_in, int qn2_in, double *Out_Vec, char Sign_Flag[],
+                  int *N_Ele, int dim_onsite, int op_site, int, EXACT_WHOLE_BASIS_Q2 *W_Basis) {
+  if (qn1_out < 0 || qn2_out < 0 || qn1_in < 0 || qn2_in < 0) {
+    char msg[160];
+    snprintf(msg, sizeof(msg), "qn1_out=%d,qn2_out=%d,qn1_in=%d,qn2_in=%d", qn1_out, qn2_out, qn1_in, qn2_in);
+    vm_fatal("EXACT_V_M_Q2", msg);
+  }
+  const bool sign = std::strcmp(Sign_Flag, "Yes") == 0;
+  vm_must(guarded([&] {
+            site_apply(M_On, W_Basis->Basis[qn1_out][qn2_out], W_Basis->Dim[qn1_out][qn2_out], W_Basis->Basis[qn1_in][qn2_in],
+                       W_Basis->Dim[qn1_in][qn2_in], dim_onsite, op_site, N_Ele, sign, Vec, Out_Vec);
+          }),
+          "EXACT_V_M_Q2");
+}
+
+void EXACT_V_M_Q3(CRS1 *M_On, int qn1_out, int qn2_out, int qn3_out, double *Vec, int qn1_in, int qn2_in, int qn3_in, double *Out_Vec,
+                  char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int, EXACT_WHOLE_BASIS_Q3 *W_Basis) {
+  if (qn1_out < 0 || qn2_out < 0 || qn3_out < 0 || qn1_in < 0 || qn2_in < 0 || qn3_in < 0) {
+    char msg[200];
+    snprintf(msg, sizeof(msg), "qn1_out=%d,qn2_out=%d,qn3_out=%d,qn1_in=%d,qn2_in=%d,qn3_in=%d", qn1_out, qn2_out, qn3_out, qn1_in,
+             qn2_in, qn3_in);
+    vm_fatal("EXACT_V_M_Q3", msg);
+  }
+  const bool sign = std::strcmp(Sign_Flag, "Yes") == 0;
+  vm_must(guarded([&] {
+            site_apply(M_On, W_Basis->Basis[qn1_out][qn2_out][qn3_out], W_Basis->Dim[qn1_out][qn2_out][qn3_out],
+                       W_Basis->Basis[qn1_in][qn2_in][qn3_in], W_Basis->Dim[qn1_in][qn2_in][qn3_in], dim_onsite, op_site, N_Ele, sign,
+                       Vec, Out_Vec);
+          }),
+          "EXACT_V_M_Q3");
+}
+
+}  // extern "C"

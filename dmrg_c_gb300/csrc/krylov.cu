@@ -1,0 +1,206 @@
+// krylov.cu -- non-template solver kernels and the dg_* solver API on CRS operators.
+#include <cstdlib>
+
+#include "krylov.cuh"
+#include "matrix.cuh"
+#include "solve.cuh"
+
+namespace dg {
+
+double wait_timeout_ms() {
+  static double v = [] {
+    const char *e = std::getenv("DG_WAIT_TIMEOUT_MS");
+    double t = e ? std::atof(e) : 0.0;
+    return t > 0 ? t : 120000.0;
+  }();
+  return v;
+}
+
+__global__ void k_random_start(double *x, int n, unsigned long long seed) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[i] = (double)((long long)(z % 100000000ull) - 50000000ll);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__restrict__ p, const double *__restrict__ y,
+                                                       double *__restrict__ x, double *__restrict__ r, Scalars *S,
+                                                       double acc_thr, int it, int max_step, Progress *prog, RedSlot slot) {
+  if (*((volatile int *)&S->done)) return;
+  const double a = S->a;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    x[i] = x[i] + a * p[i];
+    const double ri = r[i] - a * y[i];
+    r[i] = ri;
+    acc += ri * ri;
+  }
+  grid_reduce(acc, slot, [&](double t) {
+    if (t < acc_thr) {
+      S->done = 1;
+      S->iters = it;
+    } else if (it >= max_step - 1) {
+      S->done = 2;
+      S->iters = max_step;
+    }
+    S->beta = t / S->rr;
+    S->rr = t;
+    prog->value = t;
+    prog->done = S->done;
+    prog->iters = S->iters;
+    __threadfence_system();
+    prog->stamp = it;
+  });
+}
+
+__global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p,
+                                                          const Scalars *S) {
+  if (*((volatile const int *)&S->done)) return;
+  const double b = S->beta;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) p[i] = r[i] + b * p[i];
+}
+
+// V2 = Temp - delta V1 - gamma0 V0, gamma1 = ||V2||, Givens rotation, eta update and the
+// convergence test |eta| < acc (sml/MINIMUM_RESIDUAL_SYM.c:62-90).
+__global__ void __launch_bounds__(kThreads) k_mr_lanczos(int n, const double *__restrict__ temp, const double *__restrict__ v1n,
+                                                        const double *__restrict__ v0, double *__restrict__ v2, Scalars *S,
+                                                        double acc_thr, int it, int max_step, Progress *prog, RedSlot slot) {
+  if (*((volatile int *)&S->done)) return;
+  const double delta = S->delta, g0 = S->gamma0;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double v = temp[i] - delta * v1n[i] - g0 * v0[i];
+    v2[i] = v;
+    acc += v * v;
+  }
+  grid_reduce(acc, slot, [&](double t) {
+    const double gamma1 = sqrt(t);
+    const double c0 = S->c0, c1 = S->c1, s0 = S->s0, s1 = S->s1;
+    const double alpha0 = c1 * delta - c0 * s1 * g0;
+    const double alpha1 = sqrt(alpha0 * alpha0 + gamma1 * gamma1);
+    const double alpha2 = s1 * delta + c0 * c1 * g0;
+    const double alpha3 = s0 * g0;
+    const double c2 = alpha0 / alpha1;
+    const double s2 = gamma1 / alpha1;
+    S->inv_alpha1 = 1.0 / alpha1;
+    S->alpha2 = alpha2;
+    S->alpha3 = alpha3;
+    S->c2 = c2;
+    S->eta_old = S->eta;
+    S->eta = -s2 * S->eta;
+    if (fabs(S->eta) < acc_thr) {
+      S->done = 1;
+      S->iters = it;
+    }
+    // rotate (:127-133)
+    S->s0 = s1;
+    S->s1 = s2;
+    S->c0 = c1;
+    S->c1 = c2;
+    S->gamma0 = gamma1;
+    S->gamma1 = gamma1;
+    prog->value = fabs(S->eta);
+    prog->done = S->done;
+    prog->iters = S->iters;
+    __threadfence_system();
+    prog->stamp = it + 1;
+  });
+}
+
+// W2 = (1/alpha1)(V1 - alpha3 W0 - alpha2 W1); x += c2 eta W2 (:79-83, :124).  Skipped on
+// the converged iteration, as the reference returns before copying X1 into Out_Vec.
+__global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__restrict__ v1n, const double *__restrict__ w0,
+                                                       const double *__restrict__ w1, double *__restrict__ w2,
+                                                       double *__restrict__ x, const Scalars *S) {
+  if (*((volatile const int *)&S->done)) return;
+  const double ia = S->inv_alpha1, a2 = S->alpha2, a3 = S->alpha3, ce = S->c2 * S->eta_old;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double w = ia * (v1n[i] - a3 * w0[i] - a2 * w1[i]);
+    w2[i] = w;
+    x[i] = x[i] + ce * w;
+  }
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+extern "C" {
+
+void dg_solver_params_default(dg_solver_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->lanczos_acc = 1e-14;
+  p->lanczos_min_step = 1;
+  p->lanczos_max_step = 800;
+  p->lanczos_block_step = 800;
+  p->lanczos_tight = 0;
+  p->lanczos_slow = 0;
+  p->dense_below = 1000;
+  p->ii_acc = 1e-9;
+  p->ii_diag_add = 1e-11;
+  p->ii_max_step = 3;
+  p->cg_acc = 1e-7;
+  p->cg_max_step = 1000;
+  p->ii_minres = 0;
+  p->mixed = 0;
+  p->seed = 0;
+  p->lookahead = 0;
+}
+
+int dg_lanczos(dg_matrix *m, const dg_solver_params *p, const double *guess, double *eigvec, dg_solve_info *info) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && p && eigvec, DG_ERR_ARG, "null argument");
+    CrsLauncher op{m};
+    SolveOut o = solve_ground_state(op, *p, guess, eigvec, /*run_ii=*/false);
+    if (info) *info = o.info;
+    DG_REQUIRE(o.info.converged, DG_ERR_NOCONV, "Lanczos did not converge (max step %d)", p->lanczos_max_step);
+  });
+}
+
+int dg_ground_state(dg_matrix *m, const dg_solver_params *p, const double *guess, double *eigvec, dg_solve_info *info) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && p && eigvec, DG_ERR_ARG, "null argument");
+    CrsLauncher op{m};
+    SolveOut o = solve_ground_state(op, *p, guess, eigvec, /*run_ii=*/p->ii_max_step >= 0);
+    if (info) *info = o.info;
+    DG_REQUIRE(o.info.converged, DG_ERR_NOCONV, "Lanczos did not converge (max step %d)", p->lanczos_max_step);
+  });
+}
+
+int dg_inverse_iteration(dg_matrix *m, const dg_solver_params *p, double eig_val, double *eigvec, dg_solve_info *info) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && p && eigvec, DG_ERR_ARG, "null argument");
+    CrsLauncher op{m};
+    SolveOut o = solve_inverse_iteration(op, *p, eig_val, eigvec, /*shifted_check=*/true);
+    if (info) *info = o.info;
+  });
+}
+
+int dg_linear_solve(dg_matrix *m, double sigma, const double *b, double *x, double acc, int max_step, int minres, int *iters) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && b && x, DG_ERR_ARG, "null argument");
+    CrsLauncher op{m};
+    IterResult r = solve_linear(op, sigma, b, x, acc, max_step, minres != 0);
+    if (iters) *iters = r.iters;
+    DG_REQUIRE(r.converged, DG_ERR_NOCONV, "%s did not converge (max step %d)", minres ? "MINRES" : "CG", max_step);
+  });
+}
+
+int dg_residual_l1(dg_matrix *m, const double *x, double lambda, double *out) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && x && out, DG_ERR_ARG, "null argument");
+    CrsLauncher op{m};
+    *out = solve_residual(op, x, 0.0, lambda);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,718 @@
+// krylov.cuh -- Lanczos, CG, MINRES and inverse iteration on the device.
+//
+// The solvers follow the reference recurrences step by step (citations at each kernel);
+// what changes is where the work runs:
+//  * every vector pass is fused into the operator launch (scale-on-gather normalisation,
+//    dot products in the epilogue) or into one vector kernel per recurrence step, so a
+//    Lanczos step is two launches and a CG iteration three;
+//  * scalars (alpha, beta, residual norms) never leave the device inside an iteration: the
+//    last block of each reduction computes them and the next launch reads them;
+//  * the host only sees what decides termination.  Lanczos: each step's (alpha, beta) is
+//    mirrored into mapped host memory; the host runs the tridiagonal check on step b while
+//    the device is already computing steps b+1..b+lookahead (their results are discarded,
+//    they never alter steps <= b).  CG / MINRES: the device itself tests convergence and
+//    raises a gate flag that turns the speculatively enqueued iterations into no-ops.
+//  * every host wait on device progress is bounded (DG_ERR_TIMEOUT), never a device spin.
+#pragma once
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "apply.cuh"
+#include "common.cuh"
+#include "tridiag.h"
+
+namespace dg {
+
+// Device-resident scalars of one solve.
+struct Scalars {
+  double r2;        // Lanczos: <w,w> of the pending unnormalised Krylov vector
+  double xn2;       // CG: <x0,x0>; generic norm output
+  double rr;        // CG: <r,r> of the current residual
+  double a;         // CG: alpha
+  double beta;      // CG: beta
+  double res;       // residual / dot output
+  double gamma0, gamma1, delta, eta, eta_old, c0, c1, c2, s0, s1, s2, inv_alpha1, alpha2, alpha3;  // MINRES
+  int done;         // 0 running, 1 converged, 2 iteration limit
+  int iters;
+};
+
+// Host-visible progress (mapped pinned memory).
+struct Progress {
+  volatile int stamp;     // Lanczos: operator applications completed; CG/MINRES: iterations completed
+  volatile int done;
+  volatile int iters;
+  volatile double value;  // latest residual
+};
+
+// ---------------------------------------------------------------------------------
+// Per-solve workspace.
+// ---------------------------------------------------------------------------------
+struct Workspace {
+  cudaStream_t st;
+  int n;
+  int vgrid;
+  DevBuf<double> partials;
+  DevBuf<unsigned> ticket;
+  DevBuf<Scalars> sc;
+  Mapped<Progress> prog;
+  explicit Workspace(int n_, int max_grid, cudaStream_t s) : st(s), n(n_) {
+    vgrid = vector_grid(n_);
+    int g = max_grid > vgrid ? max_grid : vgrid;
+    partials.alloc(g);
+    ticket.alloc(1);
+    sc.alloc(1);
+    prog.alloc(1);
+    DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
+    DG_CUDA(cudaMemsetAsync(sc.get(), 0, sizeof(Scalars), st));
+  }
+  RedSlot slot() const { return RedSlot{partials.get(), ticket.get()}; }
+  Scalars *S() const { return sc.get(); }
+};
+
+double wait_timeout_ms();
+
+// Spin (on the host) until pred() holds; bounded.  Returns false on timeout.
+// The acquire fence orders the host's later reads of device-written mirrors after the
+// read that observed the progress stamp (needed on weakly ordered hosts such as Arm).
+template <class Pred>
+bool host_wait(cudaStream_t st, Pred pred) {
+  if (pred()) {
+    std::atomic_thread_fence(std::memory_order_acquire);
+    return true;
+  }
+  const double t0 = now_ms(), limit = wait_timeout_ms();
+  unsigned spins = 0;
+  while (!pred()) {
+    if ((++spins & 0x3ff) == 0) {
+      cudaError_t e = cudaStreamQuery(st);
+      if (e != cudaSuccess && e != cudaErrorNotReady) {
+        set_error("device error while waiting: %s", cudaGetErrorString(e));
+        throw Error{DG_ERR_CUDA};
+      }
+      if (e == cudaSuccess && !pred()) {
+        // Stream drained: whatever was going to arrive has arrived.
+        std::atomic_thread_fence(std::memory_order_acquire);
+        return pred();
+      }
+      if (now_ms() - t0 > limit) return false;
+      std::this_thread::yield();
+    }
+  }
+  std::atomic_thread_fence(std::memory_order_acquire);
+  return true;
+}
+
+// ---------------------------------------------------------------------------------
+// Vector kernels.
+// ---------------------------------------------------------------------------------
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_norm2(const VT *__restrict__ x, int n, double *out, RedSlot slot) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double v = (double)x[i];
+    acc += v * v;
+  }
+  grid_reduce(acc, slot, [&](double t) { *out = t; });
+}
+
+// x *= 1/sqrt(*r2)  (NORMALIZE, sml/NORMALIZE.c:12-18)
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_scale_rsqrt(VT *__restrict__ x, int n, const double *r2) {
+  const double s = 1.0 / sqrt(*r2);
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) x[i] = (VT)((double)x[i] * s);
+}
+
+template <class A, class B>
+__global__ void __launch_bounds__(kThreads) k_copy(const A *__restrict__ a, B *__restrict__ b, int n) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) b[i] = (B)a[i];
+}
+
+// Seeded start vector with the reference's value range (rand()%100000000 - 50000000,
+// sml/LANCZOS_SYM.c:84), drawn from a counter-based generator instead of time(NULL)/rand().
+__global__ void k_random_start(double *x, int n, unsigned long long seed);
+
+// ---- Lanczos -----------------------------------------------------------------------
+
+// Operator epilogue of Lanczos step b: y = H v_b, V[b] = v_b, D[b] = <y, v_b>
+// (sml/LANCZOS_SYM.c:139-143); mirrors D[b], O[b] to the host.
+template <class VT>
+struct EpiLanczos {
+  static constexpr bool kReduce = true;
+  double *y;
+  VT *vout;
+  double *D, *O;         // device recurrence arrays
+  double *hD, *hO;       // mapped host mirrors
+  Progress *prog;        // mapped
+  const double *r2;      // <w,w> that normalised v_b
+  int b;
+  int stamp;
+  __device__ void row(int i, double xi, double yi, double &acc) const {
+    y[i] = yi;
+    vout[i] = (VT)xi;
+    acc += yi * xi;
+  }
+  __device__ void finalize(double t) const {
+    const double o = (b > 0) ? sqrt(*r2) : 0.0;   // Off_Diag[b] = sqrt(<w,w>)  (:135)
+    D[b] = t;
+    O[b] = o;
+    hD[b] = t;
+    hO[b] = o;
+    __threadfence_system();
+    prog->stamp = stamp;
+  }
+};
+
+// w = y - D[b] v_b - O[b] v_{b-1}; r2 = <w,w>  (sml/LANCZOS_SYM.c:121-125, 240-243)
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__restrict__ y, const VT *__restrict__ v,
+                                                       const VT *__restrict__ vprev, const double *D, const double *O,
+                                                       int b, double *__restrict__ w, double *r2, RedSlot slot) {
+  const double d = D[b];
+  const double o = (b > 0) ? O[b] : 0.0;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double wi = y[i] - d * (double)v[i];
+    if (b > 0) wi = wi - o * (double)vprev[i];
+    w[i] = wi;
+    acc += wi * wi;
+  }
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+}
+
+// c[j] = <V_j, w> for j < nvec (one block per vector; fixed order within the block).
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_multidot(const VT *__restrict__ V, long ldv, int nvec, const double *__restrict__ w,
+                                                      int n, double *c) {
+  for (int j = blockIdx.x; j < nvec; j += gridDim.x) {
+    const VT *vj = V + (long)j * ldv;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) acc += (double)vj[i] * w[i];
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) c[j] = acc;
+    __syncthreads();
+  }
+}
+
+// w -= sum_j c[j] V_j; r2 = <w,w>  (classical Gram-Schmidt pass of full reorthogonalisation)
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_multisub(const VT *__restrict__ V, long ldv, int nvec, const double *__restrict__ c,
+                                                      double *__restrict__ w, int n, double *r2, RedSlot slot) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double wi = w[i];
+    for (int j = 0; j < nvec; ++j) wi -= c[j] * (double)V[(long)j * ldv + i];
+    w[i] = wi;
+    acc += wi * wi;
+  }
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+}
+
+// out_i = sum_{j<k} s_j V_j[i] in j order (sml/LANCZOS_SYM.c:195-202), then <out,out>.
+template <class VT>
+__global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, long ldv, int k, const double *__restrict__ s,
+                                                  double *__restrict__ out, int n, double *r2, RedSlot slot) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double t = 0.0;
+    for (int j = 0; j < k; ++j) t = t + s[j] * (double)V[(long)j * ldv + i];
+    out[i] = t;
+    acc += t * t;
+  }
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+}
+
+// ---- CG ------------------------------------------------------------------------------
+
+// Initial residual: x0 normalised (sml/CONJUGATE_GRADIENT_SYM.c:35), r = b - (H + sigma) x0,
+// p = r (:37-43); rr = <r,r>.
+struct EpiCgInit {
+  static constexpr bool kReduce = true;
+  const double *b;
+  double *xs;   // normalised x0
+  double *r, *p;
+  Scalars *S;
+  __device__ void row(int i, double xi, double yi, double &acc) const {
+    xs[i] = xi;
+    const double ri = b[i] - yi;
+    r[i] = ri;
+    p[i] = ri;
+    acc += ri * ri;
+  }
+  __device__ void finalize(double t) const {
+    S->rr = t;
+    S->done = 0;
+    S->iters = 0;
+  }
+};
+
+// y = (H + sigma) p, alpha = <r,r>/<p,y>  (:47-51)
+struct EpiCgAlpha {
+  static constexpr bool kReduce = true;
+  double *y;
+  Scalars *S;
+  __device__ void row(int i, double xi, double yi, double &acc) const {
+    y[i] = yi;
+    acc += xi * yi;
+  }
+  __device__ void finalize(double t) const { S->a = S->rr / t; }
+};
+
+// x += a p; r -= a y; convergence on <r,r> < acc (:53-67)
+__global__ void k_cg_update(int n, const double *__restrict__ p, const double *__restrict__ y, double *__restrict__ x,
+                            double *__restrict__ r, Scalars *S, double acc_thr, int it, int max_step, Progress *prog,
+                            RedSlot slot);
+// p = r + beta p (:93-95)
+__global__ void k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p, const Scalars *S);
+
+// ---- MINRES (sml/MINIMUM_RESIDUAL_SYM.c) ----------------------------------------------
+
+// V1 = b - (H + sigma) x  (:34-39), gamma0 = ||V1|| (:42)
+struct EpiMrInit {
+  static constexpr bool kReduce = true;
+  const double *b;
+  double *v1;
+  Scalars *S;
+  __device__ void row(int i, double, double yi, double &acc) const {
+    const double v = b[i] - yi;
+    v1[i] = v;
+    acc += v * v;
+  }
+  __device__ void finalize(double t) const {
+    S->gamma0 = sqrt(t);
+    S->eta = S->gamma0;
+    S->s0 = 0.0;
+    S->s1 = 0.0;
+    S->c0 = 1.0;
+    S->c1 = 1.0;
+    S->done = 0;
+    S->iters = 0;
+  }
+};
+
+// V1 *= 1/gamma0 (materialised), Temp = (H + sigma) V1, delta = <Temp, V1>  (:51-60)
+struct EpiMrDelta {
+  static constexpr bool kReduce = true;
+  double *v1n, *temp;
+  Scalars *S;
+  __device__ void row(int i, double xi, double yi, double &acc) const {
+    v1n[i] = xi;
+    temp[i] = yi;
+    acc += yi * xi;
+  }
+  __device__ void finalize(double t) const { S->delta = t; }
+};
+
+__global__ void k_mr_lanczos(int n, const double *__restrict__ temp, const double *__restrict__ v1n,
+                             const double *__restrict__ v0, double *__restrict__ v2, Scalars *S, double acc_thr, int it,
+                             int max_step, Progress *prog, RedSlot slot);
+__global__ void k_mr_update(int n, const double *__restrict__ v1n, const double *__restrict__ w0,
+                            const double *__restrict__ w1, double *__restrict__ w2, double *__restrict__ x, const Scalars *S);
+
+// ---------------------------------------------------------------------------------
+// Operator launchers: a small value type with
+//   int n() const;
+//   template <class XT, class Epi> void apply(const XT *x, const double *scale_src, int scale_mode,
+//        double sigma, const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) const;
+//   int grid() const;   // apply grid (for workspace sizing)
+// ---------------------------------------------------------------------------------
+
+struct LanczosResult {
+  double eig_val = 0.0;
+  int steps = 0;
+  int spmv = 0;
+  bool converged = false;
+  bool dense = false;
+};
+
+// Settings distilled from BOX_LAN.
+struct LanczosCfg {
+  double acc;
+  int min_step, max_step, max_block_step;
+  bool tight;
+  bool slow;             // LANCZOS_SLOW semantics: no restart, checks from block_step >= min_step
+  bool reorth;           // full reorthogonalisation (dense path and mixed form)
+  bool accept_at_end;    // dense path: the last step spans the whole space, accept it
+  int lookahead;
+};
+
+// Lanczos on operator op.  w_dev holds the start vector on entry (overwritten).  The
+// normalised Ritz vector is written to out_dev.
+template <class Opl>
+LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, double *out_dev, Workspace &ws) {
+  const int n = op.n();
+  cudaStream_t st = ws.st;
+  Scalars *S = ws.S();
+  LanczosResult res;
+
+  const int cap_max = cfg.max_block_step + 1;
+  DevBuf<double> D(cap_max + 1), O(cap_max + 1), y(n), c(cap_max + 1);
+  Mapped<double> hD(cap_max + 1), hO(cap_max + 1), hs(cap_max + 1);
+  DevBuf<double> s_dev(cap_max + 1);
+
+  // Krylov basis storage, grown in a stream-ordered way.
+  double *V = nullptr;
+  int cap = 0;
+  auto ensure = [&](int need) {
+    if (need <= cap) return;
+    int ncap = cap == 0 ? std::min(cap_max, std::max(need, 64)) : std::min(cap_max, std::max(need, 2 * cap));
+    double *nv = nullptr;
+    DG_CUDA(cudaMallocAsync((void **)&nv, sizeof(double) * (size_t)ncap * n, st));
+    if (V) {
+      DG_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * (size_t)cap * n, cudaMemcpyDeviceToDevice, st));
+      DG_CUDA(cudaFreeAsync(V, st));
+    }
+    V = nv;
+    cap = ncap;
+  };
+  struct FreeV {
+    double **v;
+    cudaStream_t st;
+    ~FreeV() {
+      if (*v) cudaFreeAsync(*v, st);
+    }
+  } freev{&V, st};
+
+  const RedSlot slot = ws.slot();
+  int stamp = 0;   // operator applications enqueued
+  auto enqueue_apply = [&](int b) {
+    ensure(b + 1);
+    ++stamp;
+    EpiLanczos<double> epi{y.get(), V + (size_t)b * n, D.get(), O.get(), hD.d, hO.d, ws.prog.d, &S->r2, b, stamp};
+    op.apply(w_dev, &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
+    ++res.spmv;
+  };
+  auto enqueue_update = [&](int b) {
+    const double *vprev = (b > 0) ? V + (size_t)(b - 1) * n : nullptr;
+    k_lz_update<double><<<ws.vgrid, kThreads, 0, st>>>(n, y.get(), V + (size_t)b * n, vprev, D.get(), O.get(), b, w_dev,
+                                                     &S->r2, slot); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    if (cfg.reorth) {
+      for (int pass = 0; pass < 2; ++pass) {
+        k_multidot<double><<<std::min(b + 1, 1024), kThreads, 0, st>>>(V, n, b + 1, w_dev, n, c.get()); ::dg::count_launch();
+        k_multisub<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, b + 1, c.get(), w_dev, n, &S->r2, slot); ::dg::count_launch();
+      }
+      DG_CUDA(cudaGetLastError());
+    }
+  };
+
+  // <w,w> of the start vector.
+  k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(w_dev, n, &S->r2, slot); ::dg::count_launch();
+  DG_CUDA(cudaGetLastError());
+
+  std::vector<double> d, e, z;
+  double E = 1e15;            // pow(10,15) (sml/LANCZOS_SYM.c:77)
+  int total_step = 0;
+  int n_last = 0;             // order of the last tridiagonal solved
+  std::vector<double> s_last;
+  const int W = std::max(1, cfg.lookahead);
+
+  auto finish = [&](int k, const std::vector<double> &s) {
+    for (int j = 0; j < k; ++j) hs.h[j] = s[j];
+    DG_CUDA(cudaMemcpyAsync(s_dev.get(), hs.h, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+    k_ritz<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, k, s_dev.get(), out_dev, n, &S->r2, slot); ::dg::count_launch();
+    k_scale_rsqrt<double><<<ws.vgrid, kThreads, 0, st>>>(out_dev, n, &S->r2); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaStreamSynchronize(st));
+  };
+
+  while (total_step < cfg.max_step) {
+    // One restart cycle (the whole run when max_block_step >= max_step).
+    const int base_stamp = stamp;
+    enqueue_apply(0);
+    enqueue_update(0);
+    const int nb_max = cfg.slow ? cfg.max_step - 1 : std::min(cfg.max_block_step - 1, cfg.max_step - total_step);
+    if (nb_max == 0 && cfg.accept_at_end) {
+      // 1 x 1 operator: the Rayleigh quotient of the (normalised) start vector is exact.
+      DG_CUDA(cudaStreamSynchronize(st));
+      res.eig_val = hD.h[0];
+      res.converged = true;
+      finish(1, std::vector<double>{1.0});
+      return res;
+    }
+    int enq = 0;
+    bool restart = false;
+    for (int bs = 1; bs <= nb_max; ++bs) {
+      while (enq < std::min(bs + W, nb_max)) {
+        ++enq;
+        enqueue_apply(enq);
+        enqueue_update(enq);
+      }
+      const int want = base_stamp + 1 + bs;   // stamp after apply(bs)
+      if (!host_wait(st, [&] { return ws.prog.h->stamp >= want; })) {
+        set_error("Lanczos: timed out waiting for step %d", bs);
+        throw Error{DG_ERR_TIMEOUT};
+      }
+      total_step = cfg.slow ? bs : total_step + 1;
+      // Breakdown: the start vector spans an invariant subspace of dimension bs, so
+      // ||w|| vanished and v_bs is meaningless.  The Ritz pair of T_{bs-1} is exact.
+      {
+        double scale = 0.0;
+        for (int j = 0; j < bs; ++j) scale = std::max(scale, std::fabs(hD.h[j]) + std::fabs(hO.h[j]));
+        if (!(hO.h[bs] > 1e-13 * scale) || !std::isfinite(hD.h[bs])) {
+          const int nn = bs;
+          d.assign(hD.h, hD.h + nn);
+          e.resize(nn);
+          for (int i = 1; i < nn; ++i) e[i - 1] = hO.h[i];
+          const double lam = tridiag_lowest_eigenvalue(d.data(), e.data(), nn);
+          z.resize(nn);
+          tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+          res.eig_val = lam;
+          res.steps = total_step;
+          res.converged = true;
+          finish(nn, z);
+          return res;
+        }
+      }
+      const bool check = cfg.slow ? (bs >= cfg.min_step) : (total_step >= cfg.min_step || bs == cfg.max_block_step - 1);
+      if (!check) continue;
+      const int nn = bs + 1;
+      d.assign(hD.h, hD.h + nn);
+      e.resize(nn);
+      for (int i = 1; i < nn; ++i) e[i - 1] = hO.h[i];
+      const double hint = (E < 1e14) ? E : std::numeric_limits<double>::infinity();
+      const double lam = tridiag_lowest_eigenvalue(d.data(), e.data(), nn, hint);
+      bool conv;
+      if (cfg.tight) {
+        z.resize(nn);
+        tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+        conv = std::fabs(z[nn - 1]) < cfg.acc;
+      } else {
+        conv = std::fabs(E - lam) < cfg.acc;
+      }
+      if (!conv && cfg.accept_at_end && bs == nb_max) conv = true;
+      n_last = nn;
+      if (conv) {
+        if (!cfg.tight) {
+          z.resize(nn);
+          tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+        }
+        res.eig_val = lam;
+        res.steps = total_step;
+        res.converged = true;
+        finish(nn, z);
+        return res;
+      }
+      if (!cfg.slow && bs == cfg.max_block_step - 1) {
+        // Restart from the current Ritz vector (sml/LANCZOS_SYM.c:234-256); E is not updated.
+        z.resize(nn);
+        tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+        s_last = z;
+        restart = true;
+        break;
+      }
+      E = lam;
+    }
+    if (cfg.slow) break;
+    if (!restart) break;
+    // Drain speculative work, then form the restart vector in w.
+    for (int j = 0; j < n_last; ++j) hs.h[j] = s_last[j];
+    DG_CUDA(cudaMemcpyAsync(s_dev.get(), hs.h, sizeof(double) * n_last, cudaMemcpyHostToDevice, st));
+    k_ritz<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, n_last, s_dev.get(), w_dev, n, &S->r2, slot); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaStreamSynchronize(st));
+    stamp = ws.prog.h->stamp;   // speculative applies beyond the restart point have all landed
+  }
+  res.steps = total_step;
+  res.converged = false;
+  DG_CUDA(cudaStreamSynchronize(st));
+  return res;
+}
+
+struct IterResult {
+  int iters = 0;
+  bool converged = false;
+};
+
+// CG on (op + sigma) x = b from x (normalised first).  x_dev in/out; b_dev read-only and
+// distinct from x_dev.  Reference: sml/CONJUGATE_GRADIENT_SYM.c:8-123.
+template <class Opl>
+IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_dev, double acc, int max_step, Workspace &ws,
+                   int *spmv_count) {
+  const int n = op.n();
+  cudaStream_t st = ws.st;
+  Scalars *S = ws.S();
+  const RedSlot slot = ws.slot();
+  DevBuf<double> xs(n), r(n), p(n), y(n);
+  IterResult res;
+  ws.prog.h->done = 0;
+  ws.prog.h->stamp = 0;
+  k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
+  op.apply(x_dev, &S->xn2, SCALE_RSQRT, sigma, (const int *)nullptr, EpiCgInit{b_dev, xs.get(), r.get(), p.get(), S}, slot, st);
+  DG_CUDA(cudaMemcpyAsync(x_dev, xs.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (spmv_count) ++*spmv_count;
+  const int chunk = 8;
+  int enq = 0;   // last iteration enqueued
+  auto enqueue_to = [&](int last) {
+    for (int it = enq + 1; it <= last; ++it) {
+      op.apply(p.get(), (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgAlpha{y.get(), S}, slot, st);
+      k_cg_update<<<ws.vgrid, kThreads, 0, st>>>(n, p.get(), y.get(), x_dev, r.get(), S, acc, it, max_step, ws.prog.d, slot); ::dg::count_launch();
+      k_cg_direction<<<ws.vgrid, kThreads, 0, st>>>(n, r.get(), p.get(), S); ::dg::count_launch();
+    }
+    DG_CUDA(cudaGetLastError());
+    enq = std::max(enq, last);
+  };
+  const int last_it = max_step - 1;
+  if (last_it >= 1) {
+    enqueue_to(std::min(chunk, last_it));
+    int checked = 0;
+    while (true) {
+      if (enq < last_it) enqueue_to(std::min(enq + chunk, last_it));
+      const int target = std::min(checked + chunk, last_it);
+      if (!host_wait(st, [&] { return ws.prog.h->done != 0 || ws.prog.h->stamp >= target; })) {
+        set_error("CG: timed out waiting for iteration %d", target);
+        throw Error{DG_ERR_TIMEOUT};
+      }
+      if (ws.prog.h->done) break;
+      checked = target;
+      if (checked >= last_it) break;
+    }
+  }
+  DG_CUDA(cudaStreamSynchronize(st));
+  Scalars hs;
+  DG_CUDA(cudaMemcpy(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost));
+  res.converged = hs.done == 1;
+  res.iters = hs.done ? hs.iters : max_step;
+  if (spmv_count) *spmv_count += (hs.done ? hs.iters : std::max(0, max_step - 1));
+  return res;
+}
+
+// MINRES on (op + sigma) x = b from x (not normalised).  Reference:
+// sml/MINIMUM_RESIDUAL_SYM.c:8-160 (on convergence the last X1 is not copied back, :89-114).
+template <class Opl>
+IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double *x_dev, double acc, int max_step,
+                       Workspace &ws, int *spmv_count) {
+  const int n = op.n();
+  cudaStream_t st = ws.st;
+  Scalars *S = ws.S();
+  const RedSlot slot = ws.slot();
+  DevBuf<double> vb[4], wb[3], temp(n);
+  for (auto &v : vb) {
+    v.alloc(n);
+    DG_CUDA(cudaMemsetAsync(v.get(), 0, sizeof(double) * n, st));
+  }
+  for (auto &w : wb) {
+    w.alloc(n);
+    DG_CUDA(cudaMemsetAsync(w.get(), 0, sizeof(double) * n, st));
+  }
+  IterResult res;
+  ws.prog.h->done = 0;
+  ws.prog.h->stamp = 0;
+  // ring: V0 = vb[i0], V1raw = vb[i1], V1n -> vb[i2], V2 -> vb[i3]
+  int i0 = 0, i1 = 1, i2 = 2, i3 = 3, j0 = 0, j1 = 1, j2 = 2;
+  op.apply(x_dev, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiMrInit{b_dev, vb[i1].get(), S}, slot, st);
+  if (spmv_count) ++*spmv_count;
+  const int chunk = 8;
+  int enq = -1;
+  auto enqueue_to = [&](int last) {
+    for (int it = enq + 1; it <= last; ++it) {
+      op.apply(vb[i1].get(), &S->gamma0, SCALE_RECIP, sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
+      k_mr_lanczos<<<ws.vgrid, kThreads, 0, st>>>(n, temp.get(), vb[i2].get(), vb[i0].get(), vb[i3].get(), S, acc, it, max_step,
+                                                   ws.prog.d, slot); ::dg::count_launch();
+      k_mr_update<<<ws.vgrid, kThreads, 0, st>>>(n, vb[i2].get(), wb[j0].get(), wb[j1].get(), wb[j2].get(), x_dev, S); ::dg::count_launch();
+      // V0 <- V1n, V1 <- V2 ; W0 <- W1, W1 <- W2
+      int o0 = i0, o1 = i1;
+      i0 = i2;
+      i1 = i3;
+      i2 = o0;
+      i3 = o1;
+      int q0 = j0;
+      j0 = j1;
+      j1 = j2;
+      j2 = q0;
+    }
+    DG_CUDA(cudaGetLastError());
+    enq = std::max(enq, last);
+  };
+  const int last_it = max_step - 1;
+  if (last_it >= 0) {
+    enqueue_to(std::min(chunk - 1, last_it));
+    int checked = -1;
+    while (true) {
+      if (enq < last_it) enqueue_to(std::min(enq + chunk, last_it));
+      const int target = std::min(checked + chunk, last_it);
+      if (!host_wait(st, [&] { return ws.prog.h->done != 0 || ws.prog.h->stamp >= target + 1; })) {
+        set_error("MINRES: timed out waiting for iteration %d", target);
+        throw Error{DG_ERR_TIMEOUT};
+      }
+      if (ws.prog.h->done) break;
+      checked = target;
+      if (checked >= last_it) break;
+    }
+  }
+  DG_CUDA(cudaStreamSynchronize(st));
+  Scalars hs;
+  DG_CUDA(cudaMemcpy(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost));
+  res.converged = hs.done == 1;
+  res.iters = hs.done ? hs.iters : max_step;
+  if (spmv_count) *spmv_count += (hs.done ? hs.iters + 1 : max_step);
+  return res;
+}
+
+// sum_i |lambda x_i - ((op + sigma) x)_i|, returned to the host.
+template <class Opl>
+double residual_core(const Opl &op, const double *x_dev, double sigma, double lambda, Workspace &ws) {
+  Scalars *S = ws.S();
+  op.apply(x_dev, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiResidualL1{lambda, &S->res}, ws.slot(), ws.st);
+  double out = 0.0;
+  DG_CUDA(cudaMemcpyAsync(&out, &S->res, sizeof(double), cudaMemcpyDeviceToHost, ws.st));
+  DG_CUDA(cudaStreamSynchronize(ws.st));
+  return out;
+}
+
+struct IICfg {
+  double ii_acc, ii_diag_add;
+  int ii_max_step;
+  double cg_acc;
+  int cg_max_step;
+  bool minres;
+  bool shifted_check;   // SML form: check (M + d - E) psi against d psi; OBC form: H psi against E psi
+};
+
+struct IIResult {
+  double error = 0.0;
+  int iters = 0;
+  int cg_total = 0;
+  bool converged = false;
+  std::vector<int> cg_steps;   // per inner solve (for the step files)
+};
+
+// Inverse iteration (sml/INVERSE_ITERATION_SYM.c:9-115, dmrg/DMRG_INVERSE_ITERATION_OBC.c:10-106).
+template <class Opl>
+IIResult inverse_iteration_core(const Opl &op, const IICfg &cfg, double eig_val, double *eig_dev, Workspace &ws, int *spmv_count) {
+  const int n = op.n();
+  cudaStream_t st = ws.st;
+  const double sigma = cfg.ii_diag_add - eig_val;
+  DevBuf<double> un(n);
+  DG_CUDA(cudaMemcpyAsync(un.get(), eig_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  IIResult res;
+  double error = 1000.0;
+  int iter;
+  for (iter = 0; iter <= cfg.ii_max_step; ++iter) {
+    error = cfg.shifted_check ? residual_core(op, eig_dev, sigma, cfg.ii_diag_add, ws) : residual_core(op, eig_dev, 0.0, eig_val, ws);
+    if (spmv_count) ++*spmv_count;
+    if (error < cfg.ii_acc) {
+      res.converged = true;
+      break;
+    }
+    if (!cfg.shifted_check) DG_CUDA(cudaMemcpyAsync(un.get(), eig_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    IterResult r = cfg.minres ? minres_core(op, sigma, eig_dev, un.get(), cfg.cg_acc, cfg.cg_max_step, ws, spmv_count)
+                              : cg_core(op, sigma, eig_dev, un.get(), cfg.cg_acc, cfg.cg_max_step, ws, spmv_count);
+    res.cg_steps.push_back(r.iters);
+    res.cg_total += r.iters;
+    k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(un.get(), n, &ws.S()->xn2, ws.slot()); ::dg::count_launch();
+    k_scale_rsqrt<double><<<ws.vgrid, kThreads, 0, st>>>(un.get(), n, &ws.S()->xn2); ::dg::count_launch();
+    DG_CUDA(cudaMemcpyAsync(eig_dev, un.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    DG_CUDA(cudaGetLastError());
+  }
+  res.error = error;
+  res.iters = iter;   // value the reference writes to Inv_iter_step.txt
+  DG_CUDA(cudaStreamSynchronize(st));
+  return res;
+}
+
+}  // namespace dg

@@ -1,0 +1,108 @@
+// util.cu -- error state, device / stream management, small host helpers.
+#include <atomic>
+#include <chrono>
+#include <cstdarg>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace dg {
+
+namespace {
+thread_local char g_err[1024] = {0};
+std::atomic<long> g_launches{0};
+}
+
+void count_launch(long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+const char *last_error() { return g_err; }
+
+void require_device() {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    set_error("no CUDA device available (%s)", e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+    throw Error{DG_ERR_NODEVICE};
+  }
+}
+
+cudaStream_t stream() {
+  thread_local cudaStream_t s = nullptr;
+  thread_local int dev = -1;
+  int cur = 0;
+  DG_CUDA(cudaGetDevice(&cur));
+  if (!s || dev != cur) {
+    DG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    dev = cur;
+  }
+  return s;
+}
+
+int sm_count() {
+  thread_local int cached = -1, dev = -1;
+  int cur = 0;
+  DG_CUDA(cudaGetDevice(&cur));
+  if (cached < 0 || dev != cur) {
+    DG_CUDA(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, cur));
+    dev = cur;
+  }
+  return cached;
+}
+
+int vector_grid(long n) {
+  long need = (n + kThreads - 1) / kThreads;
+  long cap = (long)sm_count() * 4;
+  if (need < 1) need = 1;
+  return (int)(need < cap ? need : cap);
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+}  // namespace dg
+
+extern "C" {
+
+const char *dg_last_error(void) { return dg::last_error(); }
+
+int dg_device_count(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return count;
+}
+
+const char *dg_version(void) { return "dmrg_gb300 0.1 (sm_103a)"; }
+
+long dg_kernel_launches(void) { return dg::g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,221 @@
+"""Loader and typed bindings of libdmrg_gb300.so (the C-ABI in include/dmrg_gb300.h).
+
+The library is built in-tree (``python -m dmrg_c_gb300.build``).  There is no fallback:
+importing the bindings raises if the shared library is missing, and every native call
+that fails raises :class:`DgError` with the library's own message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .abi import (BOX_CG, BOX_II, BOX_LAN, CRS1, DMRG_BASIS, DMRG_BOX_CG, DMRG_BOX_II, DMRG_BOX_LAN, DMRG_PARAMETER,
+                  DMRG_STATUS, DMRG_TIME, EXACT_BASIS_INFO, EXACT_HAM_INFO, EXACT_PARAMETER, EXACT_TIME,
+                  EXACT_WHOLE_BASIS_Q1, EXACT_WHOLE_BASIS_Q2, EXACT_WHOLE_BASIS_Q3, dg_ed_model, dg_solve_info,
+                  dg_solver_params)
+
+LIB_PATH = Path(__file__).resolve().parent / "libdmrg_gb300.so"
+
+DG_STATUS = {0: "DG_OK", 1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_NOMEM", 4: "DG_ERR_NOCONV", 5: "DG_ERR_TIMEOUT",
+             6: "DG_ERR_NODEVICE", 7: "DG_ERR_MATRIX"}
+
+
+class DgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{DG_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+P = C.POINTER
+vp = C.c_void_p
+dp = P(C.c_double)
+ip = P(C.c_int)
+lp = P(C.c_long)
+fp = P(C.c_float)
+
+# name -> (restype, argtypes); every declaration of include/dmrg_gb300.h
+SIGNATURES = {
+    # drop-in (reference names)
+    "MATRIX_VECTOR_PRODUCT": (None, [P(CRS1), dp, dp, C.c_int]),
+    "MATRIX_VECTOR_PRODUCT_SYM": (None, [P(CRS1), dp, dp, P(dp), C.c_int]),
+    "LANCZOS": (None, [P(BOX_LAN)]),
+    "LANCZOS_SYM": (None, [P(BOX_LAN)]),
+    "LANCZOS_SLOW": (None, [P(BOX_LAN)]),
+    "LANCZOS_SLOW_SYM": (None, [P(BOX_LAN)]),
+    "INVERSE_ITERATION": (None, [P(BOX_II)]),
+    "INVERSE_ITERATION_SYM": (None, [P(BOX_II)]),
+    "CONJUGATE_GRADIENT": (None, [P(BOX_CG)]),
+    "CONJUGATE_GRADIENT_SYM": (None, [P(BOX_CG)]),
+    "MINIMUM_RESIDUAL": (None, [P(BOX_CG)]),
+    "MINIMUM_RESIDUAL_SYM": (None, [P(BOX_CG)]),
+    "CONVERGE_CHECK": (C.c_double, [P(CRS1), dp, C.c_double, C.c_int]),
+    "CONVERGE_CHECK_SYM": (C.c_double, [P(CRS1), dp, C.c_double, C.c_int]),
+    "DMRG_DIAGONALIZE_SUPERBLOCK": (None, [P(CRS1), P(DMRG_TIME), P(DMRG_PARAMETER), P(DMRG_STATUS), C.c_int]),
+    "DMRG_DIAGONALIZE_SUPERBLOCK_SYM": (None, [P(CRS1), P(DMRG_TIME), P(DMRG_PARAMETER), P(DMRG_STATUS), C.c_int]),
+    "DMRG_MATRIX_VECTOR_PRODUCT_OBC": (None, [P(CRS1), P(CRS1), P(CRS1), P(CRS1), dp, dp, ip, C.c_int, P(DMRG_BASIS)]),
+    "DMRG_LANCZOS_SLOW_OBC": (None, [P(DMRG_BOX_LAN)]),
+    "DMRG_CONJUGATE_GRADIENT_OBC": (None, [P(DMRG_BOX_CG)]),
+    "DMRG_INVERSE_ITERATION_OBC": (None, [P(DMRG_BOX_II)]),
+    "DMRG_CONVERGE_CHECK_OBC": (C.c_double, [C.c_double, P(CRS1), P(CRS1), P(CRS1), P(CRS1), dp, dp, ip, C.c_int,
+                                            P(DMRG_BASIS)]),
+    "EXACT_DIAGONALIZE_HAMILTONIAN": (None, [P(EXACT_HAM_INFO), P(EXACT_PARAMETER), P(EXACT_TIME), C.c_int]),
+    "EXACT_V_M_Q0": (None, [P(CRS1), dp, dp, C.c_int, C.c_int, C.c_int, P(EXACT_BASIS_INFO)]),
+    "EXACT_V_M_Q1": (None, [P(CRS1), C.c_int, dp, C.c_int, dp, C.c_int, C.c_int, C.c_int, P(EXACT_WHOLE_BASIS_Q1)]),
+    "EXACT_V_M_Q2": (None, [P(CRS1), C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, C.c_char_p, ip, C.c_int, C.c_int,
+                            C.c_int, P(EXACT_WHOLE_BASIS_Q2)]),
+    "EXACT_V_M_Q3": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, dp, C.c_char_p, ip,
+                            C.c_int, C.c_int, C.c_int, P(EXACT_WHOLE_BASIS_Q3)]),
+    # native API
+    "dg_last_error": (C.c_char_p, []),
+    "dg_device_count": (C.c_int, []),
+    "dg_version": (C.c_char_p, []),
+    "dg_kernel_launches": (C.c_long, []),
+    "dg_profile_spmv": (C.c_int, [vp, vp, vp, C.c_int, C.c_size_t, P(C.c_float)]),
+    "dg_matrix_create": (C.c_int, [C.c_int, lp, ip, dp, C.c_int, C.c_int, P(vp)]),
+    "dg_matrix_create_device": (C.c_int, [C.c_int, C.c_long, vp, vp, vp, C.c_int, C.c_int, P(vp)]),
+    "dg_matrix_free": (None, [vp]),
+    "dg_matrix_info": (C.c_int, [vp, ip, lp, ip, ip]),
+    "dg_matrix_set_shape": (C.c_int, [vp, C.c_int, C.c_int]),
+    "dg_matrix_download": (C.c_int, [vp, lp, ip, dp]),
+    "dg_spmv": (C.c_int, [vp, vp, vp, C.c_double]),
+    "dg_spmv_f32": (C.c_int, [vp, vp, vp]),
+    "dg_solver_params_default": (None, [P(dg_solver_params)]),
+    "dg_lanczos": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
+    "dg_inverse_iteration": (C.c_int, [vp, P(dg_solver_params), C.c_double, vp, P(dg_solve_info)]),
+    "dg_ground_state": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
+    "dg_linear_solve": (C.c_int, [vp, C.c_double, vp, vp, C.c_double, C.c_int, C.c_int, ip]),
+    "dg_residual_l1": (C.c_int, [vp, vp, C.c_double, dp]),
+}
+
+DG_STORE_FULL, DG_STORE_LOWER_DIAG_LAST = 0, 1
+DG_VALUES_F64, DG_VALUES_F32, DG_VALUES_BOTH = 1, 2, 3
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load (once) and type the library.  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else Path(os.environ.get("DG_LIB", LIB_PATH))
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build the CUDA library first (python -m dmrg_c_gb300.build)")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        raise DgError(rc, load().dg_last_error().decode(errors="replace"))
+
+
+def kernel_launches() -> int:
+    return int(load().dg_kernel_launches())
+
+
+def device_count() -> int:
+    return int(load().dg_device_count())
+
+
+def as_ptr(a):
+    """ctypes void* for a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return C.c_void_p(a.ctypes.data)
+    return C.c_void_p(a.data_ptr())          # torch tensor
+
+
+class DeviceMatrix:
+    """A device-resident CRS operator (dg_matrix)."""
+
+    def __init__(self, crs: abi.Crs, storage: int = DG_STORE_FULL, values: int = DG_VALUES_F64):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.dg_matrix_create(crs.n, abi.ptr(crs.row, C.c_long), abi.ptr(crs.col, C.c_int),
+                                   abi.ptr(crs.val, C.c_double), storage, values, C.byref(h)))
+        self.h = h
+        n, nnz, lanes, grid = C.c_int(), C.c_long(), C.c_int(), C.c_int()
+        check(lib.dg_matrix_info(h, C.byref(n), C.byref(nnz), C.byref(lanes), C.byref(grid)))
+        self.n, self.nnz, self.lanes, self.grid = n.value, nnz.value, lanes.value, grid.value
+
+    def close(self):
+        if self.h:
+            load().dg_matrix_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_shape(self, lanes: int, grid: int):
+        check(load().dg_matrix_set_shape(self.h, lanes, grid))
+        self.lanes, self.grid = lanes, grid
+
+    def download(self):
+        row = np.empty(self.n + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        val = np.empty(self.nnz, np.float64)
+        check(load().dg_matrix_download(self.h, abi.ptr(row, C.c_long), abi.ptr(col, C.c_int), abi.ptr(val, C.c_double)))
+        return row, col, val
+
+    def spmv(self, x, y=None, sigma: float = 0.0):
+        if y is None:
+            y = np.empty(self.n, np.float64)
+        check(load().dg_spmv(self.h, as_ptr(x), as_ptr(y), sigma))
+        return y
+
+    def profile_spmv(self, x_dev, y_dev, iters=20, flush_bytes=0) -> float:
+        """Average ms per launch of the fused product kernel (CUDA events on the library stream)."""
+        ms = C.c_float()
+        check(load().dg_profile_spmv(self.h, as_ptr(x_dev), as_ptr(y_dev), iters, flush_bytes, C.byref(ms)))
+        return ms.value
+
+    def spmv_f32(self, x, y=None):
+        if y is None:
+            y = np.empty(self.n, np.float32)
+        check(load().dg_spmv_f32(self.h, as_ptr(x), as_ptr(y)))
+        return y
+
+
+def default_params(**kw) -> dg_solver_params:
+    p = dg_solver_params()
+    load().dg_solver_params_default(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def ground_state(m: DeviceMatrix, params: dg_solver_params | None = None, guess=None, out=None, lanczos_only=False):
+    """Lanczos (+ inverse iteration) on the device; returns (eigvec, dg_solve_info)."""
+    p = params or default_params()
+    if out is None:
+        out = np.empty(m.n, np.float64)
+    info = dg_solve_info()
+    fn = load().dg_lanczos if lanczos_only else load().dg_ground_state
+    check(fn(m.h, C.byref(p), as_ptr(guess), as_ptr(out), C.byref(info)))
+    return out, info
+
+
+def linear_solve(m: DeviceMatrix, b, x, sigma=0.0, acc=1e-7, max_step=1000, minres=False):
+    it = C.c_int()
+    rc = load().dg_linear_solve(m.h, sigma, as_ptr(b), as_ptr(x), acc, max_step, int(minres), C.byref(it))
+    return rc, it.value
+
+
+def residual_l1(m: DeviceMatrix, x, lam: float) -> float:
+    out = C.c_double()
+    check(load().dg_residual_l1(m.h, as_ptr(x), lam, C.byref(out)))
+    return out.value

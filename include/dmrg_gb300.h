@@ -1,0 +1,198 @@
+/*
+ * dmrg_gb300.h -- C-ABI of libdmrg_gb300.so, the GB300 (sm_103a) eigensolver hot path of dmrg_C.
+ *
+ * Two layers are exported:
+ *
+ *  1. Drop-in entry points with the reference's own names, argument lists and error
+ *     behaviour (print + append to ./SML_out/error.txt + exit(1) on fatal errors,
+ *     "continue..." on CG / inverse-iteration non-convergence, step counts appended to
+ *     ./SML_out/<NAME>_Step.txt).  Linking this library before -ldmrg -lsml -lexact
+ *     replaces the reference's archive members; the rest of the C code is unchanged.
+ *     Every prototype cites the reference declaration it replaces.
+ *
+ *  2. A status-returning native API (dg_*) used by the drop-in layer itself, by the
+ *     batched / served forms and by tests.  It never exits the process and never writes
+ *     files; failures return a non-zero dg_status and dg_last_error() describes them.
+ *
+ * All work runs on the current CUDA device.  There is no CPU fallback: when no device is
+ * present the drop-in entry points print an error and exit(1), and dg_* return
+ * DG_ERR_NODEVICE.  Host arrays passed to the drop-in layer are never modified except
+ * for the documented outputs (unlike the reference, INVERSE_ITERATION* does not shift the
+ * caller's matrix diagonal in place).
+ */
+#ifndef DMRG_GB300_H
+#define DMRG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "dmrg_gb300_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------
+ * 1. Drop-in entry points (reference names)
+ * ---------------------------------------------------------------------------------- */
+
+/* y = M x on a full CRS matrix.                         replaces include/SML.h:291 */
+void MATRIX_VECTOR_PRODUCT(CRS1 *M, double *V1, double *Out, int p_threads);
+/* y = M x on a lower-triangle CRS whose rows end with the diagonal; Temp is the
+ * reference's per-thread scratch and is neither read nor written here.
+ *                                                        replaces include/SML.h:292 */
+void MATRIX_VECTOR_PRODUCT_SYM(CRS1 *M, double *V1, double *Out, double **Temp, int p_threads);
+
+/* Lanczos ground state (stored Krylov vectors).        replaces include/SML.h:273-274 */
+void LANCZOS(BOX_LAN *Box);
+void LANCZOS_SYM(BOX_LAN *Box);
+/* Lanczos ground state, vector re-formed from the recurrence.
+ *                                                        replaces include/SML.h:271-272 */
+void LANCZOS_SLOW(BOX_LAN *Box);
+void LANCZOS_SLOW_SYM(BOX_LAN *Box);
+
+/* Inverse-iteration refinement with CG / MINRES inner solves.
+ *                                                        replaces include/SML.h:266-267 */
+void INVERSE_ITERATION(BOX_II *Box_II);
+void INVERSE_ITERATION_SYM(BOX_II *Box_II);
+/*                                                        replaces include/SML.h:172-173 */
+void CONJUGATE_GRADIENT(BOX_CG *Box);
+void CONJUGATE_GRADIENT_SYM(BOX_CG *Box);
+/*                                                        replaces include/SML.h:293-294 */
+void MINIMUM_RESIDUAL(BOX_CG *Box);
+void MINIMUM_RESIDUAL_SYM(BOX_CG *Box);
+/* L1 residual sum_i |(M v)_i - lambda v_i|.             replaces include/SML.h:174-175 */
+double CONVERGE_CHECK(CRS1 *M, double *Eig_Vec, double eig_val, int p_threads);
+double CONVERGE_CHECK_SYM(CRS1 *M, double *Eig_Vec, double eig_val, int p_threads);
+
+/* Superblock ground state (Lanczos then inverse iteration).
+ *                                                        replaces include/dmrg.h:353,406 */
+void DMRG_DIAGONALIZE_SUPERBLOCK(CRS1 *Ham, DMRG_TIME *Time, DMRG_PARAMETER *Param, DMRG_STATUS *Dmrg_Status, int p_threads);
+void DMRG_DIAGONALIZE_SUPERBLOCK_SYM(CRS1 *Ham, DMRG_TIME *Time, DMRG_PARAMETER *Param, DMRG_STATUS *Dmrg_Status, int p_threads);
+
+/* Matrix-free open-boundary superblock operator and its solvers.
+ *                                                        replaces include/dmrg.h:401-405 */
+void DMRG_MATRIX_VECTOR_PRODUCT_OBC(CRS1 *M_LLLR, CRS1 *M_LRRL, CRS1 *M_LRRL_Sign, CRS1 *M_RRRL, double *V, double *Out_V, int *Ele_RR, int p_threads, DMRG_BASIS *Dmrg_Basis);
+void DMRG_LANCZOS_SLOW_OBC(DMRG_BOX_LAN *Box);
+void DMRG_CONJUGATE_GRADIENT_OBC(DMRG_BOX_CG *Box);
+void DMRG_INVERSE_ITERATION_OBC(DMRG_BOX_II *Box_II);
+double DMRG_CONVERGE_CHECK_OBC(double eig_val, CRS1 *M_LLLR, CRS1 *M_LRRL, CRS1 *M_LRRL_Sign, CRS1 *M_RRRL, double *Eig_V, double *Temp_V, int *Ele_RR, int p_threads, DMRG_BASIS *Dmrg_Basis);
+
+/* Exact-diagonalisation ground state.                   replaces include/exact.h:118 */
+void EXACT_DIAGONALIZE_HAMILTONIAN(EXACT_HAM_INFO *Ham_Info, EXACT_PARAMETER *Param, EXACT_TIME *Time, int p_threads);
+/* Out = O_site Vec on an ED basis.                      replaces include/exact.h:119,122-124 */
+void EXACT_V_M_Q0(CRS1 *M_On, double *Vec, double *Out_Vec, int dim_onsite, int site, int p_threads, EXACT_BASIS_INFO *Basis_Info);
+void EXACT_V_M_Q1(CRS1 *M_On, int qn_out, double *Vec, int qn_in, double *Out_Vec, int dim_onsite, int site, int p_threads, EXACT_WHOLE_BASIS_Q1 *W_Basis);
+void EXACT_V_M_Q2(CRS1 *M_On, int qn1_out, int qn2_out, double *Vec, int qn1_in, int qn2_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q2 *W_Basis);
+void EXACT_V_M_Q3(CRS1 *M_On, int qn1_out, int qn2_out, int qn3_out, double *Vec, int qn1_in, int qn2_in, int qn3_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q3 *W_Basis);
+
+/* ------------------------------------------------------------------------------------
+ * 2. Native status-returning API
+ * ---------------------------------------------------------------------------------- */
+
+typedef enum {
+   DG_OK = 0,
+   DG_ERR_ARG = 1,        /* invalid argument / malformed input                       */
+   DG_ERR_CUDA = 2,       /* a CUDA runtime call failed                               */
+   DG_ERR_NOMEM = 3,      /* device allocation failed                                 */
+   DG_ERR_NOCONV = 4,     /* iteration limit reached without convergence              */
+   DG_ERR_TIMEOUT = 5,    /* a bounded host wait on device progress ran out           */
+   DG_ERR_NODEVICE = 6,   /* no CUDA device                                           */
+   DG_ERR_MATRIX = 7      /* CRS invariant violated (row order, column range, diag)   */
+} dg_status;
+
+/* Text of the last error raised on the calling thread ("" when none). */
+const char *dg_last_error(void);
+/* Number of visible CUDA devices (0 when none or the runtime fails). */
+int dg_device_count(void);
+/* Library version string. */
+const char *dg_version(void);
+/* Kernel launches issued by this library since the process started. */
+long dg_kernel_launches(void);
+
+/* Opaque device-resident sparse operator (full CRS on the device, FP64 values and,
+ * optionally, an FP32 copy of the values for the mixed-precision form). */
+typedef struct dg_matrix dg_matrix;
+
+enum { DG_STORE_FULL = 0, DG_STORE_LOWER_DIAG_LAST = 1 };
+enum { DG_VALUES_F64 = 1, DG_VALUES_F32 = 2, DG_VALUES_BOTH = 3 };
+
+/* Upload a host CRS.  storage = DG_STORE_FULL for a full matrix (MATRIX_VECTOR_PRODUCT
+ * input), DG_STORE_LOWER_DIAG_LAST for the symmetric-half input of the *_SYM entry points
+ * (expanded on the device to a full CRS whose rows are sorted by column). */
+int dg_matrix_create(int n, const long *row, const int *col, const double *val, int storage, int values, dg_matrix **out);
+/* Same, with row/col/val already in device memory (they are copied). */
+int dg_matrix_create_device(int n, long nnz, const long *row_dev, const int *col_dev, const double *val_dev, int storage, int values, dg_matrix **out);
+void dg_matrix_free(dg_matrix *m);
+/* n, stored non-zeros of the full device matrix, and the launch shape chosen for it. */
+int dg_matrix_info(const dg_matrix *m, int *n, long *nnz_full, int *lanes_per_row, int *grid);
+/* Override the launch shape (lanes per row: 1,2,4,...,32; grid blocks of 256 threads). */
+int dg_matrix_set_shape(dg_matrix *m, int lanes_per_row, int grid);
+/* Download the device full CRS (row: n+1, col/val: nnz_full). */
+int dg_matrix_download(const dg_matrix *m, long *row, int *col, double *val);
+
+/* y = (M + sigma I) x.  x and y may be host or device pointers (detected). */
+int dg_spmv(dg_matrix *m, const double *x, double *y, double sigma);
+/* Same on FP32 values and FP32 vectors with FP64 accumulation (needs DG_VALUES_F32). */
+int dg_spmv_f32(dg_matrix *m, const float *x, float *y);
+/* Average device time of the Lanczos/CG form of the product (y = M x plus the fused
+ * <x, y> reduction) over iters launches, each timed with CUDA events on the library's
+ * stream; with flush_bytes > 0 a buffer of that size is rewritten before every launch so
+ * that the matrix is read from HBM, not L2.  x_dev / y_dev must be device pointers. */
+int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch);
+
+/* Solver settings (the fields of BOX_LAN / BOX_II / BOX_CG / DMRG_PARAMETER). */
+typedef struct {
+   double lanczos_acc;      /* BOX_LAN.acc                                   */
+   int lanczos_min_step;    /* BOX_LAN.min_step                              */
+   int lanczos_max_step;    /* BOX_LAN.max_step                              */
+   int lanczos_block_step;  /* BOX_LAN.max_block_step (restart length)       */
+   int lanczos_tight;       /* 1 = "Tight", 0 = "Normal"                     */
+   int lanczos_slow;        /* 1 = LANCZOS_SLOW semantics (re-formed vector) */
+   int dense_below;         /* solve n < dense_below to machine precision (reference: 1000) */
+   double ii_acc;           /* BOX_II.ii_acc                                 */
+   double ii_diag_add;      /* BOX_II.ii_diag_add                            */
+   int ii_max_step;         /* BOX_II.ii_max_step; < 0 skips inverse iteration */
+   double cg_acc;           /* BOX_CG.acc inside inverse iteration           */
+   int cg_max_step;         /* BOX_CG.max_step inside inverse iteration      */
+   int ii_minres;           /* 1 = "MR", 0 = "CG"                            */
+   int mixed;               /* 1 = FP32 Lanczos (values + vectors) with FP64 recurrence,
+                               full reorthogonalisation and FP64 refinement   */
+   uint64_t seed;           /* start vector seed when no guess is given      */
+   int lookahead;           /* Lanczos steps kept in flight ahead of the host check (0 = auto) */
+} dg_solver_params;
+
+/* Reference defaults: main/dmrg/xxz_vf/src/main/main.c:40-49 (cg_acc 1e-6 there, 1e-7 in
+ * the other drivers). */
+void dg_solver_params_default(dg_solver_params *p);
+
+typedef struct {
+   double eig_val;          /* Lanczos eigenvalue (the reference reports this one) */
+   double error;            /* L1 residual after inverse iteration                 */
+   int lanczos_steps;       /* total Lanczos steps                                 */
+   int ii_steps;            /* outer inverse-iteration steps                       */
+   int cg_steps;            /* inner CG / MINRES iterations, summed                */
+   int spmv_count;          /* operator applications                               */
+   int converged;           /* Lanczos converged                                   */
+   int ii_converged;        /* inverse iteration met ii_acc                        */
+   int dense;               /* 1 when the n < dense_below path ran                 */
+   double ms_lanczos, ms_ii;/* device-timed phases                                 */
+} dg_solve_info;
+
+/* Lanczos only.  guess: start vector (NULL = seeded pseudo-random).  eigvec: n doubles.
+ * guess/eigvec may be host or device pointers. */
+int dg_lanczos(dg_matrix *m, const dg_solver_params *p, const double *guess, double *eigvec, dg_solve_info *info);
+/* Inverse iteration on (M - E) from eigvec (in/out). */
+int dg_inverse_iteration(dg_matrix *m, const dg_solver_params *p, double eig_val, double *eigvec, dg_solve_info *info);
+/* Lanczos + inverse iteration (the DMRG_DIAGONALIZE_SUPERBLOCK body). */
+int dg_ground_state(dg_matrix *m, const dg_solver_params *p, const double *guess, double *eigvec, dg_solve_info *info);
+/* CG on (M + sigma I) x = b from x (in/out; normalised first, as the reference does).
+ * minres = 1 runs MINRES instead (x not normalised, as the reference's MINIMUM_RESIDUAL). */
+int dg_linear_solve(dg_matrix *m, double sigma, const double *b, double *x, double acc, int max_step, int minres, int *iters);
+/* sum_i |(M x)_i - lambda x_i|. */
+int dg_residual_l1(dg_matrix *m, const double *x, double lambda, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMRG_GB300_H */

@@ -1,0 +1,60 @@
+/*
+ * dmrg_gb300_ed.h -- data-driven description of an exact-diagonalisation Hamiltonian.
+ *
+ * The reference builds ED Hamiltonians row by row in a model-specific MAKE_ELEMENT_HAM
+ * (main/exact_diag/klm_vf/src/MAKE_ELEMENT_HAM.c:11-76) out of two primitives:
+ *   EXACT_MAKE_ELEM_ON    (exact/EXACT_MAKE_ELEM_ON.c:7-31):    coef * O[site]
+ *   EXACT_MAKE_ELEM_INTER (exact/EXACT_MAKE_ELEM_INTER.c:6-36): sign * coef * O1[site1] O2[site2]
+ * applied in a fixed order, duplicates merged by summation in generation order, and a
+ * zero-valued diagonal added last.  A dg_ed_model lists the same primitives as data, in the
+ * same order, so one description drives both the GPU build and the CPU oracle.
+ */
+#ifndef DMRG_GB300_ED_H
+#define DMRG_GB300_ED_H
+
+#include "dmrg_gb300_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+   DG_ED_ONSITE = 0,    /* coef * ops[op1] acting on site1                         */
+   DG_ED_INTER = 1      /* sign * coef * ops[op1] on site1 times ops[op2] on site2  */
+};
+
+enum {
+   DG_ED_SIGN_NONE = 0,       /* sign = +1                                                    */
+   DG_ED_SIGN_SITE1 = 1,      /* sign = +1 if n_ele(site1) is odd else -1 (MAKE_ELEMENT_HAM.c:239-245) */
+   DG_ED_SIGN_SITE1_NEG = 2,  /* the opposite sign                                            */
+   DG_ED_SIGN_RANGE = 3,      /* as SITE1 with n_ele summed over sites [0, site2) (PBC bond, :257-266) */
+   DG_ED_SIGN_RANGE_NEG = 4
+};
+
+typedef struct {
+   int kind;
+   int site1, site2;
+   int op1, op2;
+   double coef;
+   int sign_mode;
+} dg_ed_term;
+
+typedef struct {
+   int n_sites;            /* L                                                   */
+   int dim_onsite;         /* d; basis codes are base-d integers, site 0 = lowest digit */
+   const int *qn1;         /* [d] first conserved quantity per local state (e.g. electrons) */
+   const int *qn2;         /* [d] second conserved quantity (e.g. 2 Sz)            */
+   int use_qn1, use_qn2;   /* which constraints apply                               */
+   int target_qn1, target_qn2;
+   int n_ops;
+   const CRS1 *ops;        /* [n_ops] d x d site operators                         */
+   int n_terms;
+   const dg_ed_term *terms;
+   const int *n_ele;       /* [d] electrons per local state (fermion signs), may be NULL */
+} dg_ed_model;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMRG_GB300_ED_H */

@@ -1,0 +1,418 @@
+"""ctypes front end of the checker libraries.
+
+TEST INFRASTRUCTURE ONLY (imported by tests/, __graft_entry__.smoke() and the CPU-baseline
+leg of bench.py).  Two libraries:
+
+* ``liboracle.so``: the project's CPU restatement of the hot path (oracle.c);
+* ``_ref/libdmrg_ref.so``: the reference's own C sources compiled where they lie (only
+  where the reference tree is present; see the Makefile).  Its functions print progress
+  and append to ./SML_out/, so calls into it run inside a scratch working directory.
+"""
+from __future__ import annotations
+
+import contextlib
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+from dmrg_c_gb300 import abi
+from dmrg_c_gb300.abi import (BOX_CG, BOX_II, BOX_LAN, CRS1, DMRG_BASIS, EXACT_BASIS_INFO, MODEL_1DKLM_VF, dg_ed_model, ptr)
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libdmrg_ref.so"
+REF_SRC = Path(os.environ.get("DMRG_REF", "/root/reference"))
+
+P = C.POINTER
+dp, ip, lp = P(C.c_double), P(C.c_int), P(C.c_long)
+
+
+class or_lanczos_cfg(C.Structure):
+    _fields_ = [("acc", C.c_double), ("min_step", C.c_int), ("max_step", C.c_int), ("max_block_step", C.c_int),
+                ("tight", C.c_int), ("slow", C.c_int), ("guess", C.c_int), ("seed", C.c_ulonglong),
+                ("dense_below", C.c_int), ("threads", C.c_int)]
+
+
+class or_lanczos_out(C.Structure):
+    _fields_ = [("eig_val", C.c_double), ("steps", C.c_int), ("converged", C.c_int), ("dense", C.c_int),
+                ("spmv", C.c_int)]
+
+
+class or_ii_cfg(C.Structure):
+    _fields_ = [("ii_acc", C.c_double), ("ii_diag_add", C.c_double), ("ii_max_step", C.c_int), ("cg_acc", C.c_double),
+                ("cg_max_step", C.c_int), ("minres", C.c_int), ("threads", C.c_int)]
+
+
+class or_ii_out(C.Structure):
+    _fields_ = [("error", C.c_double), ("iters", C.c_int), ("cg_total", C.c_int), ("converged", C.c_int),
+                ("spmv", C.c_int)]
+
+
+class or_obc(C.Structure):
+    _fields_ = [("M_LLLR", P(CRS1)), ("M_LRRL", P(CRS1)), ("M_LRRL_Sign", P(CRS1)), ("M_RRRL", P(CRS1)),
+                ("Ele_RR", ip), ("Basis", P(DMRG_BASIS))]
+
+
+_lib = None
+_ref = None
+
+
+def build_oracle() -> None:
+    subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists() or LIB.stat().st_mtime < (HERE / "oracle.c").stat().st_mtime:
+            build_oracle()
+        lib = C.CDLL(str(LIB))
+        sig = {
+            "or_spmv": (C.c_int, [P(CRS1), C.c_int, dp, dp, C.c_int]),
+            "or_tridiag_eig": (C.c_int, [dp, dp, C.c_int, dp, dp]),
+            "or_dense_lowest": (C.c_int, [dp, C.c_int, dp, dp]),
+            "or_lanczos": (C.c_int, [P(CRS1), C.c_int, P(or_lanczos_cfg), dp, P(or_lanczos_out)]),
+            "or_inverse_iteration": (C.c_int, [P(CRS1), C.c_int, P(or_ii_cfg), C.c_double, dp, P(or_ii_out)]),
+            "or_cg": (C.c_int, [P(CRS1), C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, C.c_int, ip, ip]),
+            "or_minres": (C.c_int, [P(CRS1), C.c_int, C.c_double, dp, dp, C.c_double, C.c_int, C.c_int, ip, ip]),
+            "or_converge_check": (C.c_double, [P(CRS1), C.c_int, dp, C.c_double, C.c_int]),
+            "or_obc_spmv": (C.c_int, [P(or_obc), dp, dp, C.c_int]),
+            "or_obc_lanczos_slow": (C.c_int, [P(or_obc), P(or_lanczos_cfg), dp, P(or_lanczos_out)]),
+            "or_obc_inverse_iteration": (C.c_int, [P(or_obc), P(or_ii_cfg), C.c_double, dp, P(or_ii_out)]),
+            "or_obc_cg": (C.c_int, [P(or_obc), C.c_double, dp, dp, C.c_double, C.c_int, C.c_int, ip, ip]),
+            "or_ed_dim": (C.c_long, [P(dg_ed_model), C.c_int]),
+            "or_ed_basis": (C.c_int, [P(dg_ed_model), lp, C.c_long, C.c_int]),
+            "or_ed_count": (C.c_int, [P(dg_ed_model), lp, C.c_long, lp, C.c_int]),
+            "or_ed_fill": (C.c_int, [P(dg_ed_model), lp, C.c_long, lp, ip, dp, C.c_int]),
+            "or_site_apply": (C.c_int, [P(CRS1), lp, C.c_long, lp, C.c_long, C.c_int, C.c_int, ip, dp, dp, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype, f.argtypes = res, args
+        _lib = lib
+    return _lib
+
+
+def threads_default() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+# ---------------------------------------------------------------------------------------
+# oracle (restatement)
+# ---------------------------------------------------------------------------------------
+def spmv(crs: abi.Crs, x: np.ndarray, sym: bool, threads: int | None = None) -> np.ndarray:
+    y = np.empty(crs.n)
+    x = np.ascontiguousarray(x, np.float64)
+    assert load().or_spmv(crs.ref, int(sym), ptr(x, C.c_double), ptr(y, C.c_double), threads or threads_default()) == 0
+    return y
+
+
+def tridiag_eig(d, e, vectors=True):
+    d = np.ascontiguousarray(d, np.float64)
+    e = np.ascontiguousarray(e, np.float64)
+    n = len(d)
+    w = np.empty(n)
+    z = np.empty(n * n) if vectors else None
+    rc = load().or_tridiag_eig(ptr(d, C.c_double), ptr(e, C.c_double), n, ptr(w, C.c_double),
+                               ptr(z, C.c_double) if vectors else None)
+    assert rc == 0
+    return (w, z.reshape(n, n).T) if vectors else w     # columns = eigenvectors
+
+
+def lanczos(crs: abi.Crs, sym: bool, guess=None, acc=1e-14, min_step=1, max_step=800, max_block_step=None, tight=False,
+            slow=False, seed=0, dense_below=1000, threads=None):
+    cfg = or_lanczos_cfg(acc=acc, min_step=min_step, max_step=max_step,
+                         max_block_step=max_step if max_block_step is None else max_block_step, tight=int(tight),
+                         slow=int(slow), guess=int(guess is not None), seed=seed, dense_below=dense_below,
+                         threads=threads or threads_default())
+    v = np.array(guess, dtype=np.float64) if guess is not None else np.zeros(crs.n)
+    out = or_lanczos_out()
+    rc = load().or_lanczos(crs.ref, int(sym), C.byref(cfg), ptr(v, C.c_double), C.byref(out))
+    return rc, out, v
+
+
+def inverse_iteration(crs, sym, eig_val, vec, ii_acc=1e-9, ii_diag_add=1e-11, ii_max_step=3, cg_acc=1e-7,
+                      cg_max_step=1000, minres=False, threads=None):
+    cfg = or_ii_cfg(ii_acc=ii_acc, ii_diag_add=ii_diag_add, ii_max_step=ii_max_step, cg_acc=cg_acc,
+                    cg_max_step=cg_max_step, minres=int(minres), threads=threads or threads_default())
+    v = np.array(vec, dtype=np.float64)
+    out = or_ii_out()
+    rc = load().or_inverse_iteration(crs.ref, int(sym), C.byref(cfg), eig_val, ptr(v, C.c_double), C.byref(out))
+    return rc, out, v
+
+
+def linear_solve(crs, sym, b, x0, sigma=0.0, acc=1e-7, max_step=1000, minres=False, threads=None):
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    it, cv = C.c_int(), C.c_int()
+    f = load().or_minres if minres else load().or_cg
+    rc = f(crs.ref, int(sym), sigma, ptr(b, C.c_double), ptr(x, C.c_double), acc, max_step,
+           threads or threads_default(), C.byref(it), C.byref(cv))
+    return rc, it.value, bool(cv.value), x
+
+
+def converge_check(crs, sym, x, lam, threads=None) -> float:
+    x = np.ascontiguousarray(x, np.float64)
+    return load().or_converge_check(crs.ref, int(sym), ptr(x, C.c_double), lam, threads or threads_default())
+
+
+def ed_build(model, threads=None):
+    """Basis and full CRS (row, col, val) of an ED model (see dmrg_c_gb300.ed_models)."""
+    th = threads or threads_default()
+    lib = load()
+    m = C.byref(model.struct)
+    dim = lib.or_ed_dim(m, th)
+    basis = np.empty(dim, np.int64)
+    assert lib.or_ed_basis(m, ptr(basis, C.c_long), dim, th) == 0
+    row = np.zeros(dim + 1, np.int64)
+    assert lib.or_ed_count(m, ptr(basis, C.c_long), dim, ptr(row, C.c_long), th) == 0
+    col = np.empty(max(row[-1], 1), np.int32)
+    val = np.empty(max(row[-1], 1), np.float64)
+    assert lib.or_ed_fill(m, ptr(basis, C.c_long), dim, ptr(row, C.c_long), ptr(col, C.c_int), ptr(val, C.c_double),
+                          th) == 0
+    return basis, row, col[:row[-1]], val[:row[-1]]
+
+
+def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
+    out_basis = np.ascontiguousarray(out_basis, np.int64)
+    in_basis = np.ascontiguousarray(in_basis, np.int64)
+    vec = np.ascontiguousarray(vec, np.float64)
+    out = np.empty(len(out_basis))
+    ne = np.ascontiguousarray(n_ele, np.int32) if n_ele is not None else None
+    rc = load().or_site_apply(op.ref, ptr(out_basis, C.c_long), len(out_basis), ptr(in_basis, C.c_long), len(in_basis), d,
+                              site, ptr(ne, C.c_int) if ne is not None else None, ptr(vec, C.c_double),
+                              ptr(out, C.c_double), threads or threads_default())
+    assert rc == 0
+    return out
+
+
+def obc_struct(sb):
+    """or_obc view of a superblock operator built by dmrg_c_gb300.superblock."""
+    return or_obc(M_LLLR=sb.M_LLLR.ref, M_LRRL=sb.M_LRRL.ref, M_LRRL_Sign=sb.M_LRRL_Sign.ref, M_RRRL=sb.M_RRRL.ref,
+                  Ele_RR=ptr(sb.ele_rr, C.c_int), Basis=C.pointer(sb.basis))
+
+
+def obc_spmv(sb, x, threads=None):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.empty(sb.n)
+    o = obc_struct(sb)
+    assert load().or_obc_spmv(C.byref(o), ptr(x, C.c_double), ptr(y, C.c_double), threads or threads_default()) == 0
+    return y
+
+
+def obc_lanczos_slow(sb, guess=None, acc=1e-14, min_step=1, max_step=800, tight=False, seed=0, threads=None):
+    cfg = or_lanczos_cfg(acc=acc, min_step=min_step, max_step=max_step, max_block_step=max_step, tight=int(tight),
+                         slow=1, guess=int(guess is not None), seed=seed, dense_below=0,
+                         threads=threads or threads_default())
+    v = np.array(guess, dtype=np.float64) if guess is not None else np.zeros(sb.n)
+    out = or_lanczos_out()
+    o = obc_struct(sb)
+    rc = load().or_obc_lanczos_slow(C.byref(o), C.byref(cfg), ptr(v, C.c_double), C.byref(out))
+    return rc, out, v
+
+
+def obc_inverse_iteration(sb, eig_val, vec, ii_acc=1e-9, ii_diag_add=1e-11, ii_max_step=3, cg_acc=1e-7, cg_max_step=1000,
+                          threads=None):
+    cfg = or_ii_cfg(ii_acc=ii_acc, ii_diag_add=ii_diag_add, ii_max_step=ii_max_step, cg_acc=cg_acc,
+                    cg_max_step=cg_max_step, minres=0, threads=threads or threads_default())
+    v = np.array(vec, dtype=np.float64)
+    out = or_ii_out()
+    o = obc_struct(sb)
+    rc = load().or_obc_inverse_iteration(C.byref(o), C.byref(cfg), eig_val, ptr(v, C.c_double), C.byref(out))
+    return rc, out, v
+
+
+# ---------------------------------------------------------------------------------------
+# reference build (oracle/_ref), available only where the reference tree exists
+# ---------------------------------------------------------------------------------------
+def ref_available() -> bool:
+    return REF_LIB.exists() or (REF_SRC / "sml" / "LANCZOS_SYM.c").exists()
+
+
+def load_ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+        _ref = C.CDLL(str(REF_LIB))
+    return _ref
+
+
+@contextlib.contextmanager
+def scratch_cwd():
+    old = os.getcwd()
+    with tempfile.TemporaryDirectory(prefix="dmrg_ref_") as d:
+        os.chdir(d)
+        try:
+            yield Path(d)
+        finally:
+            os.chdir(old)
+
+
+def ref_spmv(crs: abi.Crs, x, sym: bool, threads: int = 1):
+    lib = load_ref()
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros(crs.n)
+    if sym:
+        temp = [np.zeros(crs.n) for _ in range(threads)]
+        arr = (dp * threads)(*[ptr(t, C.c_double) for t in temp])
+        lib.MATRIX_VECTOR_PRODUCT_SYM(crs.ref, ptr(x, C.c_double), ptr(y, C.c_double), arr, threads)
+    else:
+        lib.MATRIX_VECTOR_PRODUCT(crs.ref, ptr(x, C.c_double), ptr(y, C.c_double), threads)
+    return y
+
+
+def _box_lan(crs, vec, val, acc, min_step, max_step, max_block_step, guess, typ, threads):
+    return BOX_LAN(M=crs.ref, Eig_Vec=ptr(vec, C.c_double), eig_val=ptr(val, C.c_double), acc=acc, min_step=min_step,
+                   max_step=max_step, max_block_step=max_block_step, p_threads=threads, Guess=guess.encode(),
+                   Type=typ.encode())
+
+
+def ref_lanczos(crs, sym, guess, slow=False, acc=1e-14, min_step=1, max_step=800, max_block_step=None, tight=False,
+                threads=1):
+    """Run the reference LANCZOS[_SLOW][_SYM] with Guess "Yes"; returns (eig_val, vec, steps)."""
+    lib = load_ref()
+    vec = np.array(guess, dtype=np.float64)
+    val = np.zeros(1)
+    box = _box_lan(crs, vec, val, acc, min_step, max_step, max_step if max_block_step is None else max_block_step,
+                   "Yes", "Tight" if tight else "Normal", threads)
+    name = ("LANCZOS_SLOW" if slow else "LANCZOS") + ("_SYM" if sym else "")
+    with scratch_cwd() as d:
+        getattr(lib, name)(C.byref(box))
+        steps = None
+        for f in d.glob("SML_out/LANCZOS*"):
+            line = f.read_text().strip().splitlines()[-1]
+            steps = int(line.split()[0])
+    return float(val[0]), vec, steps
+
+
+def ref_inverse_iteration(crs, sym, eig_val, vec, ii_acc=1e-9, ii_diag_add=1e-11, ii_max_step=3, cg_acc=1e-7,
+                          cg_max_step=1000, typ="CG", threads=1):
+    lib = load_ref()
+    v = np.array(vec, dtype=np.float64)
+    ev = np.array([eig_val])
+    box = BOX_II(M=crs.ref, ii_acc=ii_acc, ii_diag_add=ii_diag_add, ii_max_step=ii_max_step, cg_acc=cg_acc,
+                 cg_max_step=cg_max_step, error=0.0, Eig_Vec=ptr(v, C.c_double), Eig_Val=ptr(ev, C.c_double),
+                 p_threads=threads, Type=typ.encode())
+    with scratch_cwd() as d:
+        getattr(lib, "INVERSE_ITERATION_SYM" if sym else "INVERSE_ITERATION")(C.byref(box))
+        f = d / "SML_out" / "Inv_iter_step.txt"
+        iters = int(f.read_text().split()[-1]) if f.exists() else None
+    return box.error, v, iters
+
+
+def ref_linear_solve(crs, sym, b, x0, acc=1e-7, max_step=1000, minres=False, threads=1):
+    lib = load_ref()
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    box = BOX_CG(M=crs.ref, acc=acc, Vec=ptr(b, C.c_double), Out_Vec=ptr(x, C.c_double), max_step=max_step,
+                 p_threads=threads)
+    name = ("MINIMUM_RESIDUAL" if minres else "CONJUGATE_GRADIENT") + ("_SYM" if sym else "")
+    with scratch_cwd() as d:
+        getattr(lib, name)(C.byref(box))
+        files = list(d.glob("SML_out/*_Step.txt"))
+        iters = int(files[0].read_text().split()[-1]) if files else None
+    return x, iters
+
+
+def ref_converge_check(crs, sym, x, lam, threads=1):
+    lib = load_ref()
+    f = lib.CONVERGE_CHECK_SYM if sym else lib.CONVERGE_CHECK
+    f.restype = C.c_double
+    x = np.ascontiguousarray(x, np.float64)
+    return f(crs.ref, ptr(x, C.c_double), C.c_double(lam), threads)
+
+
+def ref_tridiag(d, e):
+    """The reference's LAPACK dstev_ (through the shim) on (d, e): (w, z columns)."""
+    lib = load_ref()
+    n = len(d)
+    D = np.array(d, dtype=np.float64)
+    E = np.zeros(max(n, 1))
+    E[:n - 1] = e
+    Z = np.zeros(n * n)
+    W = np.zeros(2 * n)
+    info = C.c_int()
+    nn, ldz = C.c_int(n), C.c_int(n)
+    lib.dstev_(C.c_char_p(b"V"), C.byref(nn), ptr(D, C.c_double), ptr(E, C.c_double), ptr(Z, C.c_double), C.byref(ldz),
+               ptr(W, C.c_double), C.byref(info))
+    return D, Z.reshape(n, n).T
+
+
+def ref_klm_model(L, n_ele, tot_sz, t=-1.0, J=1.0, D_z=0.0, I_xy=0.0, I_z=0.0, h_z=0.0, mu=0.0, spin_loc=1, bc="OBC"):
+    m = MODEL_1DKLM_VF()
+    m.BC = bc.encode()
+    m.p_threads = 1
+    m.spin_loc = spin_loc
+    m.tot_site = L
+    m.tot_sz = tot_sz
+    m.tot_ele = n_ele
+    m.dim_charge = 4
+    m.dim_lspin = spin_loc + 1
+    m.dim_onsite = 4 * (spin_loc + 1)
+    m.t, m.J, m.D_z, m.I_xy, m.I_z, m.h_z, m.mu = t, J, D_z, I_xy, I_z, h_z, mu
+    return m
+
+
+def ref_klm_ed(model: MODEL_1DKLM_VF, est_max_row=10000):
+    """The reference's own FIND_DIM / GET_BASIS / GET_HAM for the 1D KLM."""
+    from dmrg_c_gb300.abi import EXACT_PARAMETER, EXACT_TIME
+    lib = load_ref()
+    lib.FIND_DIM.restype = C.c_int
+    lib.GET_BASIS.restype = lp
+    lib.GET_HAM.restype = P(CRS1)
+    tm = EXACT_TIME()
+    dim = lib.FIND_DIM(C.byref(model), C.byref(tm))
+    bptr = lib.GET_BASIS(C.byref(model), C.byref(tm), dim)
+    basis = np.ctypeslib.as_array(bptr, shape=(dim,)).copy()
+    info = EXACT_BASIS_INFO(dim=dim, Basis=bptr, tot_sz=model.tot_sz, tot_ele=model.tot_ele, tot_parity=0)
+    par = EXACT_PARAMETER()
+    par.est_max_row_elem_num = est_max_row
+    with scratch_cwd():
+        H = lib.GET_HAM(C.byref(model), C.byref(info), C.byref(par), C.byref(tm)).contents
+    row = np.ctypeslib.as_array(H.Row, shape=(dim + 1,)).copy()
+    nnz = int(row[-1])
+    col = np.ctypeslib.as_array(H.Col, shape=(nnz,)).copy()
+    val = np.ctypeslib.as_array(H.Val, shape=(nnz,)).copy()
+    return basis, row, col, val
+
+
+def ref_klm_site_ops(model: MODEL_1DKLM_VF):
+    """The reference's KLM site operators (Ham_On, SpL, SmL, SzL, CUp, CUp_D, CDown, CDown_D, Zero)."""
+    lib = load_ref()
+    d = model.dim_onsite
+    out = []
+    for which in range(9):
+        row = np.zeros(d + 1, np.int64)
+        col = np.zeros(d * d, np.int32)
+        val = np.zeros(d * d)
+        nnz = lib.ref_klm_site_op(C.byref(model), which, ptr(row, C.c_long), ptr(col, C.c_int), ptr(val, C.c_double))
+        out.append((row, col[:nnz].copy(), val[:nnz].copy()))
+    return out
+
+
+def ref_site_apply(op: abi.Crs, basis, d, site, vec):
+    lib = load_ref()
+    basis = np.ascontiguousarray(basis, np.int64)
+    # The reference's binary search may read one element past the table (its end bound is
+    # inclusive, exact/EXACT_V_M_Q0.c:29): pad with a sentinel no code can equal.
+    padded = np.concatenate([basis, [np.iinfo(np.int64).max]])
+    vec = np.ascontiguousarray(vec, np.float64)
+    out = np.zeros(len(basis))
+    info = EXACT_BASIS_INFO(dim=len(basis), Basis=ptr(padded, C.c_long), tot_sz=0, tot_ele=0, tot_parity=0)
+    lib.EXACT_V_M_Q0(op.ref, ptr(vec, C.c_double), ptr(out, C.c_double), d, site, 1, C.byref(info))
+    return out
+
+
+def ref_obc_spmv(sb, x, threads=1):
+    lib = load_ref()
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros(sb.n)
+    lib.DMRG_MATRIX_VECTOR_PRODUCT_OBC(sb.M_LLLR.ref, sb.M_LRRL.ref, sb.M_LRRL_Sign.ref, sb.M_RRRL.ref,
+                                       ptr(x, C.c_double), ptr(y, C.c_double), ptr(sb.ele_rr, C.c_int), threads,
+                                       C.byref(sb.basis))
+    return y

@@ -1,0 +1,175 @@
+"""Regenerate the golden fixtures in this folder from the reference implementation.
+
+Runs the reference's own C code (compiled from the dmrg_C sources into oracle/_ref by
+oracle/Makefile) on seeded inputs and stores inputs and outputs as compressed .npz files.
+Needs the reference source tree (env DMRG_REF, default /root/reference); the fixtures are
+committed so that tests on machines without it still check against the reference.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import scipy.sparse as sp
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+import pyoracle as po  # noqa: E402
+
+from dmrg_c_gb300 import abi, ed_models, superblock  # noqa: E402
+
+
+def quiet():
+    """Silence the reference's progress output on fd 1 while it runs."""
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    saved = os.dup(1)
+    os.dup2(devnull, 1)
+    return saved
+
+
+def loud(saved):
+    os.dup2(saved, 1)
+
+
+def random_sym(n, density, seed, diag_scale=1.0):
+    rng = np.random.default_rng(seed)
+    A = sp.random(n, n, density=density, random_state=seed, data_rvs=rng.standard_normal)
+    A = (A + A.T).tocsr()
+    A.setdiag(rng.standard_normal(n) * diag_scale)
+    A.eliminate_zeros()
+    return A.tocsr()
+
+
+def sml_fixture():
+    """SpMV / Lanczos / inverse iteration / CG / MINRES on a random symmetric matrix."""
+    A = random_sym(1500, 0.008, seed=11)
+    low = abi.lower_diag_last(A)
+    full = abi.Crs.from_scipy(A)
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal(A.shape[0])
+    guess = rng.standard_normal(A.shape[0])
+    out = dict(low_row=low.row, low_col=low.col[:low.nnz], low_val=low.val[:low.nnz], full_row=full.row,
+               full_col=full.col[:full.nnz], full_val=full.val[:full.nnz], x=x, guess=guess)
+    s = quiet()
+    try:
+        out["spmv_sym"] = po.ref_spmv(low, x, True, 1)
+        out["spmv_full"] = po.ref_spmv(full, x, False, 1)
+        for name, sym, slow in (("lanczos_sym", True, False), ("lanczos_slow_sym", True, True), ("lanczos", False, False),
+                                ("lanczos_slow", False, True)):
+            E, v, steps = po.ref_lanczos(low if sym else full, sym, guess, slow=slow)
+            out[name + "_E"], out[name + "_vec"], out[name + "_steps"] = E, v, steps
+        E, v = out["lanczos_sym_E"], out["lanczos_sym_vec"]
+        err, vv, it = po.ref_inverse_iteration(low, True, E, v)
+        out["ii_sym_err"], out["ii_sym_vec"], out["ii_sym_iters"] = err, vv, it
+        err, vv, it = po.ref_inverse_iteration(full, False, E, v)
+        out["ii_err"], out["ii_vec"], out["ii_iters"] = err, vv, it
+        # CG / MINRES on a positive definite shift of A
+        B = (A + sp.identity(A.shape[0]) * (abs(E) + 1.0)).tocsr()
+        lowB = abi.lower_diag_last(B)
+        b = rng.standard_normal(A.shape[0])
+        x0 = rng.standard_normal(A.shape[0])
+        out.update(B_row=lowB.row, B_col=lowB.col[:lowB.nnz], B_val=lowB.val[:lowB.nnz], b=b, x0=x0)
+        xs, it = po.ref_linear_solve(lowB, True, b, x0, acc=1e-10, max_step=1000)
+        out["cg_x"], out["cg_iters"] = xs, it
+        xs, it = po.ref_linear_solve(lowB, True, b, x0, acc=1e-6, max_step=1000, minres=True)
+        out["mr_x"], out["mr_iters"] = xs, it
+        out["conv_sym"] = po.ref_converge_check(low, True, out["lanczos_sym_vec"], E)
+        out["conv_full"] = po.ref_converge_check(full, False, out["lanczos_sym_vec"], E)
+    finally:
+        loud(s)
+    np.savez_compressed(HERE / "sml_random1500.npz", **out)
+
+
+def tridiag_fixture():
+    rng = np.random.default_rng(21)
+    d = rng.standard_normal(120)
+    e = np.abs(rng.standard_normal(119))
+    w, z = po.ref_tridiag(d, e)
+    np.savez_compressed(HERE / "tridiag120.npz", d=d, e=e, w=w, z0=z[:, 0])
+
+
+def klm_ed_fixture():
+    """The reference's own KLM ED basis and CRS (FIND_DIM / GET_BASIS / GET_HAM) and site
+    operator tables, for two small chains."""
+    out = {}
+    for tag, (L, ne, sz, bc, kw) in {
+        "obc": (4, 4, 0, "OBC", dict(t=-1.0, J=1.5, D_z=-1.0, I_z=-1.0, I_xy=0.0, h_z=0.1)),
+        "pbc": (4, 3, 1, "PBC", dict(t=-1.0, J=1.0, D_z=0.0, I_z=0.5, I_xy=0.3, h_z=0.0, mu=0.2)),
+    }.items():
+        m = po.ref_klm_model(L, ne, sz, bc=bc, **kw)
+        basis, row, col, val = po.ref_klm_ed(m)
+        tabs = po.ref_klm_site_ops(m)
+        out[f"{tag}_params"] = np.array([L, ne, sz, kw["t"], kw.get("I_z", 0.0), kw.get("I_xy", 0.0)])
+        out[f"{tag}_basis"], out[f"{tag}_row"], out[f"{tag}_col"], out[f"{tag}_val"] = basis, row, col, val
+        for k, (r, c, v) in enumerate(tabs):
+            out[f"{tag}_op{k}_row"], out[f"{tag}_op{k}_col"], out[f"{tag}_op{k}_val"] = r, c, v
+    np.savez_compressed(HERE / "klm_ed.npz", **out)
+
+
+def vm_fixture():
+    """EXACT_V_M_Q0 on a Hubbard basis with the reference's C^dagger_up site operator."""
+    model = ed_models.hubbard_chain(6, t=-1.0, U=2.0, n_ele=6, twoSz=0)
+    basis, row, col, val = po.ed_build(model)
+    rng = np.random.default_rng(31)
+    vec = rng.standard_normal(len(basis))
+    op = model.ops[1]
+    out = dict(basis=basis, vec=vec, op_row=op.row, op_col=op.col[:op.nnz], op_val=op.val[:op.nnz])
+    for site in (0, 2, 5):
+        out[f"out_site{site}"] = po.ref_site_apply(op, basis, 4, site, vec)
+    np.savez_compressed(HERE / "vm_hubbard6.npz", **out)
+
+
+def obc_fixture():
+    """The reference's matrix-free superblock product and OBC Lanczos on a seeded
+    synthetic superblock (spin-1/2 sites, one block quantum number)."""
+    qb = superblock.spin_block_labels(40, 9, seed=41)
+    sb = superblock.synthetic_superblock(40, 2, qb, [1, -1], 0, nnz_lllr=6, nnz_lrrl=2, seed=42, with_sign=True)
+    rng = np.random.default_rng(43)
+    x = rng.standard_normal(sb.n)
+    s = quiet()
+    try:
+        y = po.ref_obc_spmv(sb, x)
+    finally:
+        loud(s)
+    out = dict(x=x, y=y, n=sb.n)
+    np.savez_compressed(HERE / "obc_synthetic.npz", **out)
+
+
+def xxz_energy_fixture():
+    """Reference LANCZOS + INVERSE_ITERATION on the XXZ L=16 Heisenberg chain (Sz=0)."""
+    model = ed_models.xxz_chain(16, Jxy=1.0, Jz=1.0)
+    basis, row, col, val = po.ed_build(model)
+    H = abi.Crs(row, col, val)
+    guess = np.random.default_rng(51).standard_normal(len(basis))
+    s = quiet()
+    try:
+        E, v, steps = po.ref_lanczos(H, False, guess)
+        err, vv, it = po.ref_inverse_iteration(H, False, E, v)
+    finally:
+        loud(s)
+    np.savez_compressed(HERE / "xxz16.npz", E=E, steps=steps, guess=guess, ii_err=err, dim=len(basis), nnz=row[-1])
+
+
+def main():
+    if not po.ref_available():
+        raise SystemExit("reference sources not found (set DMRG_REF)")
+    po.load_ref()
+    sml_fixture()
+    tridiag_fixture()
+    klm_ed_fixture()
+    vm_fixture()
+    obc_fixture()
+    xxz_energy_fixture()
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,184 @@
+"""The oracle (CPU restatement) pinned against the reference: golden fixtures produced by
+the reference's own code (always), the live reference build (where its sources exist),
+and closed-form answers."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import golden
+from dmrg_c_gb300 import abi, ed_models, superblock
+
+
+def sml_inputs():
+    g = golden("sml_random1500.npz")
+    low = abi.Crs(g["low_row"], g["low_col"], g["low_val"])
+    full = abi.Crs(g["full_row"], g["full_col"], g["full_val"])
+    return g, low, full
+
+
+# ---- golden fixtures (reference outputs) ---------------------------------------------------
+
+def test_spmv_matches_reference_golden(oracle):
+    g, low, full = sml_inputs()
+    np.testing.assert_allclose(oracle.spmv(low, g["x"], True), g["spmv_sym"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(oracle.spmv(full, g["x"], False), g["spmv_full"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name,sym,slow", [("lanczos_sym", True, False), ("lanczos_slow_sym", True, True),
+                                           ("lanczos", False, False), ("lanczos_slow", False, True)])
+def test_lanczos_matches_reference_golden(oracle, name, sym, slow):
+    g, low, full = sml_inputs()
+    rc, out, v = oracle.lanczos(low if sym else full, sym, guess=g["guess"], slow=slow)
+    assert rc == 0 and out.converged
+    E = float(g[name + "_E"])
+    assert abs(out.eig_val - E) <= 1e-12 * abs(E)
+    assert abs(out.steps - int(g[name + "_steps"])) <= 2
+    assert abs(abs(v @ g[name + "_vec"]) - 1) < 1e-9
+
+
+def test_inverse_iteration_matches_reference_golden(oracle):
+    g, low, full = sml_inputs()
+    for sym, tag in ((True, "ii_sym"), (False, "ii")):
+        rc, out, v = oracle.inverse_iteration(low if sym else full, sym, float(g["lanczos_sym_E"]), g["lanczos_sym_vec"])
+        assert out.converged and out.iters == int(g[tag + "_iters"])
+        assert out.error < 1e-9
+        assert abs(abs(v @ g[tag + "_vec"]) - 1) < 1e-12
+
+
+def test_cg_minres_match_reference_golden(oracle):
+    g = golden("sml_random1500.npz")
+    B = abi.Crs(g["B_row"], g["B_col"], g["B_val"])
+    rc, it, cv, x = oracle.linear_solve(B, True, g["b"], g["x0"], acc=1e-10, max_step=1000)
+    assert cv and abs(it - int(g["cg_iters"])) <= 1
+    np.testing.assert_allclose(x, g["cg_x"], rtol=0, atol=1e-8)
+    rc, it, cv, x = oracle.linear_solve(B, True, g["b"], g["x0"], acc=1e-6, max_step=1000, minres=True)
+    assert cv and abs(it - int(g["mr_iters"])) <= 1
+    np.testing.assert_allclose(x, g["mr_x"], rtol=0, atol=1e-6)
+
+
+def test_converge_check_golden(oracle):
+    g, low, full = sml_inputs()
+    E = float(g["lanczos_sym_E"])
+    assert oracle.converge_check(low, True, g["lanczos_sym_vec"], E) == pytest.approx(float(g["conv_sym"]), rel=1e-6)
+    assert oracle.converge_check(full, False, g["lanczos_sym_vec"], E) == pytest.approx(float(g["conv_full"]), rel=1e-6)
+
+
+def test_tridiag_matches_dstev_golden(oracle):
+    g = golden("tridiag120.npz")
+    w, z = oracle.tridiag_eig(g["d"], g["e"])
+    np.testing.assert_allclose(w, g["w"], rtol=0, atol=1e-12)
+    assert abs(abs(z[:, 0] @ g["z0"]) - 1) < 1e-12
+
+
+def klm_model_from_golden(g, tag):
+    L, ne, sz, t, I_z, I_xy = g[f"{tag}_params"]
+    tabs = [(g[f"{tag}_op{k}_row"], g[f"{tag}_op{k}_col"], g[f"{tag}_op{k}_val"]) for k in range(9)]
+    return ed_models.klm_chain_from_tables(int(L), tabs, int(ne), int(sz), t=float(t), I_z=float(I_z), I_xy=float(I_xy),
+                                           bc="PBC" if tag == "pbc" else "OBC")
+
+
+@pytest.mark.parametrize("tag", ["obc", "pbc"])
+def test_ed_build_bit_exact_vs_reference_golden(oracle, tag):
+    """Basis table and CRS arrays (row_ptr, col_idx and values) identical to the reference's
+    FIND_DIM / GET_BASIS / GET_HAM on the KLM chain."""
+    g = golden("klm_ed.npz")
+    model = klm_model_from_golden(g, tag)
+    basis, row, col, val = oracle.ed_build(model)
+    assert np.array_equal(basis, g[f"{tag}_basis"])
+    assert np.array_equal(row, g[f"{tag}_row"])
+    assert np.array_equal(col, g[f"{tag}_col"])
+    assert np.array_equal(val.view(np.int64), g[f"{tag}_val"].view(np.int64))
+
+
+def test_site_apply_matches_reference_golden(oracle):
+    g = golden("vm_hubbard6.npz")
+    op = abi.Crs(g["op_row"], g["op_col"], g["op_val"], n=4)
+    for site in (0, 2, 5):
+        out = oracle.site_apply(op, g["basis"], g["basis"], 4, site, g["vec"])
+        np.testing.assert_array_equal(out, g[f"out_site{site}"])
+
+
+def test_obc_spmv_matches_reference_golden(oracle):
+    g = golden("obc_synthetic.npz")
+    qb = superblock.spin_block_labels(40, 9, seed=41)
+    sb = superblock.synthetic_superblock(40, 2, qb, [1, -1], 0, nnz_lllr=6, nnz_lrrl=2, seed=42, with_sign=True)
+    assert sb.n == int(g["n"])
+    np.testing.assert_array_equal(oracle.obc_spmv(sb, g["x"]), g["y"])
+    np.testing.assert_allclose(sb.explicit() @ g["x"], g["y"], rtol=0, atol=1e-12)
+
+
+def test_heisenberg16_energy_golden(oracle):
+    g = golden("xxz16.npz")
+    model = ed_models.xxz_chain(16)
+    basis, row, col, val = oracle.ed_build(model)
+    assert len(basis) == int(g["dim"]) and row[-1] == int(g["nnz"])
+    rc, out, v = oracle.lanczos(abi.Crs(row, col, val), False, guess=g["guess"])
+    assert abs(out.eig_val - float(g["E"])) < 1e-12 * abs(float(g["E"]))
+
+
+# ---- closed-form answers ----------------------------------------------------------------------
+
+@pytest.mark.parametrize("L", [6, 8, 10])
+def test_free_fermion_hubbard_u0(oracle, L):
+    model = ed_models.hubbard_chain(L, t=-1.0, U=0.0, n_ele=L, twoSz=0)
+    basis, row, col, val = oracle.ed_build(model)
+    H = abi.Crs(row, col, val)
+    rc, out, v = oracle.lanczos(H, False, seed=3, dense_below=0)
+    assert out.converged
+    assert abs(out.eig_val - ed_models.free_fermion_energy(L, L // 2, L // 2)) < 1e-10
+
+
+def test_two_site_hubbard(oracle):
+    U = 3.0
+    model = ed_models.hubbard_chain(2, t=-1.0, U=U, n_ele=2, twoSz=0)
+    basis, row, col, val = oracle.ed_build(model)
+    A = sp.csr_matrix((val, col, row), shape=(len(basis), len(basis))).toarray()
+    assert np.allclose(A, A.T)
+    assert np.linalg.eigvalsh(A)[0] == pytest.approx((U - np.sqrt(U * U + 16.0)) / 2.0, abs=1e-12)
+
+
+@pytest.mark.parametrize("L", [8, 12])
+def test_xx_chain_free_fermions(oracle, L):
+    """Jz = 0: XX chain = free spinless fermions with hopping Jxy/2."""
+    model = ed_models.xxz_chain(L, Jxy=1.0, Jz=0.0)
+    basis, row, col, val = oracle.ed_build(model)
+    rc, out, v = oracle.lanczos(abi.Crs(row, col, val), False, seed=5, dense_below=0)
+    eps = np.sort(np.cos(np.pi * np.arange(1, L + 1) / (L + 1)))
+    assert abs(out.eig_val - eps[:L // 2].sum()) < 1e-10
+
+
+def test_dense_path_small(oracle):
+    A = sp.random(300, 300, density=0.05, random_state=7)
+    A = (A + A.T).tocsr()
+    low = abi.lower_diag_last(A)
+    rc, out, v = oracle.lanczos(low, True, seed=1)
+    assert out.dense and abs(out.eig_val - np.linalg.eigvalsh(A.toarray())[0]) < 1e-12
+    assert np.linalg.norm(A @ v - out.eig_val * v) < 1e-10
+
+
+# ---- live reference (where its sources are present) ------------------------------------------
+
+def test_live_reference_lanczos_cases(ref, rng):
+    for n, dens in ((1200, 0.01), (2500, 0.004)):
+        A = sp.random(n, n, density=dens, random_state=int(rng.integers(1 << 30)))
+        A = (A + A.T).tocsr()
+        A.setdiag(rng.standard_normal(n))
+        low = abi.lower_diag_last(A)
+        g = rng.standard_normal(n)
+        s = __import__("os").dup(1)
+        E, v, st = ref.ref_lanczos(low, True, g)
+        rc, out, vo = ref.lanczos(low, True, guess=g)
+        assert abs(out.eig_val - E) < 1e-12 * abs(E)
+        assert abs(abs(v @ vo) - 1) < 1e-9
+        del s
+
+
+def test_live_reference_klm_ed_random(ref):
+    for L, ne, sz in ((3, 3, 0), (4, 5, 1)):   # 2Sz has the parity of ne + L
+        m = ref.ref_klm_model(L, ne, sz, t=-1.0, J=0.7, D_z=0.2, I_z=0.3, h_z=0.05)
+        basis, row, col, val = ref.ref_klm_ed(m)
+        tabs = ref.ref_klm_site_ops(m)
+        model = ed_models.klm_chain_from_tables(L, tabs, ne, sz, t=-1.0, I_z=0.3)
+        b2, r2, c2, v2 = ref.ed_build(model)
+        assert np.array_equal(basis, b2) and np.array_equal(row, r2) and np.array_equal(col, c2)
+        assert np.array_equal(val.view(np.int64), v2.view(np.int64))
