@@ -177,6 +177,12 @@ class dg_solve_info(C.Structure):
                 ("dense", C.c_int), ("ms_lanczos", C.c_double), ("ms_ii", C.c_double)]
 
 
+class dg_tune_result(C.Structure):
+    """include/dmrg_gb300.h: dg_tune_result"""
+    _fields_ = [("format", C.c_int), ("shape", C.c_int), ("variant", C.c_int), ("grid", C.c_int), ("ms", C.c_float),
+                ("candidates", C.c_int), ("window", C.c_int)]
+
+
 class dg_ed_term(C.Structure):
     """include/dmrg_gb300_ed.h"""
     _fields_ = [("kind", C.c_int), ("site1", C.c_int), ("site2", C.c_int), ("op1", C.c_int), ("op2", C.c_int),

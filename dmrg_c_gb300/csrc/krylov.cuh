@@ -349,7 +349,10 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
   Scalars *S = ws.S();
   LanczosResult res;
 
-  const int cap_max = cfg.max_block_step + 1;
+  // Krylov vectors one cycle can hold: LANCZOS_SLOW never restarts (its max_block_step is
+  // unused by the reference), LANCZOS restarts every max_block_step steps.
+  const int cycle_len = cfg.slow ? cfg.max_step : std::min(cfg.max_block_step, cfg.max_step);
+  const int cap_max = std::max(cycle_len, 1) + 1;
   DevBuf<double> D(cap_max + 1), O(cap_max + 1), y(n), c(cap_max + 1);
   Mapped<double> hD(cap_max + 1), hO(cap_max + 1), hs(cap_max + 1);
   DevBuf<double> s_dev(cap_max + 1);

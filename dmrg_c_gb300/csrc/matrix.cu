@@ -32,8 +32,10 @@ __global__ void k_validate(const int64_t *__restrict__ row, const int *__restric
     int64_t b = row[i], e = row[i + 1];
     bool ok = (b >= 0) && (e >= b) && (e <= nnz);
     if (ok && lower) {
+      // non-empty, diagonal last, strictly increasing columns below the diagonal (the
+      // expansion's per-row column ranks require distinct columns)
       ok = (e > b) && (col[e - 1] == i);
-      for (int64_t k = b; ok && k < e - 1; ++k) ok = (col[k] >= 0) && (col[k] < i);
+      for (int64_t k = b; ok && k < e - 1; ++k) ok = (col[k] >= 0) && (col[k] < i) && (k == b || col[k] > col[k - 1]);
     } else if (ok) {
       for (int64_t k = b; ok && k < e; ++k) ok = (col[k] >= 0) && (col[k] < n);
     }
@@ -105,7 +107,136 @@ __global__ void k_to_f32(const double *__restrict__ a, long n, float *__restrict
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = (float)a[i];
 }
 
+// One block per chunk of kSellWindow slots, sorted in independent windows of `window`
+// slots (a power of two <= kSellWindow): bitonic sort of (length desc, row asc) keys in
+// shared memory.  window <= 32 keeps the identity order.  Writes -1 for slots past the
+// last row.
+__global__ void __launch_bounds__(kThreads) k_sell_window_sort(const int64_t *__restrict__ row, int n, int window, int *perm) {
+  __shared__ unsigned long long key[kSellWindow];
+  const int base = blockIdx.x * kSellWindow;
+  for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
+    const int r = base + t;
+    if (r < n) {
+      const unsigned long long len = (unsigned long long)(row[r + 1] - row[r]);
+      key[t] = ((0x7fffffffull - len) << 32) | (unsigned)r;
+    } else {
+      key[t] = ~0ull;
+    }
+  }
+  __syncthreads();
+  if (window > kSellC) {
+    for (int k = 2; k <= window; k <<= 1) {
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
+          const int u = t ^ j;
+          if (u > t) {
+            const unsigned long long a = key[t], b = key[u];
+            const bool up = (k == window) || ((t & k) == 0);   // every window ends ascending
+            if ((a > b) == up) {
+              key[t] = b;
+              key[u] = a;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+  for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
+    const unsigned long long v = key[t];
+    perm[base + t] = (v == ~0ull) ? -1 : (int)(v & 0xffffffffu);
+  }
+}
+
+// width[s] = longest row of slice s; cnt[s] = 32 * width[s].
+__global__ void k_sell_widths(const int64_t *__restrict__ row, const int *__restrict__ perm, int nslices, int *width,
+                              long long *cnt) {
+  for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < nslices; sl += gridDim.x * blockDim.x) {
+    int w = 0;
+    for (int l = 0; l < kSellC; ++l) {
+      const int r = perm[sl * kSellC + l];
+      if (r >= 0) w = max(w, (int)(row[r + 1] - row[r]));
+    }
+    width[sl] = w;
+    cnt[sl] = (long long)w * kSellC;
+  }
+}
+
+// Column-major fill of each slice; padding: value 0, column = the slot's own row (or 0).
+template <class VT>
+__global__ void k_sell_fill(const int64_t *__restrict__ row, const int *__restrict__ col, const double *__restrict__ val,
+                            const int *__restrict__ perm, const int *__restrict__ width, const int64_t *__restrict__ off,
+                            int nslices, int *scol, VT *sval) {
+  const long slots = (long)nslices * kSellC;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < slots; t += (long)gridDim.x * blockDim.x) {
+    const int sl = (int)(t / kSellC), l = (int)(t % kSellC);
+    const int r = perm[t];
+    const int w = width[sl];
+    const int64_t b = (r >= 0) ? row[r] : 0;
+    const int len = (r >= 0) ? (int)(row[r + 1] - b) : 0;
+    for (int k = 0; k < w; ++k) {
+      const int64_t dst = off[sl] + (int64_t)k * kSellC + l;
+      if (k < len) {
+        scol[dst] = col[b + k];
+        sval[dst] = (VT)val[b + k];
+      } else {
+        scol[dst] = r >= 0 ? r : 0;
+        sval[dst] = (VT)0;
+      }
+    }
+  }
+}
+
 }  // namespace
+
+void build_sell(dg_matrix *m, cudaStream_t st, int window) {
+  const int n = m->n;
+  const int nwin = (n + kSellWindow - 1) / kSellWindow;
+  const int nslots = nwin * kSellWindow;
+  const int nslices = nslots / kSellC;
+  m->nslices = nslices;
+  m->s_perm.alloc(nslots);
+  m->s_width.alloc(nslices);
+  m->s_off.alloc(nslices + 1);
+  DevBuf<long long> cnt(nslices), tmp((nslices + kScanTile - 1) / kScanTile + 2);
+  int w = kSellC;
+  while (w < window && w < kSellWindow) w <<= 1;
+  m->sell_window = w;
+  k_sell_window_sort<<<nwin, kThreads, 0, st>>>(m->row.get(), n, w, m->s_perm.get()); ::dg::count_launch();
+  k_sell_widths<<<vector_grid(nslices), kThreads, 0, st>>>(m->row.get(), m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
+  exclusive_scan(cnt.get(), nslices, m->s_off.get(), tmp.get(), st);
+  int64_t total = 0;
+  DG_CUDA(cudaMemcpyAsync(&total, m->s_off.get() + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
+  m->nnz_sell = total;
+  m->s_col.alloc(total);
+  m->s_val.alloc(total);
+  const int g = vector_grid((long)nslots);
+  k_sell_fill<double><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
+                                              m->s_off.get(), nslices, m->s_col.get(), m->s_val.get()); ::dg::count_launch();
+  if (m->has32) {
+    m->s_val32.alloc(total);
+    k_sell_fill<float><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
+                                               m->s_off.get(), nslices, m->s_col.get(), m->s_val32.get()); ::dg::count_launch();
+  }
+  DG_CUDA(cudaGetLastError());
+  choose_sell_shape(nslices, total, &m->sell_ws, &m->sell_grid);
+  DG_CUDA(cudaStreamSynchronize(st));
+}
+
+void choose_sell_shape(int nslices, long stored, int *ws, int *grid) {
+  const long target_warps = (long)sm_count() * 96;
+  const double per_row = nslices > 0 ? (double)stored / ((double)nslices * kSellC) : 0.0;
+  int w = 1;
+  if (per_row >= 24.0) {
+    w = 2;
+    while (w < 8 && (long)nslices * w < target_warps && per_row / (2 * w) >= 16.0) w <<= 1;
+  }
+  const int groups = kWarps / w;
+  const long need = (nslices + groups - 1) / groups;
+  *ws = w;
+  *grid = (int)std::max(1L, std::min(need, (long)sm_count() * 16));
+}
 
 dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *col_d, const double *val_d, int storage,
                               int values, cudaStream_t st) {
@@ -130,7 +261,7 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
   DG_REQUIRE(ends[0] == 0 && ends[1] == nnz_in, DG_ERR_MATRIX, "CRS row offsets must run from 0 to nnz (got %lld..%lld, nnz=%ld)",
              (long long)ends[0], (long long)ends[1], nnz_in);
   DG_REQUIRE(first_bad == big, DG_ERR_MATRIX,
-             lower ? "row %d violates the lower-triangle layout (non-empty row, columns < row, diagonal stored last)"
+             lower ? "row %d violates the lower-triangle layout (non-empty row, increasing columns < row, diagonal last)"
                    : "row %d has a column outside [0, n) or decreasing offsets",
              first_bad);
 
@@ -161,6 +292,7 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
       m->nnz = total;
       m->col.alloc(total);
       m->val.alloc(total);
+      DG_CUDA(cudaMemsetAsync(m->col.get(), 0, sizeof(int) * total, st));
       DevBuf<int> scol(total);
       DevBuf<double> sval(total);
       k_fill_lower<<<g, kThreads, 0, st>>>(row, col_d, val_d, m->row.get(), n, m->col.get(), m->val.get()); ::dg::count_launch();
@@ -180,6 +312,8 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
       // FP64 values are still kept: the refinement and residual of the mixed form read them.
     }
     choose_shape(n, m->nnz, &m->lanes, &m->grid);
+    build_sell(m, st, kSellWindow);
+    m->format = DG_FORMAT_SELL;
     DG_CUDA(cudaStreamSynchronize(st));
   } catch (...) {
     delete m;
@@ -241,6 +375,35 @@ int dg_matrix_set_shape(dg_matrix *m, int lanes_per_row, int grid) {
     DG_REQUIRE(grid >= 1 && grid <= (1 << 20), DG_ERR_ARG, "grid out of range");
     m->lanes = lanes_per_row;
     m->grid = grid;
+    m->format = DG_FORMAT_CSR;
+  });
+}
+
+int dg_matrix_set_format(dg_matrix *m, int format) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    DG_REQUIRE(format == DG_FORMAT_CSR || format == DG_FORMAT_SELL, DG_ERR_ARG, "unknown format %d", format);
+    m->format = format;
+  });
+}
+
+int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    DG_REQUIRE(warps_per_slice == 1 || warps_per_slice == 2 || warps_per_slice == 4 || warps_per_slice == 8, DG_ERR_ARG,
+               "warps_per_slice must be 1, 2, 4 or 8");
+    DG_REQUIRE(grid >= 1 && grid <= (1 << 20), DG_ERR_ARG, "grid out of range");
+    m->sell_ws = warps_per_slice;
+    m->sell_grid = grid;
+    m->format = DG_FORMAT_SELL;
+  });
+}
+
+int dg_matrix_format(const dg_matrix *m, int *format, long *stored) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    if (format) *format = m->format;
+    if (stored) *stored = m->format == DG_FORMAT_SELL ? m->nnz_sell : m->nnz;
   });
 }
 
@@ -273,8 +436,8 @@ int dg_spmv(dg_matrix *m, const double *x, double *y, double sigma) {
       yb.alloc(m->n);
       yp = yb.get();
     }
-    launch_apply(m->op64(), m->lanes, m->grid, m->n, xp, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr,
-                 EpiStore<double>{yp}, RedSlot{nullptr, nullptr}, st);
+    matrix_apply64(m, xp, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiStore<double>{yp},
+                   RedSlot{nullptr, nullptr}, st);
     if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, bytes, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
   });
@@ -299,8 +462,12 @@ int dg_spmv_f32(dg_matrix *m, const float *x, float *y) {
       yb.alloc(m->n);
       yp = yb.get();
     }
-    launch_apply(m->op32(), m->lanes, m->grid, m->n, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
-                 EpiStore<float>{yp}, RedSlot{nullptr, nullptr}, st);
+    if (m->format == DG_FORMAT_SELL)
+      launch_sell(m->sell32(), m->sell_grid, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
+                  EpiStore<float>{yp}, RedSlot{nullptr, nullptr}, st);
+    else
+      launch_apply(m->op32(), m->lanes, m->grid, m->n, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
+                   EpiStore<float>{yp}, RedSlot{nullptr, nullptr}, st);
     if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, bytes, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
   });
@@ -312,7 +479,7 @@ int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters,
     DG_REQUIRE(m && x_dev && y_dev && ms_per_launch && iters > 0, DG_ERR_ARG, "bad argument");
     DG_REQUIRE(is_device_ptr(x_dev) && is_device_ptr(y_dev), DG_ERR_ARG, "profiling needs device vectors");
     cudaStream_t st = stream();
-    DevBuf<double> partials(m->grid), out(1);
+    DevBuf<double> partials(std::max(m->grid, m->sell_grid)), out(1);
     DevBuf<unsigned> ticket(1);
     DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
     DevBuf<unsigned char> flush;
@@ -324,8 +491,8 @@ int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters,
     for (int it = 0; it < iters; ++it) {
       if (flush_bytes) DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
       DG_CUDA(cudaEventRecord(e0, st));
-      launch_apply(m->op64(), m->lanes, m->grid, m->n, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
-                   EpiDot<double>{y_dev, out.get()}, RedSlot{partials.get(), ticket.get()}, st);
+      matrix_apply64(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y_dev, out.get()},
+                     RedSlot{partials.get(), ticket.get()}, st);
       DG_CUDA(cudaEventRecord(e1, st));
       DG_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -335,6 +502,110 @@ int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters,
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_launch = (float)(total / iters);
+  });
+}
+
+int dg_matrix_set_sell_window(dg_matrix *m, int window) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    DG_REQUIRE(window >= 1 && window <= kSellWindow, DG_ERR_ARG, "window must be in [1, %d]", kSellWindow);
+    const int ws = m->sell_ws, var = m->sell_variant;
+    build_sell(m, stream(), window);
+    m->sell_ws = ws;
+    m->sell_variant = var;
+    m->format = DG_FORMAT_SELL;
+  });
+}
+
+int dg_matrix_set_sell_variant(dg_matrix *m, int variant) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    DG_REQUIRE(variant >= 0 && variant < V_COUNT, DG_ERR_ARG, "unknown variant %d", variant);
+    m->sell_variant = variant;
+  });
+}
+
+// Times every candidate launch configuration of the fused product (the form used inside
+// Lanczos / CG) on this matrix and keeps the fastest: sliced ELL with 1/2/4/8 warps per
+// slice x kernel variant x grid, and CSR with 1..32 lanes per row x grid.  Each candidate
+// runs once untimed, then `iters` times between CUDA events on the library stream.
+int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && iters > 0, DG_ERR_ARG, "bad argument");
+    cudaStream_t st = stream();
+    const int sms = sm_count();
+    DevBuf<double> x(m->n), y(m->n), out1(1);
+    DevBuf<double> partials((size_t)sms * 16 + 64);
+    DevBuf<unsigned> ticket(1);
+    DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
+    DG_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * m->n, st));
+    cudaEvent_t e0, e1;
+    DG_CUDA(cudaEventCreate(&e0));
+    DG_CUDA(cudaEventCreate(&e1));
+    auto time_it = [&]() -> float {
+      RedSlot slot{partials.get(), ticket.get()};
+      matrix_apply64(m, x.get(), (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
+      DG_CUDA(cudaEventRecord(e0, st));
+      for (int i = 0; i < iters; ++i)
+        matrix_apply64(m, x.get(), (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
+      DG_CUDA(cudaEventRecord(e1, st));
+      DG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      return ms / iters;
+    };
+    dg_tune_result best{};
+    best.ms = 1e30f;
+    int tried = 0;
+    const int bps_list[2] = {8, 16};
+    const int windows[2] = {kSellWindow, kSellC};
+    for (int wi = 0; wi < 2; ++wi) {
+      if (m->sell_window != windows[wi]) build_sell(m, st, windows[wi]);
+      for (int ws = 1; ws <= 8; ws <<= 1) {
+        for (int var = 0; var < V_COUNT; ++var) {
+          for (int bps : bps_list) {
+            const int groups = kWarps / ws;
+            const long need = (m->nslices + groups - 1) / groups;
+            const int grid = (int)std::max(1L, std::min(need, (long)sms * bps));
+            m->format = DG_FORMAT_SELL;
+            m->sell_ws = ws;
+            m->sell_variant = var;
+            m->sell_grid = grid;
+            const float ms = time_it();
+            ++tried;
+            if (ms < best.ms) best = dg_tune_result{DG_FORMAT_SELL, ws, var, grid, ms, 0, windows[wi]};
+          }
+        }
+      }
+    }
+    for (int L = 1; L <= 32; L <<= 1) {
+      for (int bps : bps_list) {
+        const long need = ((long)m->n * L + kThreads - 1) / kThreads;
+        const int grid = (int)std::max(1L, std::min(need, (long)sms * bps));
+        m->format = DG_FORMAT_CSR;
+        m->lanes = L;
+        m->grid = grid;
+        const float ms = time_it();
+        ++tried;
+        if (ms < best.ms) best = dg_tune_result{DG_FORMAT_CSR, L, 0, grid, ms, 0, m->sell_window};
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best.format == DG_FORMAT_SELL) {
+      if (m->sell_window != best.window) build_sell(m, st, best.window);
+      m->format = DG_FORMAT_SELL;
+      m->sell_ws = best.shape;
+      m->sell_variant = best.variant;
+      m->sell_grid = best.grid;
+    } else {
+      m->format = DG_FORMAT_CSR;
+      m->lanes = best.shape;
+      m->grid = best.grid;
+    }
+    best.candidates = tried;
+    if (out) *out = best;
   });
 }
 

@@ -3,6 +3,7 @@
 
 #include "apply.cuh"
 #include "common.cuh"
+#include "sell.cuh"
 
 struct dg_matrix {
   int n = 0;
@@ -12,11 +13,25 @@ struct dg_matrix {
   dg::DevBuf<double> val;          // nnz (FP64 values)
   dg::DevBuf<float> val32;         // nnz (FP32 values, mixed-precision form)
   bool has64 = false, has32 = false;
-  int lanes = 1;                   // lanes per row
-  int grid = 1;                    // blocks of kThreads
+  int lanes = 1;                   // lanes per row (CSR kernel)
+  int grid = 1;                    // blocks of kThreads (CSR kernel)
+  // sliced-ELL copy (sell.cuh), used when format == DG_FORMAT_SELL
+  int format = DG_FORMAT_SELL;
+  int nslices = 0;
+  long nnz_sell = 0;               // stored elements including padding
+  int sell_grid = 1;
+  int sell_ws = 1;                 // warps per slice
+  int sell_variant = 1;            // SellVariant (V_U8)
+  int sell_window = dg::kSellWindow;   // row-sorting window (<= 32: rows keep their order)
+  dg::DevBuf<int64_t> s_off;
+  dg::DevBuf<int> s_width, s_perm, s_col;
+  dg::DevBuf<double> s_val;
+  dg::DevBuf<float> s_val32;
 
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }
   dg::CrsOp<float> op32() const { return dg::CrsOp<float>{row.get(), col.get(), val32.get()}; }
+  dg::SellOp<double> sell64() const { return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant}; }
+  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant}; }
 };
 
 namespace dg {
@@ -38,6 +53,52 @@ void launch_apply(const Op &op, int lanes, int grid, int n, const XT *x, const d
   }
   DG_CUDA(cudaGetLastError());
 }
+
+// Launch the sliced-ELL apply kernel.
+template <int WS, class VT, class XT, class Epi>
+void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, const double *scale_src, int scale_mode, double sigma,
+                    const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
+  switch (op.variant) {
+    case V_U4: k_apply_sell<WS, V_U4, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_U16: k_apply_sell<WS, V_U16, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_PIPE8: k_apply_sell<WS, V_PIPE8, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    default: k_apply_sell<WS, V_U8, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+  }
+}
+
+template <class VT, class XT, class Epi>
+void launch_sell(const SellOp<VT> &op, int grid, const XT *x, const double *scale_src, int scale_mode, double sigma,
+                 const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
+  switch (op.ws) {
+    case 1: launch_sell_ws<1>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
+    case 2: launch_sell_ws<2>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
+    case 4: launch_sell_ws<4>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
+    default: launch_sell_ws<8>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
+  }
+  ::dg::count_launch();
+  DG_CUDA(cudaGetLastError());
+}
+
+// Warps per slice and grid for the sliced-ELL kernel (heuristic from measured sweeps):
+// short rows (ED matrices) one warp per slice; otherwise enough warps of work to fill every
+// SM with at least ~16 elements per warp and row.
+void choose_sell_shape(int nslices, long stored, int *ws, int *grid);
+
+// Apply the matrix in its selected format with FP64 values.
+template <class XT, class Epi>
+void matrix_apply64(const dg_matrix *m, const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+                    const Epi &epi, RedSlot slot, cudaStream_t st) {
+  if (m->format == DG_FORMAT_SELL)
+    launch_sell(m->sell64(), m->sell_grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+  else
+    launch_apply(m->op64(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+}
+
+// Blocks needed by the current format (for sizing reduction partials).
+inline int matrix_grid(const dg_matrix *m) { return m->format == DG_FORMAT_SELL ? m->sell_grid : m->grid; }
+
+// Build the sliced-ELL copy of a device CRS with the given row-sorting window.
+void build_sell(dg_matrix *m, cudaStream_t st, int window);
 
 // Build a dg_matrix from device arrays (copied / expanded).  Throws on error.
 dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *col_d, const double *val_d, int storage,

@@ -14,6 +14,7 @@
 #include <sys/stat.h>
 
 #include <cstdarg>
+#include <algorithm>
 #include <cstring>
 
 #include "solve.cuh"
@@ -149,11 +150,54 @@ void up_crs(ObcData &D, int slot, const CRS1 *M, int rows, cudaStream_t st) {
 
 }  // namespace
 
+// Host-side consistency checks: every index the kernel derives from the caller's arrays
+// must land inside the arrays it is used on (bad input is an error, never a stray access).
+static void obc_validate(const CRS1 *const M[4], const int rows[4], const int cols[4], const DMRG_BASIS *B) {
+  const char *names[4] = {"M_LLLR", "M_LRRL", "M_LRRL_Sign", "M_RRRL"};
+  for (int k = 0; k < 4; ++k) {
+    const CRS1 *A = M[k];
+    if (rows[k] == 0) continue;
+    DG_REQUIRE(A->Row && A->Row[0] == 0, DG_ERR_MATRIX, "%s: row offsets must start at 0", names[k]);
+    for (int r = 0; r < rows[k]; ++r) {
+      DG_REQUIRE(A->Row[r + 1] >= A->Row[r], DG_ERR_MATRIX, "%s: decreasing row offsets at row %d", names[k], r);
+      for (long j = A->Row[r]; j < A->Row[r + 1]; ++j)
+        DG_REQUIRE(A->Col[j] >= 0 && A->Col[j] < cols[k], DG_ERR_MATRIX, "%s: column %d out of range at row %d", names[k],
+                   A->Col[j], r);
+    }
+  }
+  const int d = B->dim_onsite;
+  auto in = [](int v, int lo, int hi) { return v >= lo && v < hi; };
+  for (int i = 0; i < B->dim_LLLR; ++i)
+    DG_REQUIRE(in(B->LL_LLLR[i], 0, B->dim_LL) && in(B->LR_LLLR[i], 0, d), DG_ERR_MATRIX, "LLLR pair %d out of range", i);
+  for (int i = 0; i < B->dim_LRRL; ++i)
+    DG_REQUIRE(in(B->LR_LRRL[i], 0, d) && in(B->RL_LRRL[i], 0, d), DG_ERR_MATRIX, "LRRL pair %d out of range", i);
+  for (int i = 0; i < B->dim_RRRL; ++i)
+    DG_REQUIRE(in(B->RR_RRRL[i], 0, B->dim_RR) && in(B->RL_RRRL[i], 0, d), DG_ERR_MATRIX, "RRRL pair %d out of range", i);
+  for (int b = 0; b < B->dim_LLLRRRRL; ++b) {
+    const int ll = B->LL_LLLRRRRL[b], lr = B->LR_LLLRRRRL[b], rr = B->RR_LLLRRRRL[b], rl = B->RL_LLLRRRRL[b];
+    DG_REQUIRE(in(ll, 0, B->dim_LL) && in(lr, 0, d) && in(rr, 0, B->dim_RR) && in(rl, 0, d), DG_ERR_MATRIX,
+               "superblock state %d out of range", b);
+    DG_REQUIRE(in(B->Inv_LLLR[ll][lr], 0, B->dim_LLLR) && in(B->Inv_LRRL[lr][rl], 0, B->dim_LRRL) &&
+                   in(B->Inv_RRRL[rr][rl], 0, B->dim_RRRL),
+               DG_ERR_MATRIX, "superblock state %d has no pair index", b);
+  }
+  const long whole = (long)B->dim_LL * d * B->dim_RR * d;
+  for (long k = 0; k < whole; ++k)
+    DG_REQUIRE(B->Inv_LLLRRRRL[k] >= -1 && B->Inv_LLLRRRRL[k] < B->dim_LLLRRRRL, DG_ERR_MATRIX,
+               "Inv_LLLRRRRL[%ld] out of range", k);
+}
+
 // Upload the operator described by the reference's DMRG_BASIS and block matrices.
 void obc_upload(ObcData &D, const CRS1 *M_LLLR, const CRS1 *M_LRRL, const CRS1 *M_LRRL_Sign, const CRS1 *M_RRRL,
                 const int *Ele_RR, const DMRG_BASIS *B) {
   DG_REQUIRE(B && M_LLLR && M_LRRL && M_LRRL_Sign && M_RRRL && Ele_RR, DG_ERR_ARG, "null argument");
   DG_REQUIRE(B->dim_LLLRRRRL > 0 && B->dim_LL > 0 && B->dim_RR > 0 && B->dim_onsite > 0, DG_ERR_ARG, "empty superblock basis");
+  {
+    const CRS1 *Ms[4] = {M_LLLR, M_LRRL, M_LRRL_Sign, M_RRRL};
+    const int rows[4] = {B->dim_LLLR, B->dim_LRRL, std::min(M_LRRL_Sign->row_dim, B->dim_LRRL), B->dim_RRRL};
+    const int cols[4] = {B->dim_LLLR, B->dim_LRRL, B->dim_LRRL, B->dim_RRRL};
+    obc_validate(Ms, rows, cols, B);
+  }
   cudaStream_t st = stream();
   D.n = B->dim_LLLRRRRL;
   D.dim_LL = B->dim_LL;

@@ -1,0 +1,174 @@
+// sell.cuh -- sliced-ELL (SELL-32-sigma) operator layout and its fused apply kernel.
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so an FP64 SpMV is bound by
+// FP64 instruction issue as much as by HBM: every FP64 add spent on combining partial sums
+// of a row (the shuffle tree of a warp-per-row kernel) is paid at the same price as a
+// useful multiply-add.  In this layout one lane owns one row, so each stored element costs
+// exactly one DFMA and no cross-lane reduction is needed:
+//
+//  * rows are optionally permuted so that, inside windows of up to kSellWindow rows, they
+//    are ordered by decreasing length (sigma sorting: less padding); without sorting,
+//    consecutive rows share a slice, which keeps the x gathers of matrices whose neighbouring
+//    rows have similar column patterns (superblocks) close together;
+//  * consecutive groups of 32 permuted rows form a slice, stored column-major and padded to
+//    the slice's longest row: element k of lane l sits at off[s] + 32 k + l, so the 32 lanes
+//    of a warp read 256 contiguous bytes of values and 128 of columns per step;
+//  * padding entries have value 0 and point at the row itself (an always-valid x index).
+//
+// With one warp per slice each row's elements are accumulated in their CRS order; with WS
+// warps per slice each warp sums every WS-th element and the partials are added in warp
+// order.  Either way the order is fixed, so the product is bitwise reproducible.
+#pragma once
+
+#include "apply.cuh"
+
+namespace dg {
+
+constexpr int kSellC = 32;
+constexpr int kSellWindow = 2048;   // largest row-sorting window (shared-memory sort)
+
+template <class VT>
+struct SellOp {
+  const int64_t *__restrict__ off;   // nslices + 1 element offsets
+  const int *__restrict__ width;     // nslices
+  const int *__restrict__ perm;      // nslices*32 original row of each slot (-1 padding)
+  const int *__restrict__ col;
+  const VT *__restrict__ val;
+  int nslices;
+  int ws;                            // warps per slice (1, 2, 4 or 8)
+  int variant;                       // SellVariant
+};
+
+// Kernel variants (chosen per matrix by the autotuner, dg_matrix_autotune).  Each issues
+// U column/value loads, then U gathers of x, then U DFMAs per group; more groups in flight
+// per warp hide the dependent col -> x load chain:
+//   V_U4 / V_U8 / V_U16  groups of 4 / 8 / 16 elements;
+//   V_PIPE8              U=8 with the next group's columns/values loaded before the current
+//                        group's multiply-adds (software pipelining).
+// Measured on GB300 (FP64, 57M-element superblock): U=4 1.6 TB/s, U=8 4.5 TB/s.
+enum SellVariant : int { V_U4 = 0, V_U8 = 1, V_U16 = 2, V_PIPE8 = 3, V_COUNT = 4 };
+
+template <bool STREAM, class T>
+__device__ __forceinline__ T ld_mat(const T *p) {
+  if constexpr (STREAM) return __ldcs(p);
+  return *p;
+}
+template <bool STREAM, class T>
+__device__ __forceinline__ T ld_vec(const T *p) {
+  if constexpr (STREAM) return __ldg(p);
+  return *p;
+}
+
+// Sum of this warp's share of one slice row.  WS warps share a slice: warp `sub` takes the
+// row elements k = sub, sub + WS, sub + 2 WS, ...; each lane owns one row.
+template <int WS, int U, bool PIPE, bool STREAM, class VT, class XT>
+__device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t base, int w, int sub, const XT *__restrict__ x,
+                                               double s) {
+  const int cnt = (w > sub) ? (w - sub + WS - 1) / WS : 0;   // elements of this warp
+  const int G = cnt / U;
+  const int64_t step = (int64_t)WS * kSellC;
+  const int64_t p0 = base + (int64_t)sub * kSellC;
+  double sum = 0.0;
+  int c[U];
+  double v[U];
+  if (PIPE && G > 0) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      c[u] = ld_mat<STREAM>(op.col + p0 + u * step);
+      v[u] = to_d(ld_mat<STREAM>(op.val + p0 + u * step));
+    }
+  }
+  for (int g = 0; g < G; ++g) {
+    const int64_t pg = p0 + (int64_t)g * U * step;
+    if (!PIPE) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        c[u] = ld_mat<STREAM>(op.col + pg + u * step);
+        v[u] = to_d(ld_mat<STREAM>(op.val + pg + u * step));
+      }
+    }
+    double xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = to_d(ld_vec<STREAM>(x + c[u]));
+    double vc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) vc[u] = v[u];
+    if (PIPE && g + 1 < G) {
+      const int64_t pn = pg + (int64_t)U * step;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        c[u] = ld_mat<STREAM>(op.col + pn + u * step);
+        v[u] = to_d(ld_mat<STREAM>(op.val + pn + u * step));
+      }
+    }
+    if (s == 1.0) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) sum += vc[u] * xv[u];
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u) sum += vc[u] * (xv[u] * s);
+    }
+  }
+  for (int j = G * U; j < cnt; ++j) {
+    const int64_t p = p0 + (int64_t)j * step;
+    const double xv = to_d(ld_vec<STREAM>(x + ld_mat<STREAM>(op.col + p)));
+    sum += to_d(ld_mat<STREAM>(op.val + p)) * ((s == 1.0) ? xv : xv * s);
+  }
+  return sum;
+}
+
+template <int WS, int VAR, class VT, class XT, class Epi>
+__global__ void __launch_bounds__(kThreads)
+k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+             Epi epi, RedSlot slot) {
+  if (gate && *((volatile const int *)gate)) return;
+  constexpr int U = (VAR == V_U4) ? 4 : (VAR == V_U16) ? 16 : 8;
+  constexpr bool PIPE = (VAR == V_PIPE8);
+  constexpr bool STREAM = false;
+  const double s = load_scale(scale_src, scale_mode);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;          // warp in block
+  const int group = wib / WS, sub = wib % WS;
+  constexpr int GROUPS = kWarps / WS;        // slices per block per trip
+  __shared__ double part[WS > 1 ? kWarps : 1][kSellC];
+  double acc = 0.0;
+  if (WS == 1) {
+    // warps advance independently (no block barrier)
+    const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
+    for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
+      const int row = op.perm[sl * kSellC + lane];
+      const double sum = sell_row_sum<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x, s);
+      if (row >= 0) {
+        const double xi = (s == 1.0) ? to_d(x[row]) : to_d(x[row]) * s;
+        const double yi = (sigma == 0.0) ? sum : sum + sigma * xi;
+        epi.row(row, xi, yi, acc);
+      }
+    }
+  } else {
+    for (int sl0 = blockIdx.x * GROUPS; sl0 < op.nslices; sl0 += gridDim.x * GROUPS) {
+      const int sl = sl0 + group;
+      const bool live = sl < op.nslices;
+      double sum = live ? sell_row_sum<WS, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], sub, x, s) : 0.0;
+      part[WS > 1 ? wib : 0][lane] = sum;
+      __syncthreads();
+      if (sub == 0) {
+#pragma unroll
+        for (int j = 1; j < WS; ++j) sum += part[WS > 1 ? wib + j : 0][lane];
+      }
+      __syncthreads();
+      if (live && sub == 0) {
+        const int row = op.perm[sl * kSellC + lane];
+        if (row >= 0) {
+          const double xi = (s == 1.0) ? to_d(x[row]) : to_d(x[row]) * s;
+          const double yi = (sigma == 0.0) ? sum : sum + sigma * xi;
+          epi.row(row, xi, yi, acc);
+        }
+      }
+    }
+  }
+  if constexpr (Epi::kReduce) {
+    grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
+  }
+}
+
+}  // namespace dg

@@ -11,11 +11,11 @@ namespace dg {
 struct CrsLauncher {
   const dg_matrix *m;
   int n() const { return m->n; }
-  int grid() const { return m->grid; }
+  int grid() const { return matrix_grid(m); }
   template <class XT, class Epi>
   void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
-    launch_apply(m->op64(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    matrix_apply64(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
   }
 };
 

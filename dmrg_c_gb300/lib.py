@@ -80,6 +80,12 @@ SIGNATURES = {
     "dg_matrix_free": (None, [vp]),
     "dg_matrix_info": (C.c_int, [vp, ip, lp, ip, ip]),
     "dg_matrix_set_shape": (C.c_int, [vp, C.c_int, C.c_int]),
+    "dg_matrix_set_format": (C.c_int, [vp, C.c_int]),
+    "dg_matrix_set_sell_shape": (C.c_int, [vp, C.c_int, C.c_int]),
+    "dg_matrix_set_sell_variant": (C.c_int, [vp, C.c_int]),
+    "dg_matrix_set_sell_window": (C.c_int, [vp, C.c_int]),
+    "dg_matrix_autotune": (C.c_int, [vp, C.c_int, P(abi.dg_tune_result)]),
+    "dg_matrix_format": (C.c_int, [vp, ip, lp]),
     "dg_matrix_download": (C.c_int, [vp, lp, ip, dp]),
     "dg_spmv": (C.c_int, [vp, vp, vp, C.c_double]),
     "dg_spmv_f32": (C.c_int, [vp, vp, vp]),
@@ -93,6 +99,7 @@ SIGNATURES = {
 
 DG_STORE_FULL, DG_STORE_LOWER_DIAG_LAST = 0, 1
 DG_VALUES_F64, DG_VALUES_F32, DG_VALUES_BOTH = 1, 2, 3
+DG_FORMAT_CSR, DG_FORMAT_SELL = 0, 1
 
 _lib = None
 
@@ -161,8 +168,31 @@ class DeviceMatrix:
             pass
 
     def set_shape(self, lanes: int, grid: int):
+        """Use the CSR kernel with this many lanes per row and blocks."""
         check(load().dg_matrix_set_shape(self.h, lanes, grid))
         self.lanes, self.grid = lanes, grid
+
+    def set_sell_shape(self, warps_per_slice: int, grid: int):
+        check(load().dg_matrix_set_sell_shape(self.h, warps_per_slice, grid))
+
+    def set_sell_variant(self, variant: int):
+        check(load().dg_matrix_set_sell_variant(self.h, variant))
+
+    def set_sell_window(self, window: int):
+        check(load().dg_matrix_set_sell_window(self.h, window))
+
+    def autotune(self, iters: int = 3) -> abi.dg_tune_result:
+        r = abi.dg_tune_result()
+        check(load().dg_matrix_autotune(self.h, iters, C.byref(r)))
+        return r
+
+    def set_format(self, fmt: int):
+        check(load().dg_matrix_set_format(self.h, fmt))
+
+    def format(self):
+        f, stored = C.c_int(), C.c_long()
+        check(load().dg_matrix_format(self.h, C.byref(f), C.byref(stored)))
+        return f.value, stored.value
 
     def download(self):
         row = np.empty(self.n + 1, np.int64)

@@ -115,6 +115,9 @@ typedef struct dg_matrix dg_matrix;
 
 enum { DG_STORE_FULL = 0, DG_STORE_LOWER_DIAG_LAST = 1 };
 enum { DG_VALUES_F64 = 1, DG_VALUES_F32 = 2, DG_VALUES_BOTH = 3 };
+/* Device layouts of the operator: CSR with a group of lanes per row, or sliced ELL with one
+ * lane per row (32-row slices, rows length-sorted within 2048-row windows). */
+enum { DG_FORMAT_CSR = 0, DG_FORMAT_SELL = 1 };
 
 /* Upload a host CRS.  storage = DG_STORE_FULL for a full matrix (MATRIX_VECTOR_PRODUCT
  * input), DG_STORE_LOWER_DIAG_LAST for the symmetric-half input of the *_SYM entry points
@@ -127,6 +130,33 @@ void dg_matrix_free(dg_matrix *m);
 int dg_matrix_info(const dg_matrix *m, int *n, long *nnz_full, int *lanes_per_row, int *grid);
 /* Override the launch shape (lanes per row: 1,2,4,...,32; grid blocks of 256 threads). */
 int dg_matrix_set_shape(dg_matrix *m, int lanes_per_row, int grid);
+/* Select the layout used by every product with this matrix (default DG_FORMAT_SELL). */
+int dg_matrix_set_format(dg_matrix *m, int format);
+/* Use the sliced-ELL kernel with warps_per_slice (1, 2, 4, 8) warps sharing a 32-row slice. */
+int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid);
+/* Sliced-ELL kernel variant: element groups of 0: 4, 1: 8 (default), 2: 16,
+ * 3: 8 with software-pipelined loads. */
+int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
+/* Rebuild the sliced-ELL copy sorting rows by length within windows of `window` rows
+ * (1..2048; <= 32 keeps the original row order). */
+int dg_matrix_set_sell_window(dg_matrix *m, int window);
+
+/* Launch configuration picked by dg_matrix_autotune. */
+typedef struct {
+   int format;        /* DG_FORMAT_CSR or DG_FORMAT_SELL                 */
+   int shape;         /* lanes per row (CSR) or warps per slice (SELL)   */
+   int variant;       /* SELL kernel variant                             */
+   int grid;          /* blocks of 256 threads                           */
+   float ms;          /* device time of one fused product, milliseconds */
+   int candidates;    /* configurations timed                            */
+   int window;        /* SELL row-sorting window                         */
+} dg_tune_result;
+
+/* Time the candidate configurations of the fused product on this matrix (iters launches
+ * each) and keep the fastest for all later products. */
+int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out);
+/* Current layout and, for DG_FORMAT_SELL, the stored elements including slice padding. */
+int dg_matrix_format(const dg_matrix *m, int *format, long *stored);
 /* Download the device full CRS (row: n+1, col/val: nnz_full). */
 int dg_matrix_download(const dg_matrix *m, long *row, int *col, double *val);
 

@@ -304,3 +304,69 @@ def test_dropin_fatal_error_exits(gpu, tmp_path):
     assert r.returncode == 1
     assert "Error in LANCZOS_SYM" in r.stdout and "not reached" not in r.stdout
     assert "Box->Guess=Maybe is error" in (tmp_path / "SML_out" / "error.txt").read_text()
+
+
+def _sell_cases(oracle, rng):
+    cases = []
+    A = sp.random(5000, 5000, density=0.002, random_state=3, format="csr")
+    A = A.tolil()
+    A[17, :4000] = rng.standard_normal(4000)          # one dense row
+    A = A.tocsr()
+    A.eliminate_zeros()
+    cases.append(("dense_row", abi.Crs.from_scipy(A), A))
+    B = sp.random(3001, 3001, density=0.001, random_state=4, format="csr")   # many empty rows
+    cases.append(("empty_rows", abi.Crs.from_scipy(B), B))
+    basis, row, col, val = oracle.ed_build(ed_models.hubbard_chain(8, U=4.0))
+    H = sp.csr_matrix((val, col, row), shape=(len(basis), len(basis)))
+    cases.append(("hubbard8", abi.Crs(row, col, val), H))
+    return cases
+
+
+def test_sell_matches_csr_and_oracle(gpu, oracle, rng):
+    for name, crs, A in _sell_cases(oracle, rng):
+        m = gpu.DeviceMatrix(crs)
+        fmt, stored = m.format()
+        assert fmt == gpu.DG_FORMAT_SELL and stored >= crs.nnz
+        x = rng.standard_normal(crs.n)
+        y_sell = m.spmv(x)
+        assert np.array_equal(y_sell, m.spmv(x)), name          # deterministic
+        m.set_format(gpu.DG_FORMAT_CSR)
+        y_csr = m.spmv(x)
+        ref = A @ x
+        assert rel_close(y_sell, ref), name
+        assert rel_close(y_csr, ref), name
+        m.set_format(gpu.DG_FORMAT_SELL)
+        assert rel_close(m.spmv(x, sigma=-0.5), ref - 0.5 * x), name
+
+
+def test_sell_solver_parity(gpu):
+    """Lanczos + inverse iteration give the same eigenpair in both layouts."""
+    g, low, full = sml_inputs()
+    m = gpu.DeviceMatrix(low, gpu.DG_STORE_LOWER_DIAG_LAST)
+    v1, i1 = gpu.ground_state(m, gpu.default_params(), guess=g["guess"])
+    m.set_format(gpu.DG_FORMAT_CSR)
+    v2, i2 = gpu.ground_state(m, gpu.default_params(), guess=g["guess"])
+    assert abs(i1.eig_val - i2.eig_val) < 1e-12 * abs(i1.eig_val)
+    assert abs(abs(v1 @ v2) - 1) < 1e-12
+
+
+@pytest.mark.parametrize("ws", [1, 2, 4, 8])
+def test_sell_warps_per_slice(gpu, oracle, rng, ws):
+    for name, crs, A in _sell_cases(oracle, rng):
+        m = gpu.DeviceMatrix(crs)
+        x = rng.standard_normal(crs.n)
+        for variant in range(4):
+            m.set_sell_shape(ws, 53)
+            m.set_sell_variant(variant)
+            y = m.spmv(x)
+            assert np.array_equal(y, m.spmv(x)), (name, variant)
+            assert rel_close(y, A @ x), (name, variant)
+
+
+def test_autotune_keeps_results(gpu, oracle, rng):
+    for name, crs, A in _sell_cases(oracle, rng):
+        m = gpu.DeviceMatrix(crs)
+        r = m.autotune(iters=2)
+        assert r.candidates >= 40 and r.ms > 0
+        x = rng.standard_normal(crs.n)
+        assert rel_close(m.spmv(x), A @ x), name
