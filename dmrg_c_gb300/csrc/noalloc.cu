@@ -1,0 +1,140 @@
+// noalloc.cu -- conjugate-gradient solve that allocates nothing.
+//
+// Some callers cannot let a library allocate device memory: code that runs inside a CUDA
+// stream capture, an application whose memory pool owns the whole device, or an embedding
+// that forbids allocation on its solve path.  dg_cg_noalloc serves them: the caller passes
+// the matrix (full CRS) and the vectors in device memory, and every temporary the solve
+// needs (three work vectors, the reduction partials and the solver scalars) lives in one
+// file-scope static device array of fixed size.  No cudaMalloc, cudaFree, pinned-host or
+// library allocation happens on this path.
+//
+// Limits and sharing:
+//  * n <= kNoAllocMaxN rows (the array holds three vectors of that length); larger systems
+//    are rejected with DG_ERR_ARG before any device work;
+//  * the array is one per device and every call on that device shares it, keeping the last
+//    call's contents; the call clears what must start at zero (reduction ticket, solver
+//    state).  Calls from one process are serialised by a mutex, but any other device work
+//    that touches the array while a call runs would race with it;
+//  * the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress, with that device current) and caches it, so make that first
+//    call before any stream capture begins.
+#include <mutex>
+
+#include "krylov.cuh"
+#include "matrix.cuh"
+
+namespace dg {
+namespace {
+
+constexpr long kNoAllocMaxN = 1L << 20;            // rows
+constexpr int kNoAllocMaxGrid = 4096;              // reduction partials
+constexpr size_t kVecBytes = sizeof(double) * (size_t)kNoAllocMaxN;
+constexpr size_t kOffR = 0, kOffP = kVecBytes, kOffY = 2 * kVecBytes;
+constexpr size_t kOffPartials = 3 * kVecBytes;
+constexpr size_t kOffScalars = kOffPartials + sizeof(double) * kNoAllocMaxGrid;
+constexpr size_t kOffProgress = kOffScalars + ((sizeof(Scalars) + 255) / 256) * 256;
+constexpr size_t kOffTicket = kOffProgress + ((sizeof(Progress) + 255) / 256) * 256;
+constexpr size_t kScratchBytes = kOffTicket + 256;
+
+// The scratch array: 3 x 8 MiB vectors + partials + state, about 24 MiB per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_noalloc_mutex;
+constexpr int kMaxDevices = 64;
+unsigned char *g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array for the current device (looked up once per device).
+unsigned char *scratch_for_current_device() {
+  int dev = 0;
+  DG_CUDA(cudaGetDevice(&dev));
+  DG_REQUIRE(dev >= 0 && dev < kMaxDevices, DG_ERR_ARG, "device %d out of range", dev);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    DG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+  }
+  return g_scratch_ptr[dev];
+}
+
+struct RawCrsLauncher {
+  CrsOp<double> op;
+  int n_, lanes, grid_;
+  int n() const { return n_; }
+  int grid() const { return grid_; }
+  template <class XT, class Epi>
+  void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
+             cudaStream_t st) const {
+    launch_apply(op, lanes, grid_, n_, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+  }
+};
+
+}  // namespace
+}  // namespace dg
+
+using namespace dg;
+
+extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, const double *val_dev, double sigma,
+                             const double *b_dev, double *x_dev, double acc, int max_step, int *iters) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(row_dev && col_dev && val_dev && b_dev && x_dev, DG_ERR_ARG, "null argument");
+    DG_REQUIRE(n > 0, DG_ERR_ARG, "n must be positive (n=%d)", n);
+    DG_REQUIRE(n <= kNoAllocMaxN, DG_ERR_ARG, "n=%d exceeds the allocation-free limit of %ld rows", n, kNoAllocMaxN);
+    DG_REQUIRE(max_step >= 1, DG_ERR_ARG, "max_step must be >= 1");
+    DG_REQUIRE(is_device_ptr(row_dev) && is_device_ptr(col_dev) && is_device_ptr(val_dev) && is_device_ptr(b_dev) &&
+                   is_device_ptr(x_dev),
+               DG_ERR_ARG, "dg_cg_noalloc takes device pointers only");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    unsigned char *base = scratch_for_current_device();
+    double *r = reinterpret_cast<double *>(base + kOffR);
+    double *p = reinterpret_cast<double *>(base + kOffP);
+    double *y = reinterpret_cast<double *>(base + kOffY);
+    double *partials = reinterpret_cast<double *>(base + kOffPartials);
+    Scalars *S = reinterpret_cast<Scalars *>(base + kOffScalars);
+    Progress *prog = reinterpret_cast<Progress *>(base + kOffProgress);
+    unsigned *ticket = reinterpret_cast<unsigned *>(base + kOffTicket);
+    cudaStream_t st = stream();
+
+    int64_t ends[2];
+    DG_CUDA(cudaMemcpyAsync(&ends[0], row_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaMemcpyAsync(&ends[1], row_dev + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    DG_REQUIRE(ends[0] == 0 && ends[1] >= 0, DG_ERR_MATRIX, "CRS row offsets must start at 0");
+    RawCrsLauncher op;
+    op.op = CrsOp<double>{reinterpret_cast<const int64_t *>(row_dev), col_dev, val_dev};
+    op.n_ = n;
+    choose_shape(n, (long)ends[1], &op.lanes, &op.grid_);
+    const int vgrid = vector_grid(n);
+    DG_REQUIRE(op.grid_ <= kNoAllocMaxGrid && vgrid <= kNoAllocMaxGrid, DG_ERR_ARG, "grid exceeds the scratch partials");
+    const RedSlot slot{partials, ticket};
+
+    // State that must start at zero: the reduction ticket and the solver scalars / progress.
+    DG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), st));
+    DG_CUDA(cudaMemsetAsync(S, 0, sizeof(Scalars), st));
+    DG_CUDA(cudaMemsetAsync(prog, 0, sizeof(Progress), st));
+
+    // x0 normalised (into y), r = b - (M + sigma) x0, p = r; then x <- normalised x0
+    // (sml/CONJUGATE_GRADIENT_SYM.c:35-43).
+    k_norm2<double><<<vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
+    op.apply(x_dev, &S->xn2, SCALE_RSQRT, sigma, (const int *)nullptr, EpiCgInit{b_dev, y, r, p, S}, slot, st);
+    DG_CUDA(cudaMemcpyAsync(x_dev, y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    const int chunk = 16;
+    int done = 0, it = 1;
+    while (it < max_step && !done) {
+      const int last = std::min(it + chunk - 1, max_step - 1);
+      for (; it <= last; ++it) {
+        op.apply(p, (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgAlpha{y, S}, slot, st);
+        k_cg_update<<<vgrid, kThreads, 0, st>>>(n, p, y, x_dev, r, S, acc, it, max_step, prog, slot); ::dg::count_launch();
+        k_cg_direction<<<vgrid, kThreads, 0, st>>>(n, r, p, S); ::dg::count_launch();
+      }
+      DG_CUDA(cudaGetLastError());
+      DG_CUDA(cudaMemcpyAsync(&done, &S->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+      DG_CUDA(cudaStreamSynchronize(st));
+    }
+    int it_done = max_step;
+    DG_CUDA(cudaMemcpyAsync(&it_done, &S->iters, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    if (iters) *iters = done ? it_done : max_step;
+    DG_REQUIRE(done == 1, DG_ERR_NOCONV, "CG did not converge (max step %d)", max_step);
+  });
+}

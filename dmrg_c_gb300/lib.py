@@ -95,6 +95,7 @@ SIGNATURES = {
     "dg_ground_state": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
     "dg_linear_solve": (C.c_int, [vp, C.c_double, vp, vp, C.c_double, C.c_int, C.c_int, ip]),
     "dg_residual_l1": (C.c_int, [vp, vp, C.c_double, dp]),
+    "dg_cg_noalloc": (C.c_int, [C.c_int, vp, vp, vp, C.c_double, vp, vp, C.c_double, C.c_int, ip]),
 }
 
 DG_STORE_FULL, DG_STORE_LOWER_DIAG_LAST = 0, 1
