@@ -64,7 +64,7 @@ WORKLOAD_DESC = {
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
 
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
@@ -78,7 +78,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -202,6 +202,9 @@ def run_gb300(args, ws, rank, local_rank):
     # roofline of the SpMV kernel
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
+    fmt, _stored = m.format()
+    kernel = ("k_apply_sell (SELL-32 sliced ELL, one lane per row, fused <x,y> epilogue)" if fmt == L.DG_FORMAT_SELL
+              else "k_apply (CSR, lanes per row, fused <x,y> epilogue)")
     spmv_ms = m.profile_spmv(x, y, iters=30, flush_bytes=FLUSH_BYTES)
     spmv_warm_ms = m.profile_spmv(x, y, iters=30, flush_bytes=0)
     B = spmv_bytes(n, nnz_full)
@@ -245,13 +248,15 @@ def run_gb300(args, ws, rank, local_rank):
                    "lanczos_acc": 1e-14, "ii_acc": 1e-9, "cg_acc": 1e-7},
         "wall_ms_per_step": wall * 1e3 / args.steps,
         "p50_ms": float(np.percentile(dev_ms, 50)), "p99_ms": float(np.percentile(dev_ms, 99)),
+        "ms_lanczos_p50": float(np.percentile([i.ms_lanczos for i in infos], 50)),
+        "ms_ii_p50": float(np.percentile([i.ms_ii for i in infos], 50)),
         "lanczos_steps": infos[-1].lanczos_steps, "cg_steps": infos[-1].cg_steps, "spmv_per_solve": infos[-1].spmv_count,
         "ii_error": infos[-1].error, "eig_val": E,
         "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "entry": "DMRG_DIAGONALIZE_SUPERBLOCK_SYM", "gs_val": st.gs_val},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_from_profile(args.workload), "peak_source": peak_kind,
-                     "kernel": "k_apply<CrsOp<double>, EpiDot> (SpMV + fused dot)", "ms_per_launch": spmv_ms,
+                     "kernel": kernel, "ms_per_launch": spmv_ms,
                      "bytes_per_launch": B, "l2_warm_ms_per_launch": spmv_warm_ms,
                      "l2_warm_gbs": B / (spmv_warm_ms * 1e-3) / 1e9},
         "gpu_launches": launches,
@@ -296,7 +301,7 @@ def run_reference(args, ws, rank):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOAD_DESC), default="klm_m128")

@@ -65,8 +65,22 @@ cudaStream_t stream();
 int sm_count();
 
 // ---------------------------------------------------------------------------------
-// RAII device / pinned buffers.
+// Device memory.  Everything the library allocates on the device comes from its own
+// stream-ordered pool (one per device), allocated and freed on the calling thread's library
+// stream.  Freed blocks stay in the pool up to DG_POOL_KEEP_MB (default 8 GiB) so that
+// repeated solves pay neither cudaMalloc nor cudaFree, which synchronise the whole device;
+// dg_release_pool() hands the cached blocks back.  Every library call synchronises its
+// stream before returning, so a buffer is never in use on another stream when it is freed.
 // ---------------------------------------------------------------------------------
+cudaMemPool_t device_pool();
+void *pool_alloc(size_t bytes, cudaStream_t st);
+void pool_free(void *p, cudaStream_t st);
+
+// Mapped pinned host memory is kept in a small per-thread cache of blocks for the same
+// reason (cudaHostAlloc / cudaFreeHost cost far more than one solver step).
+void *mapped_acquire(size_t bytes, size_t *got);
+void mapped_return(void *h, size_t bytes);
+
 template <class T>
 struct DevBuf {
   T *p = nullptr;
@@ -84,11 +98,11 @@ struct DevBuf {
   void alloc(size_t count) {
     release();
     if (count == 0) count = 1;
-    DG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    p = static_cast<T *>(pool_alloc(count * sizeof(T), stream()));
     n = count;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) pool_free(p, stream());
     p = nullptr;
     n = 0;
   }
@@ -100,6 +114,7 @@ template <class T>
 struct Mapped {
   T *h = nullptr;
   T *d = nullptr;
+  size_t bytes = 0;
   Mapped() = default;
   explicit Mapped(size_t count) { alloc(count); }
   Mapped(const Mapped &) = delete;
@@ -107,13 +122,14 @@ struct Mapped {
   ~Mapped() { release(); }
   void alloc(size_t count) {
     release();
-    DG_CUDA(cudaHostAlloc((void **)&h, count * sizeof(T), cudaHostAllocMapped));
+    h = static_cast<T *>(mapped_acquire(count * sizeof(T), &bytes));
     std::memset((void *)h, 0, count * sizeof(T));
     DG_CUDA(cudaHostGetDevicePointer((void **)&d, (void *)h, 0));
   }
   void release() {
-    if (h) cudaFreeHost(h);
+    if (h) mapped_return((void *)h, bytes);
     h = d = nullptr;
+    bytes = 0;
   }
 };
 

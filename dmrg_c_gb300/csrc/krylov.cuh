@@ -364,10 +364,10 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
     if (need <= cap) return;
     int ncap = cap == 0 ? std::min(cap_max, std::max(need, 64)) : std::min(cap_max, std::max(need, 2 * cap));
     double *nv = nullptr;
-    DG_CUDA(cudaMallocAsync((void **)&nv, sizeof(double) * (size_t)ncap * n, st));
+    nv = static_cast<double *>(pool_alloc(sizeof(double) * (size_t)ncap * n, st));
     if (V) {
       DG_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * (size_t)cap * n, cudaMemcpyDeviceToDevice, st));
-      DG_CUDA(cudaFreeAsync(V, st));
+      pool_free(V, st);
     }
     V = nv;
     cap = ncap;
@@ -375,9 +375,7 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
   struct FreeV {
     double **v;
     cudaStream_t st;
-    ~FreeV() {
-      if (*v) cudaFreeAsync(*v, st);
-    }
+    ~FreeV() { pool_free(*v, st); }
   } freev{&V, st};
 
   const RedSlot slot = ws.slot();
@@ -577,7 +575,8 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   }
   DG_CUDA(cudaStreamSynchronize(st));
   Scalars hs;
-  DG_CUDA(cudaMemcpy(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost));
+  DG_CUDA(cudaMemcpyAsync(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
   res.converged = hs.done == 1;
   res.iters = hs.done ? hs.iters : max_step;
   if (spmv_count) *spmv_count += (hs.done ? hs.iters : std::max(0, max_step - 1));
@@ -649,7 +648,8 @@ IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double 
   }
   DG_CUDA(cudaStreamSynchronize(st));
   Scalars hs;
-  DG_CUDA(cudaMemcpy(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost));
+  DG_CUDA(cudaMemcpyAsync(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
   res.converged = hs.done == 1;
   res.iters = hs.done ? hs.iters : max_step;
   if (spmv_count) *spmv_count += (hs.done ? hs.iters + 1 : max_step);

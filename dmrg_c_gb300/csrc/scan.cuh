@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_tiles(const CT *__restrict__ 
   if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(kThreads) k_scan_sums(long long *__restrict__ sums, int ntiles, long long *__restrict__ grand) {
+static __global__ void __launch_bounds__(kThreads) k_scan_sums(long long *__restrict__ sums, int ntiles, long long *__restrict__ grand) {
   // Exclusive scan of the tile sums by one block, in chunks of kThreads.
   long long carry = 0;
   for (int base = 0; base < ntiles; base += kThreads) {

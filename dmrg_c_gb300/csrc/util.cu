@@ -45,6 +45,92 @@ cudaStream_t stream() {
   return s;
 }
 
+// ---- device memory pool ---------------------------------------------------------------
+namespace {
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[kMaxPoolDevices] = {nullptr};
+
+uint64_t pool_keep_bytes() {
+  const char *s = getenv("DG_POOL_KEEP_MB");
+  if (s && *s) return (uint64_t)strtoull(s, nullptr, 10) << 20;
+  return 8ull << 30;
+}
+}  // namespace
+
+cudaMemPool_t device_pool() {
+  int dev = 0;
+  DG_CUDA(cudaGetDevice(&dev));
+  DG_REQUIRE(dev >= 0 && dev < kMaxPoolDevices, DG_ERR_ARG, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    DG_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = pool_keep_bytes();
+    DG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pools[dev] = pool;
+  }
+  return g_pools[dev];
+}
+
+void *pool_alloc(size_t bytes, cudaStream_t st) {
+  void *p = nullptr;
+  DG_CUDA(cudaMallocFromPoolAsync(&p, bytes ? bytes : 1, device_pool(), st));
+  return p;
+}
+
+void pool_free(void *p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
+// ---- mapped host blocks ------------------------------------------------------------------
+namespace {
+struct MappedBlock {
+  void *h;
+  size_t bytes;
+};
+struct MappedCache {
+  std::vector<MappedBlock> free_blocks;
+  ~MappedCache() {
+    for (auto &b : free_blocks) cudaFreeHost(b.h);
+  }
+};
+thread_local MappedCache g_mapped_cache;
+}  // namespace
+
+void *mapped_acquire(size_t bytes, size_t *got) {
+  size_t want = 4096;
+  while (want < bytes) want <<= 1;
+  auto &fb = g_mapped_cache.free_blocks;
+  for (size_t i = 0; i < fb.size(); ++i) {
+    if (fb[i].bytes >= want) {
+      MappedBlock b = fb[i];
+      fb.erase(fb.begin() + (long)i);
+      *got = b.bytes;
+      return b.h;
+    }
+  }
+  void *h = nullptr;
+  DG_CUDA(cudaHostAlloc(&h, want, cudaHostAllocMapped));
+  *got = want;
+  return h;
+}
+
+void mapped_return(void *h, size_t bytes) {
+  if (!h) return;
+  auto &fb = g_mapped_cache.free_blocks;
+  if (fb.size() >= 16) {
+    cudaFreeHost(h);
+    return;
+  }
+  fb.push_back(MappedBlock{h, bytes});
+}
+
 int sm_count() {
   thread_local int cached = -1, dev = -1;
   int cur = 0;
@@ -104,5 +190,13 @@ int dg_device_count(void) {
 const char *dg_version(void) { return "dmrg_gb300 0.1 (sm_103a)"; }
 
 long dg_kernel_launches(void) { return dg::g_launches.load(); }
+
+int dg_release_pool(void) {
+  return dg::guarded([&] {
+    dg::require_device();
+    DG_CUDA(cudaStreamSynchronize(dg::stream()));
+    DG_CUDA(cudaMemPoolTrimTo(dg::device_pool(), 0));
+  });
+}
 
 }  // extern "C"

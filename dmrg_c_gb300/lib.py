@@ -74,6 +74,7 @@ SIGNATURES = {
     "dg_device_count": (C.c_int, []),
     "dg_version": (C.c_char_p, []),
     "dg_kernel_launches": (C.c_long, []),
+    "dg_release_pool": (C.c_int, []),
     "dg_profile_spmv": (C.c_int, [vp, vp, vp, C.c_int, C.c_size_t, P(C.c_float)]),
     "dg_matrix_create": (C.c_int, [C.c_int, lp, ip, dp, C.c_int, C.c_int, P(vp)]),
     "dg_matrix_create_device": (C.c_int, [C.c_int, C.c_long, vp, vp, vp, C.c_int, C.c_int, P(vp)]),
@@ -96,6 +97,12 @@ SIGNATURES = {
     "dg_linear_solve": (C.c_int, [vp, C.c_double, vp, vp, C.c_double, C.c_int, C.c_int, ip]),
     "dg_residual_l1": (C.c_int, [vp, vp, C.c_double, dp]),
     "dg_cg_noalloc": (C.c_int, [C.c_int, vp, vp, vp, C.c_double, vp, vp, C.c_double, C.c_int, ip]),
+    "dg_ed_dim": (C.c_int, [P(abi.dg_ed_model), lp]),
+    "dg_ed_build": (C.c_int, [P(abi.dg_ed_model), P(vp)]),
+    "dg_ed_free": (None, [vp]),
+    "dg_ed_info": (C.c_int, [vp, lp, lp]),
+    "dg_ed_download": (C.c_int, [vp, lp, lp, ip, dp]),
+    "dg_ed_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
 }
 
 DG_STORE_FULL, DG_STORE_LOWER_DIAG_LAST = 0, 1
@@ -147,11 +154,14 @@ def as_ptr(a):
 class DeviceMatrix:
     """A device-resident CRS operator (dg_matrix)."""
 
-    def __init__(self, crs: abi.Crs, storage: int = DG_STORE_FULL, values: int = DG_VALUES_F64):
+    def __init__(self, crs: abi.Crs | None, storage: int = DG_STORE_FULL, values: int = DG_VALUES_F64, handle=None):
         lib = load()
-        h = C.c_void_p()
-        check(lib.dg_matrix_create(crs.n, abi.ptr(crs.row, C.c_long), abi.ptr(crs.col, C.c_int),
-                                   abi.ptr(crs.val, C.c_double), storage, values, C.byref(h)))
+        if handle is not None:
+            h = handle
+        else:
+            h = C.c_void_p()
+            check(lib.dg_matrix_create(crs.n, abi.ptr(crs.row, C.c_long), abi.ptr(crs.col, C.c_int),
+                                       abi.ptr(crs.val, C.c_double), storage, values, C.byref(h)))
         self.h = h
         n, nnz, lanes, grid = C.c_int(), C.c_long(), C.c_int(), C.c_int()
         check(lib.dg_matrix_info(h, C.byref(n), C.byref(nnz), C.byref(lanes), C.byref(grid)))
@@ -219,6 +229,51 @@ class DeviceMatrix:
             y = np.empty(self.n, np.float32)
         check(load().dg_spmv_f32(self.h, as_ptr(x), as_ptr(y)))
         return y
+
+
+class EDSystem:
+    """Basis and Hamiltonian of one ED model, enumerated and assembled on the device (dg_ed)."""
+
+    def __init__(self, model):
+        self.model = model            # keeps the dg_ed_model storage alive
+        h = C.c_void_p()
+        check(load().dg_ed_build(C.byref(model.struct), C.byref(h)))
+        self.h = h
+        dim, nnz = C.c_long(), C.c_long()
+        check(load().dg_ed_info(h, C.byref(dim), C.byref(nnz)))
+        self.dim, self.nnz = dim.value, nnz.value
+
+    def close(self):
+        if self.h:
+            load().dg_ed_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def download(self):
+        """(basis, row, col, val) as numpy arrays."""
+        basis = np.empty(self.dim, np.int64)
+        row = np.empty(self.dim + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        val = np.empty(self.nnz, np.float64)
+        check(load().dg_ed_download(self.h, abi.ptr(basis, C.c_long), abi.ptr(row, C.c_long), abi.ptr(col, C.c_int),
+                                    abi.ptr(val, C.c_double)))
+        return basis, row, col, val
+
+    def matrix(self, values: int = DG_VALUES_F64) -> DeviceMatrix:
+        h = C.c_void_p()
+        check(load().dg_ed_matrix(self.h, values, C.byref(h)))
+        return DeviceMatrix(None, handle=h)
+
+
+def ed_dim(model) -> int:
+    dim = C.c_long()
+    check(load().dg_ed_dim(C.byref(model.struct), C.byref(dim)))
+    return dim.value
 
 
 def default_params(**kw) -> dg_solver_params:

@@ -1,0 +1,128 @@
+"""SpMV rate survey of the library's operator kernels on the named superblock matrices.
+
+    python -m dmrg_c_gb300.profile_spmv                      # heuristic and autotuned rates
+    python -m dmrg_c_gb300.profile_spmv --sweep              # every SELL shape / variant / window
+    python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --format sell --launches 3
+                                                             # a few launches, for an ncu capture
+
+Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
+256 MiB buffer before every launch so the matrix is not L2-resident, "warm" does not.
+Bytes per launch are the algorithmic CRS footprint nnz_full*12 + (n+1)*4 + 2*n*8.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+from . import lib as L
+from . import workloads
+
+CASES = {
+    "xxz_m64": workloads.xxz_superblock_m64,
+    "klm_m128": workloads.klm_superblock_m128,
+    "hubbard_m512": workloads.hubbard_superblock_m512,
+}
+FLUSH = 256 << 20
+
+
+def algorithmic_bytes(n, nnz_full, s_val=8, s_vec=8):
+    return nnz_full * (s_val + 4) + (n + 1) * 4 + 2 * n * s_vec
+
+
+def _sell_grid(n, ws, sms):
+    slices = (n + 31) // 32
+    per_block = 8 // ws            # slices one 256-thread block covers per trip
+    return max(1, min(sms * 16, (slices + per_block - 1) // per_block))
+
+
+def _csr_grid(n, lanes, sms):
+    return max(1, min(sms * 16, (n * lanes + 255) // 256))
+
+
+def _rate(m, x, y, iters):
+    cold = m.profile_spmv(x, y, iters=iters, flush_bytes=FLUSH)
+    warm = m.profile_spmv(x, y, iters=iters)
+    return cold, warm
+
+
+def survey(names, sweep, iters, out):
+    import torch
+    rows = []
+    for name in names:
+        low = CASES[name](0).explicit_lower()
+        m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST)
+        n, nnz = m.n, m.nnz
+        B = algorithmic_bytes(n, nnz)
+        x = torch.randn(n, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        sms = torch.cuda.get_device_properties(x.device).multi_processor_count
+        c, w = _rate(m, x, y, iters)
+        print(f"## {name}: n={n} nnz_full={nnz} bytes={B / 1e6:.1f} MB", flush=True)
+        print(f"   heuristic: cold {c * 1e3:7.1f} us ({B / c / 1e6:5.0f} GB/s)  warm {w * 1e3:7.1f} us "
+              f"({B / w / 1e6:5.0f} GB/s)", flush=True)
+        rows.append(dict(case=name, kind="heuristic", n=n, nnz_full=nnz, bytes=B, cold_us=c * 1e3, warm_us=w * 1e3))
+        if sweep:
+            for window in (2048, 32):
+                m.set_sell_window(window)
+                for ws in (1, 2, 4, 8):
+                    for var in range(4):
+                        m.set_sell_shape(ws, _sell_grid(n, ws, sms))
+                        m.set_sell_variant(var)
+                        c, w = _rate(m, x, y, iters)
+                        print(f"   sell win={window:4d} ws={ws} var={var}: cold {c * 1e3:7.1f} us "
+                              f"({B / c / 1e6:5.0f} GB/s)  warm {w * 1e3:7.1f} us ({B / w / 1e6:5.0f} GB/s)", flush=True)
+                        rows.append(dict(case=name, kind="sell", window=window, ws=ws, variant=var, bytes=B,
+                                         cold_us=c * 1e3, warm_us=w * 1e3))
+            for lanes in (2, 4, 8, 16, 32):
+                m.set_shape(lanes, _csr_grid(n, lanes, sms))
+                c, w = _rate(m, x, y, iters)
+                print(f"   csr lanes={lanes:2d}: cold {c * 1e3:7.1f} us ({B / c / 1e6:5.0f} GB/s)  warm "
+                      f"{w * 1e3:7.1f} us ({B / w / 1e6:5.0f} GB/s)", flush=True)
+                rows.append(dict(case=name, kind="csr", lanes=lanes, bytes=B, cold_us=c * 1e3, warm_us=w * 1e3))
+        r = m.autotune(iters=5)
+        c, w = _rate(m, x, y, iters)
+        print(f"   autotuned (format={r.format} shape={r.shape} variant={r.variant} window={r.window} grid={r.grid}): "
+              f"cold {c * 1e3:7.1f} us ({B / c / 1e6:5.0f} GB/s)  warm {w * 1e3:7.1f} us ({B / w / 1e6:5.0f} GB/s)",
+              flush=True)
+        rows.append(dict(case=name, kind="autotuned", format=r.format, shape=r.shape, variant=r.variant,
+                         window=r.window, grid=r.grid, bytes=B, cold_us=c * 1e3, warm_us=w * 1e3))
+        del m
+    if out:
+        with open(out, "w") as f:
+            json.dump(rows, f, indent=1)
+
+
+def launches(name, fmt, count):
+    """`count` launches of one kernel on one matrix (nothing else on the device after setup)."""
+    import torch
+    low = CASES[name](0).explicit_lower()
+    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST)
+    x = torch.randn(m.n, dtype=torch.float64, device="cuda")
+    if fmt == "csr":
+        m.set_shape(8, _csr_grid(m.n, 8, torch.cuda.get_device_properties(x.device).multi_processor_count))
+    y = torch.empty_like(x)
+    t = m.profile_spmv(x, y, iters=count)
+    B = algorithmic_bytes(m.n, m.nnz)
+    print(f"{name} {fmt}: {t * 1e3:.1f} us per launch ({B / t / 1e6:.0f} GB/s), n={m.n} nnz_full={m.nnz}")
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--cases", nargs="*", default=list(CASES), choices=list(CASES))
+    ap.add_argument("--sweep", action="store_true")
+    ap.add_argument("--iters", type=int, default=10)
+    ap.add_argument("--json", default=None)
+    ap.add_argument("--case", choices=list(CASES), default=None)
+    ap.add_argument("--format", choices=["sell", "csr"], default="sell")
+    ap.add_argument("--launches", type=int, default=3)
+    a = ap.parse_args(argv)
+    if a.case:
+        launches(a.case, a.format, a.launches)
+    else:
+        survey(a.cases, a.sweep, a.iters, a.json)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -97,7 +97,8 @@ typedef enum {
    DG_ERR_NOCONV = 4,     /* iteration limit reached without convergence              */
    DG_ERR_TIMEOUT = 5,    /* a bounded host wait on device progress ran out           */
    DG_ERR_NODEVICE = 6,   /* no CUDA device                                           */
-   DG_ERR_MATRIX = 7      /* CRS invariant violated (row order, column range, diag)   */
+   DG_ERR_MATRIX = 7,     /* CRS invariant violated (row order, column range, diag)   */
+   DG_ERR_INTERNAL = 8    /* an internal consistency check failed                     */
 } dg_status;
 
 /* Text of the last error raised on the calling thread ("" when none). */
@@ -108,6 +109,12 @@ int dg_device_count(void);
 const char *dg_version(void);
 /* Kernel launches issued by this library since the process started. */
 long dg_kernel_launches(void);
+
+/* Device memory the library allocates comes from its own stream-ordered pool, one per
+ * device; freed blocks stay cached (up to DG_POOL_KEEP_MB, default 8192) so repeated solves
+ * do not call cudaMalloc / cudaFree.  dg_release_pool returns the cached blocks of the
+ * current device to the system.  (No counterpart in the reference.) */
+int dg_release_pool(void);
 
 /* Opaque device-resident sparse operator (full CRS on the device, FP64 values and,
  * optionally, an FP32 copy of the values for the mixed-precision form). */

@@ -12,7 +12,7 @@
 #ifndef DMRG_GB300_ED_H
 #define DMRG_GB300_ED_H
 
-#include "dmrg_gb300_types.h"
+#include "dmrg_gb300.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -52,6 +52,25 @@ typedef struct {
    const dg_ed_term *terms;
    const int *n_ele;       /* [d] electrons per local state (fermion signs), may be NULL */
 } dg_ed_model;
+
+/* ---- ED build on the device (no counterpart with this signature in the reference) ----
+ * Replaces the model driver's FIND_DIM / GET_BASIS / GET_HAM
+ * (main/exact_diag/klm_vf/src/FIND_DIM.c:11-61, GET_BASIS.c:11-55, GET_HAM.c:11-92 with
+ * MAKE_ELEMENT_HAM.c:11-76): the same ascending basis codes and the same full CRS (columns
+ * ascending, explicit diagonal, |v| <= 1e-15 dropped), bit for bit, built on the GPU.
+ * Limits: d^L < 2^62, sector dimension < 2^31, at most 256 generated elements per row. */
+typedef struct dg_ed dg_ed;
+
+/* Sector dimension (host only, no device work). */
+int dg_ed_dim(const dg_ed_model *model, long *dim);
+/* Enumerate the basis and assemble H on the current device. */
+int dg_ed_build(const dg_ed_model *model, dg_ed **out);
+void dg_ed_free(dg_ed *ed);
+int dg_ed_info(const dg_ed *ed, long *dim, long *nnz);
+/* Copy basis[dim], row[dim+1], col[nnz], val[nnz] to host arrays (any may be NULL). */
+int dg_ed_download(const dg_ed *ed, long *basis, long *row, int *col, double *val);
+/* A solver operator (dg_matrix, full storage) built from the device CRS. */
+int dg_ed_matrix(const dg_ed *ed, int values, dg_matrix **out);
 
 #ifdef __cplusplus
 }

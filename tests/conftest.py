@@ -67,3 +67,13 @@ def rng():
 
 def pytest_collection_modifyitems(config, items):
     os.environ.setdefault("OMP_NUM_THREADS", str(min(8, os.cpu_count() or 1)))
+
+
+def klm_model_from_golden(g, tag):
+    """The KLM chain of a klm_ed.npz fixture as a dg_ed_model (site operators from the
+    reference's own onsite_op builders, stored in the fixture)."""
+    from dmrg_c_gb300 import ed_models
+    L, ne, sz, t, I_z, I_xy = g[f"{tag}_params"]
+    tabs = [(g[f"{tag}_op{k}_row"], g[f"{tag}_op{k}_col"], g[f"{tag}_op{k}_val"]) for k in range(9)]
+    return ed_models.klm_chain_from_tables(int(L), tabs, int(ne), int(sz), t=float(t), I_z=float(I_z), I_xy=float(I_xy),
+                                           bc="PBC" if tag == "pbc" else "OBC")

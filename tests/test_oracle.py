@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from conftest import golden
+from conftest import golden, klm_model_from_golden
 from dmrg_c_gb300 import abi, ed_models, superblock
 
 
@@ -68,13 +68,6 @@ def test_tridiag_matches_dstev_golden(oracle):
     w, z = oracle.tridiag_eig(g["d"], g["e"])
     np.testing.assert_allclose(w, g["w"], rtol=0, atol=1e-12)
     assert abs(abs(z[:, 0] @ g["z0"]) - 1) < 1e-12
-
-
-def klm_model_from_golden(g, tag):
-    L, ne, sz, t, I_z, I_xy = g[f"{tag}_params"]
-    tabs = [(g[f"{tag}_op{k}_row"], g[f"{tag}_op{k}_col"], g[f"{tag}_op{k}_val"]) for k in range(9)]
-    return ed_models.klm_chain_from_tables(int(L), tabs, int(ne), int(sz), t=float(t), I_z=float(I_z), I_xy=float(I_xy),
-                                           bc="PBC" if tag == "pbc" else "OBC")
 
 
 @pytest.mark.parametrize("tag", ["obc", "pbc"])
