@@ -142,13 +142,13 @@ def spmv_bytes(n, nnz_full, s_val=8, s_vec=8):
 
 
 def traffic_from_profile(workload):
-    """dram bytes per launch of the SpMV kernel from the committed ncu summary, if present."""
-    f = ROOT / "profiles" / f"spmv_{workload}.json"
+    """DRAM bytes (read + write) per launch of the SpMV kernel, from the committed ncu summary
+    of this workload (profiles/k_apply_sell_<workload>.md), if present."""
+    f = ROOT / "profiles" / f"k_apply_sell_{workload}.md"
     if f.exists():
-        try:
-            return json.loads(f.read_text()).get("traffic_bytes_per_launch")
-        except ValueError:
-            return None
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
     return None
 
 

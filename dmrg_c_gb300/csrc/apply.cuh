@@ -1,7 +1,9 @@
 // apply.cuh -- the fused operator-application kernel.
 //
 // One launch computes y = (H + sigma I) (s x) for every row, where s is an optional scale
-// read from a device scalar (the lazily applied normalisation of a Krylov vector), and
+// read from a device scalar (the lazily applied normalisation of a Krylov vector; CRS and
+// SELL operators apply it once per row to the finished sum, s (H x)_i, rather than to every
+// gathered x_j: FP64 instructions are the scarce resource on GB300), and
 // hands each finished row to an epilogue that may store outputs and contribute to one
 // grid-wide deterministic reduction (a dot product, a residual norm, ...).  The epilogue's
 // finalize() runs once, in the last block, with the reduced total.
@@ -13,8 +15,9 @@
 // a fixed xor-shuffle tree, so every y_i is bitwise reproducible run to run.
 //
 // Operators (Op) provide
+//   static constexpr bool kPostScale;   // row_partial ignores s; the kernel scales the row sum
 //   __device__ double row_partial<L>(int i, int lane, const XT *x, double s) const;
-// returning the lane's partial sum of H[i][:] . (s x).
+// returning the lane's partial sum of H[i][:] . (s x) (of H[i][:] . x when kPostScale).
 #pragma once
 
 #include "common.cuh"
@@ -36,19 +39,16 @@ __device__ __forceinline__ double to_d(T v) { return (double)v; }
 // Full CRS row operator; VT is the stored value type (double, or float for the mixed form).
 template <class VT>
 struct CrsOp {
+  static constexpr bool kPostScale = true;
   const int64_t *__restrict__ row;
   const int *__restrict__ col;
   const VT *__restrict__ val;
 
   template <int L, class XT>
-  __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double s) const {
+  __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double) const {
     const int64_t b = row[i], e = row[i + 1];
     double sum = 0.0;
-    if (s == 1.0) {
-      for (int64_t k = b + lane; k < e; k += L) sum += to_d(val[k]) * to_d(x[col[k]]);
-    } else {
-      for (int64_t k = b + lane; k < e; k += L) sum += to_d(val[k]) * (to_d(x[col[k]]) * s);
-    }
+    for (int64_t k = b + lane; k < e; k += L) sum += to_d(val[k]) * to_d(x[col[k]]);
     return sum;
   }
 };
@@ -66,6 +66,7 @@ template <int L, class Op, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
 k_apply(Op op, int n, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma,
         const int *gate, Epi epi, RedSlot slot) {
+  pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
   const double s = load_scale(scale_src, scale_mode);
   constexpr int RPW = 32 / L;   // rows per warp trip
@@ -79,12 +80,14 @@ k_apply(Op op, int n, const XT *__restrict__ x, const double *scale_src, int sca
     const bool valid = i < n;
     double part = valid ? op.template row_partial<L>(i, lane, x, s) : 0.0;
     part = lanes_sum<L>(part);
+    if (Op::kPostScale && s != 1.0) part *= s;
     if (valid && lane == 0) {
       const double xi = (s == 1.0) ? to_d(x[i]) : to_d(x[i]) * s;
       const double yi = (sigma == 0.0) ? part : part + sigma * xi;
       epi.row(i, xi, yi, acc);
     }
   }
+  pdl_trigger();
   if (Epi::kReduce) {
     grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
   }

@@ -133,6 +133,35 @@ struct Mapped {
   }
 };
 
+// ---------------------------------------------------------------------------------
+// Programmatic dependent launch.  Kernels of the iterative loops are launched with the
+// programmatic-stream-serialisation attribute, so a kernel's blocks can be scheduled while
+// the previous kernel on the stream is still finishing (its reduction tail, its memory
+// flush); each such kernel executes pdl_wait() before its first read of anything earlier
+// work produced, which blocks until the previous grid has completed and its writes are
+// visible.  pdl_trigger() lets the next kernel's launch begin early.  In a kernel launched
+// without the attribute both are no-ops.
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  DG_CUDA(cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...));
+  count_launch();
+}
+
 // Is p a device (or managed) pointer?  Plain host memory (malloc) is "unregistered".
 bool is_device_ptr(const void *p);
 

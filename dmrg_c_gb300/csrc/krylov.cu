@@ -29,6 +29,7 @@ __global__ void k_random_start(double *x, int n, unsigned long long seed) {
 __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__restrict__ p, const double *__restrict__ y,
                                                        double *__restrict__ x, double *__restrict__ r, Scalars *S,
                                                        double acc_thr, int it, int max_step, Progress *prog, RedSlot slot) {
+  pdl_wait();
   if (*((volatile int *)&S->done)) return;
   const double a = S->a;
   double acc = 0.0;
@@ -38,6 +39,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__r
     r[i] = ri;
     acc += ri * ri;
   }
+  pdl_trigger();
   grid_reduce(acc, slot, [&](double t) {
     if (t < acc_thr) {
       S->done = 1;
@@ -58,9 +60,11 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__r
 
 __global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p,
                                                           const Scalars *S) {
+  pdl_wait();
   if (*((volatile const int *)&S->done)) return;
   const double b = S->beta;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) p[i] = r[i] + b * p[i];
+  pdl_trigger();
 }
 
 // V2 = Temp - delta V1 - gamma0 V0, gamma1 = ||V2||, Givens rotation, eta update and the
@@ -68,6 +72,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *
 __global__ void __launch_bounds__(kThreads) k_mr_lanczos(int n, const double *__restrict__ temp, const double *__restrict__ v1n,
                                                         const double *__restrict__ v0, double *__restrict__ v2, Scalars *S,
                                                         double acc_thr, int it, int max_step, Progress *prog, RedSlot slot) {
+  pdl_wait();
   if (*((volatile int *)&S->done)) return;
   const double delta = S->delta, g0 = S->gamma0;
   double acc = 0.0;
@@ -76,6 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_mr_lanczos(int n, const double *__
     v2[i] = v;
     acc += v * v;
   }
+  pdl_trigger();
   grid_reduce(acc, slot, [&](double t) {
     const double gamma1 = sqrt(t);
     const double c0 = S->c0, c1 = S->c1, s0 = S->s0, s1 = S->s1;
@@ -115,6 +121,7 @@ __global__ void __launch_bounds__(kThreads) k_mr_lanczos(int n, const double *__
 __global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__restrict__ v1n, const double *__restrict__ w0,
                                                        const double *__restrict__ w1, double *__restrict__ w2,
                                                        double *__restrict__ x, const Scalars *S) {
+  pdl_wait();
   if (*((volatile const int *)&S->done)) return;
   const double ia = S->inv_alpha1, a2 = S->alpha2, a3 = S->alpha3, ce = S->c2 * S->eta_old;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {

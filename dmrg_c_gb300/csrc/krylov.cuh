@@ -172,6 +172,7 @@ template <class VT>
 __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__restrict__ y, const VT *__restrict__ v,
                                                        const VT *__restrict__ vprev, const double *D, const double *O,
                                                        int b, double *__restrict__ w, double *r2, RedSlot slot) {
+  pdl_wait();
   const double d = D[b];
   const double o = (b > 0) ? O[b] : 0.0;
   double acc = 0.0;
@@ -181,6 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__r
     w[i] = wi;
     acc += wi * wi;
   }
+  pdl_trigger();
   grid_reduce(acc, slot, [&](double t) { *r2 = t; });
 }
 
@@ -389,8 +391,8 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
   };
   auto enqueue_update = [&](int b) {
     const double *vprev = (b > 0) ? V + (size_t)(b - 1) * n : nullptr;
-    k_lz_update<double><<<ws.vgrid, kThreads, 0, st>>>(n, y.get(), V + (size_t)b * n, vprev, D.get(), O.get(), b, w_dev,
-                                                     &S->r2, slot); ::dg::count_launch();
+    launch_pdl(k_lz_update<double>, ws.vgrid, kThreads, st, n, (const double *)y.get(), (const double *)(V + (size_t)b * n),
+               vprev, (const double *)D.get(), (const double *)O.get(), b, w_dev, &S->r2, slot);
     DG_CUDA(cudaGetLastError());
     if (cfg.reorth) {
       for (int pass = 0; pass < 2; ++pass) {
@@ -551,8 +553,8 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
       op.apply(p.get(), (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgAlpha{y.get(), S}, slot, st);
-      k_cg_update<<<ws.vgrid, kThreads, 0, st>>>(n, p.get(), y.get(), x_dev, r.get(), S, acc, it, max_step, ws.prog.d, slot); ::dg::count_launch();
-      k_cg_direction<<<ws.vgrid, kThreads, 0, st>>>(n, r.get(), p.get(), S); ::dg::count_launch();
+      launch_pdl(k_cg_update, ws.vgrid, kThreads, st, n, p.get(), y.get(), x_dev, r.get(), S, acc, it, max_step, ws.prog.d, slot);
+      launch_pdl(k_cg_direction, ws.vgrid, kThreads, st, n, r.get(), p.get(), S);
     }
     DG_CUDA(cudaGetLastError());
     enq = std::max(enq, last);
@@ -613,9 +615,9 @@ IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double 
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
       op.apply(vb[i1].get(), &S->gamma0, SCALE_RECIP, sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
-      k_mr_lanczos<<<ws.vgrid, kThreads, 0, st>>>(n, temp.get(), vb[i2].get(), vb[i0].get(), vb[i3].get(), S, acc, it, max_step,
-                                                   ws.prog.d, slot); ::dg::count_launch();
-      k_mr_update<<<ws.vgrid, kThreads, 0, st>>>(n, vb[i2].get(), wb[j0].get(), wb[j1].get(), wb[j2].get(), x_dev, S); ::dg::count_launch();
+      launch_pdl(k_mr_lanczos, ws.vgrid, kThreads, st, n, temp.get(), vb[i2].get(), vb[i0].get(), vb[i3].get(), S, acc, it,
+                 max_step, ws.prog.d, slot);
+      launch_pdl(k_mr_update, ws.vgrid, kThreads, st, n, vb[i2].get(), wb[j0].get(), wb[j1].get(), wb[j2].get(), x_dev, S);
       // V0 <- V1n, V1 <- V2 ; W0 <- W1, W1 <- W2
       int o0 = i0, o1 = i1;
       i0 = i2;

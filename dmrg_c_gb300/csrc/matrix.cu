@@ -229,8 +229,13 @@ void choose_sell_shape(int nslices, long stored, int *ws, int *grid) {
   const double per_row = nslices > 0 ? (double)stored / ((double)nslices * kSellC) : 0.0;
   int w = 1;
   if (per_row >= 24.0) {
+    // Split a slice over more warps while each keeps >= 32 elements of every row, or, for
+    // matrices too small to fill the GPU, while each keeps >= 8 and the doubled warp count
+    // stays under a quarter of the target.
     w = 2;
-    while (w < 8 && (long)nslices * w < target_warps && per_row / (2 * w) >= 16.0) w <<= 1;
+    while (w < 8 && (long)nslices * w < target_warps &&
+           (per_row / (2 * w) >= 32.0 || ((long)nslices * 2 * w <= target_warps / 4 && per_row / (2 * w) >= 8.0)))
+      w <<= 1;
   }
   const int groups = kWarps / w;
   const long need = (nslices + groups - 1) / groups;

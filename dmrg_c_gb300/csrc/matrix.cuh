@@ -44,12 +44,12 @@ template <class Op, class XT, class Epi>
 void launch_apply(const Op &op, int lanes, int grid, int n, const XT *x, const double *scale_src, int scale_mode,
                   double sigma, const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
   switch (lanes) {
-    case 1: k_apply<1><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
-    case 2: k_apply<2><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
-    case 4: k_apply<4><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
-    case 8: k_apply<8><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
-    case 16: k_apply<16><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
-    default: k_apply<32><<<grid, kThreads, 0, st>>>(op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); ::dg::count_launch(); break;
+    case 1: launch_pdl(k_apply<1, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case 2: launch_pdl(k_apply<2, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case 4: launch_pdl(k_apply<4, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case 8: launch_pdl(k_apply<8, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case 16: launch_pdl(k_apply<16, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    default: launch_pdl(k_apply<32, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
   }
   DG_CUDA(cudaGetLastError());
 }
@@ -59,10 +59,10 @@ template <int WS, class VT, class XT, class Epi>
 void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, const double *scale_src, int scale_mode, double sigma,
                     const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
   switch (op.variant) {
-    case V_U4: k_apply_sell<WS, V_U4, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case V_U16: k_apply_sell<WS, V_U16, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case V_PIPE8: k_apply_sell<WS, V_PIPE8, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    default: k_apply_sell<WS, V_U8, VT, XT, Epi><<<grid, kThreads, 0, st>>>(op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_U4: launch_pdl(k_apply_sell<WS, V_U4, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_U16: launch_pdl(k_apply_sell<WS, V_U16, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_PIPE8: launch_pdl(k_apply_sell<WS, V_PIPE8, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    default: launch_pdl(k_apply_sell<WS, V_U8, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
   }
 }
 
@@ -75,7 +75,6 @@ void launch_sell(const SellOp<VT> &op, int grid, const XT *x, const double *scal
     case 4: launch_sell_ws<4>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
     default: launch_sell_ws<8>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
   }
-  ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
 }
 

@@ -40,6 +40,7 @@ struct ObcOp {
     return (long)ll * d * dim_RR * d + (long)lr * dim_RR * d + (long)(rr * d + rl);
   }
 
+  static constexpr bool kPostScale = false;   // the reference scales each gathered element
   template <int L, class XT>
   __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double s) const {
     const int ll = LL[i], lr = LR[i], rr = RR[i], rl = RL[i];

@@ -62,8 +62,7 @@ __device__ __forceinline__ T ld_vec(const T *p) {
 // Sum of this warp's share of one slice row.  WS warps share a slice: warp `sub` takes the
 // row elements k = sub, sub + WS, sub + 2 WS, ...; each lane owns one row.
 template <int WS, int U, bool PIPE, bool STREAM, class VT, class XT>
-__device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t base, int w, int sub, const XT *__restrict__ x,
-                                               double s) {
+__device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t base, int w, int sub, const XT *__restrict__ x) {
   const int cnt = (w > sub) ? (w - sub + WS - 1) / WS : 0;   // elements of this warp
   const int G = cnt / U;
   const int64_t step = (int64_t)WS * kSellC;
@@ -101,18 +100,13 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
         v[u] = to_d(ld_mat<STREAM>(op.val + pn + u * step));
       }
     }
-    if (s == 1.0) {
 #pragma unroll
-      for (int u = 0; u < U; ++u) sum += vc[u] * xv[u];
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; ++u) sum += vc[u] * (xv[u] * s);
-    }
+    for (int u = 0; u < U; ++u) sum += vc[u] * xv[u];
   }
   for (int j = G * U; j < cnt; ++j) {
     const int64_t p = p0 + (int64_t)j * step;
     const double xv = to_d(ld_vec<STREAM>(x + ld_mat<STREAM>(op.col + p)));
-    sum += to_d(ld_mat<STREAM>(op.val + p)) * ((s == 1.0) ? xv : xv * s);
+    sum += to_d(ld_mat<STREAM>(op.val + p)) * xv;
   }
   return sum;
 }
@@ -121,6 +115,7 @@ template <int WS, int VAR, class VT, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
 k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma, const int *gate,
              Epi epi, RedSlot slot) {
+  pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
   constexpr int U = (VAR == V_U4) ? 4 : (VAR == V_U16) ? 16 : 8;
   constexpr bool PIPE = (VAR == V_PIPE8);
@@ -137,7 +132,8 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, i
     const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
     for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
       const int row = op.perm[sl * kSellC + lane];
-      const double sum = sell_row_sum<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x, s);
+      double sum = sell_row_sum<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x);
+      if (s != 1.0) sum *= s;   // s (H x)_i: one multiply per row instead of one per element
       if (row >= 0) {
         const double xi = (s == 1.0) ? to_d(x[row]) : to_d(x[row]) * s;
         const double yi = (sigma == 0.0) ? sum : sum + sigma * xi;
@@ -148,12 +144,13 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, i
     for (int sl0 = blockIdx.x * GROUPS; sl0 < op.nslices; sl0 += gridDim.x * GROUPS) {
       const int sl = sl0 + group;
       const bool live = sl < op.nslices;
-      double sum = live ? sell_row_sum<WS, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], sub, x, s) : 0.0;
+      double sum = live ? sell_row_sum<WS, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], sub, x) : 0.0;
       part[WS > 1 ? wib : 0][lane] = sum;
       __syncthreads();
       if (sub == 0) {
 #pragma unroll
         for (int j = 1; j < WS; ++j) sum += part[WS > 1 ? wib + j : 0][lane];
+        if (s != 1.0) sum *= s;
       }
       __syncthreads();
       if (live && sub == 0) {
@@ -166,6 +163,7 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, i
       }
     }
   }
+  pdl_trigger();
   if constexpr (Epi::kReduce) {
     grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
   }

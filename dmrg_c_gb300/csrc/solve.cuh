@@ -60,7 +60,7 @@ inline LanczosCfg lanczos_cfg_from(const dg_solver_params &p) {
   c.slow = p.lanczos_slow != 0;
   c.reorth = false;
   c.accept_at_end = false;
-  c.lookahead = p.lookahead > 0 ? p.lookahead : 4;
+  c.lookahead = p.lookahead > 0 ? p.lookahead : 2;
   return c;
 }
 
