@@ -174,7 +174,7 @@ class dg_solve_info(C.Structure):
     """include/dmrg_gb300.h: dg_solve_info"""
     _fields_ = [("eig_val", C.c_double), ("error", C.c_double), ("lanczos_steps", C.c_int), ("ii_steps", C.c_int),
                 ("cg_steps", C.c_int), ("spmv_count", C.c_int), ("converged", C.c_int), ("ii_converged", C.c_int),
-                ("dense", C.c_int), ("ms_lanczos", C.c_double), ("ms_ii", C.c_double)]
+                ("dense", C.c_int), ("ms_lanczos", C.c_double), ("ms_ii", C.c_double), ("eig_lanczos", C.c_double)]
 
 
 class dg_tune_result(C.Structure):

@@ -2,6 +2,7 @@
 #include <cstdlib>
 
 #include "krylov.cuh"
+#include "sell.cuh"
 #include "matrix.cuh"
 #include "solve.cuh"
 
@@ -129,6 +130,98 @@ __global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__r
     w2[i] = w;
     x[i] = x[i] + ce * w;
   }
+}
+
+// ---- mixed-precision Lanczos ----------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
+                                                    int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
+                                                    float *__restrict__ coef, unsigned *ticket) {
+  pdl_wait();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.y * kWarps + warp;
+  const int chunk = blockIdx.x;
+  if (j < nvec) {
+    const long r0 = (long)chunk * kMxChunk;
+    const long r1 = r0 + kMxChunk < (long)n ? r0 + kMxChunk : (long)n;
+    const float *vj = V + (long)j * ldv;
+    AccDot2 acc;
+    long i = r0 + lane;
+    for (; i + 96 < r1; i += 128) {   // four loads in flight per lane
+      float a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = vj[i + 32 * u];
+        b[u] = y[i + 32 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc.add(a[u], b[u]);
+    }
+    for (; i < r1; i += 32) acc.add(vj[i], y[i]);
+    const double t = warp_sum(acc.get());
+    if (lane == 0) partials[(long)j * nchunk + chunk] = t;
+  }
+  pdl_trigger();
+  // The last block sums the chunk partials of every vector (one warp per vector, fixed
+  // order) into the subtraction coefficients coef_j = -sig_j^2 <V_j, y>.
+  __shared__ bool s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned nblocks = gridDim.x * gridDim.y;
+    s_last = atomicAdd(ticket, 1u) == nblocks - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int jj = warp; jj < nvec; jj += kWarps) {
+    double c = 0.0;
+    for (int ch = lane; ch < nchunk; ch += 32) c += __ldcg(partials + (long)jj * nchunk + ch);
+    c = warp_sum(c);
+    if (lane == 0) coef[jj] = (float)(-c * sig[jj] * sig[jj]);
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef_g,
+                                                    const float *__restrict__ y, int n, double *r2, RedSlot slot) {
+  pdl_wait();
+  extern __shared__ float coef[];   // nvec entries
+  for (int j = threadIdx.x; j < nvec; j += blockDim.x) coef[j] = coef_g[j];
+  __syncthreads();
+  float *vout = V + (long)nvec * ldv;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    AccDot2 a;
+    a.p = y[i];
+    int j = 0;
+    for (; j + 8 <= nvec; j += 8) {   // eight loads in flight per thread
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = V[(long)(j + u) * ldv + i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) a.add(coef[j + u], v[u]);
+    }
+    for (; j < nvec; ++j) a.add(coef[j], V[(long)j * ldv + i]);
+    const double w = a.get();
+    vout[i] = (float)w;
+    acc += w * w;
+  }
+  pdl_trigger();
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+}
+
+__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
+                                                     const double *__restrict__ sig, double *__restrict__ out, int n, double *r2,
+                                                     RedSlot slot) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double t = 0.0;
+    for (int j = 0; j < k; ++j) t = t + (s[j] * sig[j]) * (double)V[(long)j * ldv + i];
+    out[i] = t;
+    acc += t * t;
+  }
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
 }
 
 }  // namespace dg

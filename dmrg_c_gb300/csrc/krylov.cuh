@@ -37,6 +37,7 @@ struct Scalars {
   double beta;      // CG: beta
   double res;       // residual / dot output
   double gamma0, gamma1, delta, eta, eta_old, c0, c1, c2, s0, s1, s2, inv_alpha1, alpha2, alpha3;  // MINRES
+  double pq, gp, thr;   // refinement CG: <p,q>, <g,p>, stopping threshold on <res,res>
   int done;         // 0 running, 1 converged, 2 iteration limit
   int iters;
 };
@@ -139,11 +140,13 @@ __global__ void k_random_start(double *x, int n, unsigned long long seed);
 // ---- Lanczos -----------------------------------------------------------------------
 
 // Operator epilogue of Lanczos step b: y = H v_b, V[b] = v_b, D[b] = <y, v_b>
-// (sml/LANCZOS_SYM.c:139-143); mirrors D[b], O[b] to the host.
-template <class VT>
+// (sml/LANCZOS_SYM.c:139-143); mirrors D[b], O[b] to the host.  In the mixed form the
+// Krylov vector is already stored (unnormalised, FP32) before the product: vout is null and
+// sig[b] records its normalisation 1/||w_b||.
+template <class VT, class YT = double>
 struct EpiLanczos {
   static constexpr bool kReduce = true;
-  double *y;
+  YT *y;
   VT *vout;
   double *D, *O;         // device recurrence arrays
   double *hD, *hO;       // mapped host mirrors
@@ -151,15 +154,17 @@ struct EpiLanczos {
   const double *r2;      // <w,w> that normalised v_b
   int b;
   int stamp;
+  double *sig = nullptr;
   __device__ void row(int i, double xi, double yi, double &acc) const {
-    y[i] = yi;
-    vout[i] = (VT)xi;
+    y[i] = (YT)yi;
+    if (vout) vout[i] = (VT)xi;
     acc += yi * xi;
   }
   __device__ void finalize(double t) const {
     const double o = (b > 0) ? sqrt(*r2) : 0.0;   // Off_Diag[b] = sqrt(<w,w>)  (:135)
     D[b] = t;
     O[b] = o;
+    if (sig) sig[b] = 1.0 / sqrt(*r2);
     hD[b] = t;
     hO[b] = o;
     __threadfence_system();
@@ -227,6 +232,29 @@ __global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, lon
   }
   grid_reduce(acc, slot, [&](double t) { *r2 = t; });
 }
+
+// ---- Lanczos, mixed-precision form ---------------------------------------------------
+// Krylov vectors are stored unnormalised in FP32 (V[j] = fl32(w_j), v_j = sig[j] V[j]); the
+// product gives y = H v_b in FP32 and every step orthogonalises y against all stored vectors
+// (classical Gram-Schmidt: c_j = <v_j, y>, w = y - sum_j c_j v_j), which subsumes the
+// three-term recurrence.  Dots and the subtraction use compensated FP32 arithmetic (Dot2),
+// the recurrence scalars and norms FP64.
+
+constexpr int kMxChunk = 1024;   // rows per dot-product chunk (one warp each)
+
+// partials[j * nchunk + chunk] = <V_j, y> over the chunk's rows, one warp per vector; the
+// last block reduces them (fixed order) to coef_j = -sig_j^2 <V_j, y> = -c_j sig_j with
+// c_j = <v_j, y>.  ticket: zero between uses.
+__global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
+                                                    int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
+                                                    float *__restrict__ coef, unsigned *ticket);
+// w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); *r2 = <w,w>.
+__global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
+                                                    const float *__restrict__ y, int n, double *r2, RedSlot slot);
+// out_i = sum_{j<k} s_j sig_j V_j[i] (FP64, j order); *r2 = <out,out>.
+__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
+                                                     const double *__restrict__ sig, double *__restrict__ out, int n, double *r2,
+                                                     RedSlot slot);
 
 // ---- CG ------------------------------------------------------------------------------
 
@@ -337,77 +365,164 @@ struct LanczosCfg {
   int min_step, max_step, max_block_step;
   bool tight;
   bool slow;             // LANCZOS_SLOW semantics: no restart, checks from block_step >= min_step
-  bool reorth;           // full reorthogonalisation (dense path and mixed form)
+  bool reorth;           // full reorthogonalisation (dense path)
   bool accept_at_end;    // dense path: the last step spans the whole space, accept it
+  bool mixed;            // FP32 operator and Krylov vectors, FP64 recurrence (mixed-precision form)
+  double mixed_rel;      // mixed form: |dE| <= mixed_rel * |E| also counts as converged
   int lookahead;
 };
 
-// Lanczos on operator op.  w_dev holds the start vector on entry (overwritten).  The
-// normalised Ritz vector is written to out_dev.
-template <class Opl>
-LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, double *out_dev, Workspace &ws) {
-  const int n = op.n();
-  cudaStream_t st = ws.st;
-  Scalars *S = ws.S();
-  LanczosResult res;
+// State shared by the host control loop and the device work of one Lanczos run.
+struct LzState {
+  int n, cap_max;
+  DevBuf<double> D, O, s_dev;
+  Mapped<double> hD, hO, hs;
+  int stamp = 0;         // operator applications enqueued
+  int spmv = 0;
+  LzState(int n_, int cap) : n(n_), cap_max(cap), D(cap + 1), O(cap + 1), s_dev(cap + 1), hD(cap + 1), hO(cap + 1), hs(cap + 1) {}
+  // Upload Ritz coefficients s[0..k) to s_dev (stream-ordered).
+  void upload_s(int k, const std::vector<double> &s, cudaStream_t st) {
+    for (int j = 0; j < k; ++j) hs.h[j] = s[j];
+    DG_CUDA(cudaMemcpyAsync(s_dev.get(), hs.h, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+  }
+};
 
-  // Krylov vectors one cycle can hold: LANCZOS_SLOW never restarts (its max_block_step is
-  // unused by the reference), LANCZOS restarts every max_block_step steps.
-  const int cycle_len = cfg.slow ? cfg.max_step : std::min(cfg.max_block_step, cfg.max_step);
-  const int cap_max = std::max(cycle_len, 1) + 1;
-  DevBuf<double> D(cap_max + 1), O(cap_max + 1), y(n), c(cap_max + 1);
-  Mapped<double> hD(cap_max + 1), hO(cap_max + 1), hs(cap_max + 1);
-  DevBuf<double> s_dev(cap_max + 1);
-
-  // Krylov basis storage, grown in a stream-ordered way.
-  double *V = nullptr;
+// Krylov basis storage of element type T, grown in a stream-ordered way.
+template <class T>
+struct KrylovBasis {
+  T *V = nullptr;
   int cap = 0;
-  auto ensure = [&](int need) {
+  long n = 0;
+  cudaStream_t st = nullptr;
+  KrylovBasis(long n_, cudaStream_t s) : n(n_), st(s) {}
+  KrylovBasis(const KrylovBasis &) = delete;
+  KrylovBasis &operator=(const KrylovBasis &) = delete;
+  ~KrylovBasis() { pool_free(V, st); }
+  void ensure(int need, int cap_max) {
     if (need <= cap) return;
-    int ncap = cap == 0 ? std::min(cap_max, std::max(need, 64)) : std::min(cap_max, std::max(need, 2 * cap));
-    double *nv = nullptr;
-    nv = static_cast<double *>(pool_alloc(sizeof(double) * (size_t)ncap * n, st));
+    const int ncap = cap == 0 ? std::min(cap_max, std::max(need, 64)) : std::min(cap_max, std::max(need, 2 * cap));
+    T *nv = static_cast<T *>(pool_alloc(sizeof(T) * (size_t)ncap * n, st));
     if (V) {
-      DG_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * (size_t)cap * n, cudaMemcpyDeviceToDevice, st));
+      DG_CUDA(cudaMemcpyAsync(nv, V, sizeof(T) * (size_t)cap * n, cudaMemcpyDeviceToDevice, st));
       pool_free(V, st);
     }
     V = nv;
     cap = ncap;
-  };
-  struct FreeV {
-    double **v;
-    cudaStream_t st;
-    ~FreeV() { pool_free(*v, st); }
-  } freev{&V, st};
+  }
+  T *vec(int j) const { return V + (size_t)j * n; }
+};
 
-  const RedSlot slot = ws.slot();
-  int stamp = 0;   // operator applications enqueued
-  auto enqueue_apply = [&](int b) {
-    ensure(b + 1);
-    ++stamp;
-    EpiLanczos<double> epi{y.get(), V + (size_t)b * n, D.get(), O.get(), hD.d, hO.d, ws.prog.d, &S->r2, b, stamp};
-    op.apply(w_dev, &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
-    ++res.spmv;
-  };
-  auto enqueue_update = [&](int b) {
-    const double *vprev = (b > 0) ? V + (size_t)(b - 1) * n : nullptr;
-    launch_pdl(k_lz_update<double>, ws.vgrid, kThreads, st, n, (const double *)y.get(), (const double *)(V + (size_t)b * n),
-               vprev, (const double *)D.get(), (const double *)O.get(), b, w_dev, &S->r2, slot);
-    DG_CUDA(cudaGetLastError());
+// FP64 form (the reference's LANCZOS*): the product normalises w on the fly and stores v_b
+// into the basis; the update kernel forms w_{b+1} by the three-term recurrence, plus two
+// Gram-Schmidt passes when cfg.reorth (dense path).
+template <class Opl>
+struct LzSteps64 {
+  const Opl &op;
+  const LanczosCfg &cfg;
+  Workspace &ws;
+  LzState &z;
+  double *w;             // start vector in, next unnormalised Krylov vector
+  DevBuf<double> y, c;
+  KrylovBasis<double> B;
+  LzSteps64(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
+      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), c(z_.cap_max + 1), B(z_.n, w_.st) {}
+  void begin_cycle() {}
+  void step(int b) {
+    cudaStream_t st = ws.st;
+    const int n = z.n;
+    Scalars *S = ws.S();
+    const RedSlot slot = ws.slot();
+    B.ensure(b + 1, z.cap_max);
+    ++z.stamp;
+    EpiLanczos<double> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, ws.prog.d, &S->r2, b, z.stamp};
+    op.apply(w, &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
+    ++z.spmv;
+    const double *vprev = (b > 0) ? B.vec(b - 1) : nullptr;
+    launch_pdl(k_lz_update<double>, ws.vgrid, kThreads, st, n, (const double *)y.get(), (const double *)B.vec(b), vprev,
+               (const double *)z.D.get(), (const double *)z.O.get(), b, w, &S->r2, slot);
     if (cfg.reorth) {
       for (int pass = 0; pass < 2; ++pass) {
-        k_multidot<double><<<std::min(b + 1, 1024), kThreads, 0, st>>>(V, n, b + 1, w_dev, n, c.get()); ::dg::count_launch();
-        k_multisub<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, b + 1, c.get(), w_dev, n, &S->r2, slot); ::dg::count_launch();
+        k_multidot<double><<<std::min(b + 1, 1024), kThreads, 0, st>>>(B.V, n, b + 1, w, n, c.get()); ::dg::count_launch();
+        k_multisub<double><<<ws.vgrid, kThreads, 0, st>>>(B.V, n, b + 1, c.get(), w, n, &S->r2, slot); ::dg::count_launch();
       }
       DG_CUDA(cudaGetLastError());
     }
-  };
+  }
+  // dst = sum_{j<k} s_j v_j with <dst,dst> in S->r2
+  void combine(int k, const std::vector<double> &s, double *dst) {
+    z.upload_s(k, s, ws.st);
+    k_ritz<double><<<ws.vgrid, kThreads, 0, ws.st>>>(B.V, z.n, k, z.s_dev.get(), dst, z.n, &ws.S()->r2, ws.slot()); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+  }
+};
+
+// Mixed-precision form: FP32 operator values and Krylov vectors (stored unnormalised with
+// their FP64 normalisations sig[j]), FP64 recurrence scalars, full reorthogonalisation of
+// every new vector against the whole basis.
+template <class Opl>
+struct LzStepsMixed {
+  const Opl &op;
+  const LanczosCfg &cfg;
+  Workspace &ws;
+  LzState &z;
+  double *w;             // FP64 start / restart vector
+  DevBuf<float> y, coef;
+  DevBuf<double> sig, partials;
+  DevBuf<unsigned> ticket;
+  KrylovBasis<float> B;
+  int nchunk;
+  LzStepsMixed(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
+      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), coef(z_.cap_max + 1), sig(z_.cap_max + 1), ticket(1), B(z_.n, w_.st) {
+    nchunk = (int)((z_.n + kMxChunk - 1) / kMxChunk);
+    partials.alloc((size_t)(z_.cap_max + 1) * nchunk);
+    DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), w_.st));
+  }
+  // V[0] = fl32(w) (unnormalised); S->r2 already holds <w,w>.
+  void begin_cycle() {
+    B.ensure(1, z.cap_max);
+    k_copy<double, float><<<ws.vgrid, kThreads, 0, ws.st>>>(w, B.vec(0), z.n); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+  }
+  void step(int b) {
+    cudaStream_t st = ws.st;
+    const int n = z.n;
+    Scalars *S = ws.S();
+    const RedSlot slot = ws.slot();
+    B.ensure(b + 2, z.cap_max);
+    ++z.stamp;
+    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, ws.prog.d, &S->r2, b, z.stamp,
+                                 sig.get()};
+    op.apply(B.vec(b), &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
+    ++z.spmv;
+    const int nvec = b + 1;
+    launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec,
+               (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get());
+    launch_pdl_smem(k_mx_sub, dim3(ws.vgrid), dim3(kThreads), sizeof(float) * nvec, st, B.V, (long)n, nvec,
+                    (const float *)coef.get(), (const float *)y.get(), n, &S->r2, slot);
+  }
+  void combine(int k, const std::vector<double> &s, double *dst) {
+    z.upload_s(k, s, ws.st);
+    k_mx_ritz<<<ws.vgrid, kThreads, 0, ws.st>>>(B.V, z.n, k, z.s_dev.get(), sig.get(), dst, z.n, &ws.S()->r2, ws.slot()); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+  }
+};
+
+// Lanczos on operator op.  w_dev holds the start vector on entry (overwritten).  The
+// normalised Ritz vector is written to out_dev.  The host runs the reference's control flow
+// (convergence checks, restarts) on mirrored recurrence scalars; Steps enqueues the device work.
+template <class Opl, class Steps>
+LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, double *out_dev, Workspace &ws, LzState &z,
+                          Steps &steps) {
+  cudaStream_t st = ws.st;
+  Scalars *S = ws.S();
+  LanczosResult res;
+  const RedSlot slot = ws.slot();
 
   // <w,w> of the start vector.
-  k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(w_dev, n, &S->r2, slot); ::dg::count_launch();
+  k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(w_dev, z.n, &S->r2, slot); ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
 
-  std::vector<double> d, e, z;
+  std::vector<double> d, e, zz;
   double E = 1e15;            // pow(10,15) (sml/LANCZOS_SYM.c:77)
   int total_step = 0;
   int n_last = 0;             // order of the last tridiagonal solved
@@ -415,24 +530,23 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
   const int W = std::max(1, cfg.lookahead);
 
   auto finish = [&](int k, const std::vector<double> &s) {
-    for (int j = 0; j < k; ++j) hs.h[j] = s[j];
-    DG_CUDA(cudaMemcpyAsync(s_dev.get(), hs.h, sizeof(double) * k, cudaMemcpyHostToDevice, st));
-    k_ritz<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, k, s_dev.get(), out_dev, n, &S->r2, slot); ::dg::count_launch();
-    k_scale_rsqrt<double><<<ws.vgrid, kThreads, 0, st>>>(out_dev, n, &S->r2); ::dg::count_launch();
+    steps.combine(k, s, out_dev);
+    k_scale_rsqrt<double><<<ws.vgrid, kThreads, 0, st>>>(out_dev, z.n, &S->r2); ::dg::count_launch();
     DG_CUDA(cudaGetLastError());
     DG_CUDA(cudaStreamSynchronize(st));
+    res.spmv = z.spmv;
   };
 
   while (total_step < cfg.max_step) {
     // One restart cycle (the whole run when max_block_step >= max_step).
-    const int base_stamp = stamp;
-    enqueue_apply(0);
-    enqueue_update(0);
+    const int base_stamp = z.stamp;
+    steps.begin_cycle();
+    steps.step(0);
     const int nb_max = cfg.slow ? cfg.max_step - 1 : std::min(cfg.max_block_step - 1, cfg.max_step - total_step);
     if (nb_max == 0 && cfg.accept_at_end) {
       // 1 x 1 operator: the Rayleigh quotient of the (normalised) start vector is exact.
       DG_CUDA(cudaStreamSynchronize(st));
-      res.eig_val = hD.h[0];
+      res.eig_val = z.hD.h[0];
       res.converged = true;
       finish(1, std::vector<double>{1.0});
       return res;
@@ -440,71 +554,69 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
     int enq = 0;
     bool restart = false;
     for (int bs = 1; bs <= nb_max; ++bs) {
-      while (enq < std::min(bs + W, nb_max)) {
-        ++enq;
-        enqueue_apply(enq);
-        enqueue_update(enq);
-      }
+      while (enq < std::min(bs + W, nb_max)) steps.step(++enq);
       const int want = base_stamp + 1 + bs;   // stamp after apply(bs)
       if (!host_wait(st, [&] { return ws.prog.h->stamp >= want; })) {
         set_error("Lanczos: timed out waiting for step %d", bs);
         throw Error{DG_ERR_TIMEOUT};
       }
       total_step = cfg.slow ? bs : total_step + 1;
+      const double *hD = z.hD.h, *hO = z.hO.h;
       // Breakdown: the start vector spans an invariant subspace of dimension bs, so
       // ||w|| vanished and v_bs is meaningless.  The Ritz pair of T_{bs-1} is exact.
       {
         double scale = 0.0;
-        for (int j = 0; j < bs; ++j) scale = std::max(scale, std::fabs(hD.h[j]) + std::fabs(hO.h[j]));
-        if (!(hO.h[bs] > 1e-13 * scale) || !std::isfinite(hD.h[bs])) {
+        for (int j = 0; j < bs; ++j) scale = std::max(scale, std::fabs(hD[j]) + std::fabs(hO[j]));
+        if (!(hO[bs] > 1e-13 * scale) || !std::isfinite(hD[bs])) {
           const int nn = bs;
-          d.assign(hD.h, hD.h + nn);
+          d.assign(hD, hD + nn);
           e.resize(nn);
-          for (int i = 1; i < nn; ++i) e[i - 1] = hO.h[i];
+          for (int i = 1; i < nn; ++i) e[i - 1] = hO[i];
           const double lam = tridiag_lowest_eigenvalue(d.data(), e.data(), nn);
-          z.resize(nn);
-          tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+          zz.resize(nn);
+          tridiag_eigenvector(d.data(), e.data(), nn, lam, zz.data());
           res.eig_val = lam;
           res.steps = total_step;
           res.converged = true;
-          finish(nn, z);
+          finish(nn, zz);
           return res;
         }
       }
       const bool check = cfg.slow ? (bs >= cfg.min_step) : (total_step >= cfg.min_step || bs == cfg.max_block_step - 1);
       if (!check) continue;
       const int nn = bs + 1;
-      d.assign(hD.h, hD.h + nn);
+      d.assign(hD, hD + nn);
       e.resize(nn);
-      for (int i = 1; i < nn; ++i) e[i - 1] = hO.h[i];
+      for (int i = 1; i < nn; ++i) e[i - 1] = hO[i];
       const double hint = (E < 1e14) ? E : std::numeric_limits<double>::infinity();
       const double lam = tridiag_lowest_eigenvalue(d.data(), e.data(), nn, hint);
       bool conv;
       if (cfg.tight) {
-        z.resize(nn);
-        tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
-        conv = std::fabs(z[nn - 1]) < cfg.acc;
+        zz.resize(nn);
+        tridiag_eigenvector(d.data(), e.data(), nn, lam, zz.data());
+        conv = std::fabs(zz[nn - 1]) < cfg.acc;
       } else {
         conv = std::fabs(E - lam) < cfg.acc;
       }
+      if (!conv && cfg.mixed && E < 1e14) conv = std::fabs(E - lam) <= cfg.mixed_rel * std::fabs(lam);
       if (!conv && cfg.accept_at_end && bs == nb_max) conv = true;
       n_last = nn;
       if (conv) {
         if (!cfg.tight) {
-          z.resize(nn);
-          tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
+          zz.resize(nn);
+          tridiag_eigenvector(d.data(), e.data(), nn, lam, zz.data());
         }
         res.eig_val = lam;
         res.steps = total_step;
         res.converged = true;
-        finish(nn, z);
+        finish(nn, zz);
         return res;
       }
       if (!cfg.slow && bs == cfg.max_block_step - 1) {
         // Restart from the current Ritz vector (sml/LANCZOS_SYM.c:234-256); E is not updated.
-        z.resize(nn);
-        tridiag_eigenvector(d.data(), e.data(), nn, lam, z.data());
-        s_last = z;
+        zz.resize(nn);
+        tridiag_eigenvector(d.data(), e.data(), nn, lam, zz.data());
+        s_last = zz;
         restart = true;
         break;
       }
@@ -513,17 +625,29 @@ LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, 
     if (cfg.slow) break;
     if (!restart) break;
     // Drain speculative work, then form the restart vector in w.
-    for (int j = 0; j < n_last; ++j) hs.h[j] = s_last[j];
-    DG_CUDA(cudaMemcpyAsync(s_dev.get(), hs.h, sizeof(double) * n_last, cudaMemcpyHostToDevice, st));
-    k_ritz<double><<<ws.vgrid, kThreads, 0, st>>>(V, n, n_last, s_dev.get(), w_dev, n, &S->r2, slot); ::dg::count_launch();
-    DG_CUDA(cudaGetLastError());
+    steps.combine(n_last, s_last, w_dev);
     DG_CUDA(cudaStreamSynchronize(st));
-    stamp = ws.prog.h->stamp;   // speculative applies beyond the restart point have all landed
+    z.stamp = ws.prog.h->stamp;   // speculative applies beyond the restart point have all landed
   }
   res.steps = total_step;
   res.converged = false;
+  res.spmv = z.spmv;
   DG_CUDA(cudaStreamSynchronize(st));
   return res;
+}
+
+template <class Opl>
+LanczosResult lanczos_core(const Opl &op, const LanczosCfg &cfg, double *w_dev, double *out_dev, Workspace &ws) {
+  // Krylov vectors one cycle can hold: LANCZOS_SLOW never restarts (its max_block_step is
+  // unused by the reference), LANCZOS restarts every max_block_step steps.
+  const int cycle_len = cfg.slow ? cfg.max_step : std::min(cfg.max_block_step, cfg.max_step);
+  LzState z(op.n(), std::max(cycle_len, 1) + 1);
+  if (cfg.mixed) {
+    LzStepsMixed<Opl> steps(op, cfg, ws, z, w_dev);
+    return lanczos_run(op, cfg, w_dev, out_dev, ws, z, steps);
+  }
+  LzSteps64<Opl> steps(op, cfg, ws, z, w_dev);
+  return lanczos_run(op, cfg, w_dev, out_dev, ws, z, steps);
 }
 
 struct IterResult {

@@ -7,6 +7,8 @@
 // summation order (bitwise reproducible) and no atomics.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "matrix.cuh"
 #include "scan.cuh"
 
@@ -478,36 +480,83 @@ int dg_spmv_f32(dg_matrix *m, const float *x, float *y) {
   });
 }
 
-int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch) {
+int dg_spmv_mixed(dg_matrix *m, const float *x, double *y) {
   return guarded([&] {
-    require_device();
-    DG_REQUIRE(m && x_dev && y_dev && ms_per_launch && iters > 0, DG_ERR_ARG, "bad argument");
-    DG_REQUIRE(is_device_ptr(x_dev) && is_device_ptr(y_dev), DG_ERR_ARG, "profiling needs device vectors");
+    DG_REQUIRE(m && x && y, DG_ERR_ARG, "null argument");
+    DG_REQUIRE(m->has32, DG_ERR_ARG, "matrix has no FP32 values (create it with DG_VALUES_F32 or DG_VALUES_BOTH)");
     cudaStream_t st = stream();
-    DevBuf<double> partials(std::max(m->grid, m->sell_grid)), out(1);
-    DevBuf<unsigned> ticket(1);
-    DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
-    DevBuf<unsigned char> flush;
-    if (flush_bytes) flush.alloc(flush_bytes);
-    cudaEvent_t e0, e1;
-    DG_CUDA(cudaEventCreate(&e0));
-    DG_CUDA(cudaEventCreate(&e1));
-    double total = 0.0;
-    for (int it = 0; it < iters; ++it) {
-      if (flush_bytes) DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
-      DG_CUDA(cudaEventRecord(e0, st));
-      matrix_apply64(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y_dev, out.get()},
-                     RedSlot{partials.get(), ticket.get()}, st);
-      DG_CUDA(cudaEventRecord(e1, st));
-      DG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      total += ms;
+    const bool xd = is_device_ptr(x), yd = is_device_ptr(y);
+    DevBuf<float> xb;
+    DevBuf<double> yb;
+    const float *xp = x;
+    double *yp = y;
+    if (!xd) {
+      xb.alloc(m->n);
+      DG_CUDA(cudaMemcpyAsync(xb.get(), x, sizeof(float) * m->n, cudaMemcpyHostToDevice, st));
+      xp = xb.get();
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    *ms_per_launch = (float)(total / iters);
+    if (!yd) {
+      yb.alloc(m->n);
+      yp = yb.get();
+    }
+    matrix_apply32(m, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiStore<double>{yp},
+                   RedSlot{nullptr, nullptr}, st);
+    if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, sizeof(double) * m->n, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
   });
+}
+
+}  // extern "C"
+
+namespace {
+// Average CUDA-event time of one fused product launch (x FP64: FP64 values; x FP32: the
+// mixed-precision product), optionally rewriting flush_bytes of memory before each launch.
+template <class XT>
+void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch) {
+  require_device();
+  DG_REQUIRE(m && x_dev && y_dev && ms_per_launch && iters > 0, DG_ERR_ARG, "bad argument");
+  DG_REQUIRE(is_device_ptr(x_dev) && is_device_ptr(y_dev), DG_ERR_ARG, "profiling needs device vectors");
+  cudaStream_t st = stream();
+  DevBuf<double> partials(std::max(m->grid, m->sell_grid)), out(1);
+  DevBuf<unsigned> ticket(1);
+  DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
+  DevBuf<unsigned char> flush;
+  if (flush_bytes) flush.alloc(flush_bytes);
+  cudaEvent_t e0, e1;
+  DG_CUDA(cudaEventCreate(&e0));
+  DG_CUDA(cudaEventCreate(&e1));
+  double total = 0.0;
+  for (int it = 0; it < iters; ++it) {
+    if (flush_bytes) DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
+    DG_CUDA(cudaEventRecord(e0, st));
+    const EpiDot<double> epi{y_dev, out.get()};
+    const RedSlot slot{partials.get(), ticket.get()};
+    if constexpr (std::is_same<XT, float>::value) {
+      DG_REQUIRE(m->has32, DG_ERR_ARG, "matrix has no FP32 values");
+      matrix_apply32(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, epi, slot, st);
+    } else {
+      matrix_apply64(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, epi, slot, st);
+    }
+    DG_CUDA(cudaEventRecord(e1, st));
+    DG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_launch = (float)(total / iters);
+}
+}  // namespace
+
+extern "C" {
+
+int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch) {
+  return guarded([&] { profile_apply(m, x_dev, y_dev, iters, flush_bytes, ms_per_launch); });
+}
+
+int dg_profile_spmv_mixed(dg_matrix *m, const float *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch) {
+  return guarded([&] { profile_apply(m, x_dev, y_dev, iters, flush_bytes, ms_per_launch); });
 }
 
 int dg_matrix_set_sell_window(dg_matrix *m, int window) {

@@ -93,6 +93,16 @@ void matrix_apply64(const dg_matrix *m, const XT *x, const double *scale_src, in
     launch_apply(m->op64(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
 }
 
+// Apply the matrix with its FP32 values (mixed-precision form; FP32 input vector).
+template <class Epi>
+void matrix_apply32(const dg_matrix *m, const float *x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+                    const Epi &epi, RedSlot slot, cudaStream_t st) {
+  if (m->format == DG_FORMAT_SELL)
+    launch_sell(m->sell32(), m->sell_grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+  else
+    launch_apply(m->op32(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+}
+
 // Blocks needed by the current format (for sizing reduction partials).
 inline int matrix_grid(const dg_matrix *m) { return m->format == DG_FORMAT_SELL ? m->sell_grid : m->grid; }
 

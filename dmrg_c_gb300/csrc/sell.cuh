@@ -59,6 +59,40 @@ __device__ __forceinline__ T ld_vec(const T *p) {
   return *p;
 }
 
+// Row accumulators.  FP64 values or vectors: one DFMA per element.  FP32 values and FP32
+// vectors (the mixed-precision form): the exact product and compensated sum of Ogita, Rump
+// & Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2): the
+// product's rounding error comes from an FMA, the sum's from Knuth's TwoSum, and both are
+// carried in a second float, so the row sum is as accurate as if accumulated in twice the
+// working precision -- on the FP32 pipes, which GB300 has ~60x more of than FP64 pipes.
+// The explicitly rounded intrinsics keep the compiler from contracting the error terms away.
+struct AccF64 {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double v, double x) { s += v * x; }
+  __device__ __forceinline__ double get() const { return s; }
+};
+struct AccDot2 {
+  float p = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v, float x) {
+    const float h = __fmul_rn(v, x);
+    const float r = __fmaf_rn(v, x, -h);            // v x = h + r exactly
+    const float t = __fadd_rn(p, h);
+    const float z = __fsub_rn(t, p);
+    const float q = __fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z));   // p + h = t + q exactly
+    p = t;
+    c = __fadd_rn(c, __fadd_rn(q, r));
+  }
+  __device__ __forceinline__ double get() const { return (double)p + (double)c; }
+};
+template <class VT, class XT>
+struct AccFor {
+  using type = AccF64;
+};
+template <>
+struct AccFor<float, float> {
+  using type = AccDot2;
+};
+
 // Sum of this warp's share of one slice row.  WS warps share a slice: warp `sub` takes the
 // row elements k = sub, sub + WS, sub + 2 WS, ...; each lane owns one row.
 template <int WS, int U, bool PIPE, bool STREAM, class VT, class XT>
@@ -67,14 +101,14 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
   const int G = cnt / U;
   const int64_t step = (int64_t)WS * kSellC;
   const int64_t p0 = base + (int64_t)sub * kSellC;
-  double sum = 0.0;
+  typename AccFor<VT, XT>::type acc;
   int c[U];
-  double v[U];
+  VT v[U];
   if (PIPE && G > 0) {
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       c[u] = ld_mat<STREAM>(op.col + p0 + u * step);
-      v[u] = to_d(ld_mat<STREAM>(op.val + p0 + u * step));
+      v[u] = ld_mat<STREAM>(op.val + p0 + u * step);
     }
   }
   for (int g = 0; g < G; ++g) {
@@ -83,13 +117,13 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         c[u] = ld_mat<STREAM>(op.col + pg + u * step);
-        v[u] = to_d(ld_mat<STREAM>(op.val + pg + u * step));
+        v[u] = ld_mat<STREAM>(op.val + pg + u * step);
       }
     }
-    double xv[U];
+    XT xv[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = to_d(ld_vec<STREAM>(x + c[u]));
-    double vc[U];
+    for (int u = 0; u < U; ++u) xv[u] = ld_vec<STREAM>(x + c[u]);
+    VT vc[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) vc[u] = v[u];
     if (PIPE && g + 1 < G) {
@@ -97,18 +131,17 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         c[u] = ld_mat<STREAM>(op.col + pn + u * step);
-        v[u] = to_d(ld_mat<STREAM>(op.val + pn + u * step));
+        v[u] = ld_mat<STREAM>(op.val + pn + u * step);
       }
     }
 #pragma unroll
-    for (int u = 0; u < U; ++u) sum += vc[u] * xv[u];
+    for (int u = 0; u < U; ++u) acc.add(vc[u], xv[u]);
   }
   for (int j = G * U; j < cnt; ++j) {
     const int64_t p = p0 + (int64_t)j * step;
-    const double xv = to_d(ld_vec<STREAM>(x + ld_mat<STREAM>(op.col + p)));
-    sum += to_d(ld_mat<STREAM>(op.val + p)) * xv;
+    acc.add(ld_mat<STREAM>(op.val + p), ld_vec<STREAM>(x + ld_mat<STREAM>(op.col + p)));
   }
-  return sum;
+  return acc.get();
 }
 
 template <int WS, int VAR, class VT, class XT, class Epi>

@@ -2,12 +2,16 @@
 // device vectors in, Lanczos (+ inverse iteration) on the device, results out.
 #pragma once
 
+#include <type_traits>
+
 #include "krylov.cuh"
 #include "matrix.cuh"
+#include "refine.cuh"
 
 namespace dg {
 
-// Operator launcher over a device CRS (FP64 values).
+// Operator launcher over a device CRS: FP64 values for FP64 input vectors, FP32 values for
+// FP32 input vectors (mixed-precision form).
 struct CrsLauncher {
   const dg_matrix *m;
   int n() const { return m->n; }
@@ -15,9 +19,15 @@ struct CrsLauncher {
   template <class XT, class Epi>
   void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
-    matrix_apply64(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    if constexpr (std::is_same<XT, float>::value) {
+      DG_REQUIRE(m->has32, DG_ERR_ARG, "the mixed form needs FP32 values (create the matrix with DG_VALUES_BOTH)");
+      matrix_apply32(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    } else {
+      matrix_apply64(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    }
   }
 };
+
 
 // A vector that is either the caller's device memory or a device copy of host memory.
 struct VecArg {
@@ -60,6 +70,8 @@ inline LanczosCfg lanczos_cfg_from(const dg_solver_params &p) {
   c.slow = p.lanczos_slow != 0;
   c.reorth = false;
   c.accept_at_end = false;
+  c.mixed = p.mixed != 0;
+  c.mixed_rel = 1e-10;
   c.lookahead = p.lookahead > 0 ? p.lookahead : 2;
   return c;
 }
@@ -120,13 +132,27 @@ SolveOut solve_ground_state(const Opl &op, const dg_solver_params &p, const doub
     cfg.accept_at_end = true;
     o.info.dense = 1;
   }
+  const bool mixed = cfg.mixed && !o.info.dense;
+  cfg.mixed = mixed;
   LanczosResult lr = lanczos_core(op, cfg, w.get(), out.dev, ws);
   DG_CUDA(cudaEventRecord(e1, st));
   o.info.eig_val = lr.eig_val;
+  o.info.eig_lanczos = lr.eig_val;
   o.info.lanczos_steps = lr.steps;
   o.info.converged = lr.converged ? 1 : 0;
   o.info.spmv_count = lr.spmv;
-  if (lr.converged && run_ii) {
+  if (lr.converged && mixed) {
+    // Mixed form: the FP32 Ritz pair is refined against the FP64 operator (Jacobi-Davidson
+    // steps with FP32 correction solves, refine.cuh); without inverse iteration only the
+    // FP64 Rayleigh quotient is taken.
+    RefineResult R = refine_core(op, p.ii_acc, run_ii ? p.ii_max_step + 1 : 0, p.cg_max_step, out.dev, ws);
+    o.info.eig_val = R.eig_val;
+    o.info.error = R.error;
+    o.info.ii_steps = R.outer;
+    o.info.cg_steps = R.inner;
+    o.info.ii_converged = R.converged ? 1 : 0;
+    o.info.spmv_count += R.spmv64 + R.inner;
+  } else if (lr.converged && run_ii) {
     IICfg ic = ii_cfg_from(p, shifted_check);
     int sp = 0;
     o.ii = inverse_iteration_core(op, ic, lr.eig_val, out.dev, ws, &sp);

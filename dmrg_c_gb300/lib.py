@@ -76,6 +76,7 @@ SIGNATURES = {
     "dg_kernel_launches": (C.c_long, []),
     "dg_release_pool": (C.c_int, []),
     "dg_profile_spmv": (C.c_int, [vp, vp, vp, C.c_int, C.c_size_t, P(C.c_float)]),
+    "dg_profile_spmv_mixed": (C.c_int, [vp, vp, vp, C.c_int, C.c_size_t, P(C.c_float)]),
     "dg_matrix_create": (C.c_int, [C.c_int, lp, ip, dp, C.c_int, C.c_int, P(vp)]),
     "dg_matrix_create_device": (C.c_int, [C.c_int, C.c_long, vp, vp, vp, C.c_int, C.c_int, P(vp)]),
     "dg_matrix_free": (None, [vp]),
@@ -90,6 +91,7 @@ SIGNATURES = {
     "dg_matrix_download": (C.c_int, [vp, lp, ip, dp]),
     "dg_spmv": (C.c_int, [vp, vp, vp, C.c_double]),
     "dg_spmv_f32": (C.c_int, [vp, vp, vp]),
+    "dg_spmv_mixed": (C.c_int, [vp, vp, vp]),
     "dg_solver_params_default": (None, [P(dg_solver_params)]),
     "dg_lanczos": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
     "dg_inverse_iteration": (C.c_int, [vp, P(dg_solver_params), C.c_double, vp, P(dg_solve_info)]),
@@ -222,6 +224,19 @@ class DeviceMatrix:
         """Average ms per launch of the fused product kernel (CUDA events on the library stream)."""
         ms = C.c_float()
         check(load().dg_profile_spmv(self.h, as_ptr(x_dev), as_ptr(y_dev), iters, flush_bytes, C.byref(ms)))
+        return ms.value
+
+    def spmv_mixed(self, x, y=None):
+        """FP32 values and FP32 x, compensated accumulation, FP64 result."""
+        if y is None:
+            y = np.empty(self.n, np.float64)
+        check(load().dg_spmv_mixed(self.h, as_ptr(x), as_ptr(y)))
+        return y
+
+    def profile_spmv_mixed(self, x32_dev, y_dev, iters=20, flush_bytes=0) -> float:
+        """Average ms per launch of the mixed-precision product kernel."""
+        ms = C.c_float()
+        check(load().dg_profile_spmv_mixed(self.h, as_ptr(x32_dev), as_ptr(y_dev), iters, flush_bytes, C.byref(ms)))
         return ms.value
 
     def spmv_f32(self, x, y=None):

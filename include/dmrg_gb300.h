@@ -171,11 +171,18 @@ int dg_matrix_download(const dg_matrix *m, long *row, int *col, double *val);
 int dg_spmv(dg_matrix *m, const double *x, double *y, double sigma);
 /* Same on FP32 values and FP32 vectors with FP64 accumulation (needs DG_VALUES_F32). */
 int dg_spmv_f32(dg_matrix *m, const float *x, float *y);
+/* y = H x with the FP32 values and an FP32 x, the row sums accumulated with compensated FP32
+ * arithmetic (as accurate as twice-FP32 accumulation) and returned in FP64: the product of
+ * the mixed-precision form. */
+int dg_spmv_mixed(dg_matrix *m, const float *x, double *y);
 /* Average device time of the Lanczos/CG form of the product (y = M x plus the fused
  * <x, y> reduction) over iters launches, each timed with CUDA events on the library's
  * stream; with flush_bytes > 0 a buffer of that size is rewritten before every launch so
  * that the matrix is read from HBM, not L2.  x_dev / y_dev must be device pointers. */
 int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch);
+/* The same for the mixed-precision product (FP32 values and x_dev, FP64 y_dev). */
+int dg_profile_spmv_mixed(dg_matrix *m, const float *x_dev, double *y_dev, int iters, size_t flush_bytes,
+                          float *ms_per_launch);
 
 /* Solver settings (the fields of BOX_LAN / BOX_II / BOX_CG / DMRG_PARAMETER). */
 typedef struct {
@@ -192,8 +199,12 @@ typedef struct {
    double cg_acc;           /* BOX_CG.acc inside inverse iteration           */
    int cg_max_step;         /* BOX_CG.max_step inside inverse iteration      */
    int ii_minres;           /* 1 = "MR", 0 = "CG"                            */
-   int mixed;               /* 1 = FP32 Lanczos (values + vectors) with FP64 recurrence,
-                               full reorthogonalisation and FP64 refinement   */
+   int mixed;               /* 1 = mixed-precision form: FP32 values and Krylov vectors
+                               (compensated FP32 sums), FP64 recurrence and full
+                               reorthogonalisation, then Jacobi-Davidson refinement
+                               against the FP64 operator until ||H psi - E psi||_2
+                               <= 1e-8 |E| or the L1 residual < ii_acc (needs
+                               DG_VALUES_BOTH)                                  */
    uint64_t seed;           /* start vector seed when no guess is given      */
    int lookahead;           /* Lanczos steps kept in flight ahead of the host check (0 = auto) */
 } dg_solver_params;
@@ -203,7 +214,8 @@ typedef struct {
 void dg_solver_params_default(dg_solver_params *p);
 
 typedef struct {
-   double eig_val;          /* Lanczos eigenvalue (the reference reports this one) */
+   double eig_val;          /* Lanczos eigenvalue (the reference reports this one); mixed
+                               form: Rayleigh quotient of the FP64-refined vector   */
    double error;            /* L1 residual after inverse iteration                 */
    int lanczos_steps;       /* total Lanczos steps                                 */
    int ii_steps;            /* outer inverse-iteration steps                       */
@@ -213,6 +225,7 @@ typedef struct {
    int ii_converged;        /* inverse iteration met ii_acc                        */
    int dense;               /* 1 when the n < dense_below path ran                 */
    double ms_lanczos, ms_ii;/* device-timed phases                                 */
+   double eig_lanczos;      /* Ritz value the Lanczos phase converged to            */
 } dg_solve_info;
 
 /* Lanczos only.  guess: start vector (NULL = seeded pseudo-random).  eigvec: n doubles.
