@@ -10,6 +10,9 @@ DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: Lanczos (acc 1e-14, Normal) then invers
 
 * ``value``: solves/s with the matrix resident on the device, device time (CUDA events of
   the library stream) summed over K steps; L2 is flushed (256 MiB rewrite) before every step.
+* ``mixed``: the same solve in the mixed-precision form (FP32 values and Krylov vectors, FP64
+  recurrence, reorthogonalisation and refinement), with its energy error and eigenvector
+  overlap against the FP64 result.
 * ``e2e``: solves/s through the drop-in C entry point DMRG_DIAGONALIZE_SUPERBLOCK_SYM from
   host arrays (upload, device expansion, solve, eigenvector download inside the timing).
 * ``roofline``: the fused SpMV kernel (product + <x,y> epilogue), CUDA-event timed with L2
@@ -160,15 +163,15 @@ def run_gb300(args, ws, rank, local_rank):
     sb, low = build_workload(args.workload, args.seed)
     n = low.n
     nnz_full = 2 * low.nnz - n
-    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST)
+    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH)
     params = L.default_params(lanczos_acc=1e-14, cg_acc=1e-7, seed=args.seed + 1)
     out = torch.empty(n, dtype=torch.float64, device="cuda")
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
 
-    def one_solve():
+    def one_solve(p=params, o=out):
         flush.fill_(1)
         torch.cuda.synchronize()
-        v, info = L.ground_state(m, params, guess=None, out=out)
+        v, info = L.ground_state(m, p, guess=None, out=o)
         if not info.converged:
             raise RuntimeError("Lanczos did not converge")
         return info
@@ -198,6 +201,27 @@ def run_gb300(args, ws, rank, local_rank):
         total_ms = float(t.item())
     eigvec = out.cpu().numpy()
     E = infos[-1].eig_val
+
+    # mixed-precision form on the same superblock and start vector
+    params_mx = L.default_params(lanczos_acc=1e-14, cg_acc=1e-7, seed=args.seed + 1, mixed=1)
+    out_mx = torch.empty(n, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        one_solve(params_mx, out_mx)
+    mx_ms, mx_infos = [], []
+    for _ in range(args.steps):
+        info = one_solve(params_mx, out_mx)
+        mx_infos.append(info)
+        mx_ms.append(info.ms_lanczos + info.ms_ii)
+    v_mx = out_mx.cpu().numpy()
+    E_mx = mx_infos[-1].eig_val
+    mixed = {"value": ws * args.steps / (sum(mx_ms) * 1e-3), "unit": "solves/s", "ms_per_step": sum(mx_ms) / args.steps,
+             "p50_ms": float(np.percentile(mx_ms, 50)), "p99_ms": float(np.percentile(mx_ms, 99)),
+             "speedup_vs_fp64": total_ms / sum(mx_ms), "eig_val": E_mx, "dE_rel_vs_fp64": abs(E_mx - E) / abs(E),
+             "overlap_vs_fp64": float(abs(v_mx @ eigvec)), "lanczos_steps": mx_infos[-1].lanczos_steps,
+             "refine_fp32_products": mx_infos[-1].cg_steps, "refine_steps": mx_infos[-1].ii_steps,
+             "residual_l1": mx_infos[-1].error,
+             "form": "FP32 values + Krylov vectors (compensated FP32 sums), FP64 recurrence + full reorthogonalisation, "
+                     "Jacobi-Davidson refinement against FP64 H"}
 
     # roofline of the SpMV kernel
     x = torch.randn(n, dtype=torch.float64, device="cuda")
@@ -261,6 +285,7 @@ def run_gb300(args, ws, rank, local_rank):
                      "l2_warm_gbs": B / (spmv_warm_ms * 1e-3) / 1e9},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "mixed": mixed,
     }
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

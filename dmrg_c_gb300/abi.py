@@ -183,6 +183,19 @@ class dg_tune_result(C.Structure):
                 ("candidates", C.c_int), ("window", C.c_int)]
 
 
+class dg_engine_config(C.Structure):
+    """include/dmrg_gb300_ed.h: dg_engine_config"""
+    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t)]
+
+
+class dg_job_result(C.Structure):
+    """include/dmrg_gb300_ed.h: dg_job_result"""
+    _fields_ = [("id", C.c_long), ("status", C.c_int), ("converged", C.c_int), ("eig_val", C.c_double),
+                ("error", C.c_double), ("lanczos_steps", C.c_int), ("cg_steps", C.c_int), ("dim", C.c_long),
+                ("nnz", C.c_long), ("t_submit_ms", C.c_double), ("t_start_ms", C.c_double), ("t_built_ms", C.c_double),
+                ("t_done_ms", C.c_double)]
+
+
 class dg_ed_term(C.Structure):
     """include/dmrg_gb300_ed.h"""
     _fields_ = [("kind", C.c_int), ("site1", C.c_int), ("site2", C.c_int), ("op1", C.c_int), ("op2", C.c_int),

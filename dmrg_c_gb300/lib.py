@@ -105,6 +105,12 @@ SIGNATURES = {
     "dg_ed_info": (C.c_int, [vp, lp, lp]),
     "dg_ed_download": (C.c_int, [vp, lp, lp, ip, dp]),
     "dg_ed_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
+    "dg_engine_create": (C.c_int, [P(abi.dg_engine_config), P(vp)]),
+    "dg_engine_submit_ed": (C.c_int, [vp, P(abi.dg_ed_model), P(dg_solver_params), C.c_long, vp]),
+    "dg_engine_poll": (C.c_int, [vp, P(abi.dg_job_result), C.c_int, ip, C.c_int]),
+    "dg_engine_pending": (C.c_int, [vp, ip, ip, P(C.c_size_t)]),
+    "dg_engine_clock_ms": (C.c_double, [vp]),
+    "dg_engine_destroy": (None, [vp]),
 }
 
 DG_STORE_FULL, DG_STORE_LOWER_DIAG_LAST = 0, 1
@@ -283,6 +289,51 @@ class EDSystem:
         h = C.c_void_p()
         check(load().dg_ed_matrix(self.h, values, C.byref(h)))
         return DeviceMatrix(None, handle=h)
+
+
+class Engine:
+    """Concurrent ED ground-state engine (dg_engine): submit models, poll results."""
+
+    def __init__(self, workers: int = 0, hbm_budget: int = 0):
+        cfg = abi.dg_engine_config(workers=workers, hbm_budget=hbm_budget)
+        h = C.c_void_p()
+        check(load().dg_engine_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, model, params: dg_solver_params, job_id: int, want_vector: bool = False):
+        vec = None
+        if want_vector:
+            vec = np.empty(ed_dim(model), np.float64)
+        self._keep[job_id] = vec
+        check(load().dg_engine_submit_ed(self.h, C.byref(model.struct), C.byref(params), job_id,
+                                         as_ptr(vec) if vec is not None else None))
+
+    def poll(self, max_results: int = 256, wait_ms: int = 0):
+        """Finished results as a list of (dg_job_result, eigenvector or None)."""
+        buf = (abi.dg_job_result * max_results)()
+        n = C.c_int()
+        check(load().dg_engine_poll(self.h, buf, max_results, C.byref(n), wait_ms))
+        return [(buf[i], self._keep.pop(buf[i].id, None)) for i in range(n.value)]
+
+    def pending(self):
+        q, r, b = C.c_int(), C.c_int(), C.c_size_t()
+        check(load().dg_engine_pending(self.h, C.byref(q), C.byref(r), C.byref(b)))
+        return q.value, r.value, b.value
+
+    def clock_ms(self) -> float:
+        return float(load().dg_engine_clock_ms(self.h))
+
+    def close(self):
+        if self.h:
+            load().dg_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ed_dim(model) -> int:

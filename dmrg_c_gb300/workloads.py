@@ -47,27 +47,27 @@ def hubbard_site_labels():
 
 
 def xxz_superblock_m64(seed=0):
-    """configs[0] shape: XXZ L=32, m=64 (block of 15 sites), 2Sz = 0."""
+    """Largest superblock of the XXZ DMRG run: L=32, m=64 (block of 15 sites), 2Sz = 0."""
     qb = _block_labels(64, 15, 0, 0, 0.95, seed, fermions=False)
     return superblock.synthetic_superblock(64, 2, qb, np.array([1, -1]), 0, nnz_lllr=29, nnz_lrrl=2, seed=seed + 1)
 
 
 def klm_superblock_m128(seed=0):
-    """configs[1] shape: KLM L=24, N_e=12, 2Sz=0, m=128 (block of 11 sites, d=8)."""
+    """Largest superblock of the Kondo-lattice DMRG run: L=24, N_e=12, 2Sz=0, m=128 (block of 11 sites, d=8)."""
     qb = _block_labels(128, 11, 5.0, 0.95, 0.85, seed)
     return superblock.synthetic_superblock(128, 8, qb, klm_site_labels(), 12 * QN_SCALE, nnz_lllr=18, nnz_lrrl=3,
                                            seed=seed + 1, with_sign=True)
 
 
 def hubbard_superblock_m512(seed=0):
-    """configs[4] shape: Hubbard L=64, half filling, 2Sz=0, m=512 (block of 31 sites, d=4)."""
+    """Largest superblock of the Hubbard DMRG run: L=64, half filling, 2Sz=0, m=512 (block of 31 sites, d=4)."""
     qb = _block_labels(512, 31, 31.0, 1.25, 0.9, seed)
     return superblock.synthetic_superblock(512, 4, qb, hubbard_site_labels(), 64 * QN_SCALE, nnz_lllr=100, nnz_lrrl=3,
                                            seed=seed + 1, with_sign=True)
 
 
 def xxz_ed_batch(count=256, seed=0):
-    """configs[2] instances: L uniform in {12,...,22}, Jz ~ U[0,2], hz ~ U[0,1], Jxy = 1, 2Sz = 0."""
+    """Batched XXZ ED instances: L uniform in {12,...,22}, Jz ~ U[0,2], hz ~ U[0,1], Jxy = 1, 2Sz = 0, OBC."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
@@ -79,8 +79,8 @@ def xxz_ed_batch(count=256, seed=0):
 
 
 def hubbard_request_trace(rate=200.0, duration=60.0, seed=1):
-    """configs[3] trace: Poisson arrivals; L in {8,10,12}, t=1 (coefficient -1), U ~ U[0,8],
-    h ~ U[0,0.5], half filling, 2Sz = 0."""
+    """Served Hubbard ED request trace: Poisson arrivals at `rate`/s for `duration` s; L in
+    {8,10,12}, t=1 (coefficient -1), U ~ U[0,8], h ~ U[0,0.5], half filling, 2Sz = 0, OBC."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:

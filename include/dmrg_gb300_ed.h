@@ -72,6 +72,41 @@ int dg_ed_download(const dg_ed *ed, long *basis, long *row, int *col, double *va
 /* A solver operator (dg_matrix, full storage) built from the device CRS. */
 int dg_ed_matrix(const dg_ed *ed, int values, dg_matrix **out);
 
+/* ---- Concurrent solve engine: batched and served ED ground states (no counterpart in the
+ * reference, whose ED driver solves one instance per run, EXACT_DIAGONALIZATION.c).
+ * Worker threads, one CUDA stream each, take jobs in submission order; a job starts when a
+ * worker is idle and its device-memory estimate fits hbm_budget next to the running jobs
+ * (a job larger than the budget runs alone).  Each job builds its basis and Hamiltonian on
+ * the device and runs dg_ground_state with its own parameters (FP64 or mixed form).  Results
+ * are identical to running the job alone. */
+typedef struct dg_engine dg_engine;
+
+typedef struct {
+   int workers;            /* jobs in flight at once (0 = 8)                           */
+   size_t hbm_budget;      /* device bytes jobs may hold together (0 = 80% of free)   */
+} dg_engine_config;
+
+typedef struct {
+   long id;                /* the submitter's tag                                      */
+   int status;             /* dg_status of the job                                     */
+   int converged;
+   double eig_val, error;  /* ground-state energy; L1 residual                         */
+   int lanczos_steps, cg_steps;
+   long dim, nnz;
+   double t_submit_ms, t_start_ms, t_built_ms, t_done_ms;   /* engine clock          */
+} dg_job_result;
+
+int dg_engine_create(const dg_engine_config *cfg, dg_engine **out);
+/* Queue one ED ground-state solve.  The model is copied; out_vec (host, dim doubles, may
+ * be NULL) receives the eigenvector and must stay valid until the job's result is polled. */
+int dg_engine_submit_ed(dg_engine *e, const dg_ed_model *model, const dg_solver_params *params, long id, double *out_vec);
+/* Move up to max finished results into out (waiting up to wait_ms for the first one). */
+int dg_engine_poll(dg_engine *e, dg_job_result *out, int max, int *count, int wait_ms);
+int dg_engine_pending(dg_engine *e, int *queued, int *running, size_t *bytes_in_use);
+double dg_engine_clock_ms(dg_engine *e);
+/* Stops the workers after their current jobs; queued jobs are dropped. */
+void dg_engine_destroy(dg_engine *e);
+
 #ifdef __cplusplus
 }
 #endif
