@@ -48,7 +48,7 @@ def main(argv=None):
     ap.add_argument("--json", default=None)
     a = ap.parse_args(argv)
     inst = workloads.xxz_ed_batch(a.count, seed=0)
-    p = L.default_params(seed=7, mixed=int(a.mixed))
+    p = L.default_params(seed=7, mixed=2 if a.mixed else 0)
     run_batch(inst[:8], p, a.workers)                       # warm-up (pool, kernels)
     wall, res = run_batch(inst, p, a.workers)
     out = {"instances": a.count, "workers": a.workers, "form": "mixed" if a.mixed else "fp64",

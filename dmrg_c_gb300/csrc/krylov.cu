@@ -211,6 +211,26 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long
   grid_reduce(acc, slot, [&](double t) { *r2 = t; });
 }
 
+__global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
+                                                       const float *__restrict__ y, const double *D, const double *O, int n,
+                                                       double *r2, RedSlot slot) {
+  pdl_wait();
+  const double a = D[b] * sig[b];
+  const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
+  const float *vb = V + (long)b * ldv;
+  const float *vp = (b > 0) ? V + (long)(b - 1) * ldv : vb;
+  float *vn = V + (long)(b + 1) * ldv;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double w = (double)y[i] - a * (double)vb[i];
+    if (b > 0) w -= c * (double)vp[i];
+    vn[i] = (float)w;
+    acc += w * w;
+  }
+  pdl_trigger();
+  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+}
+
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
                                                      const double *__restrict__ sig, double *__restrict__ out, int n, double *r2,
                                                      RedSlot slot) {

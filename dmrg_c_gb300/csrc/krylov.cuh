@@ -80,6 +80,8 @@ double wait_timeout_ms();
 // Spin (on the host) until pred() holds; bounded.  Returns false on timeout.
 // The acquire fence orders the host's later reads of device-written mirrors after the
 // read that observed the progress stamp (needed on weakly ordered hosts such as Arm).
+// The stream is queried for errors only every ~0.5 ms: driver calls from many solver
+// threads on one context serialise, and the progress flag itself lives in host memory.
 template <class Pred>
 bool host_wait(cudaStream_t st, Pred pred) {
   if (pred()) {
@@ -87,20 +89,25 @@ bool host_wait(cudaStream_t st, Pred pred) {
     return true;
   }
   const double t0 = now_ms(), limit = wait_timeout_ms();
+  double next_query = t0 + 0.5;
   unsigned spins = 0;
   while (!pred()) {
-    if ((++spins & 0x3ff) == 0) {
-      cudaError_t e = cudaStreamQuery(st);
-      if (e != cudaSuccess && e != cudaErrorNotReady) {
-        set_error("device error while waiting: %s", cudaGetErrorString(e));
-        throw Error{DG_ERR_CUDA};
+    if ((++spins & 0xff) == 0) {
+      const double t = now_ms();
+      if (t >= next_query) {
+        next_query = t + 0.5;
+        cudaError_t e = cudaStreamQuery(st);
+        if (e != cudaSuccess && e != cudaErrorNotReady) {
+          set_error("device error while waiting: %s", cudaGetErrorString(e));
+          throw Error{DG_ERR_CUDA};
+        }
+        if (e == cudaSuccess && !pred()) {
+          // Stream drained: whatever was going to arrive has arrived.
+          std::atomic_thread_fence(std::memory_order_acquire);
+          return pred();
+        }
+        if (t - t0 > limit) return false;
       }
-      if (e == cudaSuccess && !pred()) {
-        // Stream drained: whatever was going to arrive has arrived.
-        std::atomic_thread_fence(std::memory_order_acquire);
-        return pred();
-      }
-      if (now_ms() - t0 > limit) return false;
       std::this_thread::yield();
     }
   }
@@ -248,6 +255,11 @@ constexpr int kMxChunk = 1024;   // rows per dot-product chunk (one warp each)
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
                                                     int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
                                                     float *__restrict__ coef, unsigned *ticket);
+// Three-term recurrence of the mixed form without reorthogonalisation:
+// w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w); *r2 = <w,w>.
+__global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
+                                                       const float *__restrict__ y, const double *D, const double *O, int n,
+                                                       double *r2, RedSlot slot);
 // w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); *r2 = <w,w>.
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
                                                     const float *__restrict__ y, int n, double *r2, RedSlot slot);
@@ -368,6 +380,7 @@ struct LanczosCfg {
   bool reorth;           // full reorthogonalisation (dense path)
   bool accept_at_end;    // dense path: the last step spans the whole space, accept it
   bool mixed;            // FP32 operator and Krylov vectors, FP64 recurrence (mixed-precision form)
+  bool mixed_reorth;     // mixed form: orthogonalise every vector against the whole basis
   double mixed_rel;      // mixed form: |dE| <= mixed_rel * |E| also counts as converged
   int lookahead;
 };
@@ -494,6 +507,11 @@ struct LzStepsMixed {
                                  sig.get()};
     op.apply(B.vec(b), &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
     ++z.spmv;
+    if (!cfg.mixed_reorth) {
+      launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
+                 (const double *)z.D.get(), (const double *)z.O.get(), n, &S->r2, slot);
+      return;
+    }
     const int nvec = b + 1;
     launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec,
                (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get());

@@ -71,6 +71,7 @@ inline LanczosCfg lanczos_cfg_from(const dg_solver_params &p) {
   c.reorth = false;
   c.accept_at_end = false;
   c.mixed = p.mixed != 0;
+  c.mixed_reorth = p.mixed != 2;
   c.mixed_rel = 1e-10;
   c.lookahead = p.lookahead > 0 ? p.lookahead : 2;
   return c;

@@ -67,7 +67,7 @@ def main(argv=None):
     ap.add_argument("--mixed", action="store_true")
     a = ap.parse_args(argv)
     trace = workloads.hubbard_request_trace(rate=a.rate, duration=a.seconds, seed=1)
-    p = L.default_params(seed=11, mixed=int(a.mixed))
+    p = L.default_params(seed=11, mixed=2 if a.mixed else 0)
     serve(trace[:16], p, a.workers)                          # warm-up
     res, max_queue = serve(trace, p, a.workers)
     out = summarize(trace, res)

@@ -199,12 +199,17 @@ typedef struct {
    double cg_acc;           /* BOX_CG.acc inside inverse iteration           */
    int cg_max_step;         /* BOX_CG.max_step inside inverse iteration      */
    int ii_minres;           /* 1 = "MR", 0 = "CG"                            */
-   int mixed;               /* 1 = mixed-precision form: FP32 values and Krylov vectors
+   int mixed;               /* 0 = FP64 (the reference's algorithm).
+                               1 = mixed-precision form: FP32 values and Krylov vectors
                                (compensated FP32 sums), FP64 recurrence and full
                                reorthogonalisation, then Jacobi-Davidson refinement
                                against the FP64 operator until ||H psi - E psi||_2
-                               <= 1e-8 |E| or the L1 residual < ii_acc (needs
-                               DG_VALUES_BOTH)                                  */
+                               <= 1e-8 |E| or the L1 residual < ii_acc.
+                               2 = as 1 with the FP64 three-term recurrence and no
+                               reorthogonalisation (FP32 SpMV + FP64 Krylov scalars:
+                               for matrices with few entries per row, where
+                               reorthogonalisation would outweigh the product).
+                               1 and 2 need DG_VALUES_BOTH.                      */
    uint64_t seed;           /* start vector seed when no guess is given      */
    int lookahead;           /* Lanczos steps kept in flight ahead of the host check (0 = auto) */
 } dg_solver_params;

@@ -11,8 +11,8 @@ TOL_E = 1e-10
 TOL_OV = 1e-9
 
 
-def _mixed_params(gpu, **kw):
-    return gpu.default_params(mixed=1, seed=5, **kw)
+def _mixed_params(gpu, mixed=1, **kw):
+    return gpu.default_params(mixed=mixed, seed=5, **kw)
 
 
 @pytest.mark.gpu
@@ -31,9 +31,9 @@ def test_mixed_spmv_is_compensated(gpu):
     assert err < 1e-13, err
 
 
-def _check_solve(gpu, oracle, crs, storage, E_ref=None, **kw):
+def _check_solve(gpu, oracle, crs, storage, E_ref=None, mixed=1, **kw):
     m = gpu.DeviceMatrix(crs, storage, gpu.DG_VALUES_BOTH)
-    v, info = gpu.ground_state(m, _mixed_params(gpu, **kw))
+    v, info = gpu.ground_state(m, _mixed_params(gpu, mixed, **kw))
     assert info.converged
     if E_ref is None:
         rc, out, v_ref = oracle.lanczos(crs, storage == gpu.DG_STORE_LOWER_DIAG_LAST, seed=5)
@@ -62,12 +62,22 @@ def test_mixed_klm_superblock_matches_fp64_oracle(gpu, oracle):
 
 
 @pytest.mark.gpu
-def test_mixed_ed_free_fermions(gpu):
+@pytest.mark.parametrize("mixed", [1, 2])
+def test_mixed_ed_free_fermions(gpu, mixed):
     L = 10
     ed = gpu.EDSystem(ed_models.hubbard_chain(L, t=-1.0, U=0.0))
     b, row, col, val = ed.download()
     crs = abi.Crs(row, col, val, n=ed.dim)
-    _check_solve(gpu, None, crs, gpu.DG_STORE_FULL, E_ref=ed_models.free_fermion_energy(L, L // 2, L // 2))
+    _check_solve(gpu, None, crs, gpu.DG_STORE_FULL, E_ref=ed_models.free_fermion_energy(L, L // 2, L // 2), mixed=mixed)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [1, 2])
+def test_mixed_ed_matches_fp64_oracle(gpu, oracle, mixed):
+    """Interacting Hubbard and XXZ chains: the mixed forms against the FP64 oracle."""
+    for model in (ed_models.hubbard_chain(8, U=4.7, hz=0.13), ed_models.xxz_chain(16, Jz=1.3, hz=0.4)):
+        basis, row, col, val = oracle.ed_build(model)
+        _check_solve(gpu, oracle, abi.Crs(row, col, val, n=len(basis)), gpu.DG_STORE_FULL, mixed=mixed)
 
 
 @pytest.mark.gpu
