@@ -183,6 +183,20 @@ class dg_tune_result(C.Structure):
                 ("candidates", C.c_int), ("window", C.c_int)]
 
 
+class dg_sb_term(C.Structure):
+    """include/dmrg_gb300_sb.h: dg_sb_term"""
+    _fields_ = [("pos1", C.c_int), ("pos2", C.c_int), ("op1", C.c_int), ("op2", C.c_int), ("coef", C.c_double),
+                ("sign_mask", C.c_int), ("sign_even", C.c_int)]
+
+
+class dg_sb_model(C.Structure):
+    """include/dmrg_gb300_sb.h: dg_sb_model"""
+    _fields_ = [("n", C.c_int), ("dim_LL", C.c_int), ("dim_RR", C.c_int), ("dim_onsite", C.c_int),
+                ("LL", C.POINTER(C.c_short)), ("LR", C.POINTER(C.c_short)), ("RR", C.POINTER(C.c_short)),
+                ("RL", C.POINTER(C.c_short)), ("inv", C.POINTER(C.c_int)), ("n_ops", C.c_int), ("ops", C.POINTER(CRS1)),
+                ("n_terms", C.c_int), ("terms", C.POINTER(dg_sb_term)), ("ele", C.POINTER(C.c_int) * 4)]
+
+
 class dg_engine_config(C.Structure):
     """include/dmrg_gb300_ed.h: dg_engine_config"""
     _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t)]

@@ -105,6 +105,11 @@ SIGNATURES = {
     "dg_ed_info": (C.c_int, [vp, lp, lp]),
     "dg_ed_download": (C.c_int, [vp, lp, lp, ip, dp]),
     "dg_ed_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
+    "dg_sb_build": (C.c_int, [P(abi.dg_sb_model), P(vp)]),
+    "dg_sb_info": (C.c_int, [vp, ip, lp]),
+    "dg_sb_download": (C.c_int, [vp, lp, ip, dp]),
+    "dg_sb_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
+    "dg_sb_free": (None, [vp]),
     "dg_engine_create": (C.c_int, [P(abi.dg_engine_config), P(vp)]),
     "dg_engine_submit_ed": (C.c_int, [vp, P(abi.dg_ed_model), P(dg_solver_params), C.c_long, vp]),
     "dg_engine_poll": (C.c_int, [vp, P(abi.dg_job_result), C.c_int, ip, C.c_int]),
@@ -288,6 +293,43 @@ class EDSystem:
     def matrix(self, values: int = DG_VALUES_F64) -> DeviceMatrix:
         h = C.c_void_p()
         check(load().dg_ed_matrix(self.h, values, C.byref(h)))
+        return DeviceMatrix(None, handle=h)
+
+
+class SuperblockCRS:
+    """Superblock Hamiltonian (lower triangle, diagonal last) built on the device from a
+    dmrg_c_gb300.sb_models.SBModel term list (dg_sb)."""
+
+    def __init__(self, model):
+        self.model = model
+        h = C.c_void_p()
+        check(load().dg_sb_build(C.byref(model.struct), C.byref(h)))
+        self.h = h
+        n, nnz = C.c_int(), C.c_long()
+        check(load().dg_sb_info(h, C.byref(n), C.byref(nnz)))
+        self.n, self.nnz = n.value, nnz.value
+
+    def close(self):
+        if self.h:
+            load().dg_sb_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def download(self):
+        row = np.empty(self.n + 1, np.int64)
+        col = np.empty(self.nnz, np.int32)
+        val = np.empty(self.nnz, np.float64)
+        check(load().dg_sb_download(self.h, abi.ptr(row, C.c_long), abi.ptr(col, C.c_int), abi.ptr(val, C.c_double)))
+        return row, col, val
+
+    def matrix(self, values: int = DG_VALUES_F64) -> DeviceMatrix:
+        h = C.c_void_p()
+        check(load().dg_sb_matrix(self.h, values, C.byref(h)))
         return DeviceMatrix(None, handle=h)
 
 

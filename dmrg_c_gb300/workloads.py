@@ -92,3 +92,13 @@ def hubbard_request_trace(rate=200.0, duration=60.0, seed=1):
         h = float(rng.uniform(0, 0.5))
         out.append(dict(t=t, L=L, U=U, h=h, model=lambda L=L, U=U, h=h: hubbard_chain(L, t=-1.0, U=U, hz=h)))
     return out
+
+
+def hubbard_sb_model_m512(seed=0, per_row=24):
+    """Term-list form (block and site operators) of a Hubbard m=512 superblock of the same
+    basis as ``hubbard_superblock_m512``, for the GPU superblock CRS build."""
+    from . import sb_models
+    qb = _block_labels(512, 31, 31.0, 1.25, 0.9, seed)
+    sb = superblock.synthetic_superblock(512, 4, qb, hubbard_site_labels(), 64 * QN_SCALE, nnz_lllr=1, nnz_lrrl=1,
+                                         seed=seed + 1, with_sign=True)
+    return sb_models.hubbard_superblock_model(sb, qb, seed=seed + 2, per_row=per_row)

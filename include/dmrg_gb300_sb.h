@@ -1,0 +1,61 @@
+/*
+ * dmrg_gb300_sb.h -- superblock Hamiltonian CRS built on the device.
+ *
+ * Replaces the model drivers' GET_HAM_LLLRRRRL (e.g. main/dmrg/xxz_vf/src/allocations/
+ * GET_HAM_LLLRRRRL.c:11-123) with MAKE_ELEMENT_HAM_LLLRRRRL and the generic element
+ * builders DMRG_MAKE_ELEM_{LL,LR,RR,RL,LLLR,RRRL,LRRL,LRRR,LLRL,LLRR,ZERO}_LLLRRRRL
+ * (dmrg/DMRG_MAKE_ELEM_*_LLLRRRRL.c).  A superblock state is (LL, LR, RR, RL); each row's
+ * elements come from a list of terms, each one or two operators acting on one or two of the
+ * four positions, applied in the list's order.  Repeated targets are summed in generation
+ * order, a zero diagonal is added when absent, and the row keeps the lower triangle plus the
+ * diagonal (|v| > 1e-15 off the diagonal), columns ascending, diagonal last -- the layout the
+ * *_SYM solvers read.
+ */
+#ifndef DMRG_GB300_SB_H
+#define DMRG_GB300_SB_H
+
+#include "dmrg_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { DG_SB_LL = 0, DG_SB_LR = 1, DG_SB_RR = 2, DG_SB_RL = 3 };
+
+typedef struct {
+   int pos1, pos2;     /* positions acted on; pos2 = -1 for a one-operator term              */
+   int op1, op2;       /* operator indices; op1 runs in the outer loop, op2 in the inner     */
+   double coef;        /* value = sign * coef * v1 * v2 (terms with |coef| < 1e-15 are skipped) */
+   int sign_mask;      /* bit p set: ele[p][state at position p] enters the parity; 0: sign +1 */
+   int sign_even;      /* sign when the parity is even (+1 or -1); odd gives the opposite     */
+} dg_sb_term;
+
+typedef struct {
+   int n;                          /* superblock dimension (one symmetry sector)              */
+   int dim_LL, dim_RR, dim_onsite;
+   const short *LL, *LR, *RR, *RL; /* [n] position states of every superblock state           */
+   const int *inv;                 /* [dim_LL*d*dim_RR*d] Inv_LLLRRRRL, -1 outside the sector */
+   int n_ops;
+   const CRS1 *ops;                /* square operators on the position they act on            */
+   int n_terms;
+   const dg_sb_term *terms;
+   const int *ele[4];              /* electrons of each state of each position (NULL if unused) */
+} dg_sb_model;
+
+typedef struct dg_sb dg_sb;
+
+/* Build the lower-triangle + diagonal-last CRS on the current device.  Limits: n < 2^31,
+ * at most 4096 generated elements per row. */
+int dg_sb_build(const dg_sb_model *model, dg_sb **out);
+int dg_sb_info(const dg_sb *sb, int *n, long *nnz);
+/* Copy row[n+1], col[nnz], val[nnz] to host arrays (any may be NULL). */
+int dg_sb_download(const dg_sb *sb, long *row, int *col, double *val);
+/* Solver operator from the device CRS (DG_STORE_LOWER_DIAG_LAST, expanded on the device). */
+int dg_sb_matrix(const dg_sb *sb, int values, dg_matrix **out);
+void dg_sb_free(dg_sb *sb);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMRG_GB300_SB_H */

@@ -1082,3 +1082,201 @@ int or_site_apply(const CRS1 *O, const long *out_basis, long dim_out, const long
    }
    return OR_OK;
 }
+
+/* ===================================================================================
+ * Superblock Hamiltonian CRS (lower triangle, diagonal last)
+ * GET_HAM_LLLRRRRL (main/dmrg/xxz_vf/src/allocations/GET_HAM_LLLRRRRL.c:26-112) with the
+ * model's MAKE_ELEMENT_HAM_LLLRRRRL term list and the generic element builders
+ * dmrg/DMRG_MAKE_ELEM_*_LLLRRRRL.c, restated over a dg_sb_model.
+ * =================================================================================== */
+typedef struct {
+   int *slot;       /* [n] element index of a target in this row, -1 when absent */
+   int *tgt;        /* generated targets in generation order */
+   double *val;
+   int num, cap;
+} sb_row_acc;
+
+static int sb_pos_dim(const dg_sb_model *m, int p) {
+   return (p == DG_SB_LL) ? m->dim_LL : (p == DG_SB_RR) ? m->dim_RR : m->dim_onsite;
+}
+
+/* One row's generated elements (dmrg/DMRG_MAKE_ELEM_*_LLLRRRRL.c: append a new target,
+ * add into an existing one; then DMRG_MAKE_ELEM_ZERO_LLLRRRRL.c). */
+static int sb_row(const dg_sb_model *m, int b, sb_row_acc *r) {
+   const double zero = 0.000000000000001;
+   const int d = m->dim_onsite;
+   const int st[4] = {m->LL[b], m->LR[b], m->RR[b], m->RL[b]};
+   r->num = 0;
+   for (int k = 0; k < m->n_terms; k++) {
+      const dg_sb_term *t = m->terms + k;
+      if (fabs(t->coef) < zero) continue;
+      int sign = 1;
+      if (t->sign_mask) {
+         int ne = 0;
+         for (int p = 0; p < 4; p++)
+            if (t->sign_mask & (1 << p)) ne += m->ele[p][st[p]];
+         sign = (ne % 2 == 0) ? t->sign_even : -t->sign_even;
+      }
+      const CRS1 *O1 = m->ops + t->op1;
+      const CRS1 *O2 = (t->pos2 >= 0) ? m->ops + t->op2 : NULL;
+      for (long i = O1->Row[st[t->pos1]]; i < O1->Row[st[t->pos1] + 1]; i++) {
+         const long j0 = O2 ? O2->Row[st[t->pos2]] : 0, j1 = O2 ? O2->Row[st[t->pos2] + 1] : 1;
+         for (long j = j0; j < j1; j++) {
+            int ns[4] = {st[0], st[1], st[2], st[3]};
+            ns[t->pos1] = O1->Col[i];
+            double val;
+            if (O2) {
+               ns[t->pos2] = O2->Col[j];
+               val = sign * t->coef * O1->Val[i] * O2->Val[j];
+            } else {
+               val = t->coef * O1->Val[i];
+            }
+            const long sup = (((long)ns[0] * d + ns[1]) * m->dim_RR + ns[2]) * d + ns[3];
+            const int inv = m->inv[sup];
+            if (fabs(val) > zero && inv >= 0) {
+               if (r->slot[inv] == -1) {
+                  if (r->num >= r->cap) return OR_NOMEM;
+                  r->slot[inv] = r->num;
+                  r->tgt[r->num] = inv;
+                  r->val[r->num] = val;
+                  r->num++;
+               } else {
+                  r->val[r->slot[inv]] = r->val[r->slot[inv]] + val;
+               }
+            }
+         }
+      }
+   }
+   if (r->slot[b] == -1) {
+      if (r->num >= r->cap) return OR_NOMEM;
+      r->slot[b] = r->num;
+      r->tgt[r->num] = b;
+      r->val[r->num] = 0.0;
+      r->num++;
+   }
+   return OR_OK;
+}
+
+static void sb_row_reset(sb_row_acc *r) {
+   for (int e = 0; e < r->num; e++) r->slot[r->tgt[e]] = -1;
+}
+
+static int sb_acc_init(const dg_sb_model *m, sb_row_acc *r) {
+   long cap = 1;
+   for (int k = 0; k < m->n_terms; k++) {
+      const dg_sb_term *t = m->terms + k;
+      int w1 = 0, w2 = 1;
+      const CRS1 *O1 = m->ops + t->op1;
+      for (int s = 0; s < sb_pos_dim(m, t->pos1); s++) w1 = (int)fmax(w1, O1->Row[s + 1] - O1->Row[s]);
+      if (t->pos2 >= 0) {
+         const CRS1 *O2 = m->ops + t->op2;
+         w2 = 0;
+         for (int s = 0; s < sb_pos_dim(m, t->pos2); s++) w2 = (int)fmax(w2, O2->Row[s + 1] - O2->Row[s]);
+      }
+      cap += (long)w1 * w2;
+   }
+   if (cap > m->n) cap = m->n;
+   r->cap = (int)cap;
+   r->slot = malloc(sizeof(int) * m->n);
+   r->tgt = malloc(sizeof(int) * cap);
+   r->val = malloc(sizeof(double) * cap);
+   if (!r->slot || !r->tgt || !r->val) return OR_NOMEM;
+   for (int i = 0; i < m->n; i++) r->slot[i] = -1;
+   r->num = 0;
+   return OR_OK;
+}
+
+static void sb_acc_free(sb_row_acc *r) {
+   free(r->slot);
+   free(r->tgt);
+   free(r->val);
+}
+
+typedef struct {
+   int c;
+   double v;
+} sb_cv;
+
+static int sb_cv_cmp(const void *a, const void *b) {
+   const int x = ((const sb_cv *)a)->c, y = ((const sb_cv *)b)->c;
+   return (x > y) - (x < y);
+}
+
+/* GET_HAM_LLLRRRRL.c:49-51 keep rule; pass 1 counts into row[b + 1], then the prefix. */
+int or_sb_count(const dg_sb_model *m, long *row, int threads) {
+   const double zero = pow(10, -15);
+   int err = 0;
+   row[0] = 0;
+#pragma omp parallel num_threads(threads)
+   {
+      sb_row_acc r;
+      if (sb_acc_init(m, &r)) {
+#pragma omp atomic write
+         err = 1;
+      } else {
+#pragma omp for schedule(static)
+         for (int b = 0; b < m->n; b++) {
+            long cnt = 0;
+            if (sb_row(m, b, &r)) {
+#pragma omp atomic write
+               err = 1;
+            }
+            for (int e = 0; e < r.num; e++) {
+               const int inv = r.tgt[e];
+               if ((0 <= inv && inv <= b && fabs(r.val[e]) > zero) || inv == b) cnt++;
+            }
+            row[b + 1] = cnt;
+            sb_row_reset(&r);
+         }
+      }
+      sb_acc_free(&r);
+   }
+   for (int b = 0; b < m->n; b++) row[b + 1] += row[b];
+   return err ? OR_NOMEM : OR_OK;
+}
+
+/* Pass 2 fills, then the columns of every row are sorted (SORT_COLUMN_CRS1). */
+int or_sb_fill(const dg_sb_model *m, const long *row, int *col, double *val, int threads) {
+   const double zero = pow(10, -15);
+   int err = 0;
+#pragma omp parallel num_threads(threads)
+   {
+      sb_row_acc r;
+      sb_cv *tmp = NULL;
+      if (sb_acc_init(m, &r) || !(tmp = malloc(sizeof(sb_cv) * r.cap))) {
+#pragma omp atomic write
+         err = 1;
+      } else {
+#pragma omp for schedule(static)
+         for (int b = 0; b < m->n; b++) {
+            if (sb_row(m, b, &r)) {
+#pragma omp atomic write
+               err = 1;
+            }
+            int k = 0;
+            for (int e = 0; e < r.num; e++) {
+               const int inv = r.tgt[e];
+               if ((0 <= inv && inv <= b && fabs(r.val[e]) > zero) || inv == b) {
+                  tmp[k].c = inv;
+                  tmp[k].v = r.val[e];
+                  k++;
+               }
+            }
+            sb_row_reset(&r);
+            if (row[b] + k != row[b + 1]) {
+#pragma omp atomic write
+               err = 2;
+               continue;
+            }
+            qsort(tmp, k, sizeof(sb_cv), sb_cv_cmp);
+            for (int e = 0; e < k; e++) {
+               col[row[b] + e] = tmp[e].c;
+               val[row[b] + e] = tmp[e].v;
+            }
+         }
+      }
+      free(tmp);
+      sb_acc_free(&r);
+   }
+   return err ? OR_ARG : OR_OK;
+}

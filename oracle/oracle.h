@@ -16,6 +16,7 @@
 
 #include "dmrg_gb300_types.h"
 #include "dmrg_gb300_ed.h"
+#include "dmrg_gb300_sb.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -97,6 +98,9 @@ int or_ed_basis(const dg_ed_model *m, long *basis, long dim, int threads);
 int or_ed_count(const dg_ed_model *m, const long *basis, long dim, long *row, int threads);
 int or_ed_fill(const dg_ed_model *m, const long *basis, long dim, const long *row, int *col, double *val, int threads);
 /* Out = O_site Vec on ED bases (exact/EXACT_V_M_Q0..Q3.c); n_ele may be NULL (no sign). */
+/* Superblock Hamiltonian, lower triangle + diagonal last: row[n+1] (count), then col/val. */
+int or_sb_count(const dg_sb_model *m, long *row, int threads);
+int or_sb_fill(const dg_sb_model *m, const long *row, int *col, double *val, int threads);
 int or_site_apply(const CRS1 *op, const long *out_basis, long dim_out, const long *in_basis, long dim_in, int dim_onsite, int site,
                   const int *n_ele, const double *vec, double *out, int threads);
 

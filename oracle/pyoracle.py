@@ -89,6 +89,8 @@ def load() -> C.CDLL:
             "or_ed_count": (C.c_int, [P(dg_ed_model), lp, C.c_long, lp, C.c_int]),
             "or_ed_fill": (C.c_int, [P(dg_ed_model), lp, C.c_long, lp, ip, dp, C.c_int]),
             "or_site_apply": (C.c_int, [P(CRS1), lp, C.c_long, lp, C.c_long, C.c_int, C.c_int, ip, dp, dp, C.c_int]),
+            "or_sb_count": (C.c_int, [P(abi.dg_sb_model), lp, C.c_int]),
+            "or_sb_fill": (C.c_int, [P(abi.dg_sb_model), lp, ip, dp, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -175,6 +177,34 @@ def ed_build(model, threads=None):
     assert lib.or_ed_fill(m, ptr(basis, C.c_long), dim, ptr(row, C.c_long), ptr(col, C.c_int), ptr(val, C.c_double),
                           th) == 0
     return basis, row, col[:row[-1]], val[:row[-1]]
+
+
+def sb_build(model, threads=None):
+    """Superblock lower-triangle CRS (row, col, val) of a dmrg_c_gb300.sb_models.SBModel."""
+    th = threads or threads_default()
+    lib = load()
+    n = model.n
+    row = np.zeros(n + 1, np.int64)
+    assert lib.or_sb_count(C.byref(model.struct), ptr(row, C.c_long), th) == 0
+    col = np.empty(max(row[-1], 1), np.int32)
+    val = np.empty(max(row[-1], 1), np.float64)
+    assert lib.or_sb_fill(C.byref(model.struct), ptr(row, C.c_long), ptr(col, C.c_int), ptr(val, C.c_double), th) == 0
+    return row, col[:row[-1]], val[:row[-1]]
+
+
+def ref_sb_build(model, cap=None):
+    """The same through the reference's own DMRG_MAKE_ELEM_*_LLLRRRRL builders (oracle/_ref)."""
+    lib = load_ref()
+    lib.ref_sb_build.restype = C.c_int
+    lib.ref_sb_build.argtypes = [P(abi.dg_sb_model), lp, ip, dp, C.c_long]
+    n = model.n
+    cap = cap or n * 64
+    row = np.zeros(n + 1, np.int64)
+    col = np.empty(cap, np.int32)
+    val = np.empty(cap, np.float64)
+    rc = lib.ref_sb_build(C.byref(model.struct), ptr(row, C.c_long), ptr(col, C.c_int), ptr(val, C.c_double), cap)
+    assert rc == 0, rc
+    return row, col[:row[-1]].copy(), val[:row[-1]].copy()
 
 
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):

@@ -113,6 +113,19 @@ def klm_ed_fixture():
     np.savez_compressed(HERE / "klm_ed.npz", **out)
 
 
+def sb_fixture():
+    """The reference's superblock element builders (DMRG_MAKE_ELEM_*_LLLRRRRL) driven over a
+    seeded Hubbard-type term list (OBC and PBC bonds): lower-triangle CRS arrays."""
+    from dmrg_c_gb300 import sb_models
+    out = {}
+    for tag, pbc in (("obc", False), ("pbc", True)):
+        m = sb_models.small_hubbard_model(pbc)
+        row, col, val = po.ref_sb_build(m)
+        out[f"{tag}_row"], out[f"{tag}_col"], out[f"{tag}_val"] = row, col, val
+        out[f"{tag}_inv_checksum"] = np.int64(int(m.inv.astype(np.int64).sum()))
+    np.savez_compressed(HERE / "sb_hubbard.npz", **out)
+
+
 def vm_fixture():
     """EXACT_V_M_Q0 on a Hubbard basis with the reference's C^dagger_up site operator."""
     model = ed_models.hubbard_chain(6, t=-1.0, U=2.0, n_ele=6, twoSz=0)
@@ -164,6 +177,7 @@ def main():
     sml_fixture()
     tridiag_fixture()
     klm_ed_fixture()
+    sb_fixture()
     vm_fixture()
     obc_fixture()
     xxz_energy_fixture()
