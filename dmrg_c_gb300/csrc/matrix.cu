@@ -223,6 +223,10 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   }
   DG_CUDA(cudaGetLastError());
   choose_sell_shape(nslices, total, &m->sell_ws, &m->sell_grid);
+  // Measured on GB300 (superblocks of 3.6 k - 228 k rows): with one or two warps per slice
+  // the software-pipelined 8-element groups are fastest, with four or eight the 16-element
+  // groups (more loads in flight per warp).
+  m->sell_variant = (m->sell_ws >= 4) ? V_U16 : V_PIPE8;
   DG_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -79,8 +79,8 @@ void launch_sell(const SellOp<VT> &op, int grid, const XT *x, const double *scal
 }
 
 // Warps per slice and grid for the sliced-ELL kernel (heuristic from measured sweeps):
-// short rows (ED matrices) one warp per slice; otherwise enough warps of work to fill every
-// SM with at least ~16 elements per warp and row.
+// short rows (ED matrices) one warp per slice; otherwise split slices over more warps while
+// each keeps >= 32 elements of every row (or >= 8 for matrices too small to fill the GPU).
 void choose_sell_shape(int nslices, long stored, int *ws, int *grid);
 
 // Apply the matrix in its selected format with FP64 values.

@@ -4,6 +4,10 @@
     python -m dmrg_c_gb300.profile_spmv --sweep              # every SELL shape / variant / window
     python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --format sell --launches 3
                                                              # a few launches, for an ncu capture
+    python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --mixed --launches 3
+                                                             # the mixed-precision product
+    python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
+    python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
 
 Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
 256 MiB buffer before every launch so the matrix is not L2-resident, "warm" does not.
@@ -93,18 +97,44 @@ def survey(names, sweep, iters, out):
             json.dump(rows, f, indent=1)
 
 
-def launches(name, fmt, count):
+def launches(name, fmt, count, mixed=False):
     """`count` launches of one kernel on one matrix (nothing else on the device after setup)."""
     import torch
     low = CASES[name](0).explicit_lower()
-    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST)
+    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH if mixed else L.DG_VALUES_F64)
     x = torch.randn(m.n, dtype=torch.float64, device="cuda")
     if fmt == "csr":
         m.set_shape(8, _csr_grid(m.n, 8, torch.cuda.get_device_properties(x.device).multi_processor_count))
     y = torch.empty_like(x)
-    t = m.profile_spmv(x, y, iters=count)
-    B = algorithmic_bytes(m.n, m.nnz)
-    print(f"{name} {fmt}: {t * 1e3:.1f} us per launch ({B / t / 1e6:.0f} GB/s), n={m.n} nnz_full={m.nnz}")
+    if mixed:
+        t = m.profile_spmv_mixed(x.float(), y, iters=count)
+        B = algorithmic_bytes(m.n, m.nnz, 4, 4)
+    else:
+        t = m.profile_spmv(x, y, iters=count)
+        B = algorithmic_bytes(m.n, m.nnz)
+    print(f"{name} {fmt}{' mixed' if mixed else ''}: {t * 1e3:.1f} us per launch ({B / t / 1e6:.0f} GB/s), "
+          f"n={m.n} nnz_full={m.nnz}")
+
+
+BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512")
+
+
+def build(which, repeats=3):
+    """Device builds: ED basis + Hamiltonian, or the superblock CRS (wall time per build)."""
+    import time
+    from . import ed_models
+    if which.startswith("ed_"):
+        model = ed_models.hubbard_chain(12, U=4.0, hz=0.2) if which == "ed_hubbard12" else ed_models.xxz_chain(22, Jz=1.3)
+        make = lambda: L.EDSystem(model)  # noqa: E731
+    else:
+        model = workloads.hubbard_sb_model_m512(0)
+        make = lambda: L.SuperblockCRS(model)  # noqa: E731
+    for k in range(repeats):
+        t0 = time.perf_counter()
+        s = make()
+        dt = time.perf_counter() - t0
+        print(f"{which}: {dt * 1e3:.1f} ms (n={getattr(s, 'dim', getattr(s, 'n', 0))}, nnz={s.nnz})", flush=True)
+        s.close()
 
 
 def main(argv=None):
@@ -116,9 +146,13 @@ def main(argv=None):
     ap.add_argument("--case", choices=list(CASES), default=None)
     ap.add_argument("--format", choices=["sell", "csr"], default="sell")
     ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--build", choices=BUILDS, default=None)
     a = ap.parse_args(argv)
-    if a.case:
-        launches(a.case, a.format, a.launches)
+    if a.build:
+        build(a.build)
+    elif a.case:
+        launches(a.case, a.format, a.launches, a.mixed)
     else:
         survey(a.cases, a.sweep, a.iters, a.json)
     return 0
