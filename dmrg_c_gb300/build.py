@@ -25,7 +25,7 @@ BUILD = ROOT / "_build" / "lib"
 LIB = PKG / "libdmrg_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 

@@ -99,6 +99,9 @@ SIGNATURES = {
     "dg_linear_solve": (C.c_int, [vp, C.c_double, vp, vp, C.c_double, C.c_int, C.c_int, ip]),
     "dg_residual_l1": (C.c_int, [vp, vp, C.c_double, dp]),
     "dg_cg_noalloc": (C.c_int, [C.c_int, vp, vp, vp, C.c_double, vp, vp, C.c_double, C.c_int, ip]),
+    "FIND_DIM": (C.c_int, [P(abi.MODEL_1DKLM_VF), P(EXACT_TIME)]),
+    "GET_BASIS": (lp, [P(abi.MODEL_1DKLM_VF), P(EXACT_TIME), C.c_int]),
+    "GET_HAM": (P(CRS1), [P(abi.MODEL_1DKLM_VF), P(EXACT_BASIS_INFO), P(EXACT_PARAMETER), P(EXACT_TIME)]),
     "dg_ed_dim": (C.c_int, [P(abi.dg_ed_model), lp]),
     "dg_ed_build": (C.c_int, [P(abi.dg_ed_model), P(vp)]),
     "dg_ed_free": (None, [vp]),

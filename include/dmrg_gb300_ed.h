@@ -72,6 +72,16 @@ int dg_ed_download(const dg_ed *ed, long *basis, long *row, int *col, double *va
 /* A solver operator (dg_matrix, full storage) built from the device CRS. */
 int dg_ed_matrix(const dg_ed *ed, int values, dg_matrix **out);
 
+/* ---- Drop-ins for the KLM exact-diagonalisation driver ----------------------------------
+ * main/exact_diag/klm_vf/include/Header.h:54-58: the basis count, the sorted basis and the
+ * Hamiltonian CRS of the 1D Kondo lattice, computed on the GPU from the model's term list
+ * and site operators (onsite_op/ONSITE_*_SZBASIS_KLM.c conventions), with the driver's own
+ * output allocations (malloc-based, released by FREE_ARRAY_LINT1 / FREE_CRS1), timing fields
+ * and error exits.  Values and ordering are bit-exact to the driver's. */
+int FIND_DIM(MODEL_1DKLM_VF *Model, EXACT_TIME *Time);
+long *GET_BASIS(MODEL_1DKLM_VF *Model, EXACT_TIME *Time, int dim);
+CRS1 *GET_HAM(MODEL_1DKLM_VF *Model, EXACT_BASIS_INFO *Basis_Info, EXACT_PARAMETER *Param, EXACT_TIME *Time);
+
 /* ---- Concurrent solve engine: batched and served ED ground states (no counterpart in the
  * reference, whose ED driver solves one instance per run, EXACT_DIAGONALIZATION.c).
  * Worker threads, one CUDA stream each, take jobs in submission order; a job starts when a

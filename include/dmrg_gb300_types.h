@@ -11,6 +11,7 @@
  *   DMRG_BOX_LAN, DMRG_BOX_CG, DMRG_BOX_II include/dmrg.h:269-328
  *   EXACT_PARAMETER, EXACT_TIME           include/exact.h:14-37, 39-51
  *   EXACT_HAM_INFO, EXACT_BASIS_INFO      include/exact.h:54-74
+ *   MODEL_1DKLM_VF                        include/model.h:22-45
  *   EXACT_WHOLE_BASIS_Q1..Q3              include/exact.h:89-111
  *
  * Each group is guarded by the reference header's own include guard (SML_h, dmrg_h,
@@ -289,6 +290,35 @@ typedef struct {
    int max_dim;
 } EXACT_WHOLE_BASIS_Q3;
 #endif /* exact_h */
+
+/* The 1D Kondo-lattice model parameters (the KLM exact-diagonalisation driver's model).
+ * Guarded by the reference's model.h guard: include the reference's model.h first when a
+ * translation unit needs its other MODEL_* types as well. */
+#ifndef model_h
+#define model_h
+
+typedef struct {
+   char BC[1000];
+   int p_threads;
+   int spin_loc;
+   int tot_site;
+   int tot_sz;
+   int tot_ele;
+   int dim_onsite;
+   int dim_lspin;
+   int dim_charge;
+   int cf_origin;
+   double avg_range;
+   double t;
+   double J;
+   double D_z;
+   double I_xy;
+   double I_z;
+   double h_z;
+   double mu;
+} MODEL_1DKLM_VF;
+
+#endif /* model_h */
 
 #ifdef __cplusplus
 }

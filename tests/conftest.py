@@ -77,3 +77,17 @@ def klm_model_from_golden(g, tag):
     tabs = [(g[f"{tag}_op{k}_row"], g[f"{tag}_op{k}_col"], g[f"{tag}_op{k}_val"]) for k in range(9)]
     return ed_models.klm_chain_from_tables(int(L), tabs, int(ne), int(sz), t=float(t), I_z=float(I_z), I_xy=float(I_xy),
                                            bc="PBC" if tag == "pbc" else "OBC")
+
+
+def klm_driver_model(g, tag):
+    """The MODEL_1DKLM_VF of a klm_ed.npz fixture (the reference driver's model struct)."""
+    from dmrg_c_gb300 import abi
+    L, ne, sz, t, J, D_z, I_xy, I_z, h_z, mu, pbc = g[f"{tag}_model"]
+    m = abi.MODEL_1DKLM_VF()
+    m.BC = b"PBC" if pbc else b"OBC"
+    m.p_threads = 1
+    m.spin_loc = 1
+    m.tot_site, m.tot_ele, m.tot_sz = int(L), int(ne), int(sz)
+    m.dim_charge, m.dim_lspin, m.dim_onsite = 4, 2, 8
+    m.t, m.J, m.D_z, m.I_xy, m.I_z, m.h_z, m.mu = t, J, D_z, I_xy, I_z, h_z, mu
+    return m

@@ -107,6 +107,9 @@ def klm_ed_fixture():
         basis, row, col, val = po.ref_klm_ed(m)
         tabs = po.ref_klm_site_ops(m)
         out[f"{tag}_params"] = np.array([L, ne, sz, kw["t"], kw.get("I_z", 0.0), kw.get("I_xy", 0.0)])
+        # every MODEL_1DKLM_VF parameter: L, N_e, 2Sz, t, J, D_z, I_xy, I_z, h_z, mu, PBC
+        out[f"{tag}_model"] = np.array([L, ne, sz, kw["t"], kw.get("J", 0.0), kw.get("D_z", 0.0), kw.get("I_xy", 0.0),
+                                        kw.get("I_z", 0.0), kw.get("h_z", 0.0), kw.get("mu", 0.0), bc == "PBC"])
         out[f"{tag}_basis"], out[f"{tag}_row"], out[f"{tag}_col"], out[f"{tag}_val"] = basis, row, col, val
         for k, (r, c, v) in enumerate(tabs):
             out[f"{tag}_op{k}_row"], out[f"{tag}_op{k}_col"], out[f"{tag}_op{k}_val"] = r, c, v
