@@ -6,6 +6,7 @@
 // a full CRS whose rows are sorted by column, so every SpMV is a pure gather with a fixed
 // summation order (bitwise reproducible) and no atomics.
 #include <algorithm>
+#include <climits>
 
 #include <type_traits>
 
@@ -86,21 +87,75 @@ __global__ void k_fill_upper(const int64_t *__restrict__ row, const int *__restr
   }
 }
 
-// Sort each row's upper segment by column (columns in a segment are distinct): every
-// element's destination is its rank within the segment.
-__global__ void k_rank_upper(const int64_t *__restrict__ row, const int64_t *__restrict__ frow, int n,
-                             const int *__restrict__ scol, const double *__restrict__ sval, int *fcol, double *fval) {
-  const int lane = threadIdx.x & 31;
+// Sort each row's upper segment by column (columns in a segment are distinct).  A warp per
+// row: segments of up to 64 entries rank every element against the others through register
+// shuffles (destination = rank); up to kSortCap entries are bitonic-sorted in shared memory
+// as keys (column << 32 | slot) with the values gathered by slot; longer segments fall back to
+// a rank count from memory.
+constexpr int kSortCap = 256;
+
+__global__ void __launch_bounds__(kThreads) k_rank_upper(const int64_t *__restrict__ row, const int64_t *__restrict__ frow, int n,
+                                                        const int *__restrict__ scol, const double *__restrict__ sval, int *fcol,
+                                                        double *fval) {
+  __shared__ unsigned long long keys[kWarps][kSortCap];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned long long *key = keys[wib];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int i = warp; i < n; i += nw) {
     const int64_t b = frow[i] + (row[i + 1] - row[i]), e = frow[i + 1];
-    const int64_t m = e - b;
-    for (int64_t t = lane; t < m; t += 32) {
-      const int c = scol[b + t];
-      int64_t rank = 0;
-      for (int64_t u = 0; u < m; ++u) rank += (scol[b + u] < c);
-      fcol[b + rank] = c;
-      fval[b + rank] = sval[b + t];
+    const int m = (int)(e - b);
+    if (m <= 64) {
+      const int c0 = (lane < m) ? scol[b + lane] : INT_MAX;
+      const int c1 = (lane + 32 < m) ? scol[b + 32 + lane] : INT_MAX;
+      int r0 = 0, r1 = 0;
+      for (int u = 0; u < 32; ++u) {
+        const int v0 = __shfl_sync(0xffffffffu, c0, u), v1 = __shfl_sync(0xffffffffu, c1, u);
+        r0 += (v0 < c0) + (v1 < c0);
+        r1 += (v0 < c1) + (v1 < c1);
+      }
+      if (lane < m) {
+        fcol[b + r0] = c0;
+        fval[b + r0] = sval[b + lane];
+      }
+      if (lane + 32 < m) {
+        fcol[b + r1] = c1;
+        fval[b + r1] = sval[b + 32 + lane];
+      }
+    } else if (m <= kSortCap) {
+      int P = 1;
+      while (P < m) P <<= 1;
+      for (int t = lane; t < P; t += 32)
+        key[t] = (t < m) ? (((unsigned long long)(unsigned)scol[b + t] << 32) | (unsigned)t) : ~0ull;
+      __syncwarp();
+      for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+          for (int t = lane; t < P; t += 32) {
+            const int u = t ^ j;
+            if (u > t) {
+              const unsigned long long a = key[t], c = key[u];
+              if ((a > c) == ((t & k) == 0)) {
+                key[t] = c;
+                key[u] = a;
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+      for (int t = lane; t < m; t += 32) {
+        const unsigned long long kk = key[t];
+        fcol[b + t] = (int)(kk >> 32);
+        fval[b + t] = sval[b + (int)(kk & 0xffffffffu)];
+      }
+      __syncwarp();
+    } else {
+      for (int64_t t = lane; t < m; t += 32) {
+        const int c = scol[b + t];
+        int64_t rank = 0;
+        for (int64_t u = 0; u < m; ++u) rank += (scol[b + u] < c);
+        fcol[b + rank] = c;
+        fval[b + rank] = sval[b + t];
+      }
     }
   }
 }
