@@ -1,0 +1,58 @@
+"""bench.py's multi-process path (replicas only: no data-path collective) with two gloo
+ranks on the CPU: the job's time is the slowest replica's, its rate sums the replicas, and
+the reference arm runs on rank 0 only."""
+import os
+import socket
+import sys
+
+import pytest
+import torch.multiprocessing as mp
+
+from conftest import ROOT
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank(rank, port, out):
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE="2", LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=2)
+    ws, r, lr = bench.dist_info()
+    bench.replica_barrier(ws)
+    my_ms = 100.0 if rank == 0 else 150.0          # rank 1 is the slower replica
+    t = bench.replica_time(my_ms, ws, device="cpu")
+    out[rank] = (ws, r, t, bench.job_rate(10, ws, t))
+    dist.destroy_process_group()
+
+
+def test_two_gloo_replicas_take_the_slowest_time():
+    port = _free_port()
+    with mp.Manager() as mgr:
+        out = mgr.dict()
+        mp.start_processes(_rank, args=(port, out), nprocs=2, join=True, start_method="spawn")
+        res = dict(out)
+    for rank in (0, 1):
+        ws, r, t, rate = res[rank]
+        assert ws == 2 and r == rank
+        assert t == 150.0
+        assert rate == pytest.approx(2 * 10 / 0.150)
+
+
+def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class A:
+        workload = "xxz_m64"
+        seed = 0
+        steps = 1
+        warmup = 0
+    assert bench.run_reference(A(), 2, 1) is None
