@@ -57,3 +57,16 @@ def test_engine_budget_serialises_large_jobs(gpu):
     r0, r1 = res[0], res[1]
     assert r0.status == 0 and r1.status == 0
     assert r1.t_start_ms >= r0.t_done_ms or r0.t_start_ms >= r1.t_done_ms
+
+
+@pytest.mark.gpu
+def test_engine_refuses_bad_jobs_at_submission(gpu):
+    eng = gpu.Engine(workers=2)
+    with pytest.raises(gpu.DgError):
+        eng.submit(ed_models.xxz_chain(6, twoSz=1), gpu.default_params(), 0)     # empty sector
+    bad = ed_models.xxz_chain(6)
+    bad.struct.terms[0].op1 = 99
+    with pytest.raises(gpu.DgError):
+        eng.submit(bad, gpu.default_params(), 1)
+    assert eng.pending()[:2] == (0, 0)
+    eng.close()

@@ -42,3 +42,29 @@ def test_sb_matrix_ground_state_matches_oracle(gpu, oracle):
     row, col, val = oracle.sb_build(m)
     rc, out, vr = oracle.lanczos(abi.Crs(row, col, val, n=m.n), True, seed=4)
     assert abs(info.eig_val - out.eig_val) <= 1e-12 * abs(out.eig_val)
+
+
+@pytest.mark.gpu
+def test_sb_build_rejects_malformed_models(gpu):
+    """Bad positions, operator indices, signs without electron tables and out-of-range basis
+    states are refused on the host, before any kernel runs."""
+    from dmrg_c_gb300.sb_models import SBModel
+
+    def variant(**change):
+        m = sb_models.small_hubbard_model(False)
+        terms = [list(t) for t in m.terms]
+        ele = list(m.ele)
+        LLv = m.LL.copy()
+        if "pos" in change:
+            terms[4][0] = change["pos"]
+        if "op" in change:
+            terms[4][2] = change["op"]
+        if "noele" in change:
+            ele[0] = None
+        if "state" in change:
+            LLv[3] = change["state"]
+        return SBModel(m.n, m.dim_LL, m.dim_RR, m.d, LLv, m.LR, m.RR, m.RL, m.inv, m.ops, [tuple(t) for t in terms], ele)
+
+    for bad in (dict(pos=7), dict(op=999), dict(noele=True), dict(state=40)):
+        with pytest.raises(gpu.DgError):
+            gpu.SuperblockCRS(variant(**bad))
