@@ -18,6 +18,8 @@ DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: Lanczos (acc 1e-14, Normal) then invers
 * ``roofline``: the fused SpMV kernel (product + <x,y> epilogue), CUDA-event timed with L2
   flushed before each launch; algorithmic bytes nnz_full*12 + (n+1)*4 + 2*n*8.
 * ``cpu_baseline``: the oracle's OpenMP restatement of the same solve on all host cores.
+* ``roofline_hbm_case``: the HBM-bound product (Hubbard m=512 superblock, 0.69 GB), FP64 with the
+  autotuned shape and the mixed-precision product, L2 flushed before every launch.
 
 ``--impl reference`` times the CPU path (the oracle port of the reference's LANCZOS_SYM +
 INVERSE_ITERATION_SYM; the reference itself cannot be built on the benchmark host) on the
@@ -168,15 +170,42 @@ def spmv_bytes(n, nnz_full, s_val=8, s_vec=8):
     return nnz_full * (s_val + 4) + (n + 1) * 4 + 2 * n * s_vec
 
 
-def traffic_from_profile(workload):
+def traffic_from_profile(workload, mixed=False):
     """DRAM bytes (read + write) per launch of the SpMV kernel, from the committed ncu summary
-    of this workload (profiles/k_apply_sell_<workload>.md), if present."""
-    f = ROOT / "profiles" / f"k_apply_sell_{workload}.md"
+    of this workload (profiles/k_apply_sell_[mixed_]<workload>.md), if present."""
+    f = ROOT / "profiles" / f"k_apply_sell_{'mixed_' if mixed else ''}{workload}.md"
     if f.exists():
         for line in f.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
                 return int(line.split(":")[1])
     return None
+
+
+def hbm_case_roofline(peak, peak_kind):
+    """The HBM-bound product: the Hubbard m=512 superblock (n = 227,652, 57.1 M stored, 0.69 GB),
+    FP64 with the autotuned shape and the mixed-precision product, CUDA-event timed with L2
+    flushed before every launch (the matrix is 5x the L2)."""
+    import torch
+    from dmrg_c_gb300 import lib as L
+    low = build_workload("hubbard_m512", 0)[1]
+    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH)
+    x = torch.randn(m.n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    t_heur = m.profile_spmv(x, y, iters=20, flush_bytes=FLUSH_BYTES)
+    t32 = m.profile_spmv_mixed(x.float(), y, iters=20, flush_bytes=FLUSH_BYTES)   # heuristic shape
+    tune = m.autotune(iters=5)                                                    # FP64 shapes
+    t64 = m.profile_spmv(x, y, iters=20, flush_bytes=FLUSH_BYTES)
+    B64, B32 = spmv_bytes(m.n, m.nnz), spmv_bytes(m.n, m.nnz, 4, 4)
+    a64, a32 = B64 / (t64 * 1e-3) / 1e9, B32 / (t32 * 1e-3) / 1e9
+    out = {"workload": "hubbard_m512 superblock SpMV", "n": m.n, "nnz_full": m.nnz, "bound": "hbm", "unit": "GB/s",
+           "peak": peak, "peak_source": peak_kind,
+           "fp64": {"kernel": f"k_apply_sell<double> (autotuned: WS={tune.shape} variant={tune.variant} window={tune.window})",
+                    "ms_per_launch": t64, "bytes_per_launch": B64, "achieved": a64, "frac": a64 / peak,
+                    "traffic": traffic_from_profile("hubbard_m512"), "heuristic_ms_per_launch": t_heur},
+           "mixed": {"kernel": "k_apply_sell<float> (compensated FP32 sums, heuristic shape)", "ms_per_launch": t32, "bytes_per_launch": B32,
+                     "achieved": a32, "frac": a32 / peak, "traffic": traffic_from_profile("hubbard_m512", mixed=True)}}
+    m.close()
+    return out
 
 
 def run_gb300(args, ws, rank, local_rank):
@@ -312,6 +341,8 @@ def run_gb300(args, ws, rank, local_rank):
         "mixed": mixed,
         "mixed_fp32_spmv": mixed_rec,
     }
+    if rank == 0 and not args.no_hbm_case:
+        result["roofline_hbm_case"] = hbm_case_roofline(peak, peak_kind)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         secs, E_cpu, v_cpu, st_cpu, cg_cpu = oracle_solve(low, args.seed + 1, threads)
@@ -357,6 +388,7 @@ def main(argv=None):
     ap.add_argument("--workload", choices=sorted(WORKLOAD_DESC), default="klm_m128")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-hbm-case", action="store_true", help="skip the m=512 superblock product roofline")
     args = ap.parse_args(argv)
     ws, rank, local_rank = dist_info()
     if args.impl == "reference":

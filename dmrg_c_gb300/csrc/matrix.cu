@@ -635,6 +635,7 @@ int dg_matrix_set_sell_variant(dg_matrix *m, int variant) {
     DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
     DG_REQUIRE(variant >= 0 && variant < V_COUNT, DG_ERR_ARG, "unknown variant %d", variant);
     m->sell_variant = variant;
+    m->sell_variant32 = variant;
   });
 }
 

@@ -21,7 +21,9 @@ struct dg_matrix {
   long nnz_sell = 0;               // stored elements including padding
   int sell_grid = 1;
   int sell_ws = 1;                 // warps per slice
-  int sell_variant = 1;            // SellVariant (V_U8)
+  int sell_variant = 1;            // SellVariant of the FP64 product (V_U8)
+  int sell_variant32 = 1;          // SellVariant of the FP32 (mixed) product: 8-element groups
+                                   // measured fastest there at every warps-per-slice count
   int sell_window = dg::kSellWindow;   // row-sorting window (<= 32: rows keep their order)
   dg::DevBuf<int64_t> s_off;
   dg::DevBuf<int> s_width, s_perm, s_col;
@@ -31,7 +33,7 @@ struct dg_matrix {
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }
   dg::CrsOp<float> op32() const { return dg::CrsOp<float>{row.get(), col.get(), val32.get()}; }
   dg::SellOp<double> sell64() const { return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant}; }
-  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant}; }
+  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant32}; }
 };
 
 namespace dg {

@@ -141,8 +141,9 @@ int dg_matrix_set_shape(dg_matrix *m, int lanes_per_row, int grid);
 int dg_matrix_set_format(dg_matrix *m, int format);
 /* Use the sliced-ELL kernel with warps_per_slice (1, 2, 4, 8) warps sharing a 32-row slice. */
 int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid);
-/* Sliced-ELL kernel variant: element groups of 0: 4, 1: 8 (default), 2: 16,
- * 3: 8 with software-pipelined loads. */
+/* Sliced-ELL kernel variant: element groups of 0: 4, 1: 8, 2: 16, 3: 8 with
+ * software-pipelined loads.  The FP64 product's default follows the warps per slice (3 for
+ * 1-2 warps, 2 for 4-8), the FP32 (mixed) product's is 1; this call sets both. */
 int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
 /* Rebuild the sliced-ELL copy sorting rows by length within windows of `window` rows
  * (1..2048; <= 32 keeps the original row order). */
