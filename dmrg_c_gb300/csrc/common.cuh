@@ -190,17 +190,22 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Sum of v over the block; valid in thread 0.
+// Sum of v over a block of kThreads threads; valid in thread 0.  The values are transposed
+// through shared memory so that warp 0 alone adds them: each lane sums the kWarps values of
+// its column (a pairwise tree, 7 adds), then one shuffle tree (5 adds).  That is 12 warp-wide
+// FP64 adds a block instead of 45 for a shuffle tree in every warp -- on GB300 each FP64 add
+// occupies the same scarce FP64 pipe as the products' multiply-adds, and in a vector kernel
+// with ~3 FP64 operations per element the per-warp trees cost more than the useful work.
 __device__ __forceinline__ double block_sum(double v) {
-  __shared__ double sm[kWarps];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  v = warp_sum(v);
-  __syncthreads();
-  if (lane == 0) sm[w] = v;
+  static_assert(kWarps == 8, "column sum below is written for 8 warps");
+  __shared__ double sm[kThreads];
+  __syncthreads();   // an earlier block_sum's readers are done with sm
+  sm[threadIdx.x] = v;
   __syncthreads();
   double r = 0.0;
-  if (w == 0) {
-    r = (lane < kWarps) ? sm[lane] : 0.0;
+  if (threadIdx.x < 32) {
+    const double *c = sm + threadIdx.x;
+    r = ((c[0] + c[32]) + (c[64] + c[96])) + ((c[128] + c[160]) + (c[192] + c[224]));
     r = warp_sum(r);
   }
   return r;

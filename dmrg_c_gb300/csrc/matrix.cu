@@ -278,10 +278,13 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   }
   DG_CUDA(cudaGetLastError());
   choose_sell_shape(nslices, total, &m->sell_ws, &m->sell_grid);
-  // Measured on GB300 (superblocks of 3.6 k - 228 k rows): with one or two warps per slice
-  // the software-pipelined 8-element groups are fastest, with four or eight the 16-element
-  // groups (more loads in flight per warp).
-  m->sell_variant = (m->sell_ws >= 4) ? V_U16 : V_PIPE8;
+  // Measured on GB300.  Superblocks (3.6 k - 228 k rows, 24+ stored elements a row): with one
+  // or two warps per slice the software-pipelined 8-element groups are fastest, with four or
+  // eight the 16-element groups (more loads in flight per warp).  ED Hamiltonians (0.7 - 0.85 M
+  // rows of ~12 elements, one warp per slice): a whole row fits one 16-element group, and the
+  // pipelined form, which has no second group to overlap, is the slowest (12-14 % behind).
+  const double per_row = (double)total / ((double)nslices * kSellC);
+  m->sell_variant = (m->sell_ws >= 4 || per_row < 24.0) ? V_U16 : V_PIPE8;
   DG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -585,7 +588,7 @@ void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size
   DG_CUDA(cudaEventCreate(&e0));
   DG_CUDA(cudaEventCreate(&e1));
   double total = 0.0;
-  for (int it = 0; it < iters; ++it) {
+  for (int it = -1; it < iters; ++it) {   // it = -1: untimed launch (module load, first-touch costs)
     if (flush_bytes) DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
     DG_CUDA(cudaEventRecord(e0, st));
     const EpiDot<double> epi{y_dev, out.get()};
@@ -600,7 +603,7 @@ void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size
     DG_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    total += ms;
+    if (it >= 0) total += ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -1,4 +1,4 @@
-"""SpMV rate survey of the library's operator kernels on the named superblock matrices.
+"""SpMV rate survey of the library's operator kernels on the named superblock and ED matrices.
 
     python -m dmrg_c_gb300.profile_spmv                      # heuristic and autotuned rates
     python -m dmrg_c_gb300.profile_spmv --sweep              # every SELL shape / variant / window
@@ -6,6 +6,8 @@
                                                              # a few launches, for an ncu capture
     python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --mixed --launches 3
                                                              # the mixed-precision product
+    python -m dmrg_c_gb300.profile_spmv --sweep --cases xxz_ed22 hubbard_ed12
+                                                             # the ED Hamiltonians
     python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
     python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
 
@@ -19,6 +21,7 @@ import argparse
 import json
 import sys
 
+from . import ed_models
 from . import lib as L
 from . import workloads
 
@@ -27,6 +30,22 @@ CASES = {
     "klm_m128": workloads.klm_superblock_m128,
     "hubbard_m512": workloads.hubbard_superblock_m512,
 }
+# ED Hamiltonians (full storage, built on the device): the largest batched-XXZ and served-Hubbard sizes
+ED_CASES = {
+    "xxz_ed22": lambda: ed_models.xxz_chain(22, Jz=1.3, hz=0.4),
+    "hubbard_ed12": lambda: ed_models.hubbard_chain(12, U=4.0, hz=0.2),
+}
+
+
+def _matrix(name, values=None):
+    """Device matrix of a named case (superblock: host lower CRS uploaded; ED: built on the device)."""
+    values = L.DG_VALUES_F64 if values is None else values
+    if name in ED_CASES:
+        ed = L.EDSystem(ED_CASES[name]())
+        m = ed.matrix(values)
+        ed.close()
+        return m
+    return L.DeviceMatrix(CASES[name](0).explicit_lower(), L.DG_STORE_LOWER_DIAG_LAST, values)
 FLUSH = 256 << 20
 
 
@@ -45,21 +64,23 @@ def _csr_grid(n, lanes, sms):
 
 
 def _rate(m, x, y, iters):
-    cold = m.profile_spmv(x, y, iters=iters, flush_bytes=FLUSH)
-    warm = m.profile_spmv(x, y, iters=iters)
+    prof = m.profile_spmv_mixed if x.dtype != y.dtype else m.profile_spmv
+    cold = prof(x, y, iters=iters, flush_bytes=FLUSH)
+    warm = prof(x, y, iters=iters)
     return cold, warm
 
 
-def survey(names, sweep, iters, out):
+def survey(names, sweep, iters, out, mixed=False):
+    """Heuristic, swept and autotuned rates; with `mixed` the FP32-value product (FP32 x, FP64 y).
+    The sweep sets the FP64 and the FP32 variant together; the autotuner tunes the FP64 product."""
     import torch
     rows = []
     for name in names:
-        low = CASES[name](0).explicit_lower()
-        m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST)
+        m = _matrix(name, L.DG_VALUES_BOTH if mixed else L.DG_VALUES_F64)
         n, nnz = m.n, m.nnz
-        B = algorithmic_bytes(n, nnz)
-        x = torch.randn(n, dtype=torch.float64, device="cuda")
-        y = torch.empty_like(x)
+        B = algorithmic_bytes(n, nnz, 4, 4) if mixed else algorithmic_bytes(n, nnz)
+        x = torch.randn(n, dtype=torch.float32 if mixed else torch.float64, device="cuda")
+        y = torch.empty(n, dtype=torch.float64, device="cuda")
         sms = torch.cuda.get_device_properties(x.device).multi_processor_count
         c, w = _rate(m, x, y, iters)
         print(f"## {name}: n={n} nnz_full={nnz} bytes={B / 1e6:.1f} MB", flush=True)
@@ -100,8 +121,7 @@ def survey(names, sweep, iters, out):
 def launches(name, fmt, count, mixed=False):
     """`count` launches of one kernel on one matrix (nothing else on the device after setup)."""
     import torch
-    low = CASES[name](0).explicit_lower()
-    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH if mixed else L.DG_VALUES_F64)
+    m = _matrix(name, L.DG_VALUES_BOTH if mixed else L.DG_VALUES_F64)
     x = torch.randn(m.n, dtype=torch.float64, device="cuda")
     if fmt == "csr":
         m.set_shape(8, _csr_grid(m.n, 8, torch.cuda.get_device_properties(x.device).multi_processor_count))
@@ -139,11 +159,11 @@ def build(which, repeats=3):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("--cases", nargs="*", default=list(CASES), choices=list(CASES))
+    ap.add_argument("--cases", nargs="*", default=list(CASES), choices=list(CASES) + list(ED_CASES))
     ap.add_argument("--sweep", action="store_true")
     ap.add_argument("--iters", type=int, default=10)
     ap.add_argument("--json", default=None)
-    ap.add_argument("--case", choices=list(CASES), default=None)
+    ap.add_argument("--case", choices=list(CASES) + list(ED_CASES), default=None)
     ap.add_argument("--format", choices=["sell", "csr"], default="sell")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--mixed", action="store_true")
@@ -154,7 +174,7 @@ def main(argv=None):
     elif a.case:
         launches(a.case, a.format, a.launches, a.mixed)
     else:
-        survey(a.cases, a.sweep, a.iters, a.json)
+        survey(a.cases, a.sweep, a.iters, a.json, a.mixed)
     return 0
 
 
