@@ -24,13 +24,24 @@
 
 namespace dg {
 
-// How the input scale s is derived from a device scalar.
-enum ScaleMode : int { SCALE_ONE = 0, SCALE_RSQRT = 1, SCALE_RECIP = 2 };
+// The input scale s: 1, or a device scalar that the kernel which formed it already derived
+// (1/sqrt(<w,w>) of NORMALIZE, 1/gamma0 of MINIMUM_RESIDUAL).  An FP64 square root or
+// division is a long sequence of FP64 instructions; on GB300's few FP64 pipes, evaluated by
+// every thread of a product it costs as much FP64 issue as the product's multiply-adds, so
+// it is evaluated once, by the producer's last block.
+enum ScaleMode : int { SCALE_ONE = 0, SCALE_MUL = 1 };
 
-__device__ __forceinline__ double load_scale(const double *sp, int mode) {
-  if (mode == SCALE_RSQRT) return 1.0 / sqrt(*sp);   // NORMALIZE: norm = 1.0/sqrt(sum)
-  if (mode == SCALE_RECIP) return 1.0 / (*sp);      // MINIMUM_RESIDUAL: temp = 1.0/gamma0
-  return 1.0;
+__device__ __forceinline__ double load_scale(const double *sp, int mode) { return mode == SCALE_MUL ? *sp : 1.0; }
+
+// A squared norm with its normalising scale rs = 1/sqrt(v), both written by the last block of
+// the kernel that reduces v.
+struct Norm2 {
+  double v;
+  double rs;
+};
+__device__ __forceinline__ void set_norm2(Norm2 *p, double t) {
+  p->v = t;
+  p->rs = 1.0 / sqrt(t);
 }
 
 template <class T>

@@ -51,10 +51,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__r
     }
     S->beta = t / S->rr;
     S->rr = t;
-    prog->value = t;
     prog->done = S->done;
-    prog->iters = S->iters;
-    __threadfence_system();
     prog->stamp = it;
   });
 }
@@ -108,11 +105,9 @@ __global__ void __launch_bounds__(kThreads) k_mr_lanczos(int n, const double *__
     S->c0 = c1;
     S->c1 = c2;
     S->gamma0 = gamma1;
+    S->inv_gamma0 = 1.0 / gamma1;
     S->gamma1 = gamma1;
-    prog->value = fabs(S->eta);
     prog->done = S->done;
-    prog->iters = S->iters;
-    __threadfence_system();
     prog->stamp = it + 1;
   });
 }
@@ -184,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef_g,
-                                                    const float *__restrict__ y, int n, double *r2, RedSlot slot) {
+                                                    const float *__restrict__ y, int n, Norm2 *r2, RedSlot slot) {
   pdl_wait();
   extern __shared__ float coef[];   // nvec entries
   for (int j = threadIdx.x; j < nvec; j += blockDim.x) coef[j] = coef_g[j];
@@ -208,12 +203,12 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long
     acc += w * w;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
                                                        const float *__restrict__ y, const double *D, const double *O, int n,
-                                                       double *r2, RedSlot slot) {
+                                                       Norm2 *r2, RedSlot slot) {
   pdl_wait();
   const double a = D[b] * sig[b];
   const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
@@ -228,11 +223,11 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
     acc += w * w;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
-                                                     const double *__restrict__ sig, double *__restrict__ out, int n, double *r2,
+                                                     const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
                                                      RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
@@ -241,7 +236,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ 
     out[i] = t;
     acc += t * t;
   }
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 }  // namespace dg

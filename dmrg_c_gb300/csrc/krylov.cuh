@@ -30,24 +30,26 @@ namespace dg {
 
 // Device-resident scalars of one solve.
 struct Scalars {
-  double r2;        // Lanczos: <w,w> of the pending unnormalised Krylov vector
-  double xn2;       // CG: <x0,x0>; generic norm output
+  Norm2 r2;         // Lanczos: <w,w> of the pending unnormalised Krylov vector
+  Norm2 xn2;        // CG: <x0,x0>; generic norm output
   double rr;        // CG: <r,r> of the current residual
   double a;         // CG: alpha
   double beta;      // CG: beta
   double res;       // residual / dot output
   double gamma0, gamma1, delta, eta, eta_old, c0, c1, c2, s0, s1, s2, inv_alpha1, alpha2, alpha3;  // MINRES
+  double inv_gamma0;    // MINRES: 1/gamma0, the scale of the next product
   double pq, gp, thr;   // refinement CG: <p,q>, <g,p>, stopping threshold on <res,res>
   int done;         // 0 running, 1 converged, 2 iteration limit
   int iters;
 };
 
-// Host-visible progress (mapped pinned memory).
+// Host-visible progress of CG / MINRES / refinement (mapped pinned memory).  The device
+// writes it without a fence: the host uses it for flow control only (whether to enqueue more
+// gated iterations, when to stop waiting), and reads the results from device memory after a
+// stream synchronisation, so seeing the two fields late or in either order is harmless.
 struct Progress {
-  volatile int stamp;     // Lanczos: operator applications completed; CG/MINRES: iterations completed
+  volatile int stamp;     // iterations completed
   volatile int done;
-  volatile int iters;
-  volatile double value;  // latest residual
 };
 
 // ---------------------------------------------------------------------------------
@@ -79,7 +81,7 @@ double wait_timeout_ms();
 
 // Spin (on the host) until pred() holds; bounded.  Returns false on timeout.
 // The acquire fence orders the host's later reads of device-written mirrors after the
-// read that observed the progress stamp (needed on weakly ordered hosts such as Arm).
+// reads that observed them landed (needed on weakly ordered hosts such as Arm).
 // The stream is queried for errors only every ~0.5 ms: driver calls from many solver
 // threads on one context serialise, and the progress flag itself lives in host memory.
 template <class Pred>
@@ -119,19 +121,19 @@ bool host_wait(cudaStream_t st, Pred pred) {
 // Vector kernels.
 // ---------------------------------------------------------------------------------
 template <class VT>
-__global__ void __launch_bounds__(kThreads) k_norm2(const VT *__restrict__ x, int n, double *out, RedSlot slot) {
+__global__ void __launch_bounds__(kThreads) k_norm2(const VT *__restrict__ x, int n, Norm2 *out, RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     double v = (double)x[i];
     acc += v * v;
   }
-  grid_reduce(acc, slot, [&](double t) { *out = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(out, t); });
 }
 
-// x *= 1/sqrt(*r2)  (NORMALIZE, sml/NORMALIZE.c:12-18)
+// x *= 1/sqrt(<x,x>)  (NORMALIZE, sml/NORMALIZE.c:12-18)
 template <class VT>
-__global__ void __launch_bounds__(kThreads) k_scale_rsqrt(VT *__restrict__ x, int n, const double *r2) {
-  const double s = 1.0 / sqrt(*r2);
+__global__ void __launch_bounds__(kThreads) k_scale_rsqrt(VT *__restrict__ x, int n, const Norm2 *r2) {
+  const double s = r2->rs;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) x[i] = (VT)((double)x[i] * s);
 }
 
@@ -146,6 +148,14 @@ __global__ void k_random_start(double *x, int n, unsigned long long seed);
 
 // ---- Lanczos -----------------------------------------------------------------------
 
+// Host mirrors of the Lanczos recurrence scalars are armed with this bit pattern (a negative
+// NaN with a fixed payload; GPU arithmetic only produces the canonical NaN) before a cycle;
+// the host takes slot j as written once hD[j] and hO[j] both differ from it.  Each slot is an
+// aligned 8-byte word written by one store, so it cannot be seen half written, and no fence
+// or progress counter has to order the mirrors: the last block of the product writes them
+// and ends, and no system-scope fence sits on the Lanczos step's critical path.
+constexpr uint64_t kLzSentinel = 0xFFF4A5A5A5A5A5A5ull;
+
 // Operator epilogue of Lanczos step b: y = H v_b, V[b] = v_b, D[b] = <y, v_b>
 // (sml/LANCZOS_SYM.c:139-143); mirrors D[b], O[b] to the host.  In the mixed form the
 // Krylov vector is already stored (unnormalised, FP32) before the product: vout is null and
@@ -156,11 +166,9 @@ struct EpiLanczos {
   YT *y;
   VT *vout;
   double *D, *O;         // device recurrence arrays
-  double *hD, *hO;       // mapped host mirrors
-  Progress *prog;        // mapped
-  const double *r2;      // <w,w> that normalised v_b
+  double *hD, *hO;       // mapped host mirrors (armed with kLzSentinel)
+  const Norm2 *r2;       // <w,w> that normalised v_b
   int b;
-  int stamp;
   double *sig = nullptr;
   __device__ void row(int i, double xi, double yi, double &acc) const {
     y[i] = (YT)yi;
@@ -168,14 +176,12 @@ struct EpiLanczos {
     acc += yi * xi;
   }
   __device__ void finalize(double t) const {
-    const double o = (b > 0) ? sqrt(*r2) : 0.0;   // Off_Diag[b] = sqrt(<w,w>)  (:135)
+    const double o = (b > 0) ? sqrt(r2->v) : 0.0;   // Off_Diag[b] = sqrt(<w,w>)  (:135)
     D[b] = t;
     O[b] = o;
-    if (sig) sig[b] = 1.0 / sqrt(*r2);
+    if (sig) sig[b] = r2->rs;
     hD[b] = t;
     hO[b] = o;
-    __threadfence_system();
-    prog->stamp = stamp;
   }
 };
 
@@ -183,7 +189,7 @@ struct EpiLanczos {
 template <class VT>
 __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__restrict__ y, const VT *__restrict__ v,
                                                        const VT *__restrict__ vprev, const double *D, const double *O,
-                                                       int b, double *__restrict__ w, double *r2, RedSlot slot) {
+                                                       int b, double *__restrict__ w, Norm2 *r2, RedSlot slot) {
   pdl_wait();
   const double d = D[b];
   const double o = (b > 0) ? O[b] : 0.0;
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__r
     acc += wi * wi;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 // c[j] = <V_j, w> for j < nvec (one block per vector; fixed order within the block).
@@ -215,7 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_multidot(const VT *__restrict__ V,
 // w -= sum_j c[j] V_j; r2 = <w,w>  (classical Gram-Schmidt pass of full reorthogonalisation)
 template <class VT>
 __global__ void __launch_bounds__(kThreads) k_multisub(const VT *__restrict__ V, long ldv, int nvec, const double *__restrict__ c,
-                                                      double *__restrict__ w, int n, double *r2, RedSlot slot) {
+                                                      double *__restrict__ w, int n, Norm2 *r2, RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     double wi = w[i];
@@ -223,13 +229,13 @@ __global__ void __launch_bounds__(kThreads) k_multisub(const VT *__restrict__ V,
     w[i] = wi;
     acc += wi * wi;
   }
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 // out_i = sum_{j<k} s_j V_j[i] in j order (sml/LANCZOS_SYM.c:195-202), then <out,out>.
 template <class VT>
 __global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, long ldv, int k, const double *__restrict__ s,
-                                                  double *__restrict__ out, int n, double *r2, RedSlot slot) {
+                                                  double *__restrict__ out, int n, Norm2 *r2, RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     double t = 0.0;
@@ -237,7 +243,7 @@ __global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, lon
     out[i] = t;
     acc += t * t;
   }
-  grid_reduce(acc, slot, [&](double t) { *r2 = t; });
+  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
 }
 
 // ---- Lanczos, mixed-precision form ---------------------------------------------------
@@ -259,13 +265,13 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
 // w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w); *r2 = <w,w>.
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
                                                        const float *__restrict__ y, const double *D, const double *O, int n,
-                                                       double *r2, RedSlot slot);
+                                                       Norm2 *r2, RedSlot slot);
 // w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); *r2 = <w,w>.
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
-                                                    const float *__restrict__ y, int n, double *r2, RedSlot slot);
+                                                    const float *__restrict__ y, int n, Norm2 *r2, RedSlot slot);
 // out_i = sum_{j<k} s_j sig_j V_j[i] (FP64, j order); *r2 = <out,out>.
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
-                                                     const double *__restrict__ sig, double *__restrict__ out, int n, double *r2,
+                                                     const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
                                                      RedSlot slot);
 
 // ---- CG ------------------------------------------------------------------------------
@@ -326,6 +332,7 @@ struct EpiMrInit {
   }
   __device__ void finalize(double t) const {
     S->gamma0 = sqrt(t);
+    S->inv_gamma0 = 1.0 / S->gamma0;
     S->eta = S->gamma0;
     S->s0 = 0.0;
     S->s1 = 0.0;
@@ -390,9 +397,21 @@ struct LzState {
   int n, cap_max;
   DevBuf<double> D, O, s_dev;
   Mapped<double> hD, hO, hs;
-  int stamp = 0;         // operator applications enqueued
   int spmv = 0;
   LzState(int n_, int cap) : n(n_), cap_max(cap), D(cap + 1), O(cap + 1), s_dev(cap + 1), hD(cap + 1), hO(cap + 1), hs(cap + 1) {}
+  // Arm the host mirrors (no kernel that writes them may be in flight).
+  void arm() {
+    for (int j = 0; j <= cap_max; ++j) {
+      std::memcpy((void *)(hD.h + j), &kLzSentinel, sizeof(double));
+      std::memcpy((void *)(hO.h + j), &kLzSentinel, sizeof(double));
+    }
+  }
+  // Have the mirrors of step j arrived?
+  bool landed(int j) const {
+    const volatile uint64_t *d = reinterpret_cast<const volatile uint64_t *>(hD.h + j);
+    const volatile uint64_t *o = reinterpret_cast<const volatile uint64_t *>(hO.h + j);
+    return *d != kLzSentinel && *o != kLzSentinel;
+  }
   // Upload Ritz coefficients s[0..k) to s_dev (stream-ordered).
   void upload_s(int k, const std::vector<double> &s, cudaStream_t st) {
     for (int j = 0; j < k; ++j) hs.h[j] = s[j];
@@ -446,9 +465,8 @@ struct LzSteps64 {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 1, z.cap_max);
-    ++z.stamp;
-    EpiLanczos<double> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, ws.prog.d, &S->r2, b, z.stamp};
-    op.apply(w, &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
+    EpiLanczos<double> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, &S->r2, b};
+    op.apply(w, &S->r2.rs, SCALE_MUL, 0.0, (const int *)nullptr, epi, slot, st);
     ++z.spmv;
     const double *vprev = (b > 0) ? B.vec(b - 1) : nullptr;
     launch_pdl(k_lz_update<double>, ws.vgrid, kThreads, st, n, (const double *)y.get(), (const double *)B.vec(b), vprev,
@@ -502,10 +520,8 @@ struct LzStepsMixed {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 2, z.cap_max);
-    ++z.stamp;
-    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, ws.prog.d, &S->r2, b, z.stamp,
-                                 sig.get()};
-    op.apply(B.vec(b), &S->r2, SCALE_RSQRT, 0.0, (const int *)nullptr, epi, slot, st);
+    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, &S->r2, b, sig.get()};
+    op.apply(B.vec(b), &S->r2.rs, SCALE_MUL, 0.0, (const int *)nullptr, epi, slot, st);
     ++z.spmv;
     if (!cfg.mixed_reorth) {
       launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
@@ -556,8 +572,10 @@ LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, d
   };
 
   while (total_step < cfg.max_step) {
-    // One restart cycle (the whole run when max_block_step >= max_step).
-    const int base_stamp = z.stamp;
+    // One restart cycle (the whole run when max_block_step >= max_step).  Nothing that
+    // writes the mirrors is in flight here (first cycle, or drained at the restart).
+    z.arm();
+    int landed = 0;        // mirror slots seen written this cycle
     steps.begin_cycle();
     steps.step(0);
     const int nb_max = cfg.slow ? cfg.max_step - 1 : std::min(cfg.max_block_step - 1, cfg.max_step - total_step);
@@ -573,8 +591,10 @@ LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, d
     bool restart = false;
     for (int bs = 1; bs <= nb_max; ++bs) {
       while (enq < std::min(bs + W, nb_max)) steps.step(++enq);
-      const int want = base_stamp + 1 + bs;   // stamp after apply(bs)
-      if (!host_wait(st, [&] { return ws.prog.h->stamp >= want; })) {
+      if (!host_wait(st, [&] {
+            while (landed <= bs && z.landed(landed)) ++landed;
+            return landed > bs;
+          })) {
         set_error("Lanczos: timed out waiting for step %d", bs);
         throw Error{DG_ERR_TIMEOUT};
       }
@@ -644,8 +664,7 @@ LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, d
     if (!restart) break;
     // Drain speculative work, then form the restart vector in w.
     steps.combine(n_last, s_last, w_dev);
-    DG_CUDA(cudaStreamSynchronize(st));
-    z.stamp = ws.prog.h->stamp;   // speculative applies beyond the restart point have all landed
+    DG_CUDA(cudaStreamSynchronize(st));   // speculative applies beyond the restart point have landed
   }
   res.steps = total_step;
   res.converged = false;
@@ -687,7 +706,7 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   ws.prog.h->done = 0;
   ws.prog.h->stamp = 0;
   k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
-  op.apply(x_dev, &S->xn2, SCALE_RSQRT, sigma, (const int *)nullptr, EpiCgInit{b_dev, xs.get(), r.get(), p.get(), S}, slot, st);
+  op.apply(x_dev, &S->xn2.rs, SCALE_MUL, sigma, (const int *)nullptr, EpiCgInit{b_dev, xs.get(), r.get(), p.get(), S}, slot, st);
   DG_CUDA(cudaMemcpyAsync(x_dev, xs.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   if (spmv_count) ++*spmv_count;
   const int chunk = 8;
@@ -756,7 +775,7 @@ IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double 
   int enq = -1;
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
-      op.apply(vb[i1].get(), &S->gamma0, SCALE_RECIP, sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
+      op.apply(vb[i1].get(), &S->inv_gamma0, SCALE_MUL, sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
       launch_pdl(k_mr_lanczos, ws.vgrid, kThreads, st, n, temp.get(), vb[i2].get(), vb[i0].get(), vb[i3].get(), S, acc, it,
                  max_step, ws.prog.d, slot);
       launch_pdl(k_mr_update, ws.vgrid, kThreads, st, n, vb[i2].get(), wb[j0].get(), wb[j1].get(), wb[j2].get(), x_dev, S);

@@ -116,7 +116,7 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
     // x0 normalised (into y), r = b - (M + sigma) x0, p = r; then x <- normalised x0
     // (sml/CONJUGATE_GRADIENT_SYM.c:35-43).
     k_norm2<double><<<vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
-    op.apply(x_dev, &S->xn2, SCALE_RSQRT, sigma, (const int *)nullptr, EpiCgInit{b_dev, y, r, p, S}, slot, st);
+    op.apply(x_dev, &S->xn2.rs, SCALE_MUL, sigma, (const int *)nullptr, EpiCgInit{b_dev, y, r, p, S}, slot, st);
     DG_CUDA(cudaMemcpyAsync(x_dev, y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     const int chunk = 16;
     int done = 0, it = 1;

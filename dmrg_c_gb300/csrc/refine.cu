@@ -9,7 +9,7 @@ __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *
                                                            Progress *prog, RedSlot slot) {
   pdl_wait();
   if (*((volatile int *)&S->done)) return;
-  const double a = S->rr / S->pq, gp = S->gp;
+  const double a = S->a, gp = S->gp;
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     t[i] = t[i] + a * (double)p32[i];
@@ -28,10 +28,7 @@ __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *
     }
     S->beta = tot / S->rr;
     S->rr = tot;
-    prog->value = tot;
     prog->done = S->done;
-    prog->iters = S->iters;
-    __threadfence_system();
     prog->stamp = it;
   });
 }

@@ -32,7 +32,10 @@ struct EpiRefineAlpha {
     q[i] = yi;
     acc += xi * yi;
   }
-  __device__ void finalize(double t) const { S->pq = t; }
+  __device__ void finalize(double t) const {
+    S->pq = t;
+    S->a = S->rr / t;   // once here, not per thread of the update
+  }
 };
 
 // t += a p32; res -= a (q - <g,p32> psi); convergence on <res,res> < S->thr.
