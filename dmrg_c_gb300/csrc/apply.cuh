@@ -99,8 +99,11 @@ k_apply(Op op, int n, const XT *__restrict__ x, const double *scale_src, int sca
     }
   }
   pdl_trigger();
-  if (Epi::kReduce) {
-    grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
+  if constexpr (Epi::kReduce) {
+    if constexpr (is_deferred<Epi>::value)
+      block_partial(acc, slot.partials);
+    else
+      grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
   }
 }
 

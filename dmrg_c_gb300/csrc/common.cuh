@@ -169,6 +169,8 @@ void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st
 
 // Is p a device (or managed) pointer?  Plain host memory (malloc) is "unregistered".
 bool is_device_ptr(const void *p);
+// Is p device memory the host cannot read (not managed, not host)?
+bool is_device_only_ptr(const void *p);
 
 // ---------------------------------------------------------------------------------
 // Launch geometry.
@@ -241,6 +243,39 @@ __device__ __forceinline__ void grid_reduce(double v, RedSlot slot, Fin fin) {
     }
   }
 }
+
+// Reductions finished by the consumer.  The producing kernel only writes one partial per
+// block (block_partial) and ends; every block of the kernel that needs the total sums the
+// partials itself after its pdl_wait (sum_partials), in the same fixed order as grid_reduce's
+// last block, so the total is bitwise the same in every block and run to run.  That takes the
+// serial last-block tail (ticket atomic, fences, re-reading the partials, the final sum, all
+// while the other SMs idle) off the critical path between two dependent kernels.
+__device__ __forceinline__ void block_partial(double v, double *partials) {
+  const double b = block_sum(v);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
+}
+
+// Sum of count partials written by the previous kernel; valid in every thread.
+__device__ __forceinline__ double sum_partials(const double *partials, int count) {
+  __shared__ double s_total;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) s += __ldcg(partials + i);
+  s = block_sum(s);
+  if (threadIdx.x == 0) s_total = s;
+  __syncthreads();
+  return s_total;
+}
+
+// Epilogue trait: kDeferred epilogues leave their reduction to the consumer (block partials
+// in slot.partials, no finalize).
+template <class E, class = void>
+struct is_deferred {
+  static constexpr bool value = false;
+};
+template <class E>
+struct is_deferred<E, decltype((void)E::kDeferred)> {
+  static constexpr bool value = E::kDeferred;
+};
 
 // ---------------------------------------------------------------------------------
 // Host-side helpers.

@@ -28,11 +28,15 @@ __global__ void k_random_start(double *x, int n, unsigned long long seed) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__restrict__ p, const double *__restrict__ y,
-                                                       double *__restrict__ x, double *__restrict__ r, Scalars *S,
-                                                       double acc_thr, int it, int max_step, Progress *prog, RedSlot slot) {
+                                                       double *__restrict__ x, double *__restrict__ r, const Scalars *S, int it,
+                                                       const double *pp, int pcount, double *up) {
   pdl_wait();
-  if (*((volatile int *)&S->done)) return;
-  const double a = S->a;
+  if (*((volatile const int *)&S->done)) return;
+  __shared__ double s_a;
+  const double py = sum_partials(pp, pcount);
+  if (threadIdx.x == 0) s_a = S->rrs[it & 1] / py;   // one division per block
+  __syncthreads();
+  const double a = s_a;
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     x[i] = x[i] + a * p[i];
@@ -41,26 +45,35 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__r
     acc += ri * ri;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) {
-    if (t < acc_thr) {
-      S->done = 1;
-      S->iters = it;
-    } else if (it >= max_step - 1) {
-      S->done = 2;
-      S->iters = max_step;
-    }
-    S->beta = t / S->rr;
-    S->rr = t;
-    prog->done = S->done;
-    prog->stamp = it;
-  });
+  block_partial(acc, up);
 }
 
-__global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p,
-                                                          const Scalars *S) {
+__global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p, Scalars *S,
+                                                          int it, int max_step, double acc_thr, const double *up, int ucount,
+                                                          Progress *prog) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
-  const double b = S->beta;
+  __shared__ double s_b;
+  const double t = sum_partials(up, ucount);
+  const bool converged = t < acc_thr, last = it >= max_step - 1;
+  if (threadIdx.x == 0) {
+    if (blockIdx.x == 0) {
+      if (converged) {
+        S->done = 1;
+        S->iters = it;
+      } else if (last) {
+        S->done = 2;
+        S->iters = max_step;
+      }
+      S->rrs[(it + 1) & 1] = t;   // the other slot: this kernel's blocks read rrs[it & 1]
+      prog->done = S->done;
+      prog->stamp = it;
+    }
+    s_b = t / S->rrs[it & 1];
+  }
+  __syncthreads();
+  if (converged || last) return;   // the same decision in every block
+  const double b = s_b;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) p[i] = r[i] + b * p[i];
   pdl_trigger();
 }

@@ -32,7 +32,8 @@ namespace dg {
 struct Scalars {
   Norm2 r2;         // Lanczos: <w,w> of the pending unnormalised Krylov vector
   Norm2 xn2;        // CG: <x0,x0>; generic norm output
-  double rr;        // CG: <r,r> of the current residual
+  double rr;        // refinement CG: <r,r> of the current residual
+  double rrs[2];    // CG: <r,r> entering iteration it is rrs[it & 1]
   double a;         // CG: alpha
   double beta;      // CG: beta
   double res;       // residual / dot output
@@ -59,7 +60,7 @@ struct Workspace {
   cudaStream_t st;
   int n;
   int vgrid;
-  DevBuf<double> partials;
+  DevBuf<double> partials, partials2;   // partials2: a second slot for consumer-finished reductions
   DevBuf<unsigned> ticket;
   DevBuf<Scalars> sc;
   Mapped<Progress> prog;
@@ -67,6 +68,7 @@ struct Workspace {
     vgrid = vector_grid(n_);
     int g = max_grid > vgrid ? max_grid : vgrid;
     partials.alloc(g);
+    partials2.alloc(g);
     ticket.alloc(1);
     sc.alloc(1);
     prog.alloc(1);
@@ -292,30 +294,33 @@ struct EpiCgInit {
     acc += ri * ri;
   }
   __device__ void finalize(double t) const {
-    S->rr = t;
+    S->rrs[1] = t;   // enters iteration 1
     S->done = 0;
     S->iters = 0;
   }
 };
 
-// y = (H + sigma) p, alpha = <r,r>/<p,y>  (:47-51)
-struct EpiCgAlpha {
+// y = (H + sigma) p with block partials of <p,y> (:47-51); alpha = <r,r>/<p,y> is formed by
+// every block of the update kernel from those partials.
+struct EpiCgDot {
   static constexpr bool kReduce = true;
+  static constexpr bool kDeferred = true;
   double *y;
-  Scalars *S;
   __device__ void row(int i, double xi, double yi, double &acc) const {
     y[i] = yi;
     acc += xi * yi;
   }
-  __device__ void finalize(double t) const { S->a = S->rr / t; }
+  __device__ void finalize(double) const {}
 };
 
-// x += a p; r -= a y; convergence on <r,r> < acc (:53-67)
+// Iteration it: alpha = rrs[it&1] / <p,y> (the product's pcount partials in pp); x += a p;
+// r -= a y; block partials of <r,r> into up (:51-63).
 __global__ void k_cg_update(int n, const double *__restrict__ p, const double *__restrict__ y, double *__restrict__ x,
-                            double *__restrict__ r, Scalars *S, double acc_thr, int it, int max_step, Progress *prog,
-                            RedSlot slot);
-// p = r + beta p (:93-95)
-__global__ void k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p, const Scalars *S);
+                            double *__restrict__ r, const Scalars *S, int it, const double *pp, int pcount, double *up);
+// Iteration it: <r,r> from the update's ucount partials; convergence (<r,r> < acc_thr) or the
+// iteration limit ends the solve (block 0 records it); otherwise p = r + beta p (:64-95).
+__global__ void k_cg_direction(int n, const double *__restrict__ r, double *__restrict__ p, Scalars *S, int it, int max_step,
+                               double acc_thr, const double *up, int ucount, Progress *prog);
 
 // ---- MINRES (sml/MINIMUM_RESIDUAL_SYM.c) ----------------------------------------------
 
@@ -711,11 +716,15 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   if (spmv_count) ++*spmv_count;
   const int chunk = 8;
   int enq = 0;   // last iteration enqueued
+  const int pgrid = op.grid();
+  double *up = ws.partials2.get();
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
-      op.apply(p.get(), (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgAlpha{y.get(), S}, slot, st);
-      launch_pdl(k_cg_update, ws.vgrid, kThreads, st, n, p.get(), y.get(), x_dev, r.get(), S, acc, it, max_step, ws.prog.d, slot);
-      launch_pdl(k_cg_direction, ws.vgrid, kThreads, st, n, r.get(), p.get(), S);
+      op.apply(p.get(), (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgDot{y.get()}, slot, st);
+      launch_pdl(k_cg_update, ws.vgrid, kThreads, st, n, (const double *)p.get(), (const double *)y.get(), x_dev, r.get(),
+                 (const Scalars *)S, it, (const double *)slot.partials, pgrid, up);
+      launch_pdl(k_cg_direction, ws.vgrid, kThreads, st, n, (const double *)r.get(), p.get(), S, it, max_step, acc,
+                 (const double *)up, ws.vgrid, ws.prog.d);
     }
     DG_CUDA(cudaGetLastError());
     enq = std::max(enq, last);

@@ -28,25 +28,41 @@ void choose_shape(int n, long nnz, int *lanes, int *grid) {
 
 namespace {
 
+// The build kernels below take one row (or slice) per warp, lanes over its entries; their grid
+// gives every row its own warp up to 16 blocks per SM (a thread or warp walking many rows one
+// after another is bound by its chain of dependent loads, not by bandwidth).
+int warp_grid(long rows) { return (int)std::max(1L, std::min((rows * 32 + kThreads - 1) / kThreads, (long)sm_count() * 16)); }
+
 // Checks of the CRS invariants; bad holds the smallest offending row (INT_MAX if none).
-__global__ void k_validate(const int64_t *__restrict__ row, const int *__restrict__ col, int n, long nnz, int lower,
-                           int *bad) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int64_t b = row[i], e = row[i + 1];
+__global__ void __launch_bounds__(kThreads) k_validate(const int64_t *__restrict__ row, const int *__restrict__ col, int n, long nnz,
+                                                      int lower, int *bad) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = warp; i < n; i += nw) {
+    const int64_t b = row[i], e = row[i + 1];
     bool ok = (b >= 0) && (e >= b) && (e <= nnz);
     if (ok && lower) {
       // non-empty, diagonal last, strictly increasing columns below the diagonal (the
       // expansion's per-row column ranks require distinct columns)
       ok = (e > b) && (col[e - 1] == i);
-      for (int64_t k = b; ok && k < e - 1; ++k) ok = (col[k] >= 0) && (col[k] < i) && (k == b || col[k] > col[k - 1]);
+      if (ok)
+        for (int64_t k = b + lane; k < e - 1; k += 32) {
+          const int c = col[k];
+          ok = ok && (c >= 0) && (c < i) && (k == b || c > col[k - 1]);
+        }
     } else if (ok) {
-      for (int64_t k = b; ok && k < e; ++k) ok = (col[k] >= 0) && (col[k] < n);
+      for (int64_t k = b + lane; k < e; k += 32) {
+        const int c = col[k];
+        ok = ok && (c >= 0) && (c < n);
+      }
     }
-    if (!ok) atomicMin(bad, i);
+    if (__any_sync(0xffffffffu, !ok) && lane == 0) atomicMin(bad, i);
   }
 }
 
 // colcnt[c] += 1 for every strict-lower entry (r, c).
+// (A thread per row: with a warp per row, neighbouring rows' atomics, which mostly hit the same
+// columns, arrive together and serialise; measured 9.7 vs 15.0 us on a 56 k-row superblock.)
 __global__ void k_count_upper(const int64_t *__restrict__ row, const int *__restrict__ col, int n, int *colcnt) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     for (int64_t k = row[i]; k < row[i + 1] - 1; ++k) atomicAdd(colcnt + col[k], 1);
@@ -74,10 +90,14 @@ __global__ void k_fill_lower(const int64_t *__restrict__ row, const int *__restr
 
 // Scatter the transpose of the strict lower part into staging slots after each full
 // row's lower part (slot order within a row is arbitrary here; sorted afterwards).
-__global__ void k_fill_upper(const int64_t *__restrict__ row, const int *__restrict__ col, const double *__restrict__ val,
-                             const int64_t *__restrict__ frow, int n, int *fillctr, int *scol, double *sval) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    for (int64_t k = row[r]; k < row[r + 1] - 1; ++k) {
+__global__ void __launch_bounds__(kThreads) k_fill_upper(const int64_t *__restrict__ row, const int *__restrict__ col,
+                                                        const double *__restrict__ val, const int64_t *__restrict__ frow, int n,
+                                                        int *fillctr, int *scol, double *sval) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int r = warp; r < n; r += nw) {
+    const int64_t e = row[r + 1] - 1;
+    for (int64_t k = row[r] + lane; k < e; k += 32) {
       const int c = col[k];
       const int64_t lower_len = row[c + 1] - row[c];
       const int64_t pos = frow[c] + lower_len + atomicAdd(fillctr + c, 1);
@@ -168,10 +188,12 @@ __global__ void k_to_f32(const double *__restrict__ a, long n, float *__restrict
 // slots (a power of two <= kSellWindow): bitonic sort of (length desc, row asc) keys in
 // shared memory.  window <= 32 keeps the identity order.  Writes -1 for slots past the
 // last row.
-__global__ void __launch_bounds__(kThreads) k_sell_window_sort(const int64_t *__restrict__ row, int n, int window, int *perm) {
+constexpr int kSortThreads = kSellWindow / 2;   // one compare-exchange per thread and stage
+
+__global__ void __launch_bounds__(kSortThreads) k_sell_window_sort(const int64_t *__restrict__ row, int n, int window, int *perm) {
   __shared__ unsigned long long key[kSellWindow];
   const int base = blockIdx.x * kSellWindow;
-  for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
+  for (int t = threadIdx.x; t < kSellWindow; t += kSortThreads) {
     const int r = base + t;
     if (r < n) {
       const unsigned long long len = (unsigned long long)(row[r + 1] - row[r]);
@@ -184,38 +206,37 @@ __global__ void __launch_bounds__(kThreads) k_sell_window_sort(const int64_t *__
   if (window > kSellC) {
     for (int k = 2; k <= window; k <<= 1) {
       for (int j = k >> 1; j > 0; j >>= 1) {
-        for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
-          const int u = t ^ j;
-          if (u > t) {
-            const unsigned long long a = key[t], b = key[u];
-            const bool up = (k == window) || ((t & k) == 0);   // every window ends ascending
-            if ((a > b) == up) {
-              key[t] = b;
-              key[u] = a;
-            }
-          }
+        // thread p owns the pair (t, t | j) whose lower index t has bit j clear
+        const int p = threadIdx.x;
+        const int t = ((p & ~(j - 1)) << 1) | (p & (j - 1)), u = t | j;
+        const unsigned long long a = key[t], b = key[u];
+        const bool up = (k == window) || ((t & k) == 0);   // every window ends ascending
+        if ((a > b) == up) {
+          key[t] = b;
+          key[u] = a;
         }
         __syncthreads();
       }
     }
   }
-  for (int t = threadIdx.x; t < kSellWindow; t += kThreads) {
+  for (int t = threadIdx.x; t < kSellWindow; t += kSortThreads) {
     const unsigned long long v = key[t];
     perm[base + t] = (v == ~0ull) ? -1 : (int)(v & 0xffffffffu);
   }
 }
 
 // width[s] = longest row of slice s; cnt[s] = 32 * width[s].
-__global__ void k_sell_widths(const int64_t *__restrict__ row, const int *__restrict__ perm, int nslices, int *width,
-                              long long *cnt) {
-  for (int sl = blockIdx.x * blockDim.x + threadIdx.x; sl < nslices; sl += gridDim.x * blockDim.x) {
-    int w = 0;
-    for (int l = 0; l < kSellC; ++l) {
-      const int r = perm[sl * kSellC + l];
-      if (r >= 0) w = max(w, (int)(row[r + 1] - row[r]));
+__global__ void __launch_bounds__(kThreads) k_sell_widths(const int64_t *__restrict__ row, const int *__restrict__ perm, int nslices,
+                                                         int *width, long long *cnt) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int sl = warp; sl < nslices; sl += nw) {
+    const int r = perm[sl * kSellC + lane];
+    const int w = (int)__reduce_max_sync(0xffffffffu, r >= 0 ? (unsigned)(row[r + 1] - row[r]) : 0u);
+    if (lane == 0) {
+      width[sl] = w;
+      cnt[sl] = (long long)w * kSellC;
     }
-    width[sl] = w;
-    cnt[sl] = (long long)w * kSellC;
   }
 }
 
@@ -231,15 +252,30 @@ __global__ void k_sell_fill(const int64_t *__restrict__ row, const int *__restri
     const int w = width[sl];
     const int64_t b = (r >= 0) ? row[r] : 0;
     const int len = (r >= 0) ? (int)(row[r + 1] - b) : 0;
-    for (int k = 0; k < w; ++k) {
-      const int64_t dst = off[sl] + (int64_t)k * kSellC + l;
-      if (k < len) {
-        scol[dst] = col[b + k];
-        sval[dst] = (VT)val[b + k];
-      } else {
-        scol[dst] = r >= 0 ? r : 0;
-        sval[dst] = (VT)0;
+    const int64_t o = off[sl] + l;
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {   // four loads in flight per lane
+      int c[4];
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = col[b + k + u];
+        v[u] = val[b + k + u];
       }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        scol[o + (int64_t)(k + u) * kSellC] = c[u];
+        sval[o + (int64_t)(k + u) * kSellC] = (VT)v[u];
+      }
+    }
+    for (; k < len; ++k) {
+      scol[o + (int64_t)k * kSellC] = col[b + k];
+      sval[o + (int64_t)k * kSellC] = (VT)val[b + k];
+    }
+    const int pad = r >= 0 ? r : 0;
+    for (; k < w; ++k) {
+      scol[o + (int64_t)k * kSellC] = pad;
+      sval[o + (int64_t)k * kSellC] = (VT)0;
     }
   }
 }
@@ -259,8 +295,8 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   int w = kSellC;
   while (w < window && w < kSellWindow) w <<= 1;
   m->sell_window = w;
-  k_sell_window_sort<<<nwin, kThreads, 0, st>>>(m->row.get(), n, w, m->s_perm.get()); ::dg::count_launch();
-  k_sell_widths<<<vector_grid(nslices), kThreads, 0, st>>>(m->row.get(), m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
+  k_sell_window_sort<<<nwin, kSortThreads, 0, st>>>(m->row.get(), n, w, m->s_perm.get()); ::dg::count_launch();
+  k_sell_widths<<<warp_grid(nslices), kThreads, 0, st>>>(m->row.get(), m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
   exclusive_scan(cnt.get(), nslices, m->s_off.get(), tmp.get(), st);
   int64_t total = 0;
   DG_CUDA(cudaMemcpyAsync(&total, m->s_off.get() + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -314,12 +350,12 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
   DG_REQUIRE(values >= DG_VALUES_F64 && values <= DG_VALUES_BOTH, DG_ERR_ARG, "unknown values flag %d", values);
   const int64_t *row = reinterpret_cast<const int64_t *>(row_d);
   const int lower = storage == DG_STORE_LOWER_DIAG_LAST;
-  const int g = vector_grid(n);
+  const int g = vector_grid(n), gw = warp_grid(n);
 
   DevBuf<int> bad(1);
   int big = 0x7fffffff;
   DG_CUDA(cudaMemcpyAsync(bad.get(), &big, sizeof(int), cudaMemcpyHostToDevice, st));
-  k_validate<<<g, kThreads, 0, st>>>(row, col_d, n, nnz_in, lower, bad.get()); ::dg::count_launch();
+  k_validate<<<gw, kThreads, 0, st>>>(row, col_d, n, nnz_in, lower, bad.get()); ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
   int first_bad = 0;
   int64_t ends[2];
@@ -364,9 +400,9 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
       DG_CUDA(cudaMemsetAsync(m->col.get(), 0, sizeof(int) * total, st));
       DevBuf<int> scol(total);
       DevBuf<double> sval(total);
-      k_fill_lower<<<g, kThreads, 0, st>>>(row, col_d, val_d, m->row.get(), n, m->col.get(), m->val.get()); ::dg::count_launch();
-      k_fill_upper<<<g, kThreads, 0, st>>>(row, col_d, val_d, m->row.get(), n, fillctr.get(), scol.get(), sval.get()); ::dg::count_launch();
-      k_rank_upper<<<g, kThreads, 0, st>>>(row, m->row.get(), n, scol.get(), sval.get(), m->col.get(), m->val.get()); ::dg::count_launch();
+      k_fill_lower<<<gw, kThreads, 0, st>>>(row, col_d, val_d, m->row.get(), n, m->col.get(), m->val.get()); ::dg::count_launch();
+      k_fill_upper<<<gw, kThreads, 0, st>>>(row, col_d, val_d, m->row.get(), n, fillctr.get(), scol.get(), sval.get()); ::dg::count_launch();
+      k_rank_upper<<<gw, kThreads, 0, st>>>(row, m->row.get(), n, scol.get(), sval.get(), m->col.get(), m->val.get()); ::dg::count_launch();
       DG_CUDA(cudaGetLastError());
       DG_CUDA(cudaStreamSynchronize(st));
     }
@@ -411,6 +447,8 @@ int dg_matrix_create(int n, const long *row, const int *col, const double *val, 
     require_device();
     DG_REQUIRE(out && row && col && val, DG_ERR_ARG, "null argument");
     DG_REQUIRE(n > 0, DG_ERR_ARG, "matrix dimension must be positive (n=%d)", n);
+    DG_REQUIRE(!is_device_only_ptr(row) && !is_device_only_ptr(col) && !is_device_only_ptr(val), DG_ERR_ARG,
+               "dg_matrix_create reads host arrays; device arrays go to dg_matrix_create_device");
     const long nnz = row[n];
     DG_REQUIRE(row[0] == 0 && nnz >= 0, DG_ERR_MATRIX, "CRS row offsets must start at 0");
     cudaStream_t st = stream();

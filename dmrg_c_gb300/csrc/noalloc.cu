@@ -31,7 +31,8 @@ constexpr int kNoAllocMaxGrid = 4096;              // reduction partials
 constexpr size_t kVecBytes = sizeof(double) * (size_t)kNoAllocMaxN;
 constexpr size_t kOffR = 0, kOffP = kVecBytes, kOffY = 2 * kVecBytes;
 constexpr size_t kOffPartials = 3 * kVecBytes;
-constexpr size_t kOffScalars = kOffPartials + sizeof(double) * kNoAllocMaxGrid;
+constexpr size_t kOffPartials2 = kOffPartials + sizeof(double) * kNoAllocMaxGrid;   // update -> direction
+constexpr size_t kOffScalars = kOffPartials2 + sizeof(double) * kNoAllocMaxGrid;
 constexpr size_t kOffProgress = kOffScalars + ((sizeof(Scalars) + 255) / 256) * 256;
 constexpr size_t kOffTicket = kOffProgress + ((sizeof(Progress) + 255) / 256) * 256;
 constexpr size_t kScratchBytes = kOffTicket + 256;
@@ -90,6 +91,7 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
     double *p = reinterpret_cast<double *>(base + kOffP);
     double *y = reinterpret_cast<double *>(base + kOffY);
     double *partials = reinterpret_cast<double *>(base + kOffPartials);
+    double *partials2 = reinterpret_cast<double *>(base + kOffPartials2);
     Scalars *S = reinterpret_cast<Scalars *>(base + kOffScalars);
     Progress *prog = reinterpret_cast<Progress *>(base + kOffProgress);
     unsigned *ticket = reinterpret_cast<unsigned *>(base + kOffTicket);
@@ -123,9 +125,9 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
     while (it < max_step && !done) {
       const int last = std::min(it + chunk - 1, max_step - 1);
       for (; it <= last; ++it) {
-        op.apply(p, (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgAlpha{y, S}, slot, st);
-        k_cg_update<<<vgrid, kThreads, 0, st>>>(n, p, y, x_dev, r, S, acc, it, max_step, prog, slot); ::dg::count_launch();
-        k_cg_direction<<<vgrid, kThreads, 0, st>>>(n, r, p, S); ::dg::count_launch();
+        op.apply(p, (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgDot{y}, slot, st);
+        k_cg_update<<<vgrid, kThreads, 0, st>>>(n, p, y, x_dev, r, S, it, partials, op.grid_, partials2); ::dg::count_launch();
+        k_cg_direction<<<vgrid, kThreads, 0, st>>>(n, r, p, S, it, max_step, acc, partials2, vgrid, prog); ::dg::count_launch();
       }
       DG_CUDA(cudaGetLastError());
       DG_CUDA(cudaMemcpyAsync(&done, &S->done, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -198,7 +198,10 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, i
   }
   pdl_trigger();
   if constexpr (Epi::kReduce) {
-    grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
+    if constexpr (is_deferred<Epi>::value)
+      block_partial(acc, slot.partials);
+    else
+      grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
   }
 }
 

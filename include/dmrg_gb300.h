@@ -128,7 +128,8 @@ enum { DG_FORMAT_CSR = 0, DG_FORMAT_SELL = 1 };
 
 /* Upload a host CRS.  storage = DG_STORE_FULL for a full matrix (MATRIX_VECTOR_PRODUCT
  * input), DG_STORE_LOWER_DIAG_LAST for the symmetric-half input of the *_SYM entry points
- * (expanded on the device to a full CRS whose rows are sorted by column). */
+ * (expanded on the device to a full CRS whose rows are sorted by column).  row/col/val must
+ * be host (or managed) memory: device pointers are rejected with DG_ERR_ARG. */
 int dg_matrix_create(int n, const long *row, const int *col, const double *val, int storage, int values, dg_matrix **out);
 /* Same, with row/col/val already in device memory (they are copied). */
 int dg_matrix_create_device(int n, long nnz, const long *row_dev, const int *col_dev, const double *val_dev, int storage, int values, dg_matrix **out);

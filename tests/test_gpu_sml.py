@@ -96,6 +96,19 @@ def test_matrix_validation_errors(gpu):
         gpu.DeviceMatrix(bad2)
 
 
+def test_matrix_create_rejects_device_arrays(gpu):
+    """The host-array entry reads row[n] on the host: device arrays get DG_ERR_ARG, not a crash."""
+    torch = pytest.importorskip("torch")
+    g, low, full = sml_inputs()
+    dev = [torch.from_numpy(a).cuda() for a in (full.row, full.col, full.val)]
+    lib = gpu.load()
+    h = C.c_void_p()
+    rc = lib.dg_matrix_create(full.n, C.cast(dev[0].data_ptr(), C.POINTER(C.c_long)), C.cast(dev[1].data_ptr(), C.POINTER(C.c_int)),
+                              C.cast(dev[2].data_ptr(), C.POINTER(C.c_double)), gpu.DG_STORE_FULL, gpu.DG_VALUES_F64, C.byref(h))
+    assert rc == 1 and not h.value
+    assert b"dg_matrix_create_device" in lib.dg_last_error()
+
+
 @pytest.mark.parametrize("name,sym,slow", [("lanczos_sym", True, False), ("lanczos_slow_sym", True, True),
                                            ("lanczos", False, False), ("lanczos_slow", False, True)])
 def test_lanczos_golden(gpu, name, sym, slow):
