@@ -24,15 +24,6 @@
 
 namespace dg {
 
-// The input scale s: 1, or a device scalar that the kernel which formed it already derived
-// (1/sqrt(<w,w>) of NORMALIZE, 1/gamma0 of MINIMUM_RESIDUAL).  An FP64 square root or
-// division is a long sequence of FP64 instructions; on GB300's few FP64 pipes, evaluated by
-// every thread of a product it costs as much FP64 issue as the product's multiply-adds, so
-// it is evaluated once, by the producer's last block.
-enum ScaleMode : int { SCALE_ONE = 0, SCALE_MUL = 1 };
-
-__device__ __forceinline__ double load_scale(const double *sp, int mode) { return mode == SCALE_MUL ? *sp : 1.0; }
-
 // A squared norm with its normalising scale rs = 1/sqrt(v), both written by the last block of
 // the kernel that reduces v.
 struct Norm2 {
@@ -42,6 +33,61 @@ struct Norm2 {
 __device__ __forceinline__ void set_norm2(Norm2 *p, double t) {
   p->v = t;
   p->rs = 1.0 / sqrt(t);
+}
+
+// The input scale s of a product (the kernel applies the operator to s x).  An FP64 square
+// root or division is a long sequence of FP64 instructions; on GB300's few FP64 pipes,
+// evaluated by every thread of a product it costs as much FP64 issue as the product's
+// multiply-adds, so it is formed once: by the last block of the kernel that reduced <w,w>
+// (NORM2), or, when that kernel left block partials, once per block of the product (PARTIALS).
+//   ONE       s = 1
+//   MUL       s = *p                       (MINIMUM_RESIDUAL: 1/gamma0)
+//   NORM2     s = rs of the Norm2 at p      (NORMALIZE: 1/sqrt(<w,w>)), r2 = its v
+//   PARTIALS  r2 = sum of count block partials at p, s = 1/sqrt(r2)
+struct Scale {
+  enum Mode : int { ONE = 0, MUL = 1, NORM2 = 2, PARTIALS = 3 };
+  const double *p = nullptr;
+  int mode = ONE;
+  int count = 0;
+  static Scale mul(const double *q) { return Scale{q, MUL, 0}; }
+  static Scale norm2(const Norm2 *q) { return Scale{reinterpret_cast<const double *>(q), NORM2, 0}; }
+  static Scale partials(const double *q, int c) { return Scale{q, PARTIALS, c}; }
+};
+
+struct ScaleVal {
+  double s;
+  double r2;   // <w,w> behind s (NORM2, PARTIALS), else 0
+};
+
+// Every thread of the block must call it (PARTIALS synchronises the block).
+__device__ __forceinline__ ScaleVal load_scale(const Scale &sc) {
+  if (sc.mode == Scale::MUL) return ScaleVal{*sc.p, 0.0};
+  if (sc.mode == Scale::NORM2) return ScaleVal{sc.p[1], sc.p[0]};
+  if (sc.mode == Scale::PARTIALS) {
+    __shared__ double s_rs;
+    const double r2 = sum_partials(sc.p, sc.count);
+    if (threadIdx.x == 0) s_rs = 1.0 / sqrt(r2);
+    __syncthreads();
+    return ScaleVal{s_rs, r2};
+  }
+  return ScaleVal{1.0, 0.0};
+}
+
+// Epilogue trait: kBegin epilogues have begin(r2, s), called by every thread once the input
+// scale is known.
+template <class E, class = void>
+struct has_begin {
+  static constexpr bool value = false;
+};
+template <class E>
+struct has_begin<E, decltype((void)E::kBegin)> {
+  static constexpr bool value = E::kBegin;
+};
+template <class Epi>
+__device__ __forceinline__ double begin_scale(const Scale &sc, const Epi &epi) {
+  const ScaleVal v = load_scale(sc);
+  if constexpr (has_begin<Epi>::value) epi.begin(v.r2, v.s);
+  return v.s;
 }
 
 template <class T>
@@ -75,11 +121,11 @@ __device__ __forceinline__ double lanes_sum(double v) {
 // (speculatively enqueued iterations after an iterative solver has converged).
 template <int L, class Op, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
-k_apply(Op op, int n, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma,
+k_apply(Op op, int n, const XT *__restrict__ x, Scale sc, double sigma,
         const int *gate, Epi epi, RedSlot slot) {
   pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
-  const double s = load_scale(scale_src, scale_mode);
+  const double s = begin_scale(sc, epi);
   constexpr int RPW = 32 / L;   // rows per warp trip
   const int lane_w = threadIdx.x & 31;
   const int sub = lane_w / L, lane = lane_w % L;

@@ -158,42 +158,63 @@ __global__ void k_random_start(double *x, int n, unsigned long long seed);
 // and ends, and no system-scope fence sits on the Lanczos step's critical path.
 constexpr uint64_t kLzSentinel = 0xFFF4A5A5A5A5A5A5ull;
 
-// Operator epilogue of Lanczos step b: y = H v_b, V[b] = v_b, D[b] = <y, v_b>
-// (sml/LANCZOS_SYM.c:139-143); mirrors D[b], O[b] to the host.  In the mixed form the
-// Krylov vector is already stored (unnormalised, FP32) before the product: vout is null and
-// sig[b] records its normalisation 1/||w_b||.
-template <class VT, class YT = double>
+// Operator epilogue of Lanczos step b: y = H v_b, V[b] = v_b (sml/LANCZOS_SYM.c:139-143).
+// begin(): once the input scale 1/||w_b|| is known, block 0 records Off_Diag[b] = ||w_b|| (:135)
+// in O and its host mirror, and, in the mixed form, sig[b] = 1/||w_b|| (the Krylov vector is
+// then already stored, unnormalised, in FP32: vout is null).  Diag[b] = <y, v_b>: with DEFER the
+// product leaves block partials that the update kernel sums (it records D[b]); otherwise the
+// product's last block records it.
+template <class VT, class YT = double, bool DEFER = false>
 struct EpiLanczos {
   static constexpr bool kReduce = true;
+  static constexpr bool kDeferred = DEFER;
+  static constexpr bool kBegin = true;
   YT *y;
   VT *vout;
   double *D, *O;         // device recurrence arrays
   double *hD, *hO;       // mapped host mirrors (armed with kLzSentinel)
-  const Norm2 *r2;       // <w,w> that normalised v_b
   int b;
   double *sig = nullptr;
+  __device__ void begin(double r2, double s) const {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      const double o = (b > 0) ? sqrt(r2) : 0.0;
+      O[b] = o;
+      hO[b] = o;
+      if (sig) sig[b] = s;
+    }
+  }
   __device__ void row(int i, double xi, double yi, double &acc) const {
     y[i] = (YT)yi;
     if (vout) vout[i] = (VT)xi;
     acc += yi * xi;
   }
   __device__ void finalize(double t) const {
-    const double o = (b > 0) ? sqrt(r2->v) : 0.0;   // Off_Diag[b] = sqrt(<w,w>)  (:135)
     D[b] = t;
-    O[b] = o;
-    if (sig) sig[b] = r2->rs;
     hD[b] = t;
-    hO[b] = o;
   }
 };
 
-// w = y - D[b] v_b - O[b] v_{b-1}; r2 = <w,w>  (sml/LANCZOS_SYM.c:121-125, 240-243)
+// Step b: D[b] = <y, v_b> summed from the product's pcount block partials (block 0 records it
+// and its host mirror), or, with pcount 0, as the product's last block recorded it;
+// w = y - D[b] v_b - O[b] v_{b-1} (sml/LANCZOS_SYM.c:121-125, 240-243).
+// <w,w>: with r2 null, block partials into out.partials for the next product to sum; else the
+// last block forms the Norm2 *r2.
 template <class VT>
 __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__restrict__ y, const VT *__restrict__ v,
-                                                       const VT *__restrict__ vprev, const double *D, const double *O,
-                                                       int b, double *__restrict__ w, Norm2 *r2, RedSlot slot) {
+                                                       const VT *__restrict__ vprev, double *D, double *hD, const double *O,
+                                                       int b, double *__restrict__ w, const double *pp, int pcount, RedSlot out,
+                                                       Norm2 *r2) {
   pdl_wait();
-  const double d = D[b];
+  double d;
+  if (pcount > 0) {
+    d = sum_partials(pp, pcount);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      D[b] = d;
+      hD[b] = d;
+    }
+  } else {
+    d = D[b];
+  }
   const double o = (b > 0) ? O[b] : 0.0;
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
@@ -203,7 +224,10 @@ __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__r
     acc += wi * wi;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
+  if (r2)
+    grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });
+  else
+    block_partial(acc, out.partials);
 }
 
 // c[j] = <V_j, w> for j < nvec (one block per vector; fixed order within the block).
@@ -370,9 +394,10 @@ __global__ void k_mr_update(int n, const double *__restrict__ v1n, const double 
 // ---------------------------------------------------------------------------------
 // Operator launchers: a small value type with
 //   int n() const;
-//   template <class XT, class Epi> void apply(const XT *x, const double *scale_src, int scale_mode,
+//   template <class XT, class Epi> void apply(const XT *x, Scale sc,
 //        double sigma, const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) const;
-//   int grid() const;   // apply grid (for workspace sizing)
+//   int grid() const;   // apply grid (workspace sizing; number of block partials a product leaves)
+//   long nnz() const;   // stored elements (or an estimate; 0 if unknown)
 // ---------------------------------------------------------------------------------
 
 struct LanczosResult {
@@ -461,8 +486,17 @@ struct LzSteps64 {
   double *w;             // start vector in, next unnormalised Krylov vector
   DevBuf<double> y, c;
   KrylovBasis<double> B;
+  // Reductions are left to the consuming kernel (the update sums the product's partials of
+  // <y,v>, the next product those of <w,w>) only when the product has >= kDeferWork stored
+  // elements a block: every consumer block then sums the partials itself, and each product
+  // block also forms 1/sqrt(<w,w>), ~70 FP64 warp instructions a block.  That is a latency win
+  // for a superblock product (KLM m=128: 8 k elements a block) but a throughput loss for an ED
+  // product of short rows (XXZ L=22: 3.5 k), where the producers' last blocks do it once.
+  static constexpr long kDeferWork = 6144;
+  bool defer;
   LzSteps64(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
-      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), c(z_.cap_max + 1), B(z_.n, w_.st) {}
+      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), c(z_.cap_max + 1), B(z_.n, w_.st),
+        defer(o.nnz() >= kDeferWork * (long)o.grid()) {}
   void begin_cycle() {}
   void step(int b) {
     cudaStream_t st = ws.st;
@@ -470,12 +504,22 @@ struct LzSteps64 {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 1, z.cap_max);
-    EpiLanczos<double> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, &S->r2, b};
-    op.apply(w, &S->r2.rs, SCALE_MUL, 0.0, (const int *)nullptr, epi, slot, st);
+    // 1/||w||: from the Norm2 of the start / restart vector, of a reorthogonalisation pass or
+    // of the previous update's last block; or, when the product has work enough per block to
+    // absorb it, summed by every product block from the previous update's block partials.
+    const Scale sc = (b > 0 && !cfg.reorth && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
+    if (defer) {
+      EpiLanczos<double, double, true> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, b};
+      op.apply(w, sc, 0.0, (const int *)nullptr, epi, slot, st);
+    } else {
+      EpiLanczos<double, double, false> epi{y.get(), B.vec(b), z.D.get(), z.O.get(), z.hD.d, z.hO.d, b};
+      op.apply(w, sc, 0.0, (const int *)nullptr, epi, slot, st);
+    }
     ++z.spmv;
     const double *vprev = (b > 0) ? B.vec(b - 1) : nullptr;
     launch_pdl(k_lz_update<double>, ws.vgrid, kThreads, st, n, (const double *)y.get(), (const double *)B.vec(b), vprev,
-               (const double *)z.D.get(), (const double *)z.O.get(), b, w, &S->r2, slot);
+               z.D.get(), z.hD.d, (const double *)z.O.get(), b, w, (const double *)slot.partials, defer ? op.grid() : 0,
+               RedSlot{ws.partials2.get(), ws.ticket.get()}, defer ? (Norm2 *)nullptr : &S->r2);
     if (cfg.reorth) {
       for (int pass = 0; pass < 2; ++pass) {
         k_multidot<double><<<std::min(b + 1, 1024), kThreads, 0, st>>>(B.V, n, b + 1, w, n, c.get()); ::dg::count_launch();
@@ -525,8 +569,8 @@ struct LzStepsMixed {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 2, z.cap_max);
-    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, &S->r2, b, sig.get()};
-    op.apply(B.vec(b), &S->r2.rs, SCALE_MUL, 0.0, (const int *)nullptr, epi, slot, st);
+    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
+    op.apply(B.vec(b), Scale::norm2(&S->r2), 0.0, (const int *)nullptr, epi, slot, st);
     ++z.spmv;
     if (!cfg.mixed_reorth) {
       launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
@@ -711,7 +755,7 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   ws.prog.h->done = 0;
   ws.prog.h->stamp = 0;
   k_norm2<double><<<ws.vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
-  op.apply(x_dev, &S->xn2.rs, SCALE_MUL, sigma, (const int *)nullptr, EpiCgInit{b_dev, xs.get(), r.get(), p.get(), S}, slot, st);
+  op.apply(x_dev, Scale::norm2(&S->xn2), sigma, (const int *)nullptr, EpiCgInit{b_dev, xs.get(), r.get(), p.get(), S}, slot, st);
   DG_CUDA(cudaMemcpyAsync(x_dev, xs.get(), sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   if (spmv_count) ++*spmv_count;
   const int chunk = 8;
@@ -720,7 +764,7 @@ IterResult cg_core(const Opl &op, double sigma, const double *b_dev, double *x_d
   double *up = ws.partials2.get();
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
-      op.apply(p.get(), (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgDot{y.get()}, slot, st);
+      op.apply(p.get(), Scale{}, sigma, &S->done, EpiCgDot{y.get()}, slot, st);
       launch_pdl(k_cg_update, ws.vgrid, kThreads, st, n, (const double *)p.get(), (const double *)y.get(), x_dev, r.get(),
                  (const Scalars *)S, it, (const double *)slot.partials, pgrid, up);
       launch_pdl(k_cg_direction, ws.vgrid, kThreads, st, n, (const double *)r.get(), p.get(), S, it, max_step, acc,
@@ -778,13 +822,13 @@ IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double 
   ws.prog.h->stamp = 0;
   // ring: V0 = vb[i0], V1raw = vb[i1], V1n -> vb[i2], V2 -> vb[i3]
   int i0 = 0, i1 = 1, i2 = 2, i3 = 3, j0 = 0, j1 = 1, j2 = 2;
-  op.apply(x_dev, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiMrInit{b_dev, vb[i1].get(), S}, slot, st);
+  op.apply(x_dev, Scale{}, sigma, (const int *)nullptr, EpiMrInit{b_dev, vb[i1].get(), S}, slot, st);
   if (spmv_count) ++*spmv_count;
   const int chunk = 8;
   int enq = -1;
   auto enqueue_to = [&](int last) {
     for (int it = enq + 1; it <= last; ++it) {
-      op.apply(vb[i1].get(), &S->inv_gamma0, SCALE_MUL, sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
+      op.apply(vb[i1].get(), Scale::mul(&S->inv_gamma0), sigma, &S->done, EpiMrDelta{vb[i2].get(), temp.get(), S}, slot, st);
       launch_pdl(k_mr_lanczos, ws.vgrid, kThreads, st, n, temp.get(), vb[i2].get(), vb[i0].get(), vb[i3].get(), S, acc, it,
                  max_step, ws.prog.d, slot);
       launch_pdl(k_mr_update, ws.vgrid, kThreads, st, n, vb[i2].get(), wb[j0].get(), wb[j1].get(), wb[j2].get(), x_dev, S);
@@ -832,7 +876,7 @@ IterResult minres_core(const Opl &op, double sigma, const double *b_dev, double 
 template <class Opl>
 double residual_core(const Opl &op, const double *x_dev, double sigma, double lambda, Workspace &ws) {
   Scalars *S = ws.S();
-  op.apply(x_dev, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiResidualL1{lambda, &S->res}, ws.slot(), ws.st);
+  op.apply(x_dev, Scale{}, sigma, (const int *)nullptr, EpiResidualL1{lambda, &S->res}, ws.slot(), ws.st);
   double out = 0.0;
   DG_CUDA(cudaMemcpyAsync(&out, &S->res, sizeof(double), cudaMemcpyDeviceToHost, ws.st));
   DG_CUDA(cudaStreamSynchronize(ws.st));

@@ -543,7 +543,7 @@ int dg_spmv(dg_matrix *m, const double *x, double *y, double sigma) {
       yb.alloc(m->n);
       yp = yb.get();
     }
-    matrix_apply64(m, xp, (const double *)nullptr, SCALE_ONE, sigma, (const int *)nullptr, EpiStore<double>{yp},
+    matrix_apply64(m, xp, Scale{}, sigma, (const int *)nullptr, EpiStore<double>{yp},
                    RedSlot{nullptr, nullptr}, st);
     if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, bytes, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
@@ -570,10 +570,10 @@ int dg_spmv_f32(dg_matrix *m, const float *x, float *y) {
       yp = yb.get();
     }
     if (m->format == DG_FORMAT_SELL)
-      launch_sell(m->sell32(), m->sell_grid, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
+      launch_sell(m->sell32(), m->sell_grid, xp, Scale{}, 0.0, (const int *)nullptr,
                   EpiStore<float>{yp}, RedSlot{nullptr, nullptr}, st);
     else
-      launch_apply(m->op32(), m->lanes, m->grid, m->n, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr,
+      launch_apply(m->op32(), m->lanes, m->grid, m->n, xp, Scale{}, 0.0, (const int *)nullptr,
                    EpiStore<float>{yp}, RedSlot{nullptr, nullptr}, st);
     if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, bytes, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
@@ -599,7 +599,7 @@ int dg_spmv_mixed(dg_matrix *m, const float *x, double *y) {
       yb.alloc(m->n);
       yp = yb.get();
     }
-    matrix_apply32(m, xp, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiStore<double>{yp},
+    matrix_apply32(m, xp, Scale{}, 0.0, (const int *)nullptr, EpiStore<double>{yp},
                    RedSlot{nullptr, nullptr}, st);
     if (!yd) DG_CUDA(cudaMemcpyAsync(y, yp, sizeof(double) * m->n, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
@@ -633,9 +633,9 @@ void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size
     const RedSlot slot{partials.get(), ticket.get()};
     if constexpr (std::is_same<XT, float>::value) {
       DG_REQUIRE(m->has32, DG_ERR_ARG, "matrix has no FP32 values");
-      matrix_apply32(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, epi, slot, st);
+      matrix_apply32(m, x_dev, Scale{}, 0.0, (const int *)nullptr, epi, slot, st);
     } else {
-      matrix_apply64(m, x_dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, epi, slot, st);
+      matrix_apply64(m, x_dev, Scale{}, 0.0, (const int *)nullptr, epi, slot, st);
     }
     DG_CUDA(cudaEventRecord(e1, st));
     DG_CUDA(cudaEventSynchronize(e1));
@@ -700,10 +700,10 @@ int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out) {
     DG_CUDA(cudaEventCreate(&e1));
     auto time_it = [&]() -> float {
       RedSlot slot{partials.get(), ticket.get()};
-      matrix_apply64(m, x.get(), (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
+      matrix_apply64(m, x.get(), Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
       DG_CUDA(cudaEventRecord(e0, st));
       for (int i = 0; i < iters; ++i)
-        matrix_apply64(m, x.get(), (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
+        matrix_apply64(m, x.get(), Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), out1.get()}, slot, st);
       DG_CUDA(cudaEventRecord(e1, st));
       DG_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;

@@ -43,39 +43,39 @@ void choose_shape(int n, long nnz, int *lanes, int *grid);
 
 // Launch k_apply with the matrix's lane count (runtime switch over L).
 template <class Op, class XT, class Epi>
-void launch_apply(const Op &op, int lanes, int grid, int n, const XT *x, const double *scale_src, int scale_mode,
+void launch_apply(const Op &op, int lanes, int grid, int n, const XT *x, Scale sc,
                   double sigma, const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
   switch (lanes) {
-    case 1: launch_pdl(k_apply<1, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case 2: launch_pdl(k_apply<2, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case 4: launch_pdl(k_apply<4, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case 8: launch_pdl(k_apply<8, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case 16: launch_pdl(k_apply<16, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    default: launch_pdl(k_apply<32, Op, XT, Epi>, grid, kThreads, st, op, n, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case 1: launch_pdl(k_apply<1, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
+    case 2: launch_pdl(k_apply<2, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
+    case 4: launch_pdl(k_apply<4, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
+    case 8: launch_pdl(k_apply<8, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
+    case 16: launch_pdl(k_apply<16, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
+    default: launch_pdl(k_apply<32, Op, XT, Epi>, grid, kThreads, st, op, n, x, sc, sigma, gate, epi, slot); break;
   }
   DG_CUDA(cudaGetLastError());
 }
 
 // Launch the sliced-ELL apply kernel.
 template <int WS, class VT, class XT, class Epi>
-void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, const double *scale_src, int scale_mode, double sigma,
+void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma,
                     const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
   switch (op.variant) {
-    case V_U4: launch_pdl(k_apply_sell<WS, V_U4, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case V_U16: launch_pdl(k_apply_sell<WS, V_U16, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    case V_PIPE8: launch_pdl(k_apply_sell<WS, V_PIPE8, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
-    default: launch_pdl(k_apply_sell<WS, V_U8, VT, XT, Epi>, grid, kThreads, st, op, x, scale_src, scale_mode, sigma, gate, epi, slot); break;
+    case V_U4: launch_pdl(k_apply_sell<WS, V_U4, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
+    case V_U16: launch_pdl(k_apply_sell<WS, V_U16, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
+    case V_PIPE8: launch_pdl(k_apply_sell<WS, V_PIPE8, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
+    default: launch_pdl(k_apply_sell<WS, V_U8, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
   }
 }
 
 template <class VT, class XT, class Epi>
-void launch_sell(const SellOp<VT> &op, int grid, const XT *x, const double *scale_src, int scale_mode, double sigma,
+void launch_sell(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma,
                  const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
   switch (op.ws) {
-    case 1: launch_sell_ws<1>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
-    case 2: launch_sell_ws<2>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
-    case 4: launch_sell_ws<4>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
-    default: launch_sell_ws<8>(op, grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st); break;
+    case 1: launch_sell_ws<1>(op, grid, x, sc, sigma, gate, epi, slot, st); break;
+    case 2: launch_sell_ws<2>(op, grid, x, sc, sigma, gate, epi, slot, st); break;
+    case 4: launch_sell_ws<4>(op, grid, x, sc, sigma, gate, epi, slot, st); break;
+    default: launch_sell_ws<8>(op, grid, x, sc, sigma, gate, epi, slot, st); break;
   }
   DG_CUDA(cudaGetLastError());
 }
@@ -87,22 +87,22 @@ void choose_sell_shape(int nslices, long stored, int *ws, int *grid);
 
 // Apply the matrix in its selected format with FP64 values.
 template <class XT, class Epi>
-void matrix_apply64(const dg_matrix *m, const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+void matrix_apply64(const dg_matrix *m, const XT *x, Scale sc, double sigma, const int *gate,
                     const Epi &epi, RedSlot slot, cudaStream_t st) {
   if (m->format == DG_FORMAT_SELL)
-    launch_sell(m->sell64(), m->sell_grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_sell(m->sell64(), m->sell_grid, x, sc, sigma, gate, epi, slot, st);
   else
-    launch_apply(m->op64(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_apply(m->op64(), m->lanes, m->grid, m->n, x, sc, sigma, gate, epi, slot, st);
 }
 
 // Apply the matrix with its FP32 values (mixed-precision form; FP32 input vector).
 template <class Epi>
-void matrix_apply32(const dg_matrix *m, const float *x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+void matrix_apply32(const dg_matrix *m, const float *x, Scale sc, double sigma, const int *gate,
                     const Epi &epi, RedSlot slot, cudaStream_t st) {
   if (m->format == DG_FORMAT_SELL)
-    launch_sell(m->sell32(), m->sell_grid, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_sell(m->sell32(), m->sell_grid, x, sc, sigma, gate, epi, slot, st);
   else
-    launch_apply(m->op32(), m->lanes, m->grid, m->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_apply(m->op32(), m->lanes, m->grid, m->n, x, sc, sigma, gate, epi, slot, st);
 }
 
 // Blocks needed by the current format (for sizing reduction partials).

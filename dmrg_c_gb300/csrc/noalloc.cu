@@ -62,10 +62,11 @@ struct RawCrsLauncher {
   int n_, lanes, grid_;
   int n() const { return n_; }
   int grid() const { return grid_; }
+  long nnz() const { return 0; }
   template <class XT, class Epi>
-  void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
+  void apply(const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
-    launch_apply(op, lanes, grid_, n_, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_apply(op, lanes, grid_, n_, x, sc, sigma, gate, epi, slot, st);
   }
 };
 
@@ -118,14 +119,14 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
     // x0 normalised (into y), r = b - (M + sigma) x0, p = r; then x <- normalised x0
     // (sml/CONJUGATE_GRADIENT_SYM.c:35-43).
     k_norm2<double><<<vgrid, kThreads, 0, st>>>(x_dev, n, &S->xn2, slot); ::dg::count_launch();
-    op.apply(x_dev, &S->xn2.rs, SCALE_MUL, sigma, (const int *)nullptr, EpiCgInit{b_dev, y, r, p, S}, slot, st);
+    op.apply(x_dev, Scale::norm2(&S->xn2), sigma, (const int *)nullptr, EpiCgInit{b_dev, y, r, p, S}, slot, st);
     DG_CUDA(cudaMemcpyAsync(x_dev, y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     const int chunk = 16;
     int done = 0, it = 1;
     while (it < max_step && !done) {
       const int last = std::min(it + chunk - 1, max_step - 1);
       for (; it <= last; ++it) {
-        op.apply(p, (const double *)nullptr, SCALE_ONE, sigma, &S->done, EpiCgDot{y}, slot, st);
+        op.apply(p, Scale{}, sigma, &S->done, EpiCgDot{y}, slot, st);
         k_cg_update<<<vgrid, kThreads, 0, st>>>(n, p, y, x_dev, r, S, it, partials, op.grid_, partials2); ::dg::count_launch();
         k_cg_direction<<<vgrid, kThreads, 0, st>>>(n, r, p, S, it, max_step, acc, partials2, vgrid, prog); ::dg::count_launch();
       }

@@ -118,10 +118,11 @@ struct ObcLauncher {
   const ObcData *D;
   int n() const { return D->n; }
   int grid() const { return D->grid; }
+  long nnz() const { return D->nnz_est; }
   template <class XT, class Epi>
-  void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
+  void apply(const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
-    launch_apply(D->op(), D->lanes, D->grid, D->n, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+    launch_apply(D->op(), D->lanes, D->grid, D->n, x, sc, sigma, gate, epi, slot, st);
   }
 };
 
@@ -317,7 +318,7 @@ void DMRG_MATRIX_VECTOR_PRODUCT_OBC(CRS1 *M_LLLR, CRS1 *M_LRRL, CRS1 *M_LRRL_Sig
     VecArg x(V, D.n, true, false, st);
     VecArg y(Out_V, D.n, false, true, st);
     ObcLauncher op{&D};
-    op.apply(x.dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiStore<double>{y.dev}, RedSlot{nullptr, nullptr}, st);
+    op.apply(x.dev, Scale{}, 0.0, (const int *)nullptr, EpiStore<double>{y.dev}, RedSlot{nullptr, nullptr}, st);
     y.commit(st);
   });
 }
@@ -334,7 +335,7 @@ double DMRG_CONVERGE_CHECK_OBC(double eig_val, CRS1 *M_LLLR, CRS1 *M_LRRL, CRS1 
     VecArg x(Eig_V, D.n, true, false, st);
     VecArg y(Temp_V, D.n, false, true, st);
     ObcLauncher op{&D};
-    op.apply(x.dev, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiStoreResidual{y.dev, eig_val, &ws.S()->res},
+    op.apply(x.dev, Scale{}, 0.0, (const int *)nullptr, EpiStoreResidual{y.dev, eig_val, &ws.S()->res},
              ws.slot(), st);
     DG_CUDA(cudaMemcpyAsync(&out, &ws.S()->res, sizeof(double), cudaMemcpyDeviceToHost, st));
     y.commit(st);

@@ -95,7 +95,7 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     return fetch(out1.get());
   };
   // y = H psi, theta = <psi, y>
-  op.apply(psi, (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), &S->res}, slot, st);
+  op.apply(psi, Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), &S->res}, slot, st);
   ++R.spmv64;
   double theta = fetch(&S->res);
   double l1 = resid(theta);
@@ -105,7 +105,7 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     const double tau = std::min(1e-1, std::max(1e-4, 0.5 * kMixedRes * std::fabs(theta) / rn));
     // g = (H32 - theta) fl32(psi): makes <psi, q> = <g, p32> available without a second reduction
     k_copy<double, float><<<vg, kThreads, 0, st>>>(psi, psi32.get(), n); ::dg::count_launch();
-    op.apply(psi32.get(), (const double *)nullptr, SCALE_ONE, -theta, (const int *)nullptr, EpiStore<double>{g.get()}, slot, st);
+    op.apply(psi32.get(), Scale{}, -theta, (const int *)nullptr, EpiStore<double>{g.get()}, slot, st);
     ++R.inner;
     // res = -(r - <psi,r> psi), t = 0, p = res
     const double c = dot(psi, r.get());
@@ -133,7 +133,7 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     int enq = 0, checked = 0;
     auto enqueue_to = [&](int last) {
       for (int it = enq + 1; it <= last; ++it) {
-        op.apply(p32.get(), (const double *)nullptr, SCALE_ONE, -theta, &S->done, EpiRefineAlpha{q.get(), S}, slot, st);
+        op.apply(p32.get(), Scale{}, -theta, &S->done, EpiRefineAlpha{q.get(), S}, slot, st);
         launch_pdl(k_refine_update, vg, kThreads, st, n, (const float *)p32.get(), (const double *)q.get(), (const double *)psi,
                    t.get(), res.get(), S, it, max_inner, ws.prog.d, slot);
         launch_pdl(k_refine_direction, vg, kThreads, st, n, (const double *)res.get(), p.get(), p32.get(),
@@ -165,7 +165,7 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     if (!(nt2 > 0.0)) break;
     axpby(0.0, psi, 1.0 / std::sqrt(nt2), t.get());
     // z = H t_hat; Rayleigh-Ritz on span{psi, t_hat}
-    op.apply((const double *)t.get(), (const double *)nullptr, SCALE_ONE, 0.0, (const int *)nullptr, EpiDot<double>{z.get(), &S->res},
+    op.apply((const double *)t.get(), Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{z.get(), &S->res},
              slot, st);
     ++R.spmv64;
     const double a22 = fetch(&S->res);

@@ -146,14 +146,14 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
 
 template <int WS, int VAR, class VT, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
-k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, const double *scale_src, int scale_mode, double sigma, const int *gate,
+k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, const int *gate,
              Epi epi, RedSlot slot) {
   pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
   constexpr int U = (VAR == V_U4) ? 4 : (VAR == V_U16) ? 16 : 8;
   constexpr bool PIPE = (VAR == V_PIPE8);
   constexpr bool STREAM = false;
-  const double s = load_scale(scale_src, scale_mode);
+  const double s = begin_scale(sc, epi);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;          // warp in block
   const int group = wib / WS, sub = wib % WS;

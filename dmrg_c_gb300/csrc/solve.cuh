@@ -16,14 +16,15 @@ struct CrsLauncher {
   const dg_matrix *m;
   int n() const { return m->n; }
   int grid() const { return matrix_grid(m); }
+  long nnz() const { return m->nnz; }
   template <class XT, class Epi>
-  void apply(const XT *x, const double *scale_src, int scale_mode, double sigma, const int *gate, const Epi &epi, RedSlot slot,
+  void apply(const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
     if constexpr (std::is_same<XT, float>::value) {
       DG_REQUIRE(m->has32, DG_ERR_ARG, "the mixed form needs FP32 values (create the matrix with DG_VALUES_BOTH)");
-      matrix_apply32(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+      matrix_apply32(m, x, sc, sigma, gate, epi, slot, st);
     } else {
-      matrix_apply64(m, x, scale_src, scale_mode, sigma, gate, epi, slot, st);
+      matrix_apply64(m, x, sc, sigma, gate, epi, slot, st);
     }
   }
 };
