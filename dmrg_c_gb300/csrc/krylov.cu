@@ -220,10 +220,20 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
-                                                       const float *__restrict__ y, const double *D, const double *O, int n,
-                                                       Norm2 *r2, RedSlot slot) {
+                                                       const float *__restrict__ y, double *D, double *hD, const double *O, int n,
+                                                       const double *pp, int pcount, RedSlot out, Norm2 *r2) {
   pdl_wait();
-  const double a = D[b] * sig[b];
+  double d;
+  if (pcount > 0) {
+    d = sum_partials(pp, pcount);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      D[b] = d;
+      hD[b] = d;
+    }
+  } else {
+    d = D[b];
+  }
+  const double a = d * sig[b];
   const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
   const float *vb = V + (long)b * ldv;
   const float *vp = (b > 0) ? V + (long)(b - 1) * ldv : vb;
@@ -236,7 +246,10 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
     acc += w * w;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
+  if (r2)
+    grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });
+  else
+    block_partial(acc, out.partials);
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,

@@ -32,14 +32,12 @@ namespace dg {
 struct Scalars {
   Norm2 r2;         // Lanczos: <w,w> of the pending unnormalised Krylov vector
   Norm2 xn2;        // CG: <x0,x0>; generic norm output
-  double rr;        // refinement CG: <r,r> of the current residual
   double rrs[2];    // CG: <r,r> entering iteration it is rrs[it & 1]
-  double a;         // CG: alpha
-  double beta;      // CG: beta
   double res;       // residual / dot output
   double gamma0, gamma1, delta, eta, eta_old, c0, c1, c2, s0, s1, s2, inv_alpha1, alpha2, alpha3;  // MINRES
   double inv_gamma0;    // MINRES: 1/gamma0, the scale of the next product
-  double pq, gp, thr;   // refinement CG: <p,q>, <g,p>, stopping threshold on <res,res>
+  double thr;           // refinement CG: stopping threshold on <res,res>
+  double rrs_ref[2];    // refinement CG: <res,res> entering iteration it is rrs_ref[it & 1]
   int done;         // 0 running, 1 converged, 2 iteration limit
   int iters;
 };
@@ -60,7 +58,7 @@ struct Workspace {
   cudaStream_t st;
   int n;
   int vgrid;
-  DevBuf<double> partials, partials2;   // partials2: a second slot for consumer-finished reductions
+  DevBuf<double> partials, partials2, partials3;   // 2, 3: more slots for consumer-finished reductions
   DevBuf<unsigned> ticket;
   DevBuf<Scalars> sc;
   Mapped<Progress> prog;
@@ -69,6 +67,7 @@ struct Workspace {
     int g = max_grid > vgrid ? max_grid : vgrid;
     partials.alloc(g);
     partials2.alloc(g);
+    partials3.alloc(g);
     ticket.alloc(1);
     sc.alloc(1);
     prog.alloc(1);
@@ -288,10 +287,12 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
                                                     int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
                                                     float *__restrict__ coef, unsigned *ticket);
 // Three-term recurrence of the mixed form without reorthogonalisation:
-// w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w); *r2 = <w,w>.
+// w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w).  D[b] as in
+// k_lz_update (summed from the product's pcount partials, or as its last block recorded it);
+// <w,w> into block partials (r2 null) or the Norm2 *r2.
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
-                                                       const float *__restrict__ y, const double *D, const double *O, int n,
-                                                       Norm2 *r2, RedSlot slot);
+                                                       const float *__restrict__ y, double *D, double *hD, const double *O, int n,
+                                                       const double *pp, int pcount, RedSlot out, Norm2 *r2);
 // w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); *r2 = <w,w>.
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
                                                     const float *__restrict__ y, int n, Norm2 *r2, RedSlot slot);
@@ -474,6 +475,10 @@ struct KrylovBasis {
   T *vec(int j) const { return V + (size_t)j * n; }
 };
 
+// Stored elements a product block needs before Lanczos leaves its reductions to the consumer
+// (LzSteps64, LzStepsMixed).
+constexpr long kLzDeferWork = 6144;
+
 // FP64 form (the reference's LANCZOS*): the product normalises w on the fly and stores v_b
 // into the basis; the update kernel forms w_{b+1} by the three-term recurrence, plus two
 // Gram-Schmidt passes when cfg.reorth (dense path).
@@ -492,11 +497,10 @@ struct LzSteps64 {
   // block also forms 1/sqrt(<w,w>), ~70 FP64 warp instructions a block.  That is a latency win
   // for a superblock product (KLM m=128: 8 k elements a block) but a throughput loss for an ED
   // product of short rows (XXZ L=22: 3.5 k), where the producers' last blocks do it once.
-  static constexpr long kDeferWork = 6144;
   bool defer;
   LzSteps64(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
       : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), c(z_.cap_max + 1), B(z_.n, w_.st),
-        defer(o.nnz() >= kDeferWork * (long)o.grid()) {}
+        defer(o.nnz() >= kLzDeferWork * (long)o.grid()) {}
   void begin_cycle() {}
   void step(int b) {
     cudaStream_t st = ws.st;
@@ -569,14 +573,26 @@ struct LzStepsMixed {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 2, z.cap_max);
+    if (!cfg.mixed_reorth) {
+      // as LzSteps64: reductions finished by the consumer on products with enough work a block
+      const bool defer = op.nnz() >= kLzDeferWork * (long)op.grid();
+      const Scale sc = (b > 0 && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
+      if (defer) {
+        EpiLanczos<float, float, true> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
+        op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
+      } else {
+        EpiLanczos<float, float, false> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
+        op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
+      }
+      ++z.spmv;
+      launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
+                 z.D.get(), z.hD.d, (const double *)z.O.get(), n, (const double *)slot.partials, defer ? op.grid() : 0,
+                 RedSlot{ws.partials2.get(), ws.ticket.get()}, defer ? (Norm2 *)nullptr : &S->r2);
+      return;
+    }
     EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
     op.apply(B.vec(b), Scale::norm2(&S->r2), 0.0, (const int *)nullptr, epi, slot, st);
     ++z.spmv;
-    if (!cfg.mixed_reorth) {
-      launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
-                 (const double *)z.D.get(), (const double *)z.O.get(), n, &S->r2, slot);
-      return;
-    }
     const int nvec = b + 1;
     launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec,
                (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get());

@@ -5,11 +5,16 @@ namespace dg {
 
 __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *__restrict__ p32, const double *__restrict__ q,
                                                            const double *__restrict__ psi, double *__restrict__ t,
-                                                           double *__restrict__ res, Scalars *S, int it, int max_step,
-                                                           Progress *prog, RedSlot slot) {
+                                                           double *__restrict__ res, const Scalars *S, int it, const double *pp,
+                                                           int pcount, const double *gpp, int gcount, double *up) {
   pdl_wait();
-  if (*((volatile int *)&S->done)) return;
-  const double a = S->a, gp = S->gp;
+  if (*((volatile const int *)&S->done)) return;
+  __shared__ double s_a;
+  const double pq = sum_partials(pp, pcount);
+  const double gp = sum_partials(gpp, gcount);
+  if (threadIdx.x == 0) s_a = S->rrs_ref[it & 1] / pq;   // one division per block
+  __syncthreads();
+  const double a = s_a;
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     t[i] = t[i] + a * (double)p32[i];
@@ -18,27 +23,41 @@ __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *
     acc += ri * ri;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double tot) {
-    if (tot < S->thr) {
-      S->done = 1;
-      S->iters = it;
-    } else if (it >= max_step) {
-      S->done = 2;
-      S->iters = max_step;
-    }
-    S->beta = tot / S->rr;
-    S->rr = tot;
-    prog->done = S->done;
-    prog->stamp = it;
-  });
+  block_partial(acc, up);
 }
 
 __global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const double *__restrict__ res, double *__restrict__ p,
                                                               float *__restrict__ p32, const double *__restrict__ g, Scalars *S,
-                                                              RedSlot slot) {
+                                                              int it, int max_step, const double *up, int ucount, double *gout,
+                                                              Progress *prog) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
-  const double b = S->beta;
+  __shared__ double s_b;
+  if (it > 0) {
+    const double tot = sum_partials(up, ucount);
+    const bool converged = tot < S->thr, last = it >= max_step;
+    if (threadIdx.x == 0) {
+      if (blockIdx.x == 0) {
+        if (converged) {
+          S->done = 1;
+          S->iters = it;
+        } else if (last) {
+          S->done = 2;
+          S->iters = max_step;
+        }
+        S->rrs_ref[(it + 1) & 1] = tot;   // the other slot: this kernel's blocks read rrs_ref[it & 1]
+        prog->done = S->done;
+        prog->stamp = it;
+      }
+      s_b = tot / S->rrs_ref[it & 1];
+    }
+    __syncthreads();
+    if (converged || last) return;   // the same decision in every block
+  } else {
+    if (threadIdx.x == 0) s_b = 0.0;
+    __syncthreads();
+  }
+  const double b = s_b;
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const double pi = res[i] + b * p[i];
@@ -48,7 +67,7 @@ __global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const doub
     acc += g[i] * (double)pf;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double tot) { S->gp = tot; });
+  block_partial(acc, gout);
 }
 
 __global__ void __launch_bounds__(kThreads) k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out,

@@ -23,28 +23,31 @@ namespace dg {
 
 constexpr double kMixedRes = 1e-8;    // accept when ||H psi - theta psi||_2 <= kMixedRes |theta|
 
-// q = (H32 - theta) p32 (row sums from the product kernel); S->pq = <p32, q>.
-struct EpiRefineAlpha {
+// q = (H32 - theta) p32 (row sums from the product kernel) with block partials of <p32, q>
+// (summed by every block of the update kernel).
+struct EpiRefineDot {
   static constexpr bool kReduce = true;
+  static constexpr bool kDeferred = true;
   double *q;
-  Scalars *S;
   __device__ void row(int i, double xi, double yi, double &acc) const {
     q[i] = yi;
     acc += xi * yi;
   }
-  __device__ void finalize(double t) const {
-    S->pq = t;
-    S->a = S->rr / t;   // once here, not per thread of the update
-  }
+  __device__ void finalize(double) const {}
 };
 
-// t += a p32; res -= a (q - <g,p32> psi); convergence on <res,res> < S->thr.
+// Iteration it of the projected correction CG.  <p32,q> from the product's pcount partials,
+// <g,p32> from the previous direction kernel's gcount partials; a = rrs_ref[it&1] / <p32,q>;
+// t += a p32; res -= a (q - <g,p32> psi); block partials of <res,res> into up.
 __global__ void k_refine_update(int n, const float *__restrict__ p32, const double *__restrict__ q, const double *__restrict__ psi,
-                                double *__restrict__ t, double *__restrict__ res, Scalars *S, int it, int max_step,
-                                Progress *prog, RedSlot slot);
-// p = res + beta p; p32 = fl32(p); S->gp = <g, p32>.
+                                double *__restrict__ t, double *__restrict__ res, const Scalars *S, int it, const double *pp,
+                                int pcount, const double *gpp, int gcount, double *up);
+// Iteration it: <res,res> from the update's ucount partials; convergence (< S->thr) or the
+// iteration limit ends the solve (block 0 records it); otherwise p = res + beta p.  it = 0:
+// the start, p = res (beta 0, no test).  Then p32 = fl32(p) and block partials of <g,p32> into gout.
 __global__ void k_refine_direction(int n, const double *__restrict__ res, double *__restrict__ p, float *__restrict__ p32,
-                                   const double *__restrict__ g, Scalars *S, RedSlot slot);
+                                   const double *__restrict__ g, Scalars *S, int it, int max_step, const double *up, int ucount,
+                                   double *gout, Progress *prog);
 // *out = sum_i x_i y_i
 __global__ void k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out, RedSlot slot);
 // *out = sum_i g_i p32_i
@@ -118,26 +121,29 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     if (!(rr0 > 0.0)) break;
     // p = res (beta = 0), p32, <g,p32>
     Scalars init{};
-    init.rr = rr0;
-    init.beta = 0.0;
+    init.rrs_ref[1] = rr0;   // enters iteration 1
     init.thr = tau * tau * rr0;
-    DG_CUDA(cudaMemcpyAsync(&S->rr, &init.rr, sizeof(double), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(&S->beta, &init.beta, sizeof(double), cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(&S->rrs_ref[1], &init.rrs_ref[1], sizeof(double), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemcpyAsync(&S->thr, &init.thr, sizeof(double), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(&S->done, 0, sizeof(int), st));
     DG_CUDA(cudaMemsetAsync(&S->iters, 0, sizeof(int), st));
-    k_refine_direction<<<vg, kThreads, 0, st>>>(n, res.get(), p.get(), p32.get(), g.get(), S, slot); ::dg::count_launch();
+    // Partials: the product's <p32,q> in slot.partials, the update's <res,res> in partials2,
+    // the direction's <g,p32> in partials3; each is summed by every block of its consumer.
+    double *up = ws.partials2.get(), *gpp = ws.partials3.get();
+    const int pgrid = op.grid();
+    k_refine_direction<<<vg, kThreads, 0, st>>>(n, res.get(), p.get(), p32.get(), g.get(), S, 0, max_inner, (const double *)up, 0,
+                                                gpp, ws.prog.d); ::dg::count_launch();
     ws.prog.h->done = 0;
     ws.prog.h->stamp = 0;
     const int chunk = 8;
     int enq = 0, checked = 0;
     auto enqueue_to = [&](int last) {
       for (int it = enq + 1; it <= last; ++it) {
-        op.apply(p32.get(), Scale{}, -theta, &S->done, EpiRefineAlpha{q.get(), S}, slot, st);
+        op.apply(p32.get(), Scale{}, -theta, &S->done, EpiRefineDot{q.get()}, slot, st);
         launch_pdl(k_refine_update, vg, kThreads, st, n, (const float *)p32.get(), (const double *)q.get(), (const double *)psi,
-                   t.get(), res.get(), S, it, max_inner, ws.prog.d, slot);
+                   t.get(), res.get(), (const Scalars *)S, it, (const double *)slot.partials, pgrid, (const double *)gpp, vg, up);
         launch_pdl(k_refine_direction, vg, kThreads, st, n, (const double *)res.get(), p.get(), p32.get(),
-                   (const double *)g.get(), S, slot);
+                   (const double *)g.get(), S, it, max_inner, (const double *)up, vg, gpp, ws.prog.d);
       }
       enq = std::max(enq, last);
     };
