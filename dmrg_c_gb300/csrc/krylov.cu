@@ -32,18 +32,29 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(int n, const double *__r
                                                        const double *pp, int pcount, double *up) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
+  // first element's operands in flight before the partial sums (see k_lz_update)
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  double x0 = 0.0, p0 = 0.0, r0 = 0.0, y0 = 0.0;
+  if (i0 < n) {
+    x0 = x[i0];
+    p0 = p[i0];
+    r0 = r[i0];
+    y0 = y[i0];
+  }
   __shared__ double s_a;
   const double py = sum_partials(pp, pcount);
   if (threadIdx.x == 0) s_a = S->rrs[it & 1] / py;   // one division per block
   __syncthreads();
   const double a = s_a;
   double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    x[i] = x[i] + a * p[i];
-    const double ri = r[i] - a * y[i];
-    r[i] = ri;
-    acc += ri * ri;
-  }
+  auto step = [&](int i, double xi, double pi, double ri, double yi) {
+    x[i] = xi + a * pi;
+    const double rn = ri - a * yi;
+    r[i] = rn;
+    acc += rn * rn;
+  };
+  if (i0 < n) step(i0, x0, p0, r0, y0);
+  for (int i = i0 + stride; i < n; i += stride) step(i, x[i], p[i], r[i], y[i]);
   pdl_trigger();
   block_partial(acc, up);
 }
@@ -53,6 +64,13 @@ __global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *
                                                           Progress *prog) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
+  // first element's operands in flight before the partial sums (see k_lz_update)
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  double r0 = 0.0, p0 = 0.0;
+  if (i0 < n) {
+    r0 = r[i0];
+    p0 = p[i0];
+  }
   __shared__ double s_b;
   const double t = sum_partials(up, ucount);
   const bool converged = t < acc_thr, last = it >= max_step - 1;
@@ -74,7 +92,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_direction(int n, const double *
   __syncthreads();
   if (converged || last) return;   // the same decision in every block
   const double b = s_b;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) p[i] = r[i] + b * p[i];
+  if (i0 < n) p[i0] = r0 + b * p0;
+  for (int i = i0 + stride; i < n; i += stride) p[i] = r[i] + b * p[i];
   pdl_trigger();
 }
 
@@ -223,6 +242,17 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
                                                        const float *__restrict__ y, double *D, double *hD, const double *O, int n,
                                                        const double *pp, int pcount, RedSlot out, Norm2 *r2) {
   pdl_wait();
+  const float *vb = V + (long)b * ldv;
+  const float *vp = (b > 0) ? V + (long)(b - 1) * ldv : vb;
+  float *vn = V + (long)(b + 1) * ldv;
+  // first element's operands in flight before the partial sums (see k_lz_update)
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  float y0 = 0.0f, b0 = 0.0f, q0 = 0.0f;
+  if (i0 < n) {
+    y0 = y[i0];
+    b0 = vb[i0];
+    q0 = vp[i0];
+  }
   double d;
   if (pcount > 0) {
     d = sum_partials(pp, pcount);
@@ -235,16 +265,15 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
   }
   const double a = d * sig[b];
   const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
-  const float *vb = V + (long)b * ldv;
-  const float *vp = (b > 0) ? V + (long)(b - 1) * ldv : vb;
-  float *vn = V + (long)(b + 1) * ldv;
   double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    double w = (double)y[i] - a * (double)vb[i];
-    if (b > 0) w -= c * (double)vp[i];
+  auto step = [&](int i, float yi, float bi, float qi) {
+    double w = (double)yi - a * (double)bi;
+    if (b > 0) w -= c * (double)qi;
     vn[i] = (float)w;
     acc += w * w;
-  }
+  };
+  if (i0 < n) step(i0, y0, b0, q0);
+  for (int i = i0 + stride; i < n; i += stride) step(i, y[i], vb[i], vp[i]);
   pdl_trigger();
   if (r2)
     grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });

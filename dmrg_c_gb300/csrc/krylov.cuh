@@ -204,6 +204,15 @@ __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__r
                                                        int b, double *__restrict__ w, const double *pp, int pcount, RedSlot out,
                                                        Norm2 *r2) {
   pdl_wait();
+  // The first element's operands are loaded before the partial sums, so that both L2 round
+  // trips overlap (at solver sizes one element is often all a thread has).
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  double y0 = 0.0, v0 = 0.0, p0 = 0.0;
+  if (i0 < n) {
+    y0 = y[i0];
+    v0 = (double)v[i0];
+    if (b > 0) p0 = (double)vprev[i0];
+  }
   double d;
   if (pcount > 0) {
     d = sum_partials(pp, pcount);
@@ -216,12 +225,14 @@ __global__ void __launch_bounds__(kThreads) k_lz_update(int n, const double *__r
   }
   const double o = (b > 0) ? O[b] : 0.0;
   double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    double wi = y[i] - d * (double)v[i];
-    if (b > 0) wi = wi - o * (double)vprev[i];
+  auto step = [&](int i, double yi, double vi, double pi) {
+    double wi = yi - d * vi;
+    if (b > 0) wi = wi - o * pi;
     w[i] = wi;
     acc += wi * wi;
-  }
+  };
+  if (i0 < n) step(i0, y0, v0, p0);
+  for (int i = i0 + stride; i < n; i += stride) step(i, y[i], (double)v[i], b > 0 ? (double)vprev[i] : 0.0);
   pdl_trigger();
   if (r2)
     grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });

@@ -9,6 +9,17 @@ __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *
                                                            int pcount, const double *gpp, int gcount, double *up) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
+  // first element's operands in flight before the partial sums (see k_lz_update)
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  double t0 = 0.0, r0 = 0.0, q0 = 0.0, s0 = 0.0;
+  float f0 = 0.0f;
+  if (i0 < n) {
+    t0 = t[i0];
+    f0 = p32[i0];
+    r0 = res[i0];
+    q0 = q[i0];
+    s0 = psi[i0];
+  }
   __shared__ double s_a;
   const double pq = sum_partials(pp, pcount);
   const double gp = sum_partials(gpp, gcount);
@@ -16,12 +27,14 @@ __global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *
   __syncthreads();
   const double a = s_a;
   double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    t[i] = t[i] + a * (double)p32[i];
-    const double ri = res[i] - a * (q[i] - gp * psi[i]);
-    res[i] = ri;
-    acc += ri * ri;
-  }
+  auto step = [&](int i, double ti, float fi, double ri, double qi, double si) {
+    t[i] = ti + a * (double)fi;
+    const double rn = ri - a * (qi - gp * si);
+    res[i] = rn;
+    acc += rn * rn;
+  };
+  if (i0 < n) step(i0, t0, f0, r0, q0, s0);
+  for (int i = i0 + stride; i < n; i += stride) step(i, t[i], p32[i], res[i], q[i], psi[i]);
   pdl_trigger();
   block_partial(acc, up);
 }
@@ -32,6 +45,14 @@ __global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const doub
                                                               Progress *prog) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
+  // first element's operands in flight before the partial sums (see k_lz_update)
+  const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
+  double r0 = 0.0, p0 = 0.0, g0 = 0.0;
+  if (i0 < n) {
+    r0 = res[i0];
+    p0 = p[i0];
+    g0 = g[i0];
+  }
   __shared__ double s_b;
   if (it > 0) {
     const double tot = sum_partials(up, ucount);
@@ -59,13 +80,15 @@ __global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const doub
   }
   const double b = s_b;
   double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const double pi = res[i] + b * p[i];
+  auto step = [&](int i, double ri, double pi0, double gi) {
+    const double pi = ri + b * pi0;
     p[i] = pi;
     const float pf = (float)pi;
     p32[i] = pf;
-    acc += g[i] * (double)pf;
-  }
+    acc += gi * (double)pf;
+  };
+  if (i0 < n) step(i0, r0, p0, g0);
+  for (int i = i0 + stride; i < n; i += stride) step(i, res[i], p[i], g[i]);
   pdl_trigger();
   block_partial(acc, gout);
 }
