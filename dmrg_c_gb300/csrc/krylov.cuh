@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <limits>
 #include <thread>
 #include <vector>
@@ -487,8 +488,14 @@ struct KrylovBasis {
 };
 
 // Stored elements a product block needs before Lanczos leaves its reductions to the consumer
-// (LzSteps64, LzStepsMixed).
+// (LzSteps64, LzStepsMixed).  DG_DEFER_REDUCTIONS=0 / =1 forces the last-block / consumer form
+// (both give bitwise the same values); unset, the work per block decides.
 constexpr long kLzDeferWork = 6144;
+inline bool lz_defer(long nnz, int grid) {
+  const char *e = std::getenv("DG_DEFER_REDUCTIONS");
+  if (e && e[0] && !e[1] && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
+  return nnz >= kLzDeferWork * (long)grid;
+}
 
 // FP64 form (the reference's LANCZOS*): the product normalises w on the fly and stores v_b
 // into the basis; the update kernel forms w_{b+1} by the three-term recurrence, plus two
@@ -511,7 +518,7 @@ struct LzSteps64 {
   bool defer;
   LzSteps64(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
       : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), c(z_.cap_max + 1), B(z_.n, w_.st),
-        defer(o.nnz() >= kLzDeferWork * (long)o.grid()) {}
+        defer(lz_defer(o.nnz(), o.grid())) {}
   void begin_cycle() {}
   void step(int b) {
     cudaStream_t st = ws.st;
@@ -586,7 +593,7 @@ struct LzStepsMixed {
     B.ensure(b + 2, z.cap_max);
     if (!cfg.mixed_reorth) {
       // as LzSteps64: reductions finished by the consumer on products with enough work a block
-      const bool defer = op.nnz() >= kLzDeferWork * (long)op.grid();
+      const bool defer = lz_defer(op.nnz(), op.grid());
       const Scale sc = (b > 0 && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
       if (defer) {
         EpiLanczos<float, float, true> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
