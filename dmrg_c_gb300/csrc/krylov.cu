@@ -163,8 +163,16 @@ __global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__r
 
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
                                                     int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket) {
+                                                    float *__restrict__ coef, unsigned *ticket, const double *pp, int pcount,
+                                                    double *D, double *hD, int bstep) {
   pdl_wait();
+  if (pcount > 0 && blockIdx.x == 0 && blockIdx.y == 0) {   // block-uniform
+    const double d = sum_partials(pp, pcount);
+    if (threadIdx.x == 0) {
+      D[bstep] = d;
+      hD[bstep] = d;
+    }
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.y * kWarps + warp;
   const int chunk = blockIdx.x;
@@ -211,7 +219,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef_g,
-                                                    const float *__restrict__ y, int n, Norm2 *r2, RedSlot slot) {
+                                                    const float *__restrict__ y, int n, RedSlot out, Norm2 *r2) {
   pdl_wait();
   extern __shared__ float coef[];   // nvec entries
   for (int j = threadIdx.x; j < nvec; j += blockDim.x) coef[j] = coef_g[j];
@@ -235,7 +243,10 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long
     acc += w * w;
   }
   pdl_trigger();
-  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
+  if (r2)
+    grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });
+  else
+    block_partial(acc, out.partials);
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,

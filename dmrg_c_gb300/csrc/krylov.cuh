@@ -290,14 +290,19 @@ __global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, lon
 // three-term recurrence.  Dots and the subtraction use compensated FP32 arithmetic (Dot2),
 // the recurrence scalars and norms FP64.
 
-constexpr int kMxChunk = 1024;   // rows per dot-product chunk (one warp each)
+// Rows per dot-product chunk (one warp each): four rounds of four loads per lane.  Measured on
+// the KLM m=128 benchmark (mixed=1 solves/s): 1024 rows 290, 512 rows 312, 256 rows 304 (more
+// chunks: more FP64 warp sums of the chunk partials).
+constexpr int kMxChunk = 512;
 
 // partials[j * nchunk + chunk] = <V_j, y> over the chunk's rows, one warp per vector; the
 // last block reduces them (fixed order) to coef_j = -sig_j^2 <V_j, y> = -c_j sig_j with
-// c_j = <v_j, y>.  ticket: zero between uses.
+// c_j = <v_j, y>.  ticket: zero between uses.  With pcount > 0, block (0, 0) also sums the
+// product's pcount block partials into D[bstep] = <y, v_bstep> and its host mirror.
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
                                                     int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket);
+                                                    float *__restrict__ coef, unsigned *ticket, const double *pp, int pcount,
+                                                    double *D, double *hD, int bstep);
 // Three-term recurrence of the mixed form without reorthogonalisation:
 // w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w).  D[b] as in
 // k_lz_update (summed from the product's pcount partials, or as its last block recorded it);
@@ -305,9 +310,10 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
                                                        const float *__restrict__ y, double *D, double *hD, const double *O, int n,
                                                        const double *pp, int pcount, RedSlot out, Norm2 *r2);
-// w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); *r2 = <w,w>.
+// w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); <w,w> into block partials (r2
+// null) or the Norm2 *r2.
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
-                                                    const float *__restrict__ y, int n, Norm2 *r2, RedSlot slot);
+                                                    const float *__restrict__ y, int n, RedSlot out, Norm2 *r2);
 // out_i = sum_{j<k} s_j sig_j V_j[i] (FP64, j order); *r2 = <out,out>.
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
                                                      const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
@@ -591,31 +597,31 @@ struct LzStepsMixed {
     Scalars *S = ws.S();
     const RedSlot slot = ws.slot();
     B.ensure(b + 2, z.cap_max);
+    // as LzSteps64: reductions finished by the consumer on products with enough work a block
+    const bool defer = lz_defer(op.nnz(), op.grid());
+    const Scale sc = (b > 0 && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
+    if (defer) {
+      EpiLanczos<float, float, true> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
+      op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
+    } else {
+      EpiLanczos<float, float, false> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
+      op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
+    }
+    ++z.spmv;
+    const RedSlot r2slot{ws.partials2.get(), ws.ticket.get()};
+    Norm2 *r2 = defer ? (Norm2 *)nullptr : &S->r2;
     if (!cfg.mixed_reorth) {
-      // as LzSteps64: reductions finished by the consumer on products with enough work a block
-      const bool defer = lz_defer(op.nnz(), op.grid());
-      const Scale sc = (b > 0 && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
-      if (defer) {
-        EpiLanczos<float, float, true> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
-        op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
-      } else {
-        EpiLanczos<float, float, false> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
-        op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
-      }
-      ++z.spmv;
       launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(),
-                 z.D.get(), z.hD.d, (const double *)z.O.get(), n, (const double *)slot.partials, defer ? op.grid() : 0,
-                 RedSlot{ws.partials2.get(), ws.ticket.get()}, defer ? (Norm2 *)nullptr : &S->r2);
+                 z.D.get(), z.hD.d, (const double *)z.O.get(), n, (const double *)slot.partials, defer ? op.grid() : 0, r2slot,
+                 r2);
       return;
     }
-    EpiLanczos<float, float> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
-    op.apply(B.vec(b), Scale::norm2(&S->r2), 0.0, (const int *)nullptr, epi, slot, st);
-    ++z.spmv;
     const int nvec = b + 1;
     launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec,
-               (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get());
+               (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get(),
+               (const double *)slot.partials, defer ? op.grid() : 0, z.D.get(), z.hD.d, b);
     launch_pdl_smem(k_mx_sub, dim3(ws.vgrid), dim3(kThreads), sizeof(float) * nvec, st, B.V, (long)n, nvec,
-                    (const float *)coef.get(), (const float *)y.get(), n, &S->r2, slot);
+                    (const float *)coef.get(), (const float *)y.get(), n, r2slot, r2);
   }
   void combine(int k, const std::vector<double> &s, double *dst) {
     z.upload_s(k, s, ws.st);
