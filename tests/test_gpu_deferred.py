@@ -41,3 +41,27 @@ def test_deferred_superblock_bitwise(gpu, monkeypatch):
     e0, v0, l0, c0 = _solve(gpu, low, 0, None, monkeypatch, "0")
     e1, v1, l1, c1 = _solve(gpu, low, 0, None, monkeypatch, "1")
     assert (l0, c0) == (l1, c1) and e0 == e1 and np.array_equal(v0, v1)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 33, 257, 2100])
+@pytest.mark.parametrize("ws", [1, 4])
+def test_deferred_small_systems(gpu, monkeypatch, n, ws):
+    """Edge sizes for the consumer form: fewer partials than threads, one slice, the 1 x 1
+    operator, several warps per slice; energies against numpy."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(n)
+    A = sp.random(n, n, density=min(1.0, 6.0 / n), random_state=n)
+    A = (A + A.T).tocsr()
+    A.setdiag(rng.standard_normal(n) - 3.0)
+    A.sort_indices()
+    low = abi.lower_diag_last(A)
+    exact = np.linalg.eigvalsh(A.toarray())[0]
+    out = []
+    for mode in ("0", "1"):
+        monkeypatch.setenv("DG_DEFER_REDUCTIONS", mode)
+        m = gpu.DeviceMatrix(low, gpu.DG_STORE_LOWER_DIAG_LAST)
+        m.set_sell_shape(ws, 3)
+        v, info = gpu.ground_state(m, gpu.default_params())
+        out.append((info.eig_val, np.array(v), info.lanczos_steps, info.cg_steps))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1]) and out[0][2:] == out[1][2:]
+    assert abs(out[0][0] - exact) <= 1e-10 * max(1.0, abs(exact))
