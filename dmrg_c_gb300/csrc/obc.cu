@@ -40,9 +40,12 @@ struct ObcOp {
     return (long)ll * d * dim_RR * d + (long)lr * dim_RR * d + (long)(rr * d + rl);
   }
 
-  static constexpr bool kPostScale = false;   // the reference scales each gathered element
+  // The scale s of a Krylov product multiplies the finished row sum (k_apply), not each gathered
+  // element: one DFMA per element.  (The reference normalises the vector first; the sums differ
+  // from it by rounding only, as a lane split of a row does anyway.)
+  static constexpr bool kPostScale = true;
   template <int L, class XT>
-  __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double s) const {
+  __device__ __forceinline__ double row_partial(int i, int lane, const XT *__restrict__ x, double) const {
     const int ll = LL[i], lr = LR[i], rr = RR[i], rl = RL[i];
     double sum = 0.0;
     {
@@ -50,27 +53,28 @@ struct ObcOp {
       for (int64_t k = lllr.row[r] + lane; k < lllr.row[r + 1]; k += L) {
         const int c = lllr.col[k];
         const int inv = inv_sup[sup(ll_lllr[c], lr_lllr[c], rr, rl)];
-        if (inv >= 0) sum += to_d(x[inv]) * s * lllr.val[k];
+        if (inv >= 0) sum += to_d(x[inv]) * lllr.val[k];
       }
     }
     const int r2 = inv_lrrl[lr * d + rl];
     for (int64_t k = lrrl.row[r2] + lane; k < lrrl.row[r2 + 1]; k += L) {
       const int c = lrrl.col[k];
       const int inv = inv_sup[sup(ll, lr_lrrl[c], rr, rl_lrrl[c])];
-      if (inv >= 0) sum += to_d(x[inv]) * s * lrrl.val[k];
+      if (inv >= 0) sum += to_d(x[inv]) * lrrl.val[k];
     }
-    const double sign = (ele_rr[rr] % 2 == 1) ? -1.0 : 1.0;
+    // (-1)^Ele_RR[RR] as a sign-bit flip of the value: exact, and no FP64 multiply per element
+    const unsigned long long flip = (ele_rr[rr] % 2 == 1) ? 0x8000000000000000ull : 0ull;
     for (int64_t k = lrrl_sign.row[r2] + lane; k < lrrl_sign.row[r2 + 1]; k += L) {
       const int c = lrrl_sign.col[k];
       const int inv = inv_sup[sup(ll, lr_lrrl[c], rr, rl_lrrl[c])];
-      if (inv >= 0) sum += to_d(x[inv]) * s * lrrl_sign.val[k] * sign;
+      if (inv >= 0) sum += to_d(x[inv]) * __longlong_as_double(__double_as_longlong(lrrl_sign.val[k]) ^ flip);
     }
     {
       const int r = inv_rrrl[rr * d + rl];
       for (int64_t k = rrrl.row[r] + lane; k < rrrl.row[r + 1]; k += L) {
         const int c = rrrl.col[k];
         const int inv = inv_sup[sup(ll, lr, rr_rrrl[c], rl_rrrl[c])];
-        if (inv >= 0) sum += to_d(x[inv]) * s * rrrl.val[k];
+        if (inv >= 0) sum += to_d(x[inv]) * rrrl.val[k];
       }
     }
     return sum;
@@ -241,7 +245,17 @@ void obc_upload(ObcData &D, const CRS1 *M_LLLR, const CRS1 *M_LRRL, const CRS1 *
     }
   }
   up_crs(D, 3, M_RRRL, B->dim_RRRL, st);
-  choose_shape(D.n, (long)D.n * std::max(1L, D.nnz_est), &D.lanes, &D.grid);
+  // Lanes per row: at least two, about 16 elements of one block-operator segment per lane (a row
+  // is four segments walked one after another).  Measured per Lanczos solve: KLM m=128
+  // superblock (segments of ~16): 2 lanes 3.7 ms, 1: 4.1, 4: 4.3, 32: 8.8; Hubbard m=512
+  // (segments of ~62): 4 lanes 23.0 ms, 2: 25.4, 8: 28.4, 32: 66.
+  {
+    const long seg = std::max(1L, D.nnz_est / 4);
+    int L = 2;
+    while (L < 32 && (long)L * 16 < seg) L <<= 1;
+    D.lanes = L;
+    D.grid = (int)std::max(1L, std::min(((long)D.n * L + kThreads - 1) / kThreads, (long)sm_count() * 8));
+  }
   DG_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -9,6 +9,7 @@
     python -m dmrg_c_gb300.profile_spmv --sweep --cases xxz_ed22 hubbard_ed12
                                                              # the ED Hamiltonians
     python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
+    python -m dmrg_c_gb300.profile_spmv --obc klm_m128       # matrix-free OBC vs explicit Lanczos
     python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
 
 Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
@@ -136,6 +137,48 @@ def launches(name, fmt, count, mixed=False):
           f"n={m.n} nnz_full={m.nnz}")
 
 
+def obc_solve(name, repeats=3):
+    """Matrix-free superblock operator against the explicit CRS on the same superblock: the drop-in
+    DMRG_LANCZOS_SLOW_OBC (block operators and basis tables uploaded, the product gathers through
+    Inv_LLLRRRRL) and LANCZOS_SLOW_SYM on the explicit lower triangle (uploaded and expanded), same
+    start vector and accuracy; wall time per call including the uploads."""
+    import ctypes as C
+    import os
+    import tempfile
+    import time
+    import numpy as np
+    from . import abi
+    sb = CASES[name](0)
+    lib = L.load()
+    guess = np.random.default_rng(3).standard_normal(sb.n)
+    low = sb.explicit_lower()
+    old = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            for form in ("obc", "explicit"):
+                for k in range(repeats):
+                    vec, val = guess.copy(), np.zeros(1)
+                    if form == "obc":
+                        box = abi.DMRG_BOX_LAN(Eig_Vec=abi.ptr(vec, C.c_double), eig_val=abi.ptr(val, C.c_double), acc=1e-14,
+                                               min_step=1, max_step=800, p_threads=1, Guess=b"Yes", Type=b"Normal",
+                                               M_LLLR=sb.M_LLLR.ref, M_LRRL=sb.M_LRRL.ref, M_LRRL_Sign=sb.M_LRRL_Sign.ref,
+                                               M_RRRL=sb.M_RRRL.ref, Ele_RR=abi.ptr(sb.ele_rr, C.c_int),
+                                               Dmrg_Basis=C.pointer(sb.basis))
+                        t0 = time.perf_counter()
+                        lib.DMRG_LANCZOS_SLOW_OBC(C.byref(box))
+                    else:
+                        box = abi.BOX_LAN(M=low.ref, Eig_Vec=abi.ptr(vec, C.c_double), eig_val=abi.ptr(val, C.c_double),
+                                          acc=1e-14, min_step=1, max_step=800, max_block_step=800, p_threads=1,
+                                          Guess=b"Yes", Type=b"Normal")
+                        t0 = time.perf_counter()
+                        lib.LANCZOS_SLOW_SYM(C.byref(box))
+                    t = time.perf_counter() - t0
+                    print(f"{name} {form}: {t * 1e3:.2f} ms per Lanczos solve (E = {val[0]:.15f})", flush=True)
+        finally:
+            os.chdir(old)
+
+
 BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512")
 
 
@@ -168,8 +211,11 @@ def main(argv=None):
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--build", choices=BUILDS, default=None)
+    ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
     a = ap.parse_args(argv)
-    if a.build:
+    if a.obc:
+        obc_solve(a.obc)
+    elif a.build:
         build(a.build)
     elif a.case:
         launches(a.case, a.format, a.launches, a.mixed)
