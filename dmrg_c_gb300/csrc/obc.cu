@@ -84,7 +84,7 @@ struct ObcOp {
 // Device copy of the operator data.
 struct ObcData {
   int n = 0, dim_LL = 0, dim_RR = 0, d = 0;
-  long nnz_est = 0;
+  long nnz_est = 0;   // estimated elements a superblock row (sum of the four operators' averages)
   DevBuf<short> LL, LR, RR, RL, ll_lllr, lr_lllr, lr_lrrl, rl_lrrl, rr_rrrl, rl_rrrl;
   DevBuf<int> inv_sup, inv_lllr, inv_lrrl, inv_rrrl, ele_rr;
   DevBuf<int64_t> row[4];
@@ -122,7 +122,7 @@ struct ObcLauncher {
   const ObcData *D;
   int n() const { return D->n; }
   int grid() const { return D->grid; }
-  long nnz() const { return D->nnz_est; }
+  long nnz() const { return (long)D->n * D->nnz_est; }   // nnz_est: elements a row
   template <class XT, class Epi>
   void apply(const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi, RedSlot slot,
              cudaStream_t st) const {
