@@ -8,6 +8,7 @@
 // Vec[j] * O[l][c] where j is the position of code_i - (l - c) dim_onsite^site in the input
 // table (binary search; absent codes contribute nothing).  With Sign_Flag "Yes" the row is
 // multiplied by (-1)^(electrons on sites < op_site) (Jordan-Wigner string, EXACT_V_M_Q2.c:31-44).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <sys/stat.h>
@@ -43,19 +44,27 @@ struct SiteOp {
   const double *val;
 };
 
+// One thread per output row (the grid covers the rows, so the binary searches of all rows are in
+// flight together).  bits > 0: dim_onsite = 2^bits, and digits come from shifts and masks instead of
+// a 64-bit division per lower site (the same values).
 __global__ void k_site_apply(const int64_t *__restrict__ out_basis, long dim_out, const int64_t *__restrict__ in_basis, long dim_in,
-                             SiteOp op, int d, int site, int64_t dim_site, const int *__restrict__ n_ele, int use_sign,
+                             SiteOp op, int d, int bits, int site, int64_t dim_site, const int *__restrict__ n_ele, int use_sign,
                              const double *__restrict__ vec, double *__restrict__ out) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < dim_out; i += (long)gridDim.x * blockDim.x) {
     const int64_t code = out_basis[i];
-    const int local = digit_of(code, site, d);
+    const int local = bits > 0 ? (int)((code >> (site * bits)) & (d - 1)) : digit_of(code, site, d);
     int sign = 1;
     if (use_sign) {
       int ne = 0;
       int64_t c = code;
       for (int s = 0; s < site; ++s) {
-        ne += n_ele[(int)(c % d)];
-        c /= d;
+        if (bits > 0) {
+          ne += n_ele[(int)(c & (d - 1))];
+          c >>= bits;
+        } else {
+          ne += n_ele[(int)(c % d)];
+          c /= d;
+        }
       }
       sign = (ne % 2 == 0) ? 1 : -1;
     }
@@ -92,8 +101,12 @@ void site_apply(const CRS1 *M_On, const long *out_basis, long dim_out, const lon
   }
   if (use_sign) DG_CUDA(cudaMemcpyAsync(ne.get(), n_ele, sizeof(int) * d, cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemcpyAsync(x.get(), vec, sizeof(double) * dim_in, cudaMemcpyHostToDevice, st));
-  k_site_apply<<<vector_grid(dim_out), kThreads, 0, st>>>(ob.get(), dim_out, ib.get(), dim_in, SiteOp{r.get(), c.get(), v.get()}, d,
-                                                          site, dim_site, ne.get(), use_sign ? 1 : 0, x.get(), y.get()); ::dg::count_launch();
+  int bits = 0;
+  while ((1 << bits) < d) ++bits;
+  if ((1 << bits) != d) bits = 0;   // not a power of two: division path
+  const long blocks = std::max(1L, std::min((dim_out + kThreads - 1) / kThreads, (long)sm_count() * 64));
+  k_site_apply<<<(int)blocks, kThreads, 0, st>>>(ob.get(), dim_out, ib.get(), dim_in, SiteOp{r.get(), c.get(), v.get()}, d, bits,
+                                                 site, dim_site, ne.get(), use_sign ? 1 : 0, x.get(), y.get()); ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
   DG_CUDA(cudaMemcpyAsync(out, y.get(), sizeof(double) * dim_out, cudaMemcpyDeviceToHost, st));
   DG_CUDA(cudaStreamSynchronize(st));

@@ -10,6 +10,7 @@
                                                              # the ED Hamiltonians
     python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
     python -m dmrg_c_gb300.profile_spmv --obc klm_m128       # matrix-free OBC vs explicit Lanczos
+    python -m dmrg_c_gb300.profile_spmv --vm                 # EXACT_V_M_Q0 on the Hubbard L=12 basis
     python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
 
 Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
@@ -179,6 +180,37 @@ def obc_solve(name, repeats=3):
             os.chdir(old)
 
 
+def vm(repeats=10):
+    """EXACT_V_M_Q0 (a site operator applied to a vector on an ED basis) on the Hubbard L=12 basis
+    (n = 853,776), from pinned host arrays: wall time per drop-in call (basis, vector and operator
+    uploaded, one binary-searched gather per stored operator element, result downloaded), at the
+    first and the last site."""
+    import ctypes as C
+    import time
+    import numpy as np
+    import torch
+    from . import abi
+    ed = L.EDSystem(ed_models.hubbard_chain(12, U=4.0, hz=0.2))
+    basis = ed.download()[0]
+    ed.close()
+    n = len(basis)
+    b_t = torch.from_numpy(basis).pin_memory()
+    v_t = torch.randn(n, dtype=torch.float64).pin_memory()
+    o_t = torch.zeros(n, dtype=torch.float64).pin_memory()
+    info = abi.EXACT_BASIS_INFO(dim=n, Basis=abi.ptr(b_t.numpy(), C.c_long), tot_sz=0, tot_ele=0, tot_parity=0)
+    op = abi.Crs(np.array([0, 1, 2, 3, 4]), np.array([0, 1, 2, 3], np.int32), np.array([0.0, 1.0, 1.0, 2.0]), n=4)
+    lib = L.load()
+    v, o = abi.ptr(v_t.numpy(), C.c_double), abi.ptr(o_t.numpy(), C.c_double)
+    for site in (0, 11):
+        lib.EXACT_V_M_Q0(op.ref, v, o, 4, site, 1, C.byref(info))   # warm
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            lib.EXACT_V_M_Q0(op.ref, v, o, 4, site, 1, C.byref(info))
+        t = (time.perf_counter() - t0) / repeats
+        print(f"EXACT_V_M_Q0 hubbard L=12 (n={n}) site {site}: {t * 1e3:.3f} ms per call "
+              f"({3 * n * 8 / t / 1e9:.1f} GB/s of host<->device vectors+basis)", flush=True)
+
+
 BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512")
 
 
@@ -212,8 +244,11 @@ def main(argv=None):
     ap.add_argument("--mixed", action="store_true")
     ap.add_argument("--build", choices=BUILDS, default=None)
     ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
+    ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
     a = ap.parse_args(argv)
-    if a.obc:
+    if a.vm:
+        vm()
+    elif a.obc:
         obc_solve(a.obc)
     elif a.build:
         build(a.build)

@@ -99,6 +99,37 @@ def test_exact_v_m_q0_golden(gpu):
         np.testing.assert_array_equal(out, g[f"out_site{site}"])
 
 
+def _q2_apply(lib, op, b_out, b_in, vec, n_ele, d, site):
+    dims = np.zeros((1, 2), np.int32)
+    dims[0, 0], dims[0, 1] = len(b_out), len(b_in)
+    row_dims = (C.POINTER(C.c_int) * 1)(abi.ptr(dims[0], C.c_int))
+    bases = (C.POINTER(C.c_long) * 2)(abi.ptr(b_out, C.c_long), abi.ptr(b_in, C.c_long))
+    row_bases = (C.POINTER(C.POINTER(C.c_long)) * 1)(C.cast(bases, C.POINTER(C.POINTER(C.c_long))))
+    W = abi.EXACT_WHOLE_BASIS_Q2(Dim=C.cast(row_dims, C.POINTER(C.POINTER(C.c_int))),
+                                 Basis=C.cast(row_bases, C.POINTER(C.POINTER(C.POINTER(C.c_long)))), max_dim=0)
+    out = np.zeros(len(b_out))
+    lib.EXACT_V_M_Q2(op.ref, 0, 0, abi.ptr(vec, C.c_double), 0, 1, abi.ptr(out, C.c_double), b"Yes",
+                     abi.ptr(n_ele, C.c_int), d, site, 1, C.byref(W))
+    return out
+
+
+def test_exact_v_m_q2_three_state_sites_vs_oracle(gpu, oracle):
+    """A local dimension that is not a power of two (the kernel's division path), with the sign
+    string: a raising operator between the digit-sum 5 and 6 sectors of six 3-state sites."""
+    lib = gpu.load()
+    L_, d = 6, 3
+    codes = np.arange(d ** L_, dtype=np.int64)
+    digit_sum = sum((codes // d ** s) % d for s in range(L_))
+    b_in = np.ascontiguousarray(codes[digit_sum == 5])
+    b_out = np.ascontiguousarray(codes[digit_sum == 6])
+    op = abi.Crs(np.array([0, 0, 1, 2]), np.array([0, 1], np.int32), np.array([1.0, np.sqrt(2.0)]), n=3)
+    n_ele = np.array([0, 1, 2], np.int32)
+    vec = np.random.default_rng(7).standard_normal(len(b_in))
+    for site in (0, 2, 5):
+        ref = oracle.site_apply(op, b_out, b_in, d, site, vec, n_ele=n_ele)
+        np.testing.assert_array_equal(_q2_apply(lib, op, b_out, b_in, vec, n_ele, d, site), ref)
+
+
 def test_exact_v_m_q2_sign_vs_oracle(gpu, oracle):
     """Q2 with the Jordan-Wigner sign, between two different (N_e, 2Sz) sectors."""
     lib = gpu.load()
