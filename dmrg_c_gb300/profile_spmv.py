@@ -11,6 +11,7 @@
     python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
     python -m dmrg_c_gb300.profile_spmv --obc klm_m128       # matrix-free OBC vs explicit Lanczos
     python -m dmrg_c_gb300.profile_spmv --vm                 # EXACT_V_M_Q0 on the Hubbard L=12 basis
+    python -m dmrg_c_gb300.profile_spmv --solvers klm_m128   # CG / MINRES / mixed solve times
     python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
 
 Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
@@ -211,6 +212,25 @@ def vm(repeats=10):
               f"({3 * n * 8 / t / 1e9:.1f} GB/s of host<->device vectors+basis)", flush=True)
 
 
+def solvers(name, repeats=5):
+    """Whole ground-state solves on one device-resident matrix with the solver forms side by side:
+    Lanczos + inverse iteration with CG or with MINRES inner solves (FP64), and the two
+    mixed-precision forms; ms per solve (device resident, library timers), steps and energy."""
+    import numpy as np
+    m = _matrix(name, L.DG_VALUES_BOTH)
+    guess = np.random.default_rng(3).standard_normal(m.n)
+    forms = (("FP64, II with CG", dict()), ("FP64, II with MINRES", dict(ii_minres=1)),
+             ("mixed=1", dict(mixed=1)), ("mixed=2", dict(mixed=2)))
+    for label, kw in forms:
+        ms, info = [], None
+        for k in range(repeats + 1):
+            v, info = L.ground_state(m, L.default_params(**kw), guess=guess)
+            if k:
+                ms.append(info.ms_lanczos + info.ms_ii)
+        print(f"{name} {label}: {np.median(ms):.3f} ms per solve (Lanczos {info.lanczos_steps} steps, inner "
+              f"{info.cg_steps} steps, E = {info.eig_val:.15f})", flush=True)
+
+
 BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512")
 
 
@@ -245,8 +265,12 @@ def main(argv=None):
     ap.add_argument("--build", choices=BUILDS, default=None)
     ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
     ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
+    ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES), default=None,
+                    help="solve times of the solver forms on one matrix")
     a = ap.parse_args(argv)
-    if a.vm:
+    if a.solvers:
+        solvers(a.solvers)
+    elif a.vm:
         vm()
     elif a.obc:
         obc_solve(a.obc)
