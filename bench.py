@@ -93,7 +93,9 @@ WORKLOAD_DESC = {
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
+    """nvidia-smi clocks / throttle reasons, sampled every 20 ms from before the warm-up; each
+    line is time-stamped on arrival and summary() keeps the samples of the timed window
+    (window(t0, t1), perf_counter seconds)."""
 
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
@@ -102,12 +104,13 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (arrival time, line)
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -117,7 +120,16 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def wait_first(self, timeout=3.0):
+        """Block until nvidia-smi has produced a line (so that the timed region is covered)."""
+        t_end = time.perf_counter() + timeout
+        while self.proc and not self.lines and time.perf_counter() < t_end:
+            time.sleep(0.005)
+
+    def window(self, t0, t1):
+        self.t0, self.t1 = t0, t1
 
     def __exit__(self, *a):
         if self.proc:
@@ -130,7 +142,12 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.t0 is not None:
+            inside = [x for x in lines if self.t0 <= x[0] <= self.t1 + 0.02]
+            # a window shorter than the sampling interval: the nearest sample stands in
+            lines = inside or sorted(lines, key=lambda x: abs(x[0] - 0.5 * (self.t0 + self.t1)))[:1]
+        for _, ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -144,7 +161,8 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm),
+                "interval_ms": 20}
 
 
 def peaks():
@@ -229,20 +247,23 @@ def run_gb300(args, ws, rank, local_rank):
             raise RuntimeError("Lanczos did not converge")
         return info
 
-    for _ in range(args.warmup):
-        one_solve()
-    replica_barrier(ws)
-    torch.cuda.synchronize()
-    launches0 = L.kernel_launches()
-    dev_ms, infos = [], []
     with ClockSampler(local_rank) as clk:
+        for _ in range(args.warmup):
+            one_solve()
+        clk.wait_first()
+        replica_barrier(ws)
+        torch.cuda.synchronize()
+        launches0 = L.kernel_launches()
+        dev_ms, infos = [], []
         t0 = time.perf_counter()
         for _ in range(args.steps):
             info = one_solve()
             infos.append(info)
             dev_ms.append(info.ms_lanczos + info.ms_ii)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        wall = t1 - t0
+        clk.window(t0, t1)
     launches = L.kernel_launches() - launches0
     replica_barrier(ws)
     total_ms = replica_time(float(sum(dev_ms)), ws)

@@ -1,6 +1,6 @@
 """bench.py's multi-process path (replicas only: no data-path collective) with two gloo
 ranks on the CPU: the job's time is the slowest replica's, its rate sums the replicas, and
-the reference arm runs on rank 0 only."""
+the reference arm runs on rank 0 only; and the clock record's timed-window filtering."""
 import os
 import socket
 import sys
@@ -56,3 +56,23 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
         steps = 1
         warmup = 0
     assert bench.run_reference(A(), 2, 1) is None
+
+
+def test_clock_summary_keeps_the_timed_window():
+    """Only nvidia-smi samples that arrived inside the timed region count; a window shorter than
+    the sampling interval falls back to the nearest sample."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    clk = bench.ClockSampler()
+    line = "{sm}, 2070, 900.0, 0x0, Not Active, Not Active, {therm}, Not Active"
+    clk.lines = [(0.00, line.format(sm=1500, therm="Active")),      # before the window (warm-up)
+                 (1.00, line.format(sm=2070, therm="Not Active")),
+                 (1.02, line.format(sm=2050, therm="Not Active")),
+                 (1.04, line.format(sm=2070, therm="Not Active")),
+                 (3.00, line.format(sm=1400, therm="Active"))]     # after it
+    clk.window(0.99, 1.05)
+    s = clk.summary()
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070 and s["reasons"] == []
+    clk.window(2.98, 2.985)
+    s = clk.summary()
+    assert s["samples"] == 1 and s["sm_mhz"] == 1400 and s["reasons"] == ["sw_thermal_slowdown"]
