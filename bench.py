@@ -16,7 +16,8 @@ DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: Lanczos (acc 1e-14, Normal) then invers
 * ``e2e``: solves/s through the drop-in C entry point DMRG_DIAGONALIZE_SUPERBLOCK_SYM from
   host arrays (upload, device expansion, solve, eigenvector download inside the timing).
 * ``roofline``: the fused SpMV kernel (product + <x,y> epilogue), CUDA-event timed with L2
-  flushed before each launch; algorithmic bytes nnz_full*12 + (n+1)*4 + 2*n*8.
+  flushed before each launch (256 MiB rewritten, then another 256 MiB read, so the rewrite's dirty
+  lines are written back before the timed launch); algorithmic bytes nnz_full*12 + (n+1)*4 + 2*n*8.
 * ``cpu_baseline``: the oracle's OpenMP restatement of the same solve on all host cores.
 * ``roofline_hbm_case``: the HBM-bound product (Hubbard m=512 superblock, 0.69 GB), FP64 with the
   autotuned shape and the mixed-precision product, L2 flushed before every launch.
@@ -217,6 +218,7 @@ def hbm_case_roofline(peak, peak_kind):
     a64, a32 = B64 / (t64 * 1e-3) / 1e9, B32 / (t32 * 1e-3) / 1e9
     out = {"workload": "hubbard_m512 superblock SpMV", "n": m.n, "nnz_full": m.nnz, "bound": "hbm", "unit": "GB/s",
            "peak": peak, "peak_source": peak_kind,
+           "l2": "flushed before every launch: 256 MiB rewritten, then another 256 MiB read",
            "fp64": {"kernel": f"k_apply_sell<double> (autotuned: WS={tune.shape} variant={tune.variant} window={tune.window})",
                     "ms_per_launch": t64, "bytes_per_launch": B64, "achieved": a64, "frac": a64 / peak,
                     "traffic": traffic_from_profile("hubbard_m512"), "heuristic_ms_per_launch": t_heur},

@@ -608,9 +608,26 @@ int dg_spmv_mixed(dg_matrix *m, const float *x, double *y) {
 
 }  // extern "C"
 
+namespace dg {
+// Reads n words (the result is never true for the data it is given: the store only keeps the
+// compiler from dropping the loads).
+__global__ void k_touch(const uint4 *__restrict__ p, size_t n, unsigned *sink) {
+  unsigned acc = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint4 v = __ldcg(p + i);
+    acc ^= v.x ^ v.y ^ v.z ^ v.w;
+  }
+  if (acc == 0x9E3779B9u && sink) *sink = acc;
+}
+}  // namespace dg
+
 namespace {
 // Average CUDA-event time of one fused product launch (x FP64: FP64 values; x FP32: the
-// mixed-precision product), optionally rewriting flush_bytes of memory before each launch.
+// mixed-precision product).  With flush_bytes > 0 the L2 is flushed before each launch: a
+// buffer of flush_bytes is rewritten, then a second one of the same size is read, so that the
+// rewrite's dirty lines are written back before the timed launch and it finds the L2 holding
+// clean lines of unrelated data (as a profiler's cache flush leaves it), not the write-back of
+// the flush itself.
 template <class XT>
 void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch) {
   require_device();
@@ -620,14 +637,23 @@ void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size
   DevBuf<double> partials(std::max(m->grid, m->sell_grid)), out(1);
   DevBuf<unsigned> ticket(1);
   DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
+  flush_bytes = (flush_bytes + 15) / 16 * 16;
   DevBuf<unsigned char> flush;
-  if (flush_bytes) flush.alloc(flush_bytes);
+  DevBuf<unsigned> sink(1);
+  if (flush_bytes) {
+    flush.alloc(2 * flush_bytes);
+    DG_CUDA(cudaMemsetAsync(flush.get() + flush_bytes, 0, flush_bytes, st));
+  }
   cudaEvent_t e0, e1;
   DG_CUDA(cudaEventCreate(&e0));
   DG_CUDA(cudaEventCreate(&e1));
   double total = 0.0;
   for (int it = -1; it < iters; ++it) {   // it = -1: untimed launch (module load, first-touch costs)
-    if (flush_bytes) DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
+    if (flush_bytes) {
+      DG_CUDA(cudaMemsetAsync(flush.get(), it & 0xff, flush_bytes, st));
+      k_touch<<<vector_grid((long)(flush_bytes / 16)), kThreads, 0, st>>>(
+          reinterpret_cast<const uint4 *>(flush.get() + flush_bytes), flush_bytes / 16, sink.get()); ::dg::count_launch();
+    }
     DG_CUDA(cudaEventRecord(e0, st));
     const EpiDot<double> epi{y_dev, out.get()};
     const RedSlot slot{partials.get(), ticket.get()};

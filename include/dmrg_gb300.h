@@ -179,8 +179,10 @@ int dg_spmv_f32(dg_matrix *m, const float *x, float *y);
 int dg_spmv_mixed(dg_matrix *m, const float *x, double *y);
 /* Average device time of the Lanczos/CG form of the product (y = M x plus the fused
  * <x, y> reduction) over iters launches after one untimed launch, each timed with CUDA events
- * on the library's stream; with flush_bytes > 0 a buffer of that size is rewritten before every launch so
- * that the matrix is read from HBM, not L2.  x_dev / y_dev must be device pointers. */
+ * on the library's stream; with flush_bytes > 0 the L2 is flushed before every launch so that the
+ * matrix is read from HBM (a buffer of flush_bytes is rewritten, then a second one of the same size
+ * is read, so the rewrite's dirty lines are written back outside the timed launch).  x_dev / y_dev
+ * must be device pointers. */
 int dg_profile_spmv(dg_matrix *m, const double *x_dev, double *y_dev, int iters, size_t flush_bytes, float *ms_per_launch);
 /* The same for the mixed-precision product (FP32 values and x_dev, FP64 y_dev). */
 int dg_profile_spmv_mixed(dg_matrix *m, const float *x_dev, double *y_dev, int iters, size_t flush_bytes,
