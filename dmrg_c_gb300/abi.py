@@ -197,6 +197,14 @@ class dg_sb_model(C.Structure):
                 ("n_terms", C.c_int), ("terms", C.POINTER(dg_sb_term)), ("ele", C.POINTER(C.c_int) * 4)]
 
 
+class dg_sb_basis_spec(C.Structure):
+    """include/dmrg_gb300_sb.h: dg_sb_basis_spec"""
+    _fields_ = [("dim_LL", C.c_int), ("dim_RR", C.c_int), ("dim_onsite", C.c_int), ("n_qn", C.c_int),
+                ("qn1_LL", C.POINTER(C.c_int)), ("qn1_RR", C.POINTER(C.c_int)), ("qn1_site", C.POINTER(C.c_int)),
+                ("qn2_LL", C.POINTER(C.c_int)), ("qn2_RR", C.POINTER(C.c_int)), ("qn2_site", C.POINTER(C.c_int)),
+                ("target1", C.c_int), ("target2", C.c_int)]
+
+
 class dg_engine_config(C.Structure):
     """include/dmrg_gb300_ed.h: dg_engine_config"""
     _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t)]

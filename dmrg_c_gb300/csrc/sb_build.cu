@@ -21,6 +21,7 @@
 
 #include "dmrg_gb300_sb.h"
 #include "matrix.cuh"
+#include "sb_basis.cuh"
 #include "scan.cuh"
 
 namespace dg {
@@ -210,16 +211,22 @@ struct dg_sb {
 namespace dg {
 namespace {
 
-dg_sb *sb_build(const dg_sb_model *m) {
+// bv: the states and Inv table already on the device (a dg_sb_basis); null: the model's host arrays.
+dg_sb *sb_build(const dg_sb_model *m, const SbBasisView *bv) {
   DG_REQUIRE(m, DG_ERR_ARG, "null model");
-  DG_REQUIRE(m->n > 0 && m->dim_LL > 0 && m->dim_RR > 0 && m->dim_onsite > 0, DG_ERR_ARG, "dimensions must be positive");
-  DG_REQUIRE(m->LL && m->LR && m->RR && m->RL && m->inv, DG_ERR_ARG, "null basis arrays");
+  const int n = bv ? bv->n : m->n, d = m->dim_onsite;
+  DG_REQUIRE(n > 0 && m->dim_LL > 0 && m->dim_RR > 0 && m->dim_onsite > 0, DG_ERR_ARG, "dimensions must be positive");
+  if (bv)
+    DG_REQUIRE(bv->dim_LL == m->dim_LL && bv->dim_RR == m->dim_RR && bv->d == m->dim_onsite, DG_ERR_ARG,
+               "the model's dimensions (%d, %d, %d) differ from the basis' (%d, %d, %d)", m->dim_LL, m->dim_RR, m->dim_onsite,
+               bv->dim_LL, bv->dim_RR, bv->d);
+  else
+    DG_REQUIRE(m->LL && m->LR && m->RR && m->RL && m->inv, DG_ERR_ARG, "null basis arrays");
   DG_REQUIRE(m->n_ops >= 1 && m->ops && m->n_terms >= 0 && (m->n_terms == 0 || m->terms), DG_ERR_ARG, "null operators/terms");
-  const int n = m->n, d = m->dim_onsite;
   const long dim_whole = (long)m->dim_LL * d * m->dim_RR * d;
   DG_REQUIRE(dim_whole < (1L << 40), DG_ERR_ARG, "Inv_LLLRRRRL too large");
-  // basis states inside their position ranges
-  for (int b = 0; b < n; ++b) {
+  // basis states inside their position ranges (a device basis is in range by construction)
+  for (int b = 0; !bv && b < n; ++b) {
     DG_REQUIRE(m->LL[b] >= 0 && m->LL[b] < m->dim_LL && m->LR[b] >= 0 && m->LR[b] < d && m->RR[b] >= 0 &&
                    m->RR[b] < m->dim_RR && m->RL[b] >= 0 && m->RL[b] < d,
                DG_ERR_ARG, "superblock state %d out of range", b);
@@ -298,17 +305,21 @@ dg_sb *sb_build(const dg_sb_model *m) {
     terms[k] = SbTermDev{t.pos1, t.pos2, t.op1, t.pos2 >= 0 ? t.op2 : 0, t.sign_mask, t.sign_even, t.coef};
   }
   DevBuf<short> sst[4];
-  const short *hst[4] = {m->LL, m->LR, m->RR, m->RL};
-  for (int p = 0; p < 4; ++p) {
-    sst[p].alloc(n);
-    DG_CUDA(cudaMemcpyAsync(sst[p].get(), hst[p], sizeof(short) * n, cudaMemcpyHostToDevice, st));
+  DevBuf<int> inv;
+  if (!bv) {
+    const short *hst[4] = {m->LL, m->LR, m->RR, m->RL};
+    for (int p = 0; p < 4; ++p) {
+      sst[p].alloc(n);
+      DG_CUDA(cudaMemcpyAsync(sst[p].get(), hst[p], sizeof(short) * n, cudaMemcpyHostToDevice, st));
+    }
+    inv.alloc(dim_whole);
+    DG_CUDA(cudaMemcpyAsync(inv.get(), m->inv, sizeof(int) * dim_whole, cudaMemcpyHostToDevice, st));
   }
-  DevBuf<int> inv(dim_whole), orb(op_row_base.size()), of(op_first.size()), oc(op_col.size()), err(1);
+  DevBuf<int> orb(op_row_base.size()), of(op_first.size()), oc(op_col.size()), err(1);
   DevBuf<int64_t> orow(op_row.size());
   DevBuf<double> ov(op_val.size());
   DevBuf<SbTermDev> td(std::max<size_t>(terms.size(), 1));
   DevBuf<int> ele[4];
-  DG_CUDA(cudaMemcpyAsync(inv.get(), m->inv, sizeof(int) * dim_whole, cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemcpyAsync(orb.get(), op_row_base.data(), sizeof(int) * op_row_base.size(), cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemcpyAsync(of.get(), op_first.data(), sizeof(int) * op_first.size(), cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemcpyAsync(oc.get(), op_col.data(), sizeof(int) * op_col.size(), cudaMemcpyHostToDevice, st));
@@ -322,7 +333,7 @@ dg_sb *sb_build(const dg_sb_model *m) {
   dev.d = d;
   dev.n_terms = m->n_terms;
   for (int p = 0; p < 4; ++p) {
-    dev.st[p] = sst[p].get();
+    dev.st[p] = bv ? bv->st[p] : sst[p].get();
     dev.ele[p] = nullptr;
     if (m->ele[p]) {
       const int dim = position_dim(m, p);
@@ -331,7 +342,7 @@ dg_sb *sb_build(const dg_sb_model *m) {
       dev.ele[p] = ele[p].get();
     }
   }
-  dev.inv = inv.get();
+  dev.inv = bv ? bv->inv : inv.get();
   dev.terms = td.get();
   dev.op_row = orow.get();
   dev.op_row_base = orb.get();
@@ -389,7 +400,18 @@ int dg_sb_build(const dg_sb_model *model, dg_sb **out) {
     require_device();
     DG_REQUIRE(out, DG_ERR_ARG, "null argument");
     *out = nullptr;
-    *out = sb_build(model);
+    *out = sb_build(model, nullptr);
+  });
+}
+
+int dg_sb_build_with_basis(const dg_sb_model *model, const dg_sb_basis *basis, dg_sb **out) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(out && basis, DG_ERR_ARG, "null argument");
+    *out = nullptr;
+    const SbBasisView bv{basis->n, basis->dim_LL, basis->dim_RR, basis->d,
+                         {basis->st[0].get(), basis->st[1].get(), basis->st[2].get(), basis->st[3].get()}, basis->inv.get()};
+    *out = sb_build(model, &bv);
   });
 }
 

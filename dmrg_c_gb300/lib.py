@@ -113,6 +113,11 @@ SIGNATURES = {
     "dg_sb_download": (C.c_int, [vp, lp, ip, dp]),
     "dg_sb_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
     "dg_sb_free": (None, [vp]),
+    "dg_sb_basis_build": (C.c_int, [P(abi.dg_sb_basis_spec), P(vp)]),
+    "dg_sb_basis_info": (C.c_int, [vp, ip]),
+    "dg_sb_basis_download": (C.c_int, [vp, P(C.c_short), P(C.c_short), P(C.c_short), P(C.c_short), ip]),
+    "dg_sb_basis_free": (None, [vp]),
+    "dg_sb_build_with_basis": (C.c_int, [P(abi.dg_sb_model), vp, P(vp)]),
     "dg_engine_create": (C.c_int, [P(abi.dg_engine_config), P(vp)]),
     "dg_engine_submit_ed": (C.c_int, [vp, P(abi.dg_ed_model), P(dg_solver_params), C.c_long, vp]),
     "dg_engine_poll": (C.c_int, [vp, P(abi.dg_job_result), C.c_int, ip, C.c_int]),
@@ -299,14 +304,61 @@ class EDSystem:
         return DeviceMatrix(None, handle=h)
 
 
+class SuperblockBasis:
+    """Superblock basis built on the device (dg_sb_basis): the states (LL, LR, RR, RL) whose
+    quantum numbers sum to the targets in the reference's order, and Inv_LLLRRRRL.
+
+    qn1 / qn2: per-state quantum numbers of the left block, the right block and a site (qn2 may
+    be None for one conserved quantity; with two, qn1 is the primary key)."""
+
+    def __init__(self, dim_LL, dim_RR, d, qn1_LL, qn1_RR, qn1_site, target1, qn2_LL=None, qn2_RR=None, qn2_site=None,
+                 target2=0):
+        two = qn2_LL is not None
+        arr = lambda a: np.ascontiguousarray(a, np.int32)   # noqa: E731
+        self._keep = [arr(a) for a in (qn1_LL, qn1_RR, qn1_site)] + ([arr(a) for a in (qn2_LL, qn2_RR, qn2_site)] if two else [])
+        k = self._keep
+        ptrs = [abi.ptr(a, C.c_int) for a in k] + ([None] * 3 if not two else [])
+        spec = abi.dg_sb_basis_spec(dim_LL=dim_LL, dim_RR=dim_RR, dim_onsite=d, n_qn=2 if two else 1,
+                                    qn1_LL=ptrs[0], qn1_RR=ptrs[1], qn1_site=ptrs[2], qn2_LL=ptrs[3], qn2_RR=ptrs[4],
+                                    qn2_site=ptrs[5], target1=target1, target2=target2)
+        h = C.c_void_p()
+        check(load().dg_sb_basis_build(C.byref(spec), C.byref(h)))
+        self.h = h
+        n = C.c_int()
+        check(load().dg_sb_basis_info(h, C.byref(n)))
+        self.n, self.dim_LL, self.dim_RR, self.d = n.value, dim_LL, dim_RR, d
+
+    def close(self):
+        if self.h:
+            load().dg_sb_basis_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def download(self):
+        """(LL, LR, RR, RL, inv) as numpy arrays."""
+        st = [np.empty(self.n, np.int16) for _ in range(4)]
+        inv = np.empty(self.dim_LL * self.d * self.dim_RR * self.d, np.int32)
+        check(load().dg_sb_basis_download(self.h, *(abi.ptr(a, C.c_short) for a in st), abi.ptr(inv, C.c_int)))
+        return (*st, inv)
+
+
 class SuperblockCRS:
     """Superblock Hamiltonian (lower triangle, diagonal last) built on the device from a
-    dmrg_c_gb300.sb_models.SBModel term list (dg_sb)."""
+    dmrg_c_gb300.sb_models.SBModel term list (dg_sb); with a SuperblockBasis the states and the
+    Inv table come from the device basis instead of the model's host arrays."""
 
-    def __init__(self, model):
+    def __init__(self, model, basis: "SuperblockBasis | None" = None):
         self.model = model
         h = C.c_void_p()
-        check(load().dg_sb_build(C.byref(model.struct), C.byref(h)))
+        if basis is None:
+            check(load().dg_sb_build(C.byref(model.struct), C.byref(h)))
+        else:
+            check(load().dg_sb_build_with_basis(C.byref(model.struct), basis.h, C.byref(h)))
         self.h = h
         n, nnz = C.c_int(), C.c_long()
         check(load().dg_sb_info(h, C.byref(n), C.byref(nnz)))

@@ -231,16 +231,36 @@ def solvers(name, repeats=5):
               f"{info.cg_steps} steps, E = {info.eig_val:.15f})", flush=True)
 
 
-BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512")
+BUILDS = ("ed_hubbard12", "ed_xxz22", "sb_m512", "sb_basis_m512")
 
 
 def build(which, repeats=3):
-    """Device builds: ED basis + Hamiltonian, or the superblock CRS (wall time per build)."""
+    """Device builds: ED basis + Hamiltonian, the superblock CRS from host basis arrays, or the
+    superblock basis and then the CRS on it (wall time per build)."""
     import time
     from . import ed_models
     if which.startswith("ed_"):
         model = ed_models.hubbard_chain(12, U=4.0, hz=0.2) if which == "ed_hubbard12" else ed_models.xxz_chain(22, Jz=1.3)
         make = lambda: L.EDSystem(model)  # noqa: E731
+    elif which == "sb_basis_m512":
+        # the m=512 superblock basis (227,652 states, 16.8 M-entry Inv table), then its CRS on it
+        qb = workloads._block_labels(512, 31, 31.0, 1.25, 0.9, 0)
+        site = workloads.hubbard_site_labels()
+        model = workloads.hubbard_sb_model_m512(0)
+
+        class _Both:
+            def __init__(self):
+                t0 = time.perf_counter()
+                self.b = L.SuperblockBasis(512, 512, 4, qb, qb, site, 64 * workloads.QN_SCALE)
+                self.t_basis = time.perf_counter() - t0
+                self.s = L.SuperblockCRS(model, basis=self.b)
+                self.n, self.nnz = self.s.n, self.s.nnz
+                print(f"  basis {self.t_basis * 1e3:.2f} ms", flush=True)
+
+            def close(self):
+                self.s.close()
+                self.b.close()
+        make = _Both
     else:
         model = workloads.hubbard_sb_model_m512(0)
         make = lambda: L.SuperblockCRS(model)  # noqa: E731

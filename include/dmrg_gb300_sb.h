@@ -54,6 +54,36 @@ int dg_sb_download(const dg_sb *sb, long *row, int *col, double *val);
 int dg_sb_matrix(const dg_sb *sb, int values, dg_matrix **out);
 void dg_sb_free(dg_sb *sb);
 
+/*
+ * Superblock basis on the device.  Replaces the model drivers' GET_BASIS_SUPERBLOCK
+ * (e.g. main/dmrg/xxz_vf/src/allocations/GET_BASIS_SUPERBLOCK.c:29-86 and
+ * main/dmrg/klm_vf/src/allocations/GET_BASIS_SUPERBLOCK.c) with DMRG_QUICK_SORT_BASIS_Q1 / _Q2
+ * (dmrg/DMRG_QUICK_SORT_BASIS_Q1.c, _Q2.c): the states (LL, LR, RR, RL) whose quantum numbers
+ * sum to the targets, ordered by (qn1 of LL+LR, qn2 of LL+LR, LL, LR, RR, RL), and the dense
+ * Inv_LLLRRRRL table (-1 outside the sector).  With n_qn = 1 only qn1 is used (the Q1 drivers'
+ * Tot_Sz); with n_qn = 2, qn1 is the primary key (the Q2 drivers' Tot_Ele) and qn2 the second
+ * (Tot_Sz).  dim_LL and dim_RR must fit a short, as the reference's basis arrays do.
+ */
+typedef struct {
+   int dim_LL, dim_RR, dim_onsite;
+   int n_qn;                                   /* 1 or 2                                     */
+   const int *qn1_LL, *qn1_RR, *qn1_site;      /* [dim_LL], [dim_RR], [dim_onsite]            */
+   const int *qn2_LL, *qn2_RR, *qn2_site;      /* used when n_qn = 2                          */
+   int target1, target2;
+} dg_sb_basis_spec;
+
+typedef struct dg_sb_basis dg_sb_basis;
+
+/* DG_ERR_ARG for an empty sector or out-of-range dimensions. */
+int dg_sb_basis_build(const dg_sb_basis_spec *spec, dg_sb_basis **out);
+int dg_sb_basis_info(const dg_sb_basis *b, int *n);
+/* Copy the states and the Inv_LLLRRRRL table (dim_LL*d*dim_RR*d entries) to host arrays (any may be NULL). */
+int dg_sb_basis_download(const dg_sb_basis *b, short *LL, short *LR, short *RR, short *RL, int *inv);
+void dg_sb_basis_free(dg_sb_basis *b);
+/* dg_sb_build with the states and Inv table taken from a device basis: model->n, LL, LR, RR, RL and
+ * inv are ignored (may be NULL); dim_LL, dim_RR and dim_onsite must match the basis. */
+int dg_sb_build_with_basis(const dg_sb_model *model, const dg_sb_basis *basis, dg_sb **out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -207,6 +207,47 @@ def ref_sb_build(model, cap=None):
     return row, col[:row[-1]].copy(), val[:row[-1]].copy()
 
 
+def sb_basis(dim_LL, dim_RR, d, qn1, qn2, targets):
+    """Superblock basis restated with numpy (GET_BASIS_SUPERBLOCK + DMRG_QUICK_SORT_BASIS_Q1/Q2):
+    qn1 = (LL, RR, site) quantum-number arrays, qn2 the same or None; states ordered by
+    (qn1 of LL+LR, qn2 of LL+LR, LL, LR, RR, RL).  Returns (LL, LR, RR, RL, inv)."""
+    LL, LR, RR, RL = (x.ravel() for x in np.meshgrid(np.arange(dim_LL), np.arange(d), np.arange(dim_RR), np.arange(d),
+                                                     indexing="ij"))
+    q = [np.asarray(a, np.int64) for a in qn1]
+    keep = q[0][LL] + q[2][LR] + q[1][RR] + q[2][RL] == targets[0]
+    k1 = q[0][LL] + q[2][LR]
+    k2 = np.zeros_like(k1)
+    if qn2 is not None:
+        r = [np.asarray(a, np.int64) for a in qn2]
+        keep &= r[0][LL] + r[2][LR] + r[1][RR] + r[2][RL] == targets[1]
+        k2 = r[0][LL] + r[2][LR]
+    LL, LR, RR, RL, k1, k2 = (x[keep] for x in (LL, LR, RR, RL, k1, k2))
+    order = np.lexsort((RL, RR, LR, LL, k2, k1))   # primary key last
+    LL, LR, RR, RL = (x[order].astype(np.int16) for x in (LL, LR, RR, RL))
+    inv = -np.ones(dim_LL * d * dim_RR * d, np.int32)
+    inv[((LL.astype(np.int64) * d + LR) * dim_RR + RR) * d + RL] = np.arange(len(LL), dtype=np.int32)
+    return LL, LR, RR, RL, inv
+
+
+def ref_sb_basis(dim_LL, dim_RR, d, qn1, qn2, targets):
+    """The same with the reference's own DMRG_QUICK_SORT_BASIS_Q1 / _Q2 ordering (oracle/_ref)."""
+    lib = load_ref()
+    sp, ip_ = P(C.c_short), P(C.c_int)
+    lib.ref_sb_basis.restype = C.c_int
+    lib.ref_sb_basis.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int] + [ip_] * 6 + [C.c_int, C.c_int] + [sp] * 4 + [ip_, C.c_int]
+    arr = lambda a: np.ascontiguousarray(a, np.int32)   # noqa: E731
+    q1 = [arr(a) for a in qn1]
+    q2 = [arr(a) for a in qn2] if qn2 is not None else [None] * 3
+    cap = dim_LL * d * dim_RR * d
+    st = [np.empty(cap, np.int16) for _ in range(4)]
+    inv = np.empty(cap, np.int32)
+    n = lib.ref_sb_basis(dim_LL, dim_RR, d, 2 if qn2 is not None else 1, *(ptr(a, C.c_int) if a is not None else None for a in q1 + q2),
+                         int(targets[0]), int(targets[1]) if qn2 is not None else 0, *(ptr(a, C.c_short) for a in st),
+                         ptr(inv, C.c_int), cap)
+    assert n > 0, n
+    return (*(a[:n].copy() for a in st), inv)
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

@@ -142,3 +142,50 @@ int ref_sb_build(const dg_sb_model *m, long *row, int *col, double *val, long ca
    free(A.Val_LLLRRRRL);
    return rc;
 }
+
+/*
+ * The superblock basis in the reference's order: the states (LL, LR, RR, RL) whose quantum
+ * numbers sum to the targets, collected by the nested loops of GET_BASIS_SUPERBLOCK
+ * (main/dmrg/xxz_vf/src/allocations/GET_BASIS_SUPERBLOCK.c:36-56; the driver's OpenMP critical
+ * section only permutes them) and ordered by the reference's own DMRG_QUICK_SORT_BASIS_Q1
+ * (n_qn = 1, key Tot of LL+LR) or DMRG_QUICK_SORT_BASIS_Q2 (n_qn = 2, keys qn1 then qn2 of
+ * LL+LR, the KLM drivers' Tot_Ele then Tot_Sz).  Fills inv (dim_LL*d*dim_RR*d, -1 outside).
+ * Returns the dimension, or -1 when it would exceed cap.
+ */
+int ref_sb_basis(int dim_LL, int dim_RR, int d, int n_qn, const int *q1_LL, const int *q1_RR, const int *q1_site,
+                 const int *q2_LL, const int *q2_RR, const int *q2_site, int t1, int t2, short *LL, short *LR, short *RR,
+                 short *RL, int *inv, int cap) {
+   short *k1 = malloc(sizeof(short) * (size_t)(cap > 0 ? cap : 1));
+   short *k2 = malloc(sizeof(short) * (size_t)(cap > 0 ? cap : 1));
+   int n = 0;
+   for (int ll = 0; ll < dim_LL; ll++)
+      for (int lr = 0; lr < d; lr++)
+         for (int rr = 0; rr < dim_RR; rr++)
+            for (int rl = 0; rl < d; rl++) {
+               const int s1 = q1_LL[ll] + q1_site[lr] + q1_RR[rr] + q1_site[rl];
+               const int s2 = n_qn == 2 ? q2_LL[ll] + q2_site[lr] + q2_RR[rr] + q2_site[rl] : 0;
+               if (s1 != t1 || (n_qn == 2 && s2 != t2)) continue;
+               if (n >= cap) {
+                  free(k1);
+                  free(k2);
+                  return -1;
+               }
+               LL[n] = (short)ll;
+               LR[n] = (short)lr;
+               RR[n] = (short)rr;
+               RL[n] = (short)rl;
+               k1[n] = (short)(q1_LL[ll] + q1_site[lr]);
+               k2[n] = (short)(n_qn == 2 ? q2_LL[ll] + q2_site[lr] : 0);
+               n++;
+            }
+   if (n_qn == 2)
+      DMRG_QUICK_SORT_BASIS_Q2(RL, RR, LR, LL, k2, k1, 0, n);
+   else
+      DMRG_QUICK_SORT_BASIS_Q1(RL, RR, LR, LL, k1, 0, n);
+   const long whole = (long)dim_LL * d * dim_RR * d;
+   for (long i = 0; i < whole; i++) inv[i] = -1;
+   for (int b = 0; b < n; b++) inv[(long)LL[b] * d * dim_RR * d + (long)LR[b] * dim_RR * d + RR[b] * d + RL[b]] = b;
+   free(k1);
+   free(k2);
+   return n;
+}

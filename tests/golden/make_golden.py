@@ -129,6 +129,30 @@ def sb_fixture():
     np.savez_compressed(HERE / "sb_hubbard.npz", **out)
 
 
+def sb_basis_fixture():
+    """Superblock bases in the reference's order (states collected as GET_BASIS_SUPERBLOCK does,
+    sorted by the reference's DMRG_QUICK_SORT_BASIS_Q1 / _Q2): a spin-1/2 case with one
+    conserved quantity (2Sz) and a Hubbard-type case with two (N_e first, then 2Sz)."""
+    rng = np.random.default_rng(11)
+    out = {}
+    # Q1: spin-1/2 sites (2Sz = +1 / -1), blocks of 40 / 36 states with 2Sz labels of 9 / 8 sites
+    q1 = (rng.choice(np.arange(-9, 10, 2), 40), rng.choice(np.arange(-8, 9, 2), 36), np.array([1, -1]))
+    LL, LR, RR, RL, inv = po.ref_sb_basis(40, 36, 2, q1, None, (1, 0))
+    out.update(q1_LL=q1[0], q1_RR=q1[1], q1_site=q1[2], q1_target=np.int32(1), q1_states=np.stack([LL, LR, RR, RL]),
+               q1_inv=inv)
+    # Q2: Hubbard sites (empty, up, down, double) as (N_e, 2Sz); blocks of 48 / 44 states
+    ne_s, sz_s = np.array([0, 1, 1, 2]), np.array([0, 1, -1, 0])
+    def block(dim):
+        ne = rng.integers(2, 9, dim)
+        sz = np.array([rng.choice(np.arange(-min(k, 8 - k), min(k, 8 - k) + 1, 2)) for k in ne])
+        return ne, sz
+    (nl, sl), (nr, sr) = block(48), block(44)
+    LL, LR, RR, RL, inv = po.ref_sb_basis(48, 44, 4, (nl, nr, ne_s), (sl, sr, sz_s), (12, 0))
+    out.update(q2_ne_LL=nl, q2_ne_RR=nr, q2_ne_site=ne_s, q2_sz_LL=sl, q2_sz_RR=sr, q2_sz_site=sz_s,
+               q2_targets=np.array([12, 0], np.int32), q2_states=np.stack([LL, LR, RR, RL]), q2_inv=inv)
+    np.savez_compressed(HERE / "sb_basis.npz", **out)
+
+
 def vm_fixture():
     """EXACT_V_M_Q0 on a Hubbard basis with the reference's C^dagger_up site operator."""
     model = ed_models.hubbard_chain(6, t=-1.0, U=2.0, n_ele=6, twoSz=0)
@@ -181,6 +205,7 @@ def main():
     tridiag_fixture()
     klm_ed_fixture()
     sb_fixture()
+    sb_basis_fixture()
     vm_fixture()
     obc_fixture()
     xxz_energy_fixture()

@@ -201,3 +201,17 @@ def test_live_reference_superblock_build(ref):
     b = ref.ref_sb_build(m)
     assert all(np.array_equal(x.view(np.int64) if x.dtype == np.float64 else x,
                               y.view(np.int64) if y.dtype == np.float64 else y) for x, y in zip(a, b))
+
+
+@pytest.mark.parametrize("case", ["q1", "q2"])
+def test_superblock_basis_matches_reference_golden(oracle, case):
+    """The numpy restatement of GET_BASIS_SUPERBLOCK orders the states exactly as the reference's
+    DMRG_QUICK_SORT_BASIS_Q1 / _Q2 do (fixture made by the reference's own sort)."""
+    g = golden("sb_basis.npz")
+    if case == "q1":
+        a = oracle.sb_basis(40, 36, 2, (g["q1_LL"], g["q1_RR"], g["q1_site"]), None, (int(g["q1_target"]), 0))
+    else:
+        a = oracle.sb_basis(48, 44, 4, (g["q2_ne_LL"], g["q2_ne_RR"], g["q2_ne_site"]),
+                            (g["q2_sz_LL"], g["q2_sz_RR"], g["q2_sz_site"]), tuple(int(t) for t in g["q2_targets"]))
+    assert np.array_equal(np.stack(a[:4]), g[f"{case}_states"])
+    assert np.array_equal(a[4], g[f"{case}_inv"])
