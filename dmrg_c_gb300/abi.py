@@ -74,6 +74,69 @@ class DMRG_BASIS(C.Structure):
                 ("Tot_Parity_LLLR", c_int_p)]
 
 
+def _whole_basis_type(depth: int, lines: str):
+    sp = c_short_p
+    ip = c_int_p
+    for _ in range(depth):
+        sp = C.POINTER(sp)
+    for _ in range(depth - 1):
+        ip = C.POINTER(ip)
+    return type(f"DMRG_WHOLE_BASIS_Q{depth}", (C.Structure,), {
+        "__doc__": lines,
+        "_fields_": [("LL_LLLRRRRL", sp), ("LR_LLLRRRRL", sp), ("RL_LLLRRRRL", sp), ("RR_LLLRRRRL", sp),
+                     ("Inv_LLLRRRRL", c_int_p), ("Dim", ip), ("max_dim", C.c_int), ("dim_RR", C.c_int),
+                     ("dim_onsite", C.c_int)]})
+
+
+DMRG_WHOLE_BASIS_Q1 = _whole_basis_type(1, "include/dmrg.h:140-152")
+DMRG_WHOLE_BASIS_Q2 = _whole_basis_type(2, "include/dmrg.h:155-167")
+DMRG_WHOLE_BASIS_Q3 = _whole_basis_type(3, "include/dmrg.h:169-181")
+DMRG_WHOLE_BASIS_Q4 = _whole_basis_type(4, "include/dmrg.h:183-195")
+WHOLE_BASIS = {1: DMRG_WHOLE_BASIS_Q1, 2: DMRG_WHOLE_BASIS_Q2, 3: DMRG_WHOLE_BASIS_Q3, 4: DMRG_WHOLE_BASIS_Q4}
+
+
+class WholeBasis:
+    """A DMRG_WHOLE_BASIS_Qk over numpy arrays.  ``sectors`` maps a k-tuple of non-negative
+    quantum-number indices to the sector's (LL, LR, RR, RL) state arrays; ``shape`` gives the
+    extent of each index (absent sectors have dimension 0); ``inv`` is the shared Inv_LLLRRRRL
+    table.  ``.struct`` / ``.ref`` view it; the arrays are kept alive by this object."""
+
+    def __init__(self, sectors: dict, shape: tuple, inv, dim_RR: int, dim_onsite: int):
+        k = len(shape)
+        self.keep = []
+        self.inv = np.ascontiguousarray(inv, np.int32)
+        dummy = np.zeros(1, np.int16)
+        self.keep.append(dummy)
+
+        def build(prefix, leaf, leaf_type):
+            # value of type leaf_type at depth k, POINTER(type at depth + 1) above it
+            depth = len(prefix)
+            if depth == k:
+                return leaf(prefix)
+            elem_t = leaf_type
+            for _ in range(k - depth - 1):
+                elem_t = C.POINTER(elem_t)
+            arr = (elem_t * shape[depth])(*[build(prefix + (i,), leaf, leaf_type) for i in range(shape[depth])])
+            self.keep.append(arr)
+            return C.cast(arr, C.POINTER(elem_t))
+
+        def states(idx):
+            def leaf(prefix):
+                st = sectors.get(prefix)
+                a = np.ascontiguousarray(st[idx], np.int16) if st is not None and len(st[0]) else dummy
+                self.keep.append(a)
+                return a.ctypes.data_as(c_short_p)
+            return build((), leaf, c_short_p)
+
+        dim = build((), lambda prefix: len(sectors[prefix][0]) if prefix in sectors else 0, C.c_int)
+        dims = [len(v[0]) for v in sectors.values()]
+        T = WHOLE_BASIS[k]
+        self.struct = T(LL_LLLRRRRL=states(0), LR_LLLRRRRL=states(1), RR_LLLRRRRL=states(2), RL_LLLRRRRL=states(3),
+                        Inv_LLLRRRRL=self.inv.ctypes.data_as(c_int_p), Dim=dim, max_dim=max(dims) if dims else 0,
+                        dim_RR=dim_RR, dim_onsite=dim_onsite)
+        self.ref = C.pointer(self.struct)
+
+
 class DMRG_STATUS(C.Structure):
     """include/dmrg.h:236-267"""
     _fields_ = [("BC", C.c_char * 1000), ("Enviro_Copy", C.c_char * 100), ("LL_site", C.c_int), ("RR_site", C.c_int),
@@ -195,6 +258,11 @@ class dg_sb_model(C.Structure):
                 ("LL", C.POINTER(C.c_short)), ("LR", C.POINTER(C.c_short)), ("RR", C.POINTER(C.c_short)),
                 ("RL", C.POINTER(C.c_short)), ("inv", C.POINTER(C.c_int)), ("n_ops", C.c_int), ("ops", C.POINTER(CRS1)),
                 ("n_terms", C.c_int), ("terms", C.POINTER(dg_sb_term)), ("ele", C.POINTER(C.c_int) * 4)]
+
+
+class dg_sb_expect_term(C.Structure):
+    """include/dmrg_gb300_sb.h"""
+    _fields_ = [("pos", C.c_int), ("op", C.c_int), ("sign", C.c_int), ("weight", C.c_int)]
 
 
 class dg_sb_basis_spec(C.Structure):

@@ -116,6 +116,7 @@ dg_sb_basis *sb_basis_build(const dg_sb_basis_spec *s) {
     b->d = d;
     for (auto &a : b->st) a.alloc(n);
     b->inv.alloc(dim_whole);
+    b->inv_len = (long)dim_whole;
     DG_CUDA(cudaMemsetAsync(b->inv.get(), 0xff, sizeof(int) * dim_whole, st));   // -1
     const int npairs = (int)pll.size();
     const long blocks = std::max(1L, std::min<long>(((long)npairs * 32 + kThreads - 1) / kThreads, (long)sm_count() * 16));
@@ -161,9 +162,8 @@ int dg_sb_basis_download(const dg_sb_basis *b, short *LL, short *LR, short *RR, 
     short *dst[4] = {LL, LR, RR, RL};
     for (int p = 0; p < 4; ++p)
       if (dst[p]) DG_CUDA(cudaMemcpyAsync(dst[p], b->st[p].get(), sizeof(short) * b->n, cudaMemcpyDeviceToHost, st));
-    if (inv)
-      DG_CUDA(cudaMemcpyAsync(inv, b->inv.get(), sizeof(int) * (size_t)b->dim_LL * b->d * b->dim_RR * b->d, cudaMemcpyDeviceToHost,
-                              st));
+    if (inv && b->inv_len > 0)
+      DG_CUDA(cudaMemcpyAsync(inv, b->inv.get(), sizeof(int) * (size_t)b->inv_len, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
   });
 }

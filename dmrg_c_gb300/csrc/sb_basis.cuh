@@ -9,6 +9,7 @@ struct dg_sb_basis {
   int n = 0, dim_LL = 0, dim_RR = 0, d = 0;
   dg::DevBuf<short> st[4];   // LL, LR, RR, RL of every state (DG_SB_* order)
   dg::DevBuf<int> inv;       // Inv_LLLRRRRL: dim_LL * d * dim_RR * d entries, -1 outside the sector
+  long inv_len = 0;          // entries of inv (0: the basis carries states only)
 };
 
 namespace dg {

@@ -409,6 +409,8 @@ int dg_sb_build_with_basis(const dg_sb_model *model, const dg_sb_basis *basis, d
     require_device();
     DG_REQUIRE(out && basis, DG_ERR_ARG, "null argument");
     *out = nullptr;
+    DG_REQUIRE(basis->inv_len == (long)basis->dim_LL * basis->d * basis->dim_RR * basis->d, DG_ERR_ARG,
+               "the basis carries no full Inv_LLLRRRRL table");
     const SbBasisView bv{basis->n, basis->dim_LL, basis->dim_RR, basis->d,
                          {basis->st[0].get(), basis->st[1].get(), basis->st[2].get(), basis->st[3].get()}, basis->inv.get()};
     *out = sb_build(model, &bv);

@@ -58,6 +58,27 @@ SIGNATURES = {
     "DMRG_DIAGONALIZE_SUPERBLOCK_SYM": (None, [P(CRS1), P(DMRG_TIME), P(DMRG_PARAMETER), P(DMRG_STATUS), C.c_int]),
     "DMRG_MATRIX_VECTOR_PRODUCT_OBC": (None, [P(CRS1), P(CRS1), P(CRS1), P(CRS1), dp, dp, ip, C.c_int, P(DMRG_BASIS)]),
     "DMRG_LANCZOS_SLOW_OBC": (None, [P(DMRG_BOX_LAN)]),
+    "DMRG_V_M_LL_Q0": (None, [P(CRS1), dp, dp, C.c_int, C.c_int, P(DMRG_BASIS)]),
+    "DMRG_V_M_LR_Q0": (None, [P(CRS1), dp, dp, C.c_int, C.c_int, P(DMRG_BASIS)]),
+    "DMRG_V_M_RR_Q0": (None, [P(CRS1), dp, dp, C.c_int, C.c_int, P(DMRG_BASIS)]),
+    "DMRG_V_M_RL_Q0": (None, [P(CRS1), dp, dp, C.c_int, C.c_int, P(DMRG_BASIS)]),
+    "DMRG_V_M_LL_Q1": (None, [P(CRS1), C.c_int, dp, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q1)]),
+    "DMRG_V_M_LR_Q1": (None, [P(CRS1), C.c_int, dp, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q1)]),
+    "DMRG_V_M_RR_Q1": (None, [P(CRS1), C.c_int, dp, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q1)]),
+    "DMRG_V_M_RL_Q1": (None, [P(CRS1), C.c_int, dp, ip, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q1)]),
+    "DMRG_V_M_LL_Q2": (None, [P(CRS1), C.c_int, C.c_int, dp, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q2)]),
+    "DMRG_V_M_LR_Q2": (None, [P(CRS1), C.c_int, C.c_int, dp, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q2)]),
+    "DMRG_V_M_RR_Q2": (None, [P(CRS1), C.c_int, C.c_int, dp, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q2)]),
+    "DMRG_V_M_RL_Q2": (None, [P(CRS1), C.c_int, C.c_int, dp, ip, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q2)]),
+    "DMRG_V_M_LL_Q3": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, dp, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q3)]),
+    "DMRG_V_M_LR_Q3": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, dp, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q3)]),
+    "DMRG_V_M_RR_Q3": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, dp, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q3)]),
+    "DMRG_V_M_RL_Q3": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, dp, ip, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q3)]),
+    "DMRG_V_M_RR_Q4": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, C.c_int, dp, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q4)]),
+    "DMRG_V_M_RL_Q4": (None, [P(CRS1), C.c_int, C.c_int, C.c_int, C.c_int, dp, ip, ip, ip, C.c_char_p, dp, C.c_int, P(abi.DMRG_WHOLE_BASIS_Q4)]),
+    "DMRG_EXPECTATION_ONSITE": (None, [P(P(CRS1)), P(CRS1), P(P(CRS1)), dp, dp, dp, C.c_int, P(DMRG_BASIS), P(DMRG_STATUS)]),
+    "DMRG_EXPECTATION_INTERSITE_Q0": (None, [P(P(CRS1)), P(P(CRS1)), P(CRS1), P(P(CRS1)), dp, C.c_int, dp, dp, dp, C.c_int,
+                                              P(DMRG_BASIS), P(DMRG_STATUS)]),
     "DMRG_CONJUGATE_GRADIENT_OBC": (None, [P(DMRG_BOX_CG)]),
     "DMRG_INVERSE_ITERATION_OBC": (None, [P(DMRG_BOX_II)]),
     "DMRG_CONVERGE_CHECK_OBC": (C.c_double, [C.c_double, P(CRS1), P(CRS1), P(CRS1), P(CRS1), dp, dp, ip, C.c_int,
@@ -108,6 +129,12 @@ SIGNATURES = {
     "dg_ed_info": (C.c_int, [vp, lp, lp]),
     "dg_ed_download": (C.c_int, [vp, lp, lp, ip, dp]),
     "dg_ed_matrix": (C.c_int, [vp, C.c_int, P(vp)]),
+    "dg_sb_basis_upload": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_short), P(C.c_short), P(C.c_short),
+                                     P(C.c_short), ip, P(vp)]),
+    "dg_sb_ops_create": (C.c_int, [C.c_int, P(P(CRS1)), ip, P(vp)]),
+    "dg_sb_ops_free": (None, [vp]),
+    "dg_sb_vm": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, ip, ip, ip, vp, C.c_long, vp]),
+    "dg_sb_expect": (C.c_int, [vp, vp, vp, C.c_int, P(abi.dg_sb_expect_term), ip, ip, ip, vp, C.c_long, vp, vp, dp]),
     "dg_sb_build": (C.c_int, [P(abi.dg_sb_model), P(vp)]),
     "dg_sb_info": (C.c_int, [vp, ip, lp]),
     "dg_sb_download": (C.c_int, [vp, lp, ip, dp]),
@@ -345,6 +372,85 @@ class SuperblockBasis:
         inv = np.empty(self.dim_LL * self.d * self.dim_RR * self.d, np.int32)
         check(load().dg_sb_basis_download(self.h, *(abi.ptr(a, C.c_short) for a in st), abi.ptr(inv, C.c_int)))
         return (*st, inv)
+
+
+def superblock_states(states, dim_LL, dim_RR, d, inv=None) -> "SuperblockBasis":
+    """A SuperblockBasis from host arrays (dg_sb_basis_upload): one sector's (LL, LR, RR, RL) and,
+    optionally, an Inv_LLLRRRRL table (a whole basis's table may index other sectors)."""
+    st = [np.ascontiguousarray(a, np.int16) for a in states]
+    inv_a = np.ascontiguousarray(inv, np.int32) if inv is not None else None
+    h = C.c_void_p()
+    check(load().dg_sb_basis_upload(len(st[0]), dim_LL, dim_RR, d, *(abi.ptr(a, C.c_short) for a in st),
+                                    abi.ptr(inv_a, C.c_int) if inv_a is not None else None, C.byref(h)))
+    b = SuperblockBasis.__new__(SuperblockBasis)
+    b.h, b.n, b.dim_LL, b.dim_RR, b.d = h, len(st[0]), dim_LL, dim_RR, d
+    return b
+
+
+class BlockOperators:
+    """Device copies of square block operators (dg_sb_ops): ops[k] (abi.Crs) acts on a position
+    with rows[k] states."""
+
+    def __init__(self, ops, rows):
+        self._ops = list(ops)
+        arr = (P(CRS1) * len(self._ops))(*[o.ref for o in self._ops])
+        r = np.ascontiguousarray(rows, np.int32)
+        h = C.c_void_p()
+        check(load().dg_sb_ops_create(len(self._ops), arr, abi.ptr(r, C.c_int), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load().dg_sb_ops_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _eles(ele):
+    if ele is None:
+        return [None, None, None], []
+    keep = [np.ascontiguousarray(a, np.int32) if a is not None else None for a in ele]
+    return [abi.ptr(a, C.c_int) if a is not None else None for a in keep], keep
+
+
+def _vec_ptr(x):
+    """(pointer, length, keep-alive) for a numpy array or a CUDA torch tensor."""
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr()), int(x.numel()), x
+    a = np.ascontiguousarray(x, np.float64)
+    return C.c_void_p(a.ctypes.data), len(a), a
+
+
+def sb_vm(out_states: "SuperblockBasis", inv_table: "SuperblockBasis", ops: BlockOperators, op: int, pos: int, v, out=None,
+          sign=False, ele=None):
+    """O_op v over out_states' states (dg_sb_vm): DMRG_V_M_<pos> on device-resident data.
+    v / out may be numpy arrays or CUDA tensors; returns out."""
+    if out is None:
+        out = np.empty(out_states.n)
+    pv, nv, kv = _vec_ptr(v)
+    po_, _, ko = _vec_ptr(out)
+    ep, ke = _eles(ele)
+    check(load().dg_sb_vm(out_states.h, inv_table.h, ops.h, op, pos, int(sign), *ep, pv, nv, po_))
+    return out
+
+
+def sb_expect(out_states: "SuperblockBasis", inv_table: "SuperblockBasis", ops: BlockOperators, terms, v, w0, w1=None,
+              ele=None):
+    """[sum_i w_t[i] (O_t v)[i] for each term] (dg_sb_expect); terms = (pos, op, sign, weight)."""
+    tt = (abi.dg_sb_expect_term * max(len(terms), 1))(*[abi.dg_sb_expect_term(*t) for t in terms])
+    out = np.empty(len(terms))
+    pv, nv, kv = _vec_ptr(v)
+    p0, _, k0 = _vec_ptr(w0)
+    p1, k1 = (None, None) if w1 is None else _vec_ptr(w1)[::2]
+    ep, ke = _eles(ele)
+    check(load().dg_sb_expect(out_states.h, inv_table.h, ops.h, len(terms), tt, *ep, pv, nv, p0, p1,
+                              out.ctypes.data_as(dp)))
+    return out
 
 
 class SuperblockCRS:

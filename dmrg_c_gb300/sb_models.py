@@ -159,3 +159,119 @@ def small_hubbard_model(pbc=False) -> SBModel:
     sb = superblock.synthetic_superblock(40, 4, qb, workloads.hubbard_site_labels(), 14 * QN_SCALE, nnz_lllr=1, nnz_lrrl=1,
                                          seed=4, with_sign=True)
     return hubbard_superblock_model(sb, qb, seed=5, per_row=3, pbc=pbc)
+
+
+# ---------------------------------------------------------------------------------------
+# Observables: block operators on a superblock whose sectors are all laid out (the inputs of
+# DMRG_V_M_* and DMRG_EXPECTATION_*).
+# ---------------------------------------------------------------------------------------
+def sector_states(q_LL, q_RR, q_site, target):
+    """States (LL, LR, RR, RL) of one sector in the reference's order (GET_BASIS_SUPERBLOCK then
+    DMRG_QUICK_SORT_BASIS: by the label of LL+LR, then LL, LR, RR, RL), labels packed N*QN_SCALE+2Sz."""
+    q_LL, q_RR, q_site = (np.asarray(a, np.int64) for a in (q_LL, q_RR, q_site))
+    d = len(q_site)
+    LL, LR, RR, RL = (x.ravel() for x in np.meshgrid(np.arange(len(q_LL)), np.arange(d), np.arange(len(q_RR)),
+                                                     np.arange(d), indexing="ij"))
+    k1 = q_LL[LL] + q_site[LR]
+    keep = k1 + q_RR[RR] + q_site[RL] == target
+    LL, LR, RR, RL, k1 = (x[keep] for x in (LL, LR, RR, RL, k1))
+    order = np.lexsort((RL, RR, LR, LL, k1))
+    return tuple(x[order].astype(np.int16) for x in (LL, LR, RR, RL))
+
+
+@dataclass
+class ObservableProblem:
+    """Block labels, every sector of the superblock and the block operators of a few sites.
+
+    ``inv`` is the whole Inv_LLLRRRRL table: each state's index inside its own sector (the
+    DMRG_WHOLE_BASIS_Qk layout); ``inv_sector(q)`` is the single-sector table of a DMRG_BASIS.
+    Operators: ``M_LL`` / ``M_RR`` conserve the block labels (site observables carried by the
+    blocks), ``M_CF`` too (correlations inside LL), ``M_On`` is a site observable, and
+    ``Cd_LL`` / ``Cd_On`` / ``Cd_RR`` raise the label by one up electron (c^dagger_up)."""
+    q_LL: np.ndarray
+    q_RR: np.ndarray
+    q_site: np.ndarray
+    ops: dict                      # name -> Crs or list of Crs
+    target: int
+
+    def __post_init__(self):
+        self.d, self.dim_LL, self.dim_RR = len(self.q_site), len(self.q_LL), len(self.q_RR)
+        k = (self.q_LL[:, None, None, None] + self.q_site[None, :, None, None] + self.q_RR[None, None, :, None]
+             + self.q_site[None, None, None, :]).ravel()
+        self.labels = np.unique(k)
+        self.sectors = {int(t): sector_states(self.q_LL, self.q_RR, self.q_site, int(t)) for t in self.labels}
+        self.inv = -np.ones(self.dim_LL * self.d * self.dim_RR * self.d, np.int32)
+        for st in self.sectors.values():
+            self.inv[self.sup(st)] = np.arange(len(st[0]), dtype=np.int32)
+        self.ele = tuple(np.rint(np.asarray(a) / QN_SCALE).astype(np.int32) for a in (self.q_LL, self.q_site, self.q_RR))
+
+    def sup(self, st):
+        d, R = self.d, self.dim_RR
+        return ((st[0].astype(np.int64) * d + st[1]) * R + st[2]) * d + st[3]
+
+    def inv_sector(self, q):
+        out = -np.ones_like(self.inv)
+        st = self.sectors[q]
+        out[self.sup(st)] = np.arange(len(st[0]), dtype=np.int32)
+        return out
+
+    def index(self, q, k):
+        """Non-negative k-tuple naming sector q in a DMRG_WHOLE_BASIS_Qk: (rank of the label) for
+        k = 1, (N - N_min, (2Sz - 2Sz_min) / 2) for k = 2, padded with zeros for k = 3, 4."""
+        if k == 1:
+            return (int(np.searchsorted(self.labels, q)),)
+        N = np.rint(self.labels / QN_SCALE).astype(np.int64)
+        sz = self.labels - N * QN_SCALE
+        n, s = int(round(q / QN_SCALE)), q - int(round(q / QN_SCALE)) * QN_SCALE
+        return (n - int(N.min()), (s - int(sz.min())) // 2) + (0,) * (k - 2)
+
+    def shape(self, k):
+        if k == 1:
+            return (len(self.labels),)
+        idx = [self.index(int(q), 2) for q in self.labels]
+        return (max(i[0] for i in idx) + 1, max(i[1] for i in idx) + 1) + (1,) * (k - 2)
+
+    def whole_basis(self, k):
+        from .abi import WholeBasis
+        return WholeBasis({self.index(q, k): st for q, st in self.sectors.items()}, self.shape(k), self.inv, self.dim_RR,
+                          self.d)
+
+    def arrays(self) -> dict:
+        """Flat arrays (labels, target and every operator's CRS) for a fixture."""
+        out = dict(q_LL=self.q_LL, q_RR=self.q_RR, q_site=self.q_site, target=np.int64(self.target))
+        for name, o in self.ops.items():
+            for i, c in enumerate(o if isinstance(o, list) else [o]):
+                out[f"op_{name}_{i}_row"], out[f"op_{name}_{i}_col"], out[f"op_{name}_{i}_val"] = c.row, c.col[:c.nnz], c.val[:c.nnz]
+        return out
+
+    @classmethod
+    def from_arrays(cls, a) -> "ObservableProblem":
+        ops = {}
+        for key in sorted(k for k in a.keys() if k.startswith("op_") and k.endswith("_row")):
+            _, name, i, _ = key.split("_")
+            c = Crs(a[key], a[f"op_{name}_{i}_col"], a[f"op_{name}_{i}_val"])
+            ops.setdefault(name, {})[int(i)] = c
+        ops = {n: (v[0] if n in ("On", "CdOn") else [v[i] for i in sorted(v)]) for n, v in ops.items()}
+        return cls(np.asarray(a["q_LL"]), np.asarray(a["q_RR"]), np.asarray(a["q_site"]), ops, int(a["target"]))
+
+
+def random_observable_problem(dim_LL=16, dim_RR=14, n_LL=3, n_RR=3, per_row=4, seed=0, n_sites=5) -> ObservableProblem:
+    """Hubbard-type blocks (labels of n_sites sites) with seeded random block operators; the
+    target is the half-filled Sz = 0 sector of 2 n_sites + 2 sites."""
+    rng = np.random.default_rng(seed)
+    from .workloads import _block_labels, hubbard_site_labels
+    qL = _block_labels(dim_LL, n_sites, n_sites, 1.0, 0.9, seed + 1)
+    qR = _block_labels(dim_RR, n_sites, n_sites, 1.0, 0.9, seed + 2)
+    qs = hubbard_site_labels()
+    up = QN_SCALE + 1
+    cupd = np.zeros((4, 4))
+    cupd[0, 1] = 1.0
+    cupd[2, 3] = 1.0
+    ops = dict(LL=[_crs(_random_sym_op(qL, per_row, rng)) for _ in range(n_LL)],
+               RR=[_crs(_random_sym_op(qR, per_row, rng)) for _ in range(n_RR)],
+               CF=[_crs(_random_sym_op(qL, per_row, rng)) for _ in range(n_LL)],
+               On=_crs(sp.csr_matrix(np.diag(rng.standard_normal(4)))),
+               CdLL=[_crs(_random_shift_op(qL, up, per_row, rng))],
+               CdRR=[_crs(_random_shift_op(qR, up, per_row, rng))],
+               CdOn=_crs(sp.csr_matrix(cupd)))
+    return ObservableProblem(qL, qR, qs, ops, (2 * n_sites + 2) * QN_SCALE)

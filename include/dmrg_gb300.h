@@ -85,6 +85,34 @@ void EXACT_V_M_Q1(CRS1 *M_On, int qn_out, double *Vec, int qn_in, double *Out_Ve
 void EXACT_V_M_Q2(CRS1 *M_On, int qn1_out, int qn2_out, double *Vec, int qn1_in, int qn2_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q2 *W_Basis);
 void EXACT_V_M_Q3(CRS1 *M_On, int qn1_out, int qn2_out, int qn3_out, double *Vec, int qn1_in, int qn2_in, int qn3_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q3 *W_Basis);
 
+/* Out = O V for a block operator on the superblock (one position of (LL, LR, RR, RL)); Q0 within
+ * one sector, Q1..Q4 into the sector the quantum numbers name.  Out is bitwise the reference's.
+ *                                                       replace include/dmrg.h:365-382 */
+void DMRG_V_M_LL_Q0(CRS1 *M_LL, double *V, double *Out_V, int dim, int p_threads, DMRG_BASIS *Dmrg_Basis);
+void DMRG_V_M_LR_Q0(CRS1 *M_LR, double *V, double *Out_V, int dim, int p_threads, DMRG_BASIS *Dmrg_Basis);
+void DMRG_V_M_RR_Q0(CRS1 *M_RR, double *V, double *Out_V, int dim, int p_threads, DMRG_BASIS *Dmrg_Basis);
+void DMRG_V_M_RL_Q0(CRS1 *M_RL, double *V, double *Out_V, int dim, int p_threads, DMRG_BASIS *Dmrg_Basis);
+void DMRG_V_M_LL_Q1(CRS1 *M_LL, int qn_out, double *V, double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q1 *Dmrg_W_Basis);
+void DMRG_V_M_LR_Q1(CRS1 *M_LR, int qn_out, double *V, int *Ele_LL, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q1 *Dmrg_W_Basis);
+void DMRG_V_M_RL_Q1(CRS1 *M_RL, int qn_out, double *V, int *Ele_LL, int *Ele_LR, int *Ele_RR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q1 *Dmrg_W_Basis);
+void DMRG_V_M_RR_Q1(CRS1 *M_RR, int qn_out, double *V, int *Ele_LL, int *Ele_LR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q1 *Dmrg_W_Basis);
+void DMRG_V_M_LL_Q2(CRS1 *M_LL, int qn1_out, int qn2_out, double *V, double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q2 *Dmrg_W_Basis);
+void DMRG_V_M_LR_Q2(CRS1 *M_LR, int qn1_out, int qn2_out, double *V, int *Ele_LL, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q2 *Dmrg_W_Basis);
+void DMRG_V_M_RL_Q2(CRS1 *M_RL, int qn1_out, int qn2_out, double *V, int *Ele_LL, int *Ele_LR, int *Ele_RR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q2 *Dmrg_W_Basis);
+void DMRG_V_M_RR_Q2(CRS1 *M_RR, int qn1_out, int qn2_out, double *V, int *Ele_LL, int *Ele_LR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q2 *Dmrg_W_Basis);
+void DMRG_V_M_LL_Q3(CRS1 *M_LL, int qn1_out, int qn2_out, int qn3_out, double *V, double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q3 *Dmrg_W_Basis);
+void DMRG_V_M_LR_Q3(CRS1 *M_LR, int qn1_out, int qn2_out, int qn3_out, double *V, int *Ele_LL, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q3 *Dmrg_W_Basis);
+void DMRG_V_M_RL_Q3(CRS1 *M_RL, int qn1_out, int qn2_out, int qn3_out, double *V, int *Ele_LL, int *Ele_LR, int *Ele_RR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q3 *Dmrg_W_Basis);
+void DMRG_V_M_RR_Q3(CRS1 *M_RR, int qn1_out, int qn2_out, int qn3_out, double *V, int *Ele_LL, int *Ele_LR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q3 *Dmrg_W_Basis);
+void DMRG_V_M_RL_Q4(CRS1 *M_RL, int qn1_out, int qn2_out, int qn3_out, int qn4_out, double *V, int *Ele_LL, int *Ele_LR, int *Ele_RR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q4 *Dmrg_W_Basis);
+void DMRG_V_M_RR_Q4(CRS1 *M_RR, int qn1_out, int qn2_out, int qn3_out, int qn4_out, double *V, int *Ele_LL, int *Ele_LR, char Sign_Flag[], double *Out_V, int p_threads, DMRG_WHOLE_BASIS_Q4 *Dmrg_W_Basis);
+/* <Vec|O_site|Vec> for every site, and <O_origin Vec|O_site Vec> (the LL sites through the
+ * correlation operators M_CF) in one device pass each.  Out within 1e-12 of the reference
+ * (only the order of the final sums differs); Temp_V / Temp_V2 receive the last site's product
+ * and Temp_V1 the origin's, as in the reference.         replace include/dmrg.h:347-348 */
+void DMRG_EXPECTATION_ONSITE(CRS1 **M_LL, CRS1 *M_On, CRS1 **M_RR, double *Out, double *Vec, double *Temp_V, int p_threads, DMRG_BASIS *Dmrg_Basis, DMRG_STATUS *Dmrg_Status);
+void DMRG_EXPECTATION_INTERSITE_Q0(CRS1 **M_CF, CRS1 **M_LL, CRS1 *M_On, CRS1 **M_RR, double *Out, int origin, double *Vec, double *Temp_V1, double *Temp_V2, int p_threads, DMRG_BASIS *Dmrg_Basis, DMRG_STATUS *Dmrg_Status);
+
 /* ------------------------------------------------------------------------------------
  * 2. Native status-returning API
  * ---------------------------------------------------------------------------------- */

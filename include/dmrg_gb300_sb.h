@@ -84,6 +84,52 @@ void dg_sb_basis_free(dg_sb_basis *b);
  * inv are ignored (may be NULL); dim_LL, dim_RR and dim_onsite must match the basis. */
 int dg_sb_build_with_basis(const dg_sb_model *model, const dg_sb_basis *basis, dg_sb **out);
 
+/*
+ * Block operators on superblock vectors and expectation values (DMRG_V_M_{LL,LR,RR,RL}_Q0..Q4,
+ * dmrg/DMRG_V_M_LL_Q0.c:5-30, dmrg/DMRG_V_M_LR_Q1.c:8-55; DMRG_EXPECTATION_ONSITE,
+ * dmrg/DMRG_EXPECTATION_ONSITE.c:3-31; DMRG_EXPECTATION_INTERSITE_Q0,
+ * dmrg/DMRG_EXPECTATION_INTERSITE_Q0.c:3-50).  For state i of an output sector and an operator O
+ * on position pos:
+ *    (O v)[i] = sum_k (sign_i * v[Inv(state i with its pos coordinate set to col k)]) * O[s_pos][k]
+ * over the row in storage order, -1 Inv entries skipped, rounded as written (bitwise the
+ * reference's).  sign_i = (-1)^(electrons at the positions before pos) when sign = 1
+ * (LR: ele_LL; RR: ele_LL + ele_LR; RL: ele_LL + ele_LR + ele_RR; ignored for LL).
+ */
+
+/* A basis from host arrays: the states of one sector and, if inv is not NULL, the
+ * dim_LL*dim_onsite*dim_RR*dim_onsite Inv_LLLRRRRL table (which may index other sectors, as a
+ * DMRG_WHOLE_BASIS_Qk's does).  States must lie inside the dimensions (DG_ERR_ARG otherwise). */
+int dg_sb_basis_upload(int n, int dim_LL, int dim_RR, int dim_onsite, const short *LL, const short *LR, const short *RR,
+                       const short *RL, const int *inv, dg_sb_basis **out);
+
+typedef struct dg_sb_ops dg_sb_ops;
+/* Device copies of square block operators: operator k has rows[k] rows and columns in
+ * [0, rows[k]) (checked), rows[k] = the states of the position it will act on. */
+int dg_sb_ops_create(int n_ops, const CRS1 *const *ops, const int *rows, dg_sb_ops **out);
+void dg_sb_ops_free(dg_sb_ops *ops);
+
+/* out = O_op v over the states of out_states, the input index taken from inv_table's Inv table
+ * (out_states itself for Q0).  v has v_len entries (an Inv entry at or beyond it is DG_ERR_ARG);
+ * ele_LL[dim_LL], ele_LR[dim_onsite], ele_RR[dim_RR] are host arrays, needed only when sign = 1.
+ * v and out may be host or device pointers. */
+int dg_sb_vm(const dg_sb_basis *out_states, const dg_sb_basis *inv_table, const dg_sb_ops *ops, int op, int pos, int sign,
+             const int *ele_LL, const int *ele_LR, const int *ele_RR, const double *v, long v_len, double *out);
+
+typedef struct {
+   int pos;      /* DG_SB_LL .. DG_SB_RL                                  */
+   int op;       /* operator index in the dg_sb_ops set                   */
+   int sign;     /* 1: the (-1)^(electrons before pos) factor             */
+   int weight;   /* 0: w0, 1: w1 multiplies the product                   */
+} dg_sb_expect_term;
+
+/* out[t] = sum_i w_{weight_t}[i] * (O_t v)[i] over the states of out_states, every term in one
+ * device pass (out is a host array of n_terms).  w0 / w1 have out_states' length (for <v|O|v>
+ * pass w0 = v); vectors may be host or device pointers.  The products are the dg_sb_vm values;
+ * the sums run in a fixed order (bitwise reproducible run to run). */
+int dg_sb_expect(const dg_sb_basis *out_states, const dg_sb_basis *inv_table, const dg_sb_ops *ops, int n_terms,
+                 const dg_sb_expect_term *terms, const int *ele_LL, const int *ele_LR, const int *ele_RR, const double *v, long v_len,
+                 const double *w0, const double *w1, double *out);
+
 #ifdef __cplusplus
 }
 #endif

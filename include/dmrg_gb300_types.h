@@ -8,6 +8,7 @@
  *   CRS1, BOX_CG, BOX_II, BOX_LAN         include/SML.h:17-28, 56-65, 67-86, 122-135
  *   DMRG_PARAMETER, DMRG_TIME             include/dmrg.h:6-38, 40-51
  *   DMRG_BASIS, DMRG_STATUS               include/dmrg.h:54-99, 236-267
+ *   DMRG_WHOLE_BASIS_Q1..Q4               include/dmrg.h:140-195
  *   DMRG_BOX_LAN, DMRG_BOX_CG, DMRG_BOX_II include/dmrg.h:269-328
  *   EXACT_PARAMETER, EXACT_TIME           include/exact.h:14-37, 39-51
  *   EXACT_HAM_INFO, EXACT_BASIS_INFO      include/exact.h:54-74
@@ -144,6 +145,56 @@ typedef struct {
    int *Tot_Ele_2_LLLR;
    int *Tot_Parity_LLLR;
 } DMRG_BASIS;
+
+/* Every sector of a superblock: per-sector state arrays indexed by the quantum numbers, the
+ * sector dimensions, and one Inv_LLLRRRRL table giving each state's index inside its sector. */
+typedef struct {
+   short **LL_LLLRRRRL;
+   short **LR_LLLRRRRL;
+   short **RL_LLLRRRRL;
+   short **RR_LLLRRRRL;
+   int *Inv_LLLRRRRL;
+   int *Dim;
+   int max_dim;
+   int dim_RR;
+   int dim_onsite;
+} DMRG_WHOLE_BASIS_Q1;
+
+typedef struct {
+   short ***LL_LLLRRRRL;
+   short ***LR_LLLRRRRL;
+   short ***RL_LLLRRRRL;
+   short ***RR_LLLRRRRL;
+   int *Inv_LLLRRRRL;
+   int **Dim;
+   int max_dim;
+   int dim_RR;
+   int dim_onsite;
+} DMRG_WHOLE_BASIS_Q2;
+
+typedef struct {
+   short ****LL_LLLRRRRL;
+   short ****LR_LLLRRRRL;
+   short ****RL_LLLRRRRL;
+   short ****RR_LLLRRRRL;
+   int *Inv_LLLRRRRL;
+   int ***Dim;
+   int max_dim;
+   int dim_RR;
+   int dim_onsite;
+} DMRG_WHOLE_BASIS_Q3;
+
+typedef struct {
+   short *****LL_LLLRRRRL;
+   short *****LR_LLLRRRRL;
+   short *****RL_LLLRRRRL;
+   short *****RR_LLLRRRRL;
+   int *Inv_LLLRRRRL;
+   int ****Dim;
+   int max_dim;
+   int dim_RR;
+   int dim_onsite;
+} DMRG_WHOLE_BASIS_Q4;
 
 typedef struct {
    char BC[1000];

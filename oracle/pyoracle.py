@@ -248,6 +248,123 @@ def ref_sb_basis(dim_LL, dim_RR, d, qn1, qn2, targets):
     return (*(a[:n].copy() for a in st), inv)
 
 
+SB_LL, SB_LR, SB_RR, SB_RL = 0, 1, 2, 3
+SB_NAMES = ("LL", "LR", "RR", "RL")
+
+
+def sb_vm(states, inv, dim_RR, d, op: abi.Crs, pos, v, ele=None):
+    """Block operator on one sector's superblock states, restated with numpy from DMRG_V_M_<pos>_Q*
+    (dmrg/DMRG_V_M_LL_Q0.c:13-28, dmrg/DMRG_V_M_LR_Q1.c:23-52, dmrg/DMRG_V_M_RR_Q2.c:23-52): for
+    state i the sum over the operator row of its pos coordinate, in storage order, of
+    (sign_i * v[Inv(i with that coordinate set to the column)]) * value, Inv = -1 entries skipped;
+    sign_i = (-1)^(electrons at the positions before pos) when ele = (ele_LL, ele_LR, ele_RR) is
+    given (Sign_Flag "Yes").  Each step is rounded as the reference's loop rounds it."""
+    c = [np.asarray(a, np.int64) for a in states]
+    n = len(c[0])
+    strides = [d * dim_RR * d, dim_RR * d, d, 1]
+    full = ((c[0] * d + c[1]) * dim_RR + c[2]) * d + c[3]
+    s = c[pos]
+    base = full - s * strides[pos]
+    sgn = np.ones(n)
+    if ele is not None and pos != SB_LL:
+        ne = np.asarray(ele[0], np.int64)[c[0]]
+        if pos >= SB_RR:
+            ne = ne + np.asarray(ele[1], np.int64)[c[1]]
+        if pos >= SB_RL:
+            ne = ne + np.asarray(ele[2], np.int64)[c[2]]
+        sgn = np.where(ne % 2 == 0, 1.0, -1.0)
+    v = np.asarray(v, np.float64)
+    start = op.row[s]
+    length = op.row[s + 1] - start
+    acc = np.zeros(n)
+    for k in range(int(length.max()) if n else 0):
+        live = np.flatnonzero(length > k)
+        idx = start[live] + k
+        j = inv[base[live] + op.col[idx].astype(np.int64) * strides[pos]]
+        ok = j >= 0
+        li = live[ok]
+        acc[li] = acc[li] + (sgn[li] * v[j[ok]]) * op.val[idx[ok]]
+    return acc
+
+
+def sb_expect(states, inv, dim_RR, d, terms, v, weights, ele=None):
+    """<w|O|v> for each term (op, pos, weight index) over one sector: the sb_vm product dotted
+    with weights[weight] (DMRG_EXPECTATION_ONSITE.c:12-29 is V_M then INNER_PRODUCT per site)."""
+    return np.array([float(np.dot(weights[w], sb_vm(states, inv, dim_RR, d, op, pos, v, ele))) for op, pos, w in terms])
+
+
+def _crs_array(ops):
+    arr = (P(CRS1) * max(len(ops), 1))(*[o.ref for o in ops])
+    return arr
+
+
+def _q0_basis(states, inv, dim_LL, dim_RR, d):
+    st = [np.ascontiguousarray(a, np.int16) for a in states]
+    inv = np.ascontiguousarray(inv, np.int32)
+    B = DMRG_BASIS(LL_LLLRRRRL=ptr(st[0], C.c_short), LR_LLLRRRRL=ptr(st[1], C.c_short), RR_LLLRRRRL=ptr(st[2], C.c_short),
+                   RL_LLLRRRRL=ptr(st[3], C.c_short), Inv_LLLRRRRL=ptr(inv, C.c_int), dim_LLLRRRRL=len(st[0]),
+                   dim_LL=dim_LL, dim_RR=dim_RR, dim_onsite=d)
+    return B, (st, inv)
+
+
+def call_vm_q0(lib, states, inv, dim_LL, dim_RR, d, op: abi.Crs, pos, v):
+    """DMRG_V_M_<pos>_Q0 of lib (the reference build or libdmrg_gb300) on host arrays."""
+    B, keep = _q0_basis(states, inv, dim_LL, dim_RR, d)
+    v = np.ascontiguousarray(v, np.float64)
+    out = np.full(len(states[0]), np.nan)
+    getattr(lib, f"DMRG_V_M_{SB_NAMES[pos]}_Q0")(op.ref, ptr(v, C.c_double), ptr(out, C.c_double), len(out), 1, C.byref(B))
+    return out
+
+
+def call_vm_whole(lib, wb, q, op: abi.Crs, pos, v, ele=None, sign=False):
+    """DMRG_V_M_<pos>_Q<k> of lib on a whole basis (abi.WholeBasis) for output sector q (a k-tuple)."""
+    k = len(q)
+    v = np.ascontiguousarray(v, np.float64)
+    dim = wb.struct.Dim
+    for i in q:
+        dim = dim[i]
+    out = np.full(int(dim), np.nan)
+    e = [np.ascontiguousarray(a, np.int32) if a is not None else None for a in (ele or (None, None, None))]
+    ep = [ptr(a, C.c_int) if a is not None else None for a in e]
+    flag = b"Yes" if sign else b"No"
+    args = [op.ref, *[C.c_int(i) for i in q], ptr(v, C.c_double)]
+    if pos == SB_LR:
+        args += [ep[0], flag]
+    elif pos == SB_RR:
+        args += [ep[0], ep[1], flag]
+    elif pos == SB_RL:
+        args += [ep[0], ep[1], ep[2], flag]
+    args += [ptr(out, C.c_double), C.c_int(1), wb.ref]
+    getattr(lib, f"DMRG_V_M_{SB_NAMES[pos]}_Q{k}")(*args)
+    return out
+
+
+def call_expectation_onsite(lib, states, inv, dim_LL, dim_RR, d, M_LL, M_On, M_RR, v):
+    """DMRG_EXPECTATION_ONSITE of lib: returns (Out, Temp_V)."""
+    B, keep = _q0_basis(states, inv, dim_LL, dim_RR, d)
+    S = abi.DMRG_STATUS(LL_site=len(M_LL) - 1, RR_site=len(M_RR) - 1, dim_LLLRRRRL=len(states[0]))
+    v = np.ascontiguousarray(v, np.float64)
+    out = np.full(len(M_LL) + len(M_RR) + 2, np.nan)
+    temp = np.full(len(v), np.nan)
+    lib.DMRG_EXPECTATION_ONSITE(_crs_array(M_LL), M_On.ref, _crs_array(M_RR), ptr(out, C.c_double), ptr(v, C.c_double),
+                                ptr(temp, C.c_double), 1, C.byref(B), C.byref(S))
+    return out, temp
+
+
+def call_expectation_intersite_q0(lib, states, inv, dim_LL, dim_RR, d, M_CF, M_LL, M_On, M_RR, origin, v):
+    """DMRG_EXPECTATION_INTERSITE_Q0 of lib: returns (Out, Temp_V1, Temp_V2)."""
+    B, keep = _q0_basis(states, inv, dim_LL, dim_RR, d)
+    LL_site, RR_site = len(M_LL) - 1, len(M_RR) - 1
+    S = abi.DMRG_STATUS(LL_site=LL_site, RR_site=RR_site, dim_LLLRRRRL=len(states[0]))
+    v = np.ascontiguousarray(v, np.float64)
+    out = np.full(LL_site + RR_site + 4, np.nan)
+    t1, t2 = np.full(len(v), np.nan), np.full(len(v), np.nan)
+    lib.DMRG_EXPECTATION_INTERSITE_Q0(_crs_array(M_CF), _crs_array(M_LL), M_On.ref, _crs_array(M_RR), ptr(out, C.c_double),
+                                      origin, ptr(v, C.c_double), ptr(t1, C.c_double), ptr(t2, C.c_double), 1, C.byref(B),
+                                      C.byref(S))
+    return out, t1, t2
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

@@ -166,6 +166,44 @@ def vm_fixture():
     np.savez_compressed(HERE / "vm_hubbard6.npz", **out)
 
 
+def sb_obs_fixture():
+    """The reference's DMRG_V_M_{LL,LR,RR,RL}_Q0..Q4 and DMRG_EXPECTATION_ONSITE /
+    _INTERSITE_Q0 on a seeded Hubbard-type superblock with every sector laid out: block
+    observables, a c^dagger_up-type operator on each position (with and without the fermion
+    sign) and site-by-site expectation values."""
+    from dmrg_c_gb300 import sb_models
+    p = sb_models.random_observable_problem(seed=5)
+    ref = po.load_ref()
+    rng = np.random.default_rng(61)
+    q0 = p.target
+    st, inv0 = p.sectors[q0], p.inv_sector(q0)
+    v = rng.standard_normal(len(st[0]))
+    out = dict(p.arrays(), v=v)
+    ops = p.ops
+    for pos, op in ((po.SB_LL, ops["LL"][0]), (po.SB_LR, ops["On"]), (po.SB_RR, ops["RR"][1]), (po.SB_RL, ops["On"])):
+        out[f"q0_{po.SB_NAMES[pos]}"] = po.call_vm_q0(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, op, pos, v)
+    # sector-changing operator: the output sector is the input's label minus one up electron
+    q_out = q0 - (sb_models.QN_SCALE + 1)
+    shift = {po.SB_LL: ops["CdLL"][0], po.SB_LR: ops["CdOn"], po.SB_RR: ops["CdRR"][0], po.SB_RL: ops["CdOn"]}
+    for k in (1, 2, 3, 4):
+        wb = p.whole_basis(k)
+        for pos, op in shift.items():
+            if k == 4 and pos in (po.SB_LL, po.SB_LR):
+                continue
+            for sign in (False, True):
+                if sign and pos == po.SB_LL:
+                    continue
+                out[f"q{k}_{po.SB_NAMES[pos]}_{int(sign)}"] = po.call_vm_whole(ref, wb, p.index(q_out, k), op, pos, v,
+                                                                              ele=p.ele, sign=sign)
+    o, t = po.call_expectation_onsite(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, ops["LL"], ops["On"], ops["RR"], v)
+    out.update(onsite=o, onsite_temp=t)
+    for origin in (0, 1, len(ops["LL"])):
+        o, t1, t2 = po.call_expectation_intersite_q0(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, ops["CF"][origin:] if origin < len(ops["LL"]) else ops["CF"][:1],
+                                                     ops["LL"], ops["On"], ops["RR"], origin, v)
+        out.update({f"inter{origin}": o, f"inter{origin}_t1": t1, f"inter{origin}_t2": t2})
+    np.savez_compressed(HERE / "sb_obs.npz", **out)
+
+
 def obc_fixture():
     """The reference's matrix-free superblock product and OBC Lanczos on a seeded
     synthetic superblock (spin-1/2 sites, one block quantum number)."""
@@ -207,6 +245,7 @@ def main():
     sb_fixture()
     sb_basis_fixture()
     vm_fixture()
+    sb_obs_fixture()
     obc_fixture()
     xxz_energy_fixture()
     for f in sorted(HERE.glob("*.npz")):

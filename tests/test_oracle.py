@@ -215,3 +215,66 @@ def test_superblock_basis_matches_reference_golden(oracle, case):
                             (g["q2_sz_LL"], g["q2_sz_RR"], g["q2_sz_site"]), tuple(int(t) for t in g["q2_targets"]))
     assert np.array_equal(np.stack(a[:4]), g[f"{case}_states"])
     assert np.array_equal(a[4], g[f"{case}_inv"])
+
+
+def _obs_problem():
+    from dmrg_c_gb300 import sb_models
+    g = golden("sb_obs.npz")
+    return sb_models.ObservableProblem.from_arrays(g), g
+
+
+def test_observable_sectors_in_reference_order(oracle):
+    """Every sector of the observable problem is laid out in the order the reference's sort gives
+    (the numpy restatement of GET_BASIS_SUPERBLOCK is pinned by the basis fixture above)."""
+    p, _ = _obs_problem()
+    for q in (p.target, p.target - 1001, p.target + 999):
+        LL, LR, RR, RL, inv = oracle.sb_basis(p.dim_LL, p.dim_RR, p.d, (p.q_LL, p.q_RR, p.q_site), None, (q, 0))
+        assert np.array_equal(np.stack([LL, LR, RR, RL]), np.stack(p.sectors[q]))
+        assert np.array_equal(inv, p.inv_sector(q))
+
+
+def test_sb_vm_matches_reference_golden(oracle):
+    """DMRG_V_M_*_Q0..Q4 restated (numpy) equal the reference's outputs bit for bit: in-sector
+    block observables, and a c^dagger_up-type operator on each position with and without the
+    fermion sign through a whole basis."""
+    p, g = _obs_problem()
+    v = g["v"]
+    q0 = p.target
+    st, inv0 = p.sectors[q0], p.inv_sector(q0)
+    for pos, op in ((0, p.ops["LL"][0]), (1, p.ops["On"]), (2, p.ops["RR"][1]), (3, p.ops["On"])):
+        y = oracle.sb_vm(st, inv0, p.dim_RR, p.d, op, pos, v)
+        assert np.array_equal(y.view(np.int64), g[f"q0_{oracle.SB_NAMES[pos]}"].view(np.int64))
+    q_out = q0 - 1001
+    shift = {0: p.ops["CdLL"][0], 1: p.ops["CdOn"], 2: p.ops["CdRR"][0], 3: p.ops["CdOn"]}
+    checked = 0
+    for key in g.keys():
+        if key[0] == "q" and key[1] in "1234" and key.count("_") == 2:
+            _, name, sign = key.split("_")
+            pos = oracle.SB_NAMES.index(name)
+            y = oracle.sb_vm(p.sectors[q_out], p.inv, p.dim_RR, p.d, shift[pos], pos, v, ele=p.ele if sign == "1" else None)
+            assert np.array_equal(y.view(np.int64), g[key].view(np.int64)), key
+            checked += 1
+    assert checked == 25
+    # the sign matters in this case
+    assert not np.array_equal(g["q1_RL_0"], g["q1_RL_1"])
+
+
+def test_sb_expectation_matches_reference_golden(oracle):
+    """DMRG_EXPECTATION_ONSITE / _INTERSITE_Q0 restated: the V_M products dotted with the
+    vector (or with the origin's product); within 1e-12 of the reference's sums."""
+    p, g = _obs_problem()
+    v = g["v"]
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    LLs, RRs, On = p.ops["LL"], p.ops["RR"], p.ops["On"]
+    terms = [(o, 0, 0) for o in LLs] + [(On, 1, 0), (On, 3, 0)] + [(o, 2, 0) for o in RRs[::-1]]
+    e = oracle.sb_expect(st, inv0, p.dim_RR, p.d, terms, v, [v])
+    scale = float(np.dot(np.abs(v), np.abs(v))) * 10
+    assert np.allclose(e, g["onsite"], rtol=0, atol=1e-12 * scale)
+    for origin in (0, 1, len(LLs)):
+        t1 = oracle.sb_vm(st, inv0, p.dim_RR, p.d, LLs[origin] if origin < len(LLs) else On, 0 if origin < len(LLs) else 1, v)
+        assert np.array_equal(t1, g[f"inter{origin}_t1"])
+        cf = p.ops["CF"][origin:] if origin < len(LLs) else []
+        terms = [(o, 0, 0) for o in cf] + [(On, 1, 1), (On, 3, 1)] + [(o, 2, 1) for o in RRs[::-1]]
+        e = oracle.sb_expect(st, inv0, p.dim_RR, p.d, terms, v, [v, t1])
+        ref = g[f"inter{origin}"][:len(terms)]
+        assert np.allclose(e, ref, rtol=0, atol=1e-12 * scale), origin
