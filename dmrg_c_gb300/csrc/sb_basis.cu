@@ -10,6 +10,7 @@
 // the few thousand pairs (dim_LL * d and dim_RR * d of them) and lays out the runs; one device
 // warp per (LL, LR) pair writes its run of states and their Inv_LLLRRRRL entries.
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <utility>
 #include <vector>
@@ -47,6 +48,42 @@ template <class T>
 void upload(DevBuf<T> &b, const std::vector<T> &h, cudaStream_t st) {
   b.alloc(std::max<size_t>(h.size(), 1));
   if (!h.empty()) DG_CUDA(cudaMemcpyAsync(b.get(), h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
+}
+
+constexpr int64_t kMaxRrrlTable = int64_t(1) << 26;   // entries of SbPairs::rrrl_pos at most
+
+// SbPairs from the builder's (LL, LR) pairs: pair p has glen[p] states starting at off[p], its
+// (RR, RL) pairs are rrrl[gstart[p] ...]; pairs of one group are adjacent.
+std::unique_ptr<SbPairs> pairs_from_groups(const std::vector<int> &pll, const std::vector<int> &plr, const std::vector<int64_t> &off,
+                                           const std::vector<int> &gstart, const std::vector<int> &glen, const std::vector<int> &rrrl,
+                                           int dLL, int dRR, int d) {
+  std::unique_ptr<SbPairs> P(new SbPairs());
+  P->dim_LL = dLL;
+  P->dim_RR = dRR;
+  P->d = d;
+  P->R = (int)pll.size();
+  P->pair_run.assign((size_t)dLL * d, -1);
+  std::vector<int> blk_g;
+  for (int r = 0; r < P->R; ++r) {
+    if (r == 0 || gstart[r] != gstart[r - 1]) {
+      P->blk_run0.push_back(r);
+      P->blk_Q.push_back(glen[r]);
+      P->blk_base.push_back(off[r]);
+      blk_g.push_back(gstart[r]);
+    }
+    P->run_ll.push_back(pll[r]);
+    P->run_lr.push_back(plr[r]);
+    P->run_blk.push_back((int)P->blk_Q.size() - 1);
+    P->pair_run[(size_t)pll[r] * d + plr[r]] = r;
+  }
+  P->B = (int)P->blk_Q.size();
+  P->blk_run0.push_back(P->R);
+  if ((int64_t)P->B * dRR * d > kMaxRrrlTable) return nullptr;
+  P->rrrl_pos.assign((size_t)P->B * dRR * d, -1);
+  for (int g = 0; g < P->B; ++g)
+    for (int t = 0; t < P->blk_Q[g]; ++t) P->rrrl_pos[(size_t)g * dRR * d + rrrl[blk_g[g] + t]] = t;
+  P->finish_and_upload();
+  return P;
 }
 
 dg_sb_basis *sb_basis_build(const dg_sb_basis_spec *s) {
@@ -120,6 +157,8 @@ dg_sb_basis *sb_basis_build(const dg_sb_basis_spec *s) {
     DG_CUDA(cudaMemsetAsync(b->inv.get(), 0xff, sizeof(int) * dim_whole, st));   // -1
     const int npairs = (int)pll.size();
     const long blocks = std::max(1L, std::min<long>(((long)npairs * 32 + kThreads - 1) / kThreads, (long)sm_count() * 16));
+    b->inv_exact = true;
+    b->pairs = pairs_from_groups(pll, plr, off, gstart, glen, rrrl, dLL, dRR, d);
     k_sb_basis_fill<<<(int)blocks, kThreads, 0, st>>>(d_pll.get(), d_plr.get(), d_off.get(), d_gstart.get(), d_glen.get(), npairs,
                                                       d_rrrl.get(), d, dRR, b->st[0].get(), b->st[1].get(), b->st[2].get(),
                                                       b->st[3].get(), b->inv.get()); ::dg::count_launch();
@@ -133,6 +172,90 @@ dg_sb_basis *sb_basis_build(const dg_sb_basis_spec *s) {
 }
 
 }  // namespace
+
+void SbPairs::finish_and_upload() {
+  rho_off.assign(B + 1, 0);
+  sig_off.assign(B + 1, 0);
+  q_off.assign(B + 1, 0);
+  for (int g = 0; g < B; ++g) {
+    const int64_t Pg = blk_run0[g + 1] - blk_run0[g], Q = blk_Q[g];
+    rho_off[g + 1] = rho_off[g] + Pg * Pg;
+    sig_off[g + 1] = sig_off[g] + Q * Q;
+    q_off[g + 1] = q_off[g] + Q;
+  }
+  cudaStream_t st = stream();
+  upload(d_run_ll, run_ll, st);
+  upload(d_run_lr, run_lr, st);
+  upload(d_run_blk, run_blk, st);
+  upload(d_blk_run0, blk_run0, st);
+  upload(d_blk_Q, blk_Q, st);
+  upload(d_pair_run, pair_run, st);
+  upload(d_rrrl_pos, rrrl_pos, st);
+  upload(d_blk_base, blk_base, st);
+  upload(d_rho_off, rho_off, st);
+  upload(d_sig_off, sig_off, st);
+  upload(d_q_off, q_off, st);
+  DG_CUDA(cudaStreamSynchronize(st));   // the host vectors may change later
+}
+
+std::unique_ptr<SbPairs> sb_pairs_from_states(long n, const short *const st[4], int dLL, int dRR, int d) {
+  if (n <= 0) return nullptr;
+  std::unique_ptr<SbPairs> P(new SbPairs());
+  P->dim_LL = dLL;
+  P->dim_RR = dRR;
+  P->d = d;
+  P->pair_run.assign((size_t)dLL * d, -1);
+  std::vector<int> owner((size_t)dRR * d, -1);   // block listing each (RR, RL) pair
+  std::vector<int64_t> run_start;
+  for (long i = 0; i < n; ++i) {
+    const int ll = st[0][i], lr = st[1][i];
+    if (ll < 0 || ll >= dLL || lr < 0 || lr >= d || st[2][i] < 0 || st[2][i] >= dRR || st[3][i] < 0 || st[3][i] >= d) return nullptr;
+    if (i == 0 || ll != st[0][i - 1] || lr != st[1][i - 1]) {
+      int &pr = P->pair_run[(size_t)ll * d + lr];
+      if (pr != -1) return nullptr;   // the states of one pair are not contiguous
+      pr = (int)P->run_ll.size();
+      P->run_ll.push_back(ll);
+      P->run_lr.push_back(lr);
+      run_start.push_back(i);
+    }
+  }
+  P->R = (int)P->run_ll.size();
+  run_start.push_back(n);
+  for (int r = 0; r < P->R; ++r) {
+    const int64_t s0 = run_start[r], len = run_start[r + 1] - s0;
+    const bool fresh = r == 0 || len != P->blk_Q.back() || st[2][s0] != st[2][P->blk_base.back()] ||
+                       st[3][s0] != st[3][P->blk_base.back()];
+    if (fresh) {
+      if (len > INT32_MAX) return nullptr;
+      P->blk_run0.push_back(r);
+      P->blk_Q.push_back((int)len);
+      P->blk_base.push_back(s0);
+    }
+    const int g = (int)P->blk_Q.size() - 1;
+    const int64_t b0 = P->blk_base.back();
+    for (int64_t t = 0; t < len; ++t) {
+      if (st[2][s0 + t] != st[2][b0 + t] || st[3][s0 + t] != st[3][b0 + t]) return nullptr;
+      if (fresh) {
+        int &o = owner[(size_t)st[2][s0 + t] * d + st[3][s0 + t]];
+        if (o != -1) return nullptr;   // an (RR, RL) pair listed twice
+        o = g;
+      }
+    }
+    P->run_blk.push_back(g);
+  }
+  P->B = (int)P->blk_Q.size();
+  P->blk_run0.push_back(P->R);
+  if ((int64_t)P->B * dRR * d > kMaxRrrlTable) return nullptr;
+  P->rrrl_pos.assign((size_t)P->B * dRR * d, -1);
+  for (int g = 0; g < P->B; ++g)
+    for (int t = 0; t < P->blk_Q[g]; ++t) {
+      const int64_t s = P->blk_base[g] + t;
+      P->rrrl_pos[(size_t)g * dRR * d + (size_t)st[2][s] * d + st[3][s]] = t;
+    }
+  P->finish_and_upload();
+  return P;
+}
+
 }  // namespace dg
 
 using namespace dg;

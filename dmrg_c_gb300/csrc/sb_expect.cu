@@ -21,6 +21,7 @@
 // second launch sums each term's block partials in a fixed order.
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -153,6 +154,158 @@ __global__ void __launch_bounds__(kThreads) k_sb_expect_sum(const double *__rest
   if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
+// ---------------------------------------------------------------------------------
+// Expectation values through reduced density matrices.  In a sector with the SbPairs block
+// structure the vector is, block by block, a row-major P x Q matrix X_g (rows: the (LL, LR) runs,
+// columns: the (RR, RL) pairs).  For an operator on LL or LR,
+//     <w|O|v> = sum over runs (a, lr) and row elements O[s][c] of O[s][c] * rho_g[(a, lr)][(c', lr')]
+// with rho_g = W_g V_g^T and (c', lr') the pair whose state replaces s by c; for RR or RL the same
+// with sigma_g = W_g^T V_g over the (RR, RL) positions.  The density matrices cost one pass over
+// the vector for all terms; each term is then a trace over its operator's elements instead of a
+// gather per element and superblock state.  Only unsigned terms whose input and output are the
+// one sector take this form.
+// ---------------------------------------------------------------------------------
+struct PairView {
+  int R, B, dim_RR, d;
+  const int *run_ll, *run_lr, *run_blk, *blk_run0, *blk_Q, *pair_run, *rrrl_pos;
+  const int64_t *blk_base, *rho_off, *sig_off, *q_off;
+};
+
+PairView pair_view(const SbPairs &P) {
+  return PairView{P.R, P.B, P.dim_RR, P.d, P.d_run_ll.get(), P.d_run_lr.get(), P.d_run_blk.get(), P.d_blk_run0.get(), P.d_blk_Q.get(),
+                  P.d_pair_run.get(), P.d_rrrl_pos.get(), P.d_blk_base.get(), P.d_rho_off.get(), P.d_sig_off.get(), P.d_q_off.get()};
+}
+
+// Largest g in [0, B) with off[g] <= e (off ascending, off[0] = 0).
+__device__ __forceinline__ int find_block(const int64_t *__restrict__ off, int B, int64_t e) {
+  int lo = 0, hi = B - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// rho_g[p][q] = sum_t w[row p][t] * v[row q][t] for every block, summed over t in order and rounded
+// as written (with w = v these are DMRG_GET_DENSITY_MATRIX's entries, bit for bit).
+__global__ void __launch_bounds__(kThreads) k_gram_rows(PairView P, const double *__restrict__ w, const double *__restrict__ v,
+                                                       double *__restrict__ rho) {
+  const int64_t total = P.rho_off[P.B];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int g = find_block(P.rho_off, P.B, e);
+    const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
+    const int64_t loc = e - P.rho_off[g];
+    const int p = (int)(loc / Pg), q = (int)(loc - (int64_t)p * Pg);
+    const double *__restrict__ x = w + P.blk_base[g] + (int64_t)p * Q;
+    const double *__restrict__ y = v + P.blk_base[g] + (int64_t)q * Q;
+    double acc = 0.0;
+    for (int t = 0; t < Q; ++t) acc = __dadd_rn(acc, __dmul_rn(x[t], y[t]));
+    rho[e] = acc;
+  }
+}
+
+// sigma_g[t][u] = sum_p w[row p][t] * v[row p][u] for every block.
+__global__ void __launch_bounds__(kThreads) k_gram_cols(PairView P, const double *__restrict__ w, const double *__restrict__ v,
+                                                       double *__restrict__ sig) {
+  const int64_t total = P.sig_off[P.B];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int g = find_block(P.sig_off, P.B, e);
+    const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
+    const int64_t loc = e - P.sig_off[g];
+    const int t = (int)(loc / Q), u = (int)(loc - (int64_t)t * Q);
+    const double *__restrict__ x = w + P.blk_base[g] + t;
+    const double *__restrict__ y = v + P.blk_base[g] + u;
+    double acc = 0.0;
+    for (int p = 0; p < Pg; ++p) acc = __dadd_rn(acc, __dmul_rn(x[(int64_t)p * Q], y[(int64_t)p * Q]));
+    sig[e] = acc;
+  }
+}
+
+struct TraceTerm {
+  const int64_t *row;
+  int pos, weight;
+};
+
+// out[term] = trace of the term's operator against rho (LL, LR) or sigma (RR, RL); one block a term.
+__global__ void __launch_bounds__(kThreads) k_sb_trace(PairView P, SbStates S, const TraceTerm *__restrict__ terms,
+                                                      const int *__restrict__ col, const double *__restrict__ val,
+                                                      const double *__restrict__ rho0, const double *__restrict__ rho1,
+                                                      const double *__restrict__ sig0, const double *__restrict__ sig1,
+                                                      double *__restrict__ out) {
+  const TraceTerm t = terms[blockIdx.x];
+  double acc = 0.0;
+  if (t.pos == DG_SB_LL || t.pos == DG_SB_LR) {
+    const double *__restrict__ rho = t.weight ? rho1 : rho0;
+    for (int r = threadIdx.x; r < P.R; r += blockDim.x) {
+      const int g = P.run_blk[r], r0 = P.blk_run0[g], Pg = P.blk_run0[g + 1] - r0;
+      const int a = P.run_ll[r], lr = P.run_lr[r];
+      const int s = t.pos == DG_SB_LL ? a : lr;
+      const double *__restrict__ rrow = rho + P.rho_off[g] + (int64_t)(r - r0) * Pg;
+      for (int64_t k = t.row[s]; k < t.row[s + 1]; ++k) {
+        const int c = col[k];
+        const int r2 = P.pair_run[t.pos == DG_SB_LL ? c * P.d + lr : a * P.d + c];
+        if (r2 >= r0 && r2 < r0 + Pg) acc += val[k] * rrow[r2 - r0];
+      }
+    }
+  } else {
+    const double *__restrict__ sig = t.weight ? sig1 : sig0;
+    const int64_t slots = P.q_off[P.B];
+    const int64_t tab = (int64_t)P.dim_RR * P.d;
+    for (int64_t u = threadIdx.x; u < slots; u += blockDim.x) {
+      const int g = find_block(P.q_off, P.B, u);
+      const int Q = P.blk_Q[g];
+      const int tt = (int)(u - P.q_off[g]);
+      const int64_t si = P.blk_base[g] + tt;
+      const int rr = S.st[DG_SB_RR][si], rl = S.st[DG_SB_RL][si];
+      const int s = t.pos == DG_SB_RR ? rr : rl;
+      const double *__restrict__ srow = sig + P.sig_off[g] + (int64_t)tt * Q;
+      const int *__restrict__ pos = P.rrrl_pos + g * tab;
+      for (int64_t k = t.row[s]; k < t.row[s + 1]; ++k) {
+        const int c = col[k];
+        const int t2 = pos[t.pos == DG_SB_RR ? c * P.d + rl : rr * P.d + c];
+        if (t2 >= 0) acc += val[k] * srow[t2];
+      }
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) out[blockIdx.x] = acc;
+}
+
+// Is inv exactly the sector's own table: Inv at every state's index is that index, and no other
+// entry is >= 0?
+__global__ void __launch_bounds__(kThreads) k_inv_exact(SbStates S, const int *__restrict__ inv, SbGeom g, int *bad,
+                                                       unsigned long long *count) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < S.n; i += stride) {
+    const int64_t sup = (((int64_t)S.st[0][i] * g.d + S.st[1][i]) * g.dim_RR + S.st[2][i]) * g.d + S.st[3][i];
+    if (sup < 0 || sup >= g.inv_len || inv[sup] != (int)i) *bad = 1;
+  }
+  unsigned long long c = 0;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < g.inv_len; e += stride) c += inv[e] >= 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+// M = X X^T for one row-major P x Q block: entry (p, q), p <= q, is sum_t X[p][t] * X[q][t] in t
+// order, rounded as written, and mirrored (DMRG_GET_DENSITY_MATRIX.c:36-100).
+__global__ void __launch_bounds__(kThreads) k_gram_dense(const double *__restrict__ X, int P, int Q, double *__restrict__ M) {
+  const int64_t total = (int64_t)P * P;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(e / P), q = (int)(e - (int64_t)p * P);
+    if (p > q) continue;
+    const double *__restrict__ x = X + (int64_t)p * Q;
+    const double *__restrict__ y = X + (int64_t)q * Q;
+    double acc = 0.0;
+    for (int t = 0; t < Q; ++t) acc = __dadd_rn(acc, __dmul_rn(x[t], y[t]));
+    M[(int64_t)p * P + q] = acc;
+    M[(int64_t)q * P + p] = acc;
+  }
+}
+
 int pos_dim(int pos, int dim_LL, int d, int dim_RR) { return pos == DG_SB_LL ? dim_LL : pos == DG_SB_RR ? dim_RR : d; }
 
 long state_grid(long n) { return std::max(1L, std::min((n + kThreads - 1) / kThreads, (long)sm_count() * 16)); }
@@ -280,13 +433,90 @@ void launch_vm(const SbStates &S, const int *inv, const SbGeom &g, const SbTerm 
   DG_CUDA(cudaGetLastError());
 }
 
-// out[t] for every term: sum over the states of w_{weight_t}[i] (O_t v)[i].
+// Sets b->inv_exact (b carries an Inv table).
+void mark_inv_exact(dg_sb_basis *b, cudaStream_t st) {
+  b->inv_exact = false;
+  if (b->n == 0 || b->inv_len == 0) return;
+  DevBuf<int> bad(1);
+  DevBuf<unsigned long long> count(1);
+  DG_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(int), st));
+  DG_CUDA(cudaMemsetAsync(count.get(), 0, sizeof(unsigned long long), st));
+  const long work = std::max((long)b->n, b->inv_len);
+  k_inv_exact<<<(int)state_grid(work), kThreads, 0, st>>>(states_of(b), b->inv.get(), SbGeom{b->d, b->dim_RR, b->inv_len}, bad.get(),
+                                                          count.get());
+  count_launch();
+  DG_CUDA(cudaGetLastError());
+  int h_bad = 0;
+  unsigned long long h_count = 0;
+  DG_CUDA(cudaMemcpyAsync(&h_bad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(&h_count, count.get(), sizeof(h_count), cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
+  b->inv_exact = h_bad == 0 && h_count == (unsigned long long)b->n;
+}
+
+// Expectation values may go through the density matrices: one sector with its own exact Inv table
+// and block structure, no signed term, the whole vector given (DG_SB_EXPECT_TRACE=0 turns it off).
+bool trace_form(const dg_sb_basis *b, const std::vector<SbTerm> &terms, long v_len) {
+  if (!b || !b->pairs || !b->inv_exact || v_len < b->n) return false;
+  const char *e = std::getenv("DG_SB_EXPECT_TRACE");
+  if (e && std::strcmp(e, "0") == 0) return false;
+  for (const SbTerm &t : terms)
+    if (t.sign) return false;
+  return true;
+}
+
+void launch_trace(const dg_sb_basis *b, const std::vector<SbTerm> &terms, const dg_sb_ops *ops, const double *v, const double *w0,
+                  const double *w1, double *dout, cudaStream_t st) {
+  const SbPairs &P = *b->pairs;
+  const PairView pv = pair_view(P);
+  bool rows[2] = {false, false}, cols[2] = {false, false};
+  std::vector<TraceTerm> tt;
+  for (const SbTerm &t : terms) {
+    (t.pos == DG_SB_LL || t.pos == DG_SB_LR ? rows : cols)[t.weight] = true;
+    tt.push_back(TraceTerm{t.row, t.pos, t.weight});
+  }
+  DevBuf<double> rho[2], sig[2];
+  const double *w[2] = {w0, w1};
+  for (int k = 0; k < 2; ++k) {
+    if (rows[k]) {
+      const int64_t total = P.rho_off[P.B];
+      rho[k].alloc(total);
+      k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, rho[k].get());
+      count_launch();
+      DG_CUDA(cudaGetLastError());
+    }
+    if (cols[k]) {
+      const int64_t total = P.sig_off[P.B];
+      sig[k].alloc(total);
+      k_gram_cols<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sig[k].get());
+      count_launch();
+      DG_CUDA(cudaGetLastError());
+    }
+  }
+  DevBuf<TraceTerm> dterms(tt.size());
+  DG_CUDA(cudaMemcpyAsync(dterms.get(), tt.data(), sizeof(TraceTerm) * tt.size(), cudaMemcpyHostToDevice, st));
+  k_sb_trace<<<(int)tt.size(), kThreads, 0, st>>>(pv, states_of(b), dterms.get(), ops->col.get(), ops->val.get(), rho[0].get(),
+                                                 rho[1].get(), sig[0].get(), sig[1].get(), dout);
+  count_launch();
+  DG_CUDA(cudaGetLastError());
+  DG_CUDA(cudaStreamSynchronize(st));   // dterms and the density matrices go out of scope
+}
+
+// out[t] for every term: sum over the states of w_{weight_t}[i] (O_t v)[i].  With one_sector (the
+// basis is both the output states and the Inv table) the density-matrix form is used when it applies.
 void launch_expect(const SbStates &S, const int *inv, const SbGeom &g, const std::vector<SbTerm> &terms, const dg_sb_ops *ops,
                    const SbParity &par, const double *v, long v_len, const double *w0, const double *w1, double *out_host, int *bad,
-                   cudaStream_t st) {
+                   cudaStream_t st, const dg_sb_basis *one_sector = nullptr) {
   const int nt = (int)terms.size();
   if (nt == 0) return;
   DG_REQUIRE(nt <= 65535, DG_ERR_ARG, "at most 65535 terms per call (got %d)", nt);
+  if (trace_form(one_sector, terms, v_len)) {
+    DevBuf<double> dout(nt);
+    launch_trace(one_sector, terms, ops, v, w0, w1, dout.get(), st);
+    DG_CUDA(cudaMemcpyAsync(out_host, dout.get(), sizeof(double) * nt, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    return;
+  }
   // enough chunks of states that the whole 2-D grid fills the device a few times over
   const long want = std::max(1L, ((long)sm_count() * 16 + nt - 1) / nt);
   const int gx = (int)std::max(1L, std::min(want, (S.n + kThreads - 1) / kThreads));
@@ -514,7 +744,9 @@ void expect_host(const HostSector &h, const std::vector<HostOp> &terms_h, const 
     launch_vm(S, s.b->inv.get(), s.g, term_of(s.ops.get(), op_index(s, all, t1_op->M), t1_op->pos, 0, 0), s.ops.get(), par, v, h.v_len,
               t1b.get(), bad.get(), st);
   }
-  launch_expect(S, s.b->inv.get(), s.g, terms, s.ops.get(), par, v, h.v_len, v, t1b.get(), Out, bad.get(), st);
+  if (h.dim_LL > 0) s.b->pairs = sb_pairs_from_states(h.n, h.st, h.dim_LL, h.dim_RR, h.d);
+  if (s.b->pairs) mark_inv_exact(s.b.get(), st);
+  launch_expect(S, s.b->inv.get(), s.g, terms, s.ops.get(), par, v, h.v_len, v, t1b.get(), Out, bad.get(), st, s.b.get());
   if (!terms.empty() && last_out) {
     launch_vm(S, s.b->inv.get(), s.g, terms.back(), s.ops.get(), par, v, h.v_len, lastb.get(), bad.get(), st);
     DG_CUDA(cudaMemcpyAsync(last_out, lastb.get(), sizeof(double) * h.n, cudaMemcpyDeviceToHost, st));
@@ -547,8 +779,11 @@ int dg_sb_basis_upload(int n, int dim_LL, int dim_RR, int dim_onsite, const shor
     DG_REQUIRE(n >= 0 && (n == 0 || (LL && LR && RR && RL)), DG_ERR_ARG, "null state arrays");
     coord_max(n, st, dims, mx);
     const long full = (long)dim_LL * dim_onsite * dim_RR * dim_onsite;
-    *out = states_upload(n, dim_LL, dim_RR, dim_onsite, st, inv, inv ? full : 0);
+    std::unique_ptr<dg_sb_basis> b(states_upload(n, dim_LL, dim_RR, dim_onsite, st, inv, inv ? full : 0));
+    b->pairs = sb_pairs_from_states(n, st, dim_LL, dim_RR, dim_onsite);
+    mark_inv_exact(b.get(), stream());
     DG_CUDA(cudaStreamSynchronize(stream()));
+    *out = b.release();
   });
 }
 
@@ -633,13 +868,14 @@ int dg_sb_expect(const dg_sb_basis *out_states, const dg_sb_basis *inv_table, co
     const double *dw0 = use[0] ? input_vec(w0, n, w0b, st) : nullptr;
     const double *dw1 = use[1] ? input_vec(w1, n, w1b, st) : nullptr;
     const SbGeom g{inv_table->d, inv_table->dim_RR, inv_table->inv_len};
-    launch_expect(states_of(out_states), inv_table->inv.get(), g, ts, ops, par.view(), dv, v_len, dw0, dw1, out, bad.get(), st);
+    launch_expect(states_of(out_states), inv_table->inv.get(), g, ts, ops, par.view(), dv, v_len, dw0, dw1, out, bad.get(), st,
+                  out_states == inv_table ? out_states : nullptr);
     check_bad(bad, st);
   });
 }
 
 // ---------------------------------------------------------------------------------
-// Reference entry points (include/dmrg.h:365-382, 347-348).
+// Reference entry points (include/dmrg.h:365-382, 360-361).
 // ---------------------------------------------------------------------------------
 #define DG_SB_RUN(who, body) sbvm_must(guarded([&] { body; }), who)
 
@@ -771,6 +1007,124 @@ void DMRG_EXPECTATION_INTERSITE_Q0(CRS1 **M_CF, CRS1 **M_LL, CRS1 *M_On, CRS1 **
   terms.push_back({M_On, DG_SB_RL, 0, 1});
   for (int site = RR_site; site >= 0; --site) terms.push_back({M_RR[site], DG_SB_RR, 0, 1});
   DG_SB_RUN("DMRG_EXPECTATION_INTERSITE_Q0", expect_host(q0_sector(B, S->dim_LLLRRRRL), terms, &t1, Vec, Out, Temp_V1, Temp_V2));
+}
+
+// ---------------------------------------------------------------------------------
+// Reduced density matrix of the LL+LR half.
+// ---------------------------------------------------------------------------------
+int dg_sb_density_info(const dg_sb_basis *b, int *n_blocks, int *n_pairs, long *n_entries) {
+  return guarded([&] {
+    DG_REQUIRE(b, DG_ERR_ARG, "null basis");
+    DG_REQUIRE(b->pairs, DG_ERR_ARG, "the basis states are not in the reference order (no block structure)");
+    if (n_blocks) *n_blocks = b->pairs->B;
+    if (n_pairs) *n_pairs = b->pairs->R;
+    if (n_entries) *n_entries = (long)b->pairs->rho_off[b->pairs->B];
+  });
+}
+
+int dg_sb_density_layout(const dg_sb_basis *b, int *pair_ll, int *pair_lr, int *block_start) {
+  return guarded([&] {
+    DG_REQUIRE(b && b->pairs, DG_ERR_ARG, "null basis or no block structure");
+    const SbPairs &P = *b->pairs;
+    if (pair_ll) std::copy(P.run_ll.begin(), P.run_ll.end(), pair_ll);
+    if (pair_lr) std::copy(P.run_lr.begin(), P.run_lr.end(), pair_lr);
+    if (block_start) std::copy(P.blk_run0.begin(), P.blk_run0.end(), block_start);
+  });
+}
+
+int dg_sb_density_matrix(const dg_sb_basis *b, const double *v, double *rho) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(b && b->pairs && v && rho, DG_ERR_ARG, "null argument or no block structure");
+    const SbPairs &P = *b->pairs;
+    cudaStream_t st = stream();
+    DevBuf<double> vb, ob;
+    const double *dv = input_vec(v, b->n, vb, st);
+    const int64_t total = P.rho_off[P.B];
+    const bool out_dev = is_device_ptr(rho);
+    double *dr = rho;
+    if (!out_dev) {
+      ob.alloc(total);
+      dr = ob.get();
+    }
+    k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pair_view(P), dv, dv, dr);
+    count_launch();
+    DG_CUDA(cudaGetLastError());
+    if (!out_dev) DG_CUDA(cudaMemcpyAsync(rho, dr, sizeof(double) * total, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+// include/dmrg.h:383 -- one block of the density matrix of the LLLR basis, as a newly allocated
+// row-pointer array (malloc per row, as GET_ARRAY_DOUBLE2 allocates, so FREE_ARRAY_DOUBLE2 frees it).
+double **DMRG_GET_DENSITY_MATRIX(int block, int *Dim_Block, DMRG_BASIS *B, double *Vec, int) {
+  const char *who = "DMRG_GET_DENSITY_MATRIX";
+  const int dim = Dim_Block[block];
+  const int dim_LLLR = B->dim_LLLR, dim_RR = B->dim_RR, d = B->dim_onsite;
+  std::vector<long> base_lllr((size_t)dim_LLLR + 1, 0);
+  for (int i = 0; i < dim_LLLR; ++i) base_lllr[i + 1] = base_lllr[i] + B->Sum_LLLR[i];
+  char msg[400];
+  if (base_lllr[dim_LLLR] != B->dim_LLLRRRRL) {
+    snprintf(msg, sizeof(msg), "Base_LLLR[%d] (%ld) != dim_LLLRRRRL (%d)", dim_LLLR, base_lllr[dim_LLLR], B->dim_LLLRRRRL);
+    sbvm_fatal(who, msg);
+  }
+  int base = 0;
+  for (int i = 0; i < block; ++i) base += Dim_Block[i];
+  double **M = static_cast<double **>(std::malloc(sizeof(double *) * std::max(dim, 1)));
+  if (!M) sbvm_fatal(who, "host allocation failed");
+  for (int r = 0; r < dim; ++r) {
+    M[r] = static_cast<double *>(std::calloc(std::max(dim, 1), sizeof(double)));
+    if (!M[r]) sbvm_fatal(who, "host allocation failed");
+  }
+  if (dim == 0) return M;
+  if (base + dim > dim_LLLR) {
+    snprintf(msg, sizeof(msg), "row_base (%d) >= dim_LLLR (%d)", base + dim - 1, dim_LLLR);
+    sbvm_fatal(who, msg);
+  }
+  const int Q = B->Sum_LLLR[base];
+  // X[row][t] = Vec[Inv(LL, LR of the row; RR, RL of its t-th state)], with the reference's checks
+  std::vector<double> X((size_t)dim * Q);
+  const long first = base_lllr[base];
+  for (int r = 0; r < dim; ++r) {
+    const int rb = base + r;
+    if (B->Sum_LLLR[rb] != Q) {
+      snprintf(msg, sizeof(msg), "Sum_LLLR[%d] (%d) != Sum_LLLR[%d] (%d)", base, Q, rb, B->Sum_LLLR[rb]);
+      sbvm_fatal(who, msg);
+    }
+    const int ll = B->LL_LLLR[rb], lr = B->LR_LLLR[rb];
+    for (int t = 0; t < Q; ++t) {
+      const long sr = base_lllr[rb] + t, s0 = first + t;
+      const int rr = B->RR_LLLRRRRL[sr], rl = B->RL_LLLRRRRL[sr];
+      if (rr != B->RR_LLLRRRRL[s0] || rl != B->RL_LLLRRRRL[s0]) {
+        snprintf(msg, sizeof(msg), "RR_row (%d) != RR_col (%d) || RL_row (%d) != RL_col (%d)", B->RR_LLLRRRRL[s0], rr,
+                 B->RL_LLLRRRRL[s0], rl);
+        sbvm_fatal(who, msg);
+      }
+      const long sup = (long)ll * d * dim_RR * d + (long)lr * dim_RR * d + (long)rr * d + rl;
+      const int inv = B->Inv_LLLRRRRL[sup];
+      if (inv < 0) {
+        snprintf(msg, sizeof(msg), "inv_row (%d) < 0", inv);
+        sbvm_fatal(who, msg);
+      }
+      X[(size_t)r * Q + t] = Vec[inv];
+    }
+  }
+  if (Q == 0) return M;
+  sbvm_must(guarded([&] {
+              require_device();
+              cudaStream_t st = stream();
+              DevBuf<double> dx(X.size()), dm((size_t)dim * dim);
+              DG_CUDA(cudaMemcpyAsync(dx.get(), X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, st));
+              k_gram_dense<<<(int)state_grid((long)dim * dim), kThreads, 0, st>>>(dx.get(), dim, Q, dm.get());
+              count_launch();
+              DG_CUDA(cudaGetLastError());
+              std::vector<double> h((size_t)dim * dim);
+              DG_CUDA(cudaMemcpyAsync(h.data(), dm.get(), sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+              DG_CUDA(cudaStreamSynchronize(st));
+              for (int r = 0; r < dim; ++r) std::memcpy(M[r], h.data() + (size_t)r * dim, sizeof(double) * dim);
+            }),
+            who);
+  return M;
 }
 
 }  // extern "C"

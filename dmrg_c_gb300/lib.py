@@ -132,6 +132,10 @@ SIGNATURES = {
     "dg_sb_basis_upload": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_short), P(C.c_short), P(C.c_short),
                                      P(C.c_short), ip, P(vp)]),
     "dg_sb_ops_create": (C.c_int, [C.c_int, P(P(CRS1)), ip, P(vp)]),
+    "dg_sb_density_info": (C.c_int, [vp, ip, ip, lp]),
+    "dg_sb_density_layout": (C.c_int, [vp, ip, ip, ip]),
+    "dg_sb_density_matrix": (C.c_int, [vp, vp, vp]),
+    "DMRG_GET_DENSITY_MATRIX": (P(dp), [C.c_int, ip, P(DMRG_BASIS), dp, C.c_int]),
     "dg_sb_ops_free": (None, [vp]),
     "dg_sb_vm": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, ip, ip, ip, vp, C.c_long, vp]),
     "dg_sb_expect": (C.c_int, [vp, vp, vp, C.c_int, P(abi.dg_sb_expect_term), ip, ip, ip, vp, C.c_long, vp, vp, dp]),

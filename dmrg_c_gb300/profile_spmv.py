@@ -212,6 +212,78 @@ def vm(repeats=10):
               f"({3 * n * 8 / t / 1e9:.1f} GB/s of host<->device vectors+basis)", flush=True)
 
 
+def observables(repeats=5, per_row=16):
+    """Site expectation values <psi|O_site|psi> over all 64 sites of the Hubbard L=64, m=512
+    superblock (half filling, 2Sz = 0): 31 block operators on each of LL and RR (conserving the
+    block labels, per_row elements a row) and one site operator on LR and RL.  Times the device
+    API (dg_sb_expect, every site in one launch, vector resident) and the drop-in
+    DMRG_EXPECTATION_ONSITE from host arrays (basis, Inv table, operators and vector uploaded,
+    Temp_V downloaded)."""
+    import ctypes as C
+    import time
+    import numpy as np
+    import scipy.sparse as sp
+    import torch
+    from . import abi, sb_models, workloads
+    qb = workloads._block_labels(512, 31, 31.0, 1.25, 0.9, 0)
+    qs = workloads.hubbard_site_labels()
+    b = L.SuperblockBasis(512, 512, 4, qb, qb, qs, 64 * workloads.QN_SCALE)
+    LL, LR, RR, RL, inv = b.download()
+    n = b.n
+    rng = np.random.default_rng(7)
+    n_block = 31
+    ops_LL = [sb_models._crs(sb_models._random_sym_op(qb, per_row, rng)) for _ in range(n_block)]
+    ops_RR = [sb_models._crs(sb_models._random_sym_op(qb, per_row, rng)) for _ in range(n_block)]
+    on = sb_models._crs(sp.csr_matrix(np.diag([0.0, 1.0, 1.0, 2.0])))
+    nnz_rows = np.mean([o.nnz / 512 for o in ops_LL])
+    v = rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    ops = L.BlockOperators(ops_LL + ops_RR + [on], [512] * (2 * n_block) + [4])
+    terms = ([(0, k, 0, 0) for k in range(n_block)] + [(1, 2 * n_block, 0, 0), (3, 2 * n_block, 0, 0)]
+             + [(2, n_block + k, 0, 0) for k in range(n_block - 1, -1, -1)])
+    vd = torch.from_numpy(v).cuda()
+    L.sb_expect(b, b, ops, terms, vd, vd)   # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        e_dev = L.sb_expect(b, b, ops, terms, vd, vd)
+    t_dev = (time.perf_counter() - t0) / repeats
+    import os
+    os.environ["DG_SB_EXPECT_TRACE"] = "0"
+    e_gat = L.sb_expect(b, b, ops, terms, vd, vd)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        e_gat = L.sb_expect(b, b, ops, terms, vd, vd)
+    t_gat = (time.perf_counter() - t0) / repeats
+    del os.environ["DG_SB_EXPECT_TRACE"]
+    print(f"observables hubbard m=512: n = {n}, {len(terms)} sites, ~{nnz_rows:.1f} elements per block-operator row", flush=True)
+    print(f"  dg_sb_expect, density-matrix form (Gram blocks + one trace launch): {t_dev * 1e3:.3f} ms per call "
+          f"({t_dev * 1e6 / len(terms):.1f} us per site)", flush=True)
+    print(f"  dg_sb_expect, per-state gather form (one launch + sum): {t_gat * 1e3:.3f} ms per call "
+          f"({t_gat * 1e6 / len(terms):.1f} us per site); max |difference| {np.abs(e_dev - e_gat).max():.2e}", flush=True)
+    # drop-in from host arrays
+    st = [np.ascontiguousarray(a) for a in (LL, LR, RR, RL)]
+    B = abi.DMRG_BASIS(LL_LLLRRRRL=abi.ptr(st[0], C.c_short), LR_LLLRRRRL=abi.ptr(st[1], C.c_short),
+                       RR_LLLRRRRL=abi.ptr(st[2], C.c_short), RL_LLLRRRRL=abi.ptr(st[3], C.c_short),
+                       Inv_LLLRRRRL=abi.ptr(inv, C.c_int), dim_LLLRRRRL=n, dim_LL=512, dim_RR=512, dim_onsite=4)
+    S = abi.DMRG_STATUS(LL_site=n_block - 1, RR_site=n_block - 1, dim_LLLRRRRL=n)
+    arr = lambda ops_: (C.POINTER(abi.CRS1) * len(ops_))(*[o.ref for o in ops_])   # noqa: E731
+    out = np.zeros(len(terms))
+    temp = np.zeros(n)
+    lib = L.load()
+    args = (arr(ops_LL), on.ref, arr(ops_RR), abi.ptr(out, C.c_double), abi.ptr(v, C.c_double), abi.ptr(temp, C.c_double), 1,
+            C.byref(B), C.byref(S))
+    lib.DMRG_EXPECTATION_ONSITE(*args)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        lib.DMRG_EXPECTATION_ONSITE(*args)
+    t_drop = (time.perf_counter() - t0) / repeats
+    print(f"  DMRG_EXPECTATION_ONSITE (host arrays, {inv.nbytes / 2**20:.0f} MiB Inv table uploaded): {t_drop * 1e3:.3f} ms per call",
+          flush=True)
+    print(f"  max |device - drop-in| = {np.abs(e_dev - out).max():.2e}", flush=True)
+
+
 def solvers(name, repeats=5):
     """Whole ground-state solves on one device-resident matrix with the solver forms side by side:
     Lanczos + inverse iteration with CG or with MINRES inner solves (FP64), and the two
@@ -285,6 +357,7 @@ def main(argv=None):
     ap.add_argument("--build", choices=BUILDS, default=None)
     ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
     ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
+    ap.add_argument("--obs", action="store_true", help="site expectation values on the Hubbard m=512 superblock")
     ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES), default=None,
                     help="solve times of the solver forms on one matrix")
     a = ap.parse_args(argv)
@@ -292,6 +365,8 @@ def main(argv=None):
         solvers(a.solvers)
     elif a.vm:
         vm()
+    elif a.obs:
+        observables()
     elif a.obc:
         obc_solve(a.obc)
     elif a.build:

@@ -109,9 +109,13 @@ void DMRG_V_M_RR_Q4(CRS1 *M_RR, int qn1_out, int qn2_out, int qn3_out, int qn4_o
 /* <Vec|O_site|Vec> for every site, and <O_origin Vec|O_site Vec> (the LL sites through the
  * correlation operators M_CF) in one device pass each.  Out within 1e-12 of the reference
  * (only the order of the final sums differs); Temp_V / Temp_V2 receive the last site's product
- * and Temp_V1 the origin's, as in the reference.         replace include/dmrg.h:347-348 */
+ * and Temp_V1 the origin's, as in the reference.         replace include/dmrg.h:360-361 */
 void DMRG_EXPECTATION_ONSITE(CRS1 **M_LL, CRS1 *M_On, CRS1 **M_RR, double *Out, double *Vec, double *Temp_V, int p_threads, DMRG_BASIS *Dmrg_Basis, DMRG_STATUS *Dmrg_Status);
 void DMRG_EXPECTATION_INTERSITE_Q0(CRS1 **M_CF, CRS1 **M_LL, CRS1 *M_On, CRS1 **M_RR, double *Out, int origin, double *Vec, double *Temp_V1, double *Temp_V2, int p_threads, DMRG_BASIS *Dmrg_Basis, DMRG_STATUS *Dmrg_Status);
+/* Block `block` of the LLLR density matrix (Dim_Block: the blocks' sizes; Dmrg_Basis's LLLR list,
+ * Sum_LLLR and superblock states), newly allocated row by row as GET_ARRAY_DOUBLE2 does; entries
+ * bitwise the reference's.                               replaces include/dmrg.h:383 */
+double **DMRG_GET_DENSITY_MATRIX(int block, int *Dim_Block, DMRG_BASIS *Dmrg_Basis, double *Vec, int p_threads);
 
 /* ------------------------------------------------------------------------------------
  * 2. Native status-returning API

@@ -130,6 +130,21 @@ int dg_sb_expect(const dg_sb_basis *out_states, const dg_sb_basis *inv_table, co
                  const dg_sb_expect_term *terms, const int *ele_LL, const int *ele_LR, const int *ele_RR, const double *v, long v_len,
                  const double *w0, const double *w1, double *out);
 
+/*
+ * Reduced density matrix of the LL+LR half of one sector (DMRG_GET_DENSITY_MATRIX,
+ * dmrg/DMRG_GET_DENSITY_MATRIX.c:6-107), for a basis whose states are in the reference's order
+ * (dg_sb_basis_build, or uploaded in that order).  The (LL, LR) pairs holding states come in
+ * blocks of one LL+LR label; block g has P_g pairs of Q_g states each, and its matrix is
+ *    rho_g[p][q] = sum_t v[state t of pair p] * v[state t of pair q]
+ * summed over t in order (bitwise the reference's entries).  rho holds the blocks one after the
+ * other, each P_g x P_g row-major.
+ */
+int dg_sb_density_info(const dg_sb_basis *b, int *n_blocks, int *n_pairs, long *n_entries);
+/* pair_ll[n_pairs], pair_lr[n_pairs] (the pairs in order), block_start[n_blocks+1] (first pair of each block). */
+int dg_sb_density_layout(const dg_sb_basis *b, int *pair_ll, int *pair_lr, int *block_start);
+/* v (the sector's vector) and rho (n_entries) may be host or device pointers. */
+int dg_sb_density_matrix(const dg_sb_basis *b, const double *v, double *rho);
+
 #ifdef __cplusplus
 }
 #endif

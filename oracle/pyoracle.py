@@ -365,6 +365,69 @@ def call_expectation_intersite_q0(lib, states, inv, dim_LL, dim_RR, d, M_CF, M_L
     return out, t1, t2
 
 
+def lllr_list(q_LL, q_site, states):
+    """The DMRG_BASIS LLLR list of a sector in the reference's order: every (LL, LR) pair sorted by
+    the label of LL+LR (then LL, LR), the number of superblock states of each pair (Sum_LLLR), the
+    pair labels and the block sizes of DMRG_GET_DENSITY_MATRIX_INFO_Q1 (runs of equal labels)."""
+    q_LL, q_site = np.asarray(q_LL, np.int64), np.asarray(q_site, np.int64)
+    d = len(q_site)
+    LL, LR = (x.ravel() for x in np.meshgrid(np.arange(len(q_LL)), np.arange(d), indexing="ij"))
+    lab = q_LL[LL] + q_site[LR]
+    order = np.lexsort((LR, LL, lab))
+    LL, LR, lab = LL[order], LR[order], lab[order]
+    cnt = np.zeros(len(q_LL) * d, np.int64)
+    np.add.at(cnt, np.asarray(states[0], np.int64) * d + np.asarray(states[1], np.int64), 1)
+    sums = cnt[LL * d + LR].astype(np.int32)
+    _, dim_block = np.unique(lab, return_counts=True)
+    return LL.astype(np.int16), LR.astype(np.int16), sums, lab, dim_block.astype(np.int32)
+
+
+def density_matrix_blocks(states, inv, d, dim_RR, v, lllr):
+    """DMRG_GET_DENSITY_MATRIX restated for every block (dmrg/DMRG_GET_DENSITY_MATRIX.c:36-100):
+    M[row][col] = sum over the row pair's states t of v[state t of row] * v[state t of col], the
+    sum taken in t order and rounded as written.  lllr = lllr_list(...)."""
+    LLl, LRl, sums, _, dim_block = lllr
+    base = np.concatenate([[0], np.cumsum(sums)])
+    out, b0 = [], 0
+    for dim in dim_block:
+        rows = np.arange(b0, b0 + dim)
+        Q = int(sums[b0])
+        X = np.zeros((dim, Q))
+        for t in range(Q):
+            s = base[rows] + t
+            sup = ((LLl[rows].astype(np.int64) * d + LRl[rows]) * dim_RR + states[2][s]) * d + states[3][s]
+            X[:, t] = v[inv[sup]]
+        M = np.zeros((dim, dim))
+        for t in range(Q):
+            M = M + X[:, t, None] * X[None, :, t]
+        out.append(M)
+        b0 += dim
+    return out
+
+
+def call_density_matrix(lib, states, inv, dim_LL, dim_RR, d, v, lllr, free):
+    """DMRG_GET_DENSITY_MATRIX of lib for every block; free(ptr) releases a row / the row array."""
+    LLl, LRl, sums, _, dim_block = lllr
+    st = [np.ascontiguousarray(a, np.int16) for a in states]
+    inv = np.ascontiguousarray(inv, np.int32)
+    LLl, LRl, sums, dim_block = (np.ascontiguousarray(a) for a in (LLl, LRl, sums, dim_block))
+    B = DMRG_BASIS(LL_LLLRRRRL=ptr(st[0], C.c_short), LR_LLLRRRRL=ptr(st[1], C.c_short), RR_LLLRRRRL=ptr(st[2], C.c_short),
+                   RL_LLLRRRRL=ptr(st[3], C.c_short), Inv_LLLRRRRL=ptr(inv, C.c_int), dim_LLLRRRRL=len(st[0]), dim_LL=dim_LL,
+                   dim_RR=dim_RR, dim_onsite=d, LL_LLLR=ptr(LLl, C.c_short), LR_LLLR=ptr(LRl, C.c_short), dim_LLLR=len(LLl),
+                   Sum_LLLR=ptr(sums, C.c_int))
+    v = np.ascontiguousarray(v, np.float64)
+    fn = lib.DMRG_GET_DENSITY_MATRIX
+    fn.restype = P(dp)
+    out = []
+    for blk, dim in enumerate(dim_block):
+        M = fn(blk, ptr(dim_block, C.c_int), C.byref(B), ptr(v, C.c_double), 1)
+        out.append(np.array([[M[r][c] for c in range(dim)] for r in range(dim)]).reshape(dim, dim))
+        for r in range(dim):
+            free(C.cast(M[r], C.c_void_p))
+        free(C.cast(M, C.c_void_p))
+    return out
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

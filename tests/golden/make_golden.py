@@ -201,6 +201,13 @@ def sb_obs_fixture():
         o, t1, t2 = po.call_expectation_intersite_q0(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, ops["CF"][origin:] if origin < len(ops["LL"]) else ops["CF"][:1],
                                                      ops["LL"], ops["On"], ops["RR"], origin, v)
         out.update({f"inter{origin}": o, f"inter{origin}_t1": t1, f"inter{origin}_t2": t2})
+    # DMRG_GET_DENSITY_MATRIX for every block of the target sector's LLLR list
+    import ctypes as C
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    lllr = po.lllr_list(p.q_LL, p.q_site, st)
+    blocks = po.call_density_matrix(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, v, lllr, libc.free)
+    out["dm_blocks"] = np.concatenate([b.ravel() for b in blocks])
     np.savez_compressed(HERE / "sb_obs.npz", **out)
 
 

@@ -163,3 +163,133 @@ def test_device_api_rejects_bad_input(gpu, big):
     e = gpu.superblock_states([np.zeros(0, np.int16)] * 4, p.dim_LL, p.dim_RR, p.d)
     assert gpu.sb_vm(e, inv_b, ops, 0, 0, v).shape == (0,)
     assert np.array_equal(gpu.sb_expect(e, inv_b, ops, [(0, 0, 0, 0)], v, np.zeros(0)), [0.0])
+
+
+def test_density_matrix_form_vs_oracle(gpu, oracle, big, monkeypatch):
+    """One sector with its own Inv table: the expectation values go through the reduced density
+    matrices of the LL+LR and RR+RL halves (a trace per term).  They agree with the oracle's
+    product-then-dot within 1e-12, and with the per-state gather form."""
+    p = big
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    b = gpu.superblock_states(st, p.dim_LL, p.dim_RR, p.d, inv=inv0)
+    nL, nR = len(p.ops["LL"]), len(p.ops["RR"])
+    ops_l = [*p.ops["LL"], *p.ops["RR"], p.ops["On"], *p.ops["CF"]]
+    rows = [p.dim_LL] * nL + [p.dim_RR] * nR + [p.d] + [p.dim_LL] * len(p.ops["CF"])
+    ops = gpu.BlockOperators(ops_l, rows)
+    rng = np.random.default_rng(8)
+    v = rng.standard_normal(b.n)
+    v /= np.linalg.norm(v)
+    w1 = oracle.sb_vm(st, inv0, p.dim_RR, p.d, p.ops["LL"][0], 0, v)
+    terms = ([(0, k, 0, 0) for k in range(nL)] + [(1, nL + nR, 0, 0), (3, nL + nR, 0, 1)]
+             + [(2, nL + k, 0, k % 2) for k in range(nR)] + [(0, nL + nR + 1 + k, 0, 1) for k in range(len(p.ops["CF"]))])
+    got = gpu.sb_expect(b, b, ops, terms, v, v, w1)
+    monkeypatch.setenv("DG_SB_EXPECT_TRACE", "0")
+    gathered = gpu.sb_expect(b, b, ops, terms, v, v, w1)
+    monkeypatch.delenv("DG_SB_EXPECT_TRACE")
+    assert not np.array_equal(_bits(got), _bits(gathered))      # the two forms really ran
+    for k, (pos, op, sign, w) in enumerate(terms):
+        y = oracle.sb_vm(st, inv0, p.dim_RR, p.d, ops_l[op], pos, v)
+        ww = (v, w1)[w]
+        want = np.dot(ww, y)
+        tol = 1e-12 * float(np.dot(np.abs(ww), np.abs(y))) + 1e-300
+        assert abs(got[k] - want) <= tol, (k, pos, got[k], want)
+        assert abs(gathered[k] - want) <= tol, (k, pos)
+    assert np.array_equal(_bits(got), _bits(gpu.sb_expect(b, b, ops, terms, v, v, w1)))   # reproducible
+
+
+def test_density_matrix_form_on_device_built_basis(gpu, oracle, big):
+    """The basis built on the device carries its block structure: the same values as above."""
+    p = big
+    b = gpu.SuperblockBasis(p.dim_LL, p.dim_RR, p.d, p.q_LL, p.q_RR, p.q_site, p.target)
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    ops_l = [p.ops["LL"][2], p.ops["RR"][3], p.ops["On"]]
+    ops = gpu.BlockOperators(ops_l, [p.dim_LL, p.dim_RR, p.d])
+    v = np.random.default_rng(9).standard_normal(b.n)
+    terms = [(0, 0, 0, 0), (2, 1, 0, 0), (1, 2, 0, 0), (3, 2, 0, 0)]
+    got = gpu.sb_expect(b, b, ops, terms, v, v)
+    for k, (pos, op, _, _) in enumerate(terms):
+        y = oracle.sb_vm(st, inv0, p.dim_RR, p.d, ops_l[op], pos, v)
+        assert abs(got[k] - np.dot(v, y)) <= 1e-12 * float(np.dot(np.abs(v), np.abs(y))), k
+
+
+def test_density_matrix_form_skips_unordered_states(gpu, oracle, big):
+    """States not in the reference's order (here: reversed) have no block structure; the values
+    still come out right (per-state form)."""
+    p = big
+    st = tuple(a[::-1].copy() for a in p.sectors[p.target])
+    inv = -np.ones_like(p.inv)
+    inv[p.sup(st)] = np.arange(len(st[0]), dtype=np.int32)
+    b = gpu.superblock_states(st, p.dim_LL, p.dim_RR, p.d, inv=inv)
+    ops = gpu.BlockOperators([p.ops["LL"][0], p.ops["RR"][0]], [p.dim_LL, p.dim_RR])
+    v = np.random.default_rng(10).standard_normal(b.n)
+    got = gpu.sb_expect(b, b, ops, [(0, 0, 0, 0), (2, 1, 0, 0)], v, v)
+    for k, (op, pos) in enumerate(((p.ops["LL"][0], 0), (p.ops["RR"][0], 2))):
+        y = oracle.sb_vm(st, inv, p.dim_RR, p.d, op, pos, v)
+        assert abs(got[k] - np.dot(v, y)) <= 1e-12 * float(np.dot(np.abs(v), np.abs(y))), k
+
+
+def test_expectation_dropin_takes_density_matrix_form(gpu, oracle, monkeypatch):
+    """DMRG_EXPECTATION_ONSITE on a reference-ordered basis goes through the density matrices
+    (its sums differ in the last bits from the per-state form; both match the reference)."""
+    p, g = _problem()
+    lib = gpu.load()
+    v = g["v"]
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    a, _ = oracle.call_expectation_onsite(lib, st, inv0, p.dim_LL, p.dim_RR, p.d, p.ops["LL"], p.ops["On"], p.ops["RR"], v)
+    monkeypatch.setenv("DG_SB_EXPECT_TRACE", "0")
+    b, _ = oracle.call_expectation_onsite(lib, st, inv0, p.dim_LL, p.dim_RR, p.d, p.ops["LL"], p.ops["On"], p.ops["RR"], v)
+    assert not np.array_equal(_bits(a), _bits(b))
+    tol = 1e-12 * float(np.dot(np.abs(v), np.abs(v))) * 10
+    assert np.allclose(a, g["onsite"], rtol=0, atol=tol) and np.allclose(b, g["onsite"], rtol=0, atol=tol)
+
+
+def _libc_free():
+    import ctypes as C
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    return libc.free
+
+
+def test_density_matrix_dropin_vs_reference_golden(gpu, oracle):
+    p, g = _problem()
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    lllr = oracle.lllr_list(p.q_LL, p.q_site, st)
+    blocks = oracle.call_density_matrix(gpu.load(), st, inv0, p.dim_LL, p.dim_RR, p.d, g["v"], lllr, _libc_free())
+    got = np.concatenate([b.ravel() for b in blocks])
+    assert np.array_equal(_bits(got), _bits(g["dm_blocks"]))
+
+
+def test_density_matrix_device_api_vs_oracle(gpu, oracle, big):
+    """dg_sb_density_matrix: every block of the pairs holding states, bitwise the oracle's."""
+    import ctypes as C
+    import torch
+    p = big
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    v = np.random.default_rng(12).standard_normal(len(st[0]))
+    lllr = oracle.lllr_list(p.q_LL, p.q_site, st)
+    want = oracle.density_matrix_blocks(st, inv0, p.d, p.dim_RR, v, lllr)
+    # the oracle's blocks restricted to pairs with states, in order
+    LLl, LRl, sums = lllr[0], lllr[1], lllr[2]
+    keep, b0 = [], 0
+    for M, dim in zip(want, lllr[4]):
+        live = np.flatnonzero(sums[b0:b0 + dim] > 0)
+        if len(live):
+            keep.append(M[np.ix_(live, live)])
+        b0 += dim
+    for b in (gpu.superblock_states(st, p.dim_LL, p.dim_RR, p.d, inv=inv0),
+              gpu.SuperblockBasis(p.dim_LL, p.dim_RR, p.d, p.q_LL, p.q_RR, p.q_site, p.target)):
+        nb, npair, ne = C.c_int(), C.c_int(), C.c_long()
+        gpu.check(gpu.load().dg_sb_density_info(b.h, C.byref(nb), C.byref(npair), C.byref(ne)))
+        assert nb.value == len(keep) and ne.value == sum(k.size for k in keep)
+        pll, plr, bs = np.empty(npair.value, np.int32), np.empty(npair.value, np.int32), np.empty(nb.value + 1, np.int32)
+        gpu.check(gpu.load().dg_sb_density_layout(b.h, pll.ctypes.data_as(C.POINTER(C.c_int)),
+                                                  plr.ctypes.data_as(C.POINTER(C.c_int)), bs.ctypes.data_as(C.POINTER(C.c_int))))
+        live = sums > 0
+        assert np.array_equal(pll, LLl[live]) and np.array_equal(plr, LRl[live])
+        rho = np.empty(ne.value)
+        gpu.check(gpu.load().dg_sb_density_matrix(b.h, C.c_void_p(v.ctypes.data), C.c_void_p(rho.ctypes.data)))
+        assert np.array_equal(_bits(rho), _bits(np.concatenate([k.ravel() for k in keep])))
+        vd = torch.from_numpy(v).cuda()
+        rd = torch.empty(ne.value, dtype=torch.float64, device="cuda")
+        gpu.check(gpu.load().dg_sb_density_matrix(b.h, C.c_void_p(vd.data_ptr()), C.c_void_p(rd.data_ptr())))
+        assert np.array_equal(_bits(rd.cpu().numpy()), _bits(rho))

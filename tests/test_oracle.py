@@ -278,3 +278,15 @@ def test_sb_expectation_matches_reference_golden(oracle):
         e = oracle.sb_expect(st, inv0, p.dim_RR, p.d, terms, v, [v, t1])
         ref = g[f"inter{origin}"][:len(terms)]
         assert np.allclose(e, ref, rtol=0, atol=1e-12 * scale), origin
+
+
+def test_density_matrix_matches_reference_golden(oracle):
+    """DMRG_GET_DENSITY_MATRIX restated (numpy, sums in the reference's order) equals the
+    reference's blocks bit for bit on the observable problem's target sector."""
+    p, g = _obs_problem()
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    lllr = oracle.lllr_list(p.q_LL, p.q_site, st)
+    blocks = oracle.density_matrix_blocks(st, inv0, p.d, p.dim_RR, g["v"], lllr)
+    got = np.concatenate([b.ravel() for b in blocks])
+    assert np.array_equal(got.view(np.int64), g["dm_blocks"].view(np.int64))
+    assert sum(b.shape[0] for b in blocks) == p.dim_LL * p.d
