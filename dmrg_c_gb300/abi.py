@@ -137,6 +137,19 @@ class WholeBasis:
         self.ref = C.pointer(self.struct)
 
 
+class CCS1(C.Structure):
+    """include/SML.h:43-54"""
+    _fields_ = [("max_val", C.c_long), ("max_col", C.c_int), ("row_dim", C.c_int), ("col_dim", C.c_int),
+                ("Col", c_long_p), ("Row", c_int_p), ("Val", c_double_p)]
+
+
+class DMRG_SYSTEM_INFO(C.Structure):
+    """include/dmrg.h:220-234"""
+    _fields_ = [("Trans_Matrix", C.POINTER(CCS1)), ("Trans_Matrix_Dagger", C.POINTER(CRS1)), ("tr_error", C.c_double),
+                ("Val_DM_Dist", c_double_p), ("sum_val_dm", C.c_double), ("dim_LLLR", C.c_int), ("dim_renorm", C.c_int),
+                ("Q_Number1", c_int_p), ("Q_Number2", c_int_p), ("Q_Number3", c_int_p)]
+
+
 class DMRG_STATUS(C.Structure):
     """include/dmrg.h:236-267"""
     _fields_ = [("BC", C.c_char * 1000), ("Enviro_Copy", C.c_char * 100), ("LL_site", C.c_int), ("RR_site", C.c_int),

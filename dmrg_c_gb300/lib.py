@@ -136,6 +136,9 @@ SIGNATURES = {
     "dg_sb_density_layout": (C.c_int, [vp, ip, ip, ip]),
     "dg_sb_density_matrix": (C.c_int, [vp, vp, vp]),
     "DMRG_GET_DENSITY_MATRIX": (P(dp), [C.c_int, ip, P(DMRG_BASIS), dp, C.c_int]),
+    "DMRG_GET_SYSTEM_INFO_Q1": (P(abi.DMRG_SYSTEM_INFO), [ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),
+    "DMRG_GET_SYSTEM_INFO_Q2": (P(abi.DMRG_SYSTEM_INFO), [ip, ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),
+    "DMRG_GET_SYSTEM_INFO_Q3": (P(abi.DMRG_SYSTEM_INFO), [ip, ip, ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),
     "dg_sb_ops_free": (None, [vp]),
     "dg_sb_vm": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.c_int, ip, ip, ip, vp, C.c_long, vp]),
     "dg_sb_expect": (C.c_int, [vp, vp, vp, C.c_int, P(abi.dg_sb_expect_term), ip, ip, ip, vp, C.c_long, vp, vp, dp]),

@@ -284,6 +284,62 @@ def observables(repeats=5, per_row=16):
     print(f"  max |device - drop-in| = {np.abs(e_dev - out).max():.2e}", flush=True)
 
 
+def truncation(repeats=3):
+    """DMRG_GET_SYSTEM_INFO_Q2 (density matrices, their eigen-decompositions, the cut and the
+    transformation matrix) on the largest superblocks of the Kondo-lattice m=128 and Hubbard m=512
+    runs, keeping m states: wall time per drop-in call from host arrays."""
+    import ctypes as C
+    import time
+    import numpy as np
+    from . import abi, sb_models, workloads
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    lib = L.load()
+    cases = (("klm m=128", workloads._block_labels(128, 11, 5.0, 0.95, 0.85, 0), workloads.klm_site_labels(), 12, 128),
+             ("hubbard m=512", workloads._block_labels(512, 31, 31.0, 1.25, 0.9, 0), workloads.hubbard_site_labels(), 64, 512))
+    for name, qb, qs, ne, m in cases:
+        d, dim = len(qs), len(qb)
+        st = sb_models.sector_states(qb, qb, qs, ne * workloads.QN_SCALE)
+        n = len(st[0])
+        inv = -np.ones(dim * d * dim * d, np.int32)
+        inv[((st[0].astype(np.int64) * d + st[1]) * dim + st[2]) * d + st[3]] = np.arange(n, dtype=np.int32)
+        # the LLLR list in the reference's order and its blocks
+        LL, LR = (x.ravel() for x in np.meshgrid(np.arange(dim), np.arange(d), indexing="ij"))
+        lab = np.asarray(qb, np.int64)[LL] + np.asarray(qs, np.int64)[LR]
+        o = np.lexsort((LR, LL, lab))
+        LL, LR, lab = LL[o].astype(np.int16), LR[o].astype(np.int16), lab[o]
+        cnt = np.zeros(dim * d, np.int64)
+        np.add.at(cnt, st[0].astype(np.int64) * d + st[1], 1)
+        sums = np.ascontiguousarray(cnt[LL.astype(np.int64) * d + LR], np.int32)
+        N = np.ascontiguousarray(np.rint(lab / workloads.QN_SCALE), np.int32)
+        sz = np.ascontiguousarray(lab - N * workloads.QN_SCALE, np.int32)
+        v = np.random.default_rng(5).standard_normal(n)
+        v /= np.linalg.norm(v)
+        sts = [np.ascontiguousarray(a) for a in st]
+        B = abi.DMRG_BASIS(LL_LLLRRRRL=abi.ptr(sts[0], C.c_short), LR_LLLRRRRL=abi.ptr(sts[1], C.c_short),
+                           RR_LLLRRRRL=abi.ptr(sts[2], C.c_short), RL_LLLRRRRL=abi.ptr(sts[3], C.c_short),
+                           Inv_LLLRRRRL=abi.ptr(inv, C.c_int), dim_LLLRRRRL=n, dim_LL=dim, dim_RR=dim, dim_onsite=d,
+                           LL_LLLR=abi.ptr(LL, C.c_short), LR_LLLR=abi.ptr(LR, C.c_short), dim_LLLR=dim * d,
+                           Sum_LLLR=abi.ptr(sums, C.c_int))
+        T = abi.DMRG_TIME()
+        blocks = np.unique(lab, return_counts=True)[1]
+        times = []
+        for it in range(repeats + 1):
+            t0 = time.perf_counter()
+            S = lib.DMRG_GET_SYSTEM_INFO_Q2(abi.ptr(N, C.c_int), abi.ptr(sz, C.c_int), C.byref(B), abi.ptr(v, C.c_double), m, 1,
+                                            C.byref(T)).contents
+            times.append(time.perf_counter() - t0)
+            kept, tr = S.dim_renorm, S.tr_error
+            for mat in (S.Trans_Matrix.contents, S.Trans_Matrix_Dagger.contents):
+                for a in (mat.Val, mat.Row, mat.Col):
+                    libc.free(C.cast(a, C.c_void_p))
+            for a in (S.Trans_Matrix, S.Trans_Matrix_Dagger, S.Val_DM_Dist, S.Q_Number1, S.Q_Number2, S.Q_Number3):
+                libc.free(C.cast(a, C.c_void_p))
+            libc.free(C.cast(C.pointer(S), C.c_void_p))
+        print(f"DMRG_GET_SYSTEM_INFO_Q2 {name}: n = {n}, {len(blocks)} density blocks (largest {blocks.max()}), kept {kept}, "
+              f"truncation error {tr:.3e}: {min(times[1:]) * 1e3:.2f} ms per call", flush=True)
+
+
 def solvers(name, repeats=5):
     """Whole ground-state solves on one device-resident matrix with the solver forms side by side:
     Lanczos + inverse iteration with CG or with MINRES inner solves (FP64), and the two
@@ -358,6 +414,7 @@ def main(argv=None):
     ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
     ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
     ap.add_argument("--obs", action="store_true", help="site expectation values on the Hubbard m=512 superblock")
+    ap.add_argument("--trunc", action="store_true", help="DMRG_GET_SYSTEM_INFO_Q2 on the KLM m=128 and Hubbard m=512 superblocks")
     ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES), default=None,
                     help="solve times of the solver forms on one matrix")
     a = ap.parse_args(argv)
@@ -367,6 +424,8 @@ def main(argv=None):
         vm()
     elif a.obs:
         observables()
+    elif a.trunc:
+        truncation()
     elif a.obc:
         obc_solve(a.obc)
     elif a.build:

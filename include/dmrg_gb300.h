@@ -116,6 +116,14 @@ void DMRG_EXPECTATION_INTERSITE_Q0(CRS1 **M_CF, CRS1 **M_LL, CRS1 *M_On, CRS1 **
  * Sum_LLLR and superblock states), newly allocated row by row as GET_ARRAY_DOUBLE2 does; entries
  * bitwise the reference's.                               replaces include/dmrg.h:383 */
 double **DMRG_GET_DENSITY_MATRIX(int block, int *Dim_Block, DMRG_BASIS *Dmrg_Basis, double *Vec, int p_threads);
+/* Truncation of the LL+LR block: density matrices and their eigen-decompositions on the device,
+ * the reference's ordering and cut rules, the kept eigenvectors as Trans_Matrix (CCS) and
+ * Trans_Matrix_Dagger (CRS), allocated so that DMRG_FREE_SYSTEM_INFO releases them.  Eigenvalues
+ * within ~1e-16 of LAPACK's, eigenvectors equal up to sign (and to a rotation inside a kept
+ * degenerate multiplet).                                replace include/dmrg.h:390-392 */
+DMRG_SYSTEM_INFO *DMRG_GET_SYSTEM_INFO_Q1(int *Q_Number, DMRG_BASIS *Dmrg_Basis, double *Vec, int max_dim, int p_threads, DMRG_TIME *Dmrg_Time);
+DMRG_SYSTEM_INFO *DMRG_GET_SYSTEM_INFO_Q2(int *Q_Number1, int *Q_Number2, DMRG_BASIS *Dmrg_Basis, double *Vec, int max_dim, int p_threads, DMRG_TIME *Dmrg_Time);
+DMRG_SYSTEM_INFO *DMRG_GET_SYSTEM_INFO_Q3(int *Q_Number1, int *Q_Number2, int *Q_Number3, DMRG_BASIS *Dmrg_Basis, double *Vec, int max_dim, int p_threads, DMRG_TIME *Dmrg_Time);
 
 /* ------------------------------------------------------------------------------------
  * 2. Native status-returning API

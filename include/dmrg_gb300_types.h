@@ -6,8 +6,10 @@
  * callers build.  The layouts below restate, field by field and in the same order:
  *
  *   CRS1, BOX_CG, BOX_II, BOX_LAN         include/SML.h:17-28, 56-65, 67-86, 122-135
+ *   CCS1                                  include/SML.h:43-54
  *   DMRG_PARAMETER, DMRG_TIME             include/dmrg.h:6-38, 40-51
  *   DMRG_BASIS, DMRG_STATUS               include/dmrg.h:54-99, 236-267
+ *   DMRG_SYSTEM_INFO                      include/dmrg.h:220-234
  *   DMRG_WHOLE_BASIS_Q1..Q4               include/dmrg.h:140-195
  *   DMRG_BOX_LAN, DMRG_BOX_CG, DMRG_BOX_II include/dmrg.h:269-328
  *   EXACT_PARAMETER, EXACT_TIME           include/exact.h:14-37, 39-51
@@ -38,6 +40,17 @@ typedef struct {
    long *Row;
    double *Val;
 } CRS1;
+
+/* Compressed column storage: Col has col_dim+1 int64 offsets, Row int32 rows. */
+typedef struct {
+   long max_val;
+   int max_col;
+   int row_dim;
+   int col_dim;
+   long *Col;
+   int *Row;
+   double *Val;
+} CCS1;
 
 typedef struct {
    CRS1 *M;
@@ -223,6 +236,21 @@ typedef struct {
    int param_iter;
    int tot_iter;
 } DMRG_STATUS;
+
+/* Truncation of the LL+LR block: the kept density-matrix eigenvectors as a CCS (LLLR x renorm)
+ * and its transpose as a CRS, the sorted spectrum, and the kept states' quantum numbers. */
+typedef struct {
+   CCS1 *Trans_Matrix;
+   CRS1 *Trans_Matrix_Dagger;
+   double tr_error;
+   double *Val_DM_Dist;
+   double sum_val_dm;
+   int dim_LLLR;
+   int dim_renorm;
+   int *Q_Number1;
+   int *Q_Number2;
+   int *Q_Number3;
+} DMRG_SYSTEM_INFO;
 
 typedef struct {
    double *Eig_Vec;

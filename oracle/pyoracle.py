@@ -428,6 +428,118 @@ def call_density_matrix(lib, states, inv, dim_LL, dim_RR, d, v, lllr, free):
     return out
 
 
+def system_info(qns, states, inv, d, dim_RR, v, lllr, max_dim):
+    """DMRG_GET_SYSTEM_INFO_Q<k> restated (dmrg/DMRG_GET_SYSTEM_INFO_Q1.c:8-213): the density
+    blocks (density_matrix_blocks), numpy's symmetric eigensolver in place of LAPACK's dsyev
+    (ascending values), a stable descending sort of all eigenvalues, the cut (max_dim, no cut
+    inside a degenerate multiplet, nothing at or below 1e-15), a stable sort of the kept states by
+    the quantum numbers qns (a list of per-pair arrays, primary first).  Returns a dict."""
+    blocks = density_matrix_blocks(states, inv, d, dim_RR, v, lllr)
+    dim_block = lllr[4]
+    starts = np.concatenate([[0], np.cumsum(dim_block)])
+    vals, vecs = zip(*[np.linalg.eigh(M) if len(M) else (np.zeros(0), np.zeros((0, 0))) for M in blocks])
+    items = [(g, i) for g in range(len(blocks)) for i in range(len(blocks[g]))]
+    order = sorted(range(len(items)), key=lambda e: -vals[items[e][0]][items[e][1]])   # stable
+    val = np.array([vals[items[e][0]][items[e][1]] for e in order])
+    dim_LLLR = len(val)
+    zero = 1e-15
+    dim_renorm = 0
+    if dim_LLLR <= max_dim:
+        for i in range(dim_LLLR, 0, -1):
+            if val[i - 1] > zero:
+                dim_renorm = i
+                break
+    else:
+        for i in range(max_dim, 0, -1):
+            if abs(val[i - 1] - val[i]) > zero and val[i - 1] > zero:
+                dim_renorm = i
+                break
+    kept = sorted(order[:dim_renorm], key=lambda e: tuple(int(q[starts[items[e][0]]]) for q in qns))
+    cols, rows, qn_out = [], [], [[] for _ in qns]
+    for e in kept:
+        g, i = items[e]
+        cols.append(vecs[g][:, i])
+        rows.append(np.arange(starts[g], starts[g + 1]))
+        for k, q in enumerate(qns):
+            qn_out[k].append(int(q[starts[g]]))
+    return dict(dim_renorm=dim_renorm, val=val, sum_val=float(np.sum(val)), tr_error=float(np.sum(val) - np.sum(val[:dim_renorm])),
+                qn=[np.array(x, np.int32) for x in qn_out], col_ptr=np.concatenate([[0], np.cumsum([len(r) for r in rows])]),
+                rows=np.concatenate(rows) if rows else np.zeros(0, int), vals=np.concatenate(cols) if cols else np.zeros(0))
+
+
+def call_system_info(lib, qns, states, inv, dim_LL, dim_RR, d, v, lllr, max_dim, free):
+    """DMRG_GET_SYSTEM_INFO_Q<len(qns)> of lib; returns the dict of system_info and releases the
+    structure as DMRG_FREE_SYSTEM_INFO does (free(ptr) on every array)."""
+    LLl, LRl, sums, _, dim_block = lllr
+    st = [np.ascontiguousarray(a, np.int16) for a in states]
+    inv = np.ascontiguousarray(inv, np.int32)
+    LLl, LRl, sums = (np.ascontiguousarray(a) for a in (LLl, LRl, sums))
+    q = [np.ascontiguousarray(a, np.int32) for a in qns]
+    B = DMRG_BASIS(LL_LLLRRRRL=ptr(st[0], C.c_short), LR_LLLRRRRL=ptr(st[1], C.c_short), RR_LLLRRRRL=ptr(st[2], C.c_short),
+                   RL_LLLRRRRL=ptr(st[3], C.c_short), Inv_LLLRRRRL=ptr(inv, C.c_int), dim_LLLRRRRL=len(st[0]), dim_LL=dim_LL,
+                   dim_RR=dim_RR, dim_onsite=d, LL_LLLR=ptr(LLl, C.c_short), LR_LLLR=ptr(LRl, C.c_short), dim_LLLR=len(LLl),
+                   Sum_LLLR=ptr(sums, C.c_int))
+    T = abi.DMRG_TIME()
+    v = np.ascontiguousarray(v, np.float64)
+    fn = getattr(lib, f"DMRG_GET_SYSTEM_INFO_Q{len(q)}")
+    fn.restype = P(abi.DMRG_SYSTEM_INFO)
+    S = fn(*[ptr(a, C.c_int) for a in q], C.byref(B), ptr(v, C.c_double), max_dim, 1, C.byref(T)).contents
+    n, dl = S.dim_renorm, S.dim_LLLR
+    TM, TD = S.Trans_Matrix.contents, S.Trans_Matrix_Dagger.contents
+    nnz = TM.Col[n]
+    out = dict(dim_renorm=n, val=np.array(S.Val_DM_Dist[:dl]), sum_val=S.sum_val_dm, tr_error=S.tr_error,
+               qn=[np.array(S.Q_Number1[:n], np.int32), np.array(S.Q_Number2[:n], np.int32), np.array(S.Q_Number3[:n], np.int32)][:len(q)],
+               col_ptr=np.array(TM.Col[:n + 1]), rows=np.array(TM.Row[:nnz]), vals=np.array(TM.Val[:nnz]),
+               d_row_ptr=np.array(TD.Row[:n + 1]), d_cols=np.array(TD.Col[:nnz]), d_vals=np.array(TD.Val[:nnz]),
+               shape=(TM.row_dim, TM.col_dim, TD.row_dim, TD.col_dim), time=T.make_dens_mat,
+               q2_sentinel=S.Q_Number2[0] if len(q) < 2 else None)
+    for m in (TM, TD):
+        for a in (m.Val, m.Row, m.Col):
+            free(C.cast(a, C.c_void_p))
+    free(C.cast(S.Trans_Matrix, C.c_void_p))
+    free(C.cast(S.Trans_Matrix_Dagger, C.c_void_p))
+    for a in (S.Val_DM_Dist, S.Q_Number1, S.Q_Number2, S.Q_Number3):
+        free(C.cast(a, C.c_void_p))
+    free(C.cast(C.pointer(S), C.c_void_p))
+    return out
+
+
+def same_truncation(a, b, tol_val=1e-13, tol_proj=1e-9):
+    """Two system_info results describe the same truncation: the same kept dimension, quantum
+    numbers and sparsity; spectra within tol_val; and, per block of equal quantum numbers, the
+    same kept subspace (projectors within tol_proj -- eigenvectors are fixed only up to sign and,
+    inside a degenerate multiplet, up to rotation).  Returns a list of differences (empty: same)."""
+    bad = []
+    tol_val = tol_val * max(1.0, abs(a["sum_val"]))
+    if a["dim_renorm"] != b["dim_renorm"]:
+        return [f"dim_renorm {a['dim_renorm']} != {b['dim_renorm']}"]
+    for k, (x, y) in enumerate(zip(a["qn"], b["qn"])):
+        if not np.array_equal(x, y):
+            bad.append(f"Q_Number{k + 1}")
+    if not (np.array_equal(a["col_ptr"], b["col_ptr"]) and np.array_equal(a["rows"], b["rows"])):
+        return bad + ["sparsity"]
+    if np.abs(a["val"] - b["val"]).max() > tol_val:
+        bad.append(f"spectrum {np.abs(a['val'] - b['val']).max():.2e}")
+    for key in ("sum_val", "tr_error"):
+        if abs(a[key] - b[key]) > tol_val:
+            bad.append(key)
+    n = a["dim_renorm"]
+    cp = a["col_ptr"]
+    j = 0
+    while j < n:
+        r0 = a["rows"][cp[j]]
+        j1 = j
+        while j1 < n and a["rows"][cp[j1]] == r0:
+            j1 += 1
+        dim = cp[j + 1] - cp[j]
+        Ta = np.stack([a["vals"][cp[c]:cp[c + 1]] for c in range(j, j1)], axis=1)
+        Tb = np.stack([b["vals"][cp[c]:cp[c + 1]] for c in range(j, j1)], axis=1)
+        if np.abs(Ta @ Ta.T - Tb @ Tb.T).max() > tol_proj or dim != Ta.shape[0]:
+            bad.append(f"subspace of the block at row {r0}")
+        j = j1
+    return bad
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

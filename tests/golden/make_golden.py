@@ -208,6 +208,20 @@ def sb_obs_fixture():
     lllr = po.lllr_list(p.q_LL, p.q_site, st)
     blocks = po.call_density_matrix(ref, st, inv0, p.dim_LL, p.dim_RR, p.d, v, lllr, libc.free)
     out["dm_blocks"] = np.concatenate([b.ravel() for b in blocks])
+    # DMRG_GET_SYSTEM_INFO_Q1 (packed labels) and _Q2 (N_e, 2Sz) at two kept dimensions, on the
+    # normalised vector (a ground state's): the cut at 1e-15 then sits far above the eigensolvers'
+    # rounding of the zero eigenvalues
+    vu = v / np.linalg.norm(v)
+    out["v_unit"] = vu
+    lab = lllr[3]
+    N = np.rint(lab / sb_models.QN_SCALE).astype(np.int32)
+    for tag, qns in (("q1", [lab.astype(np.int32)]), ("q2", [N, (lab - N * sb_models.QN_SCALE).astype(np.int32)])):
+        for max_dim in (20, 10000):
+            r = po.call_system_info(ref, qns, st, inv0, p.dim_LL, p.dim_RR, p.d, vu, lllr, max_dim, libc.free)
+            for k in ("dim_renorm", "val", "sum_val", "tr_error", "col_ptr", "rows", "vals"):
+                out[f"si_{tag}_{max_dim}_{k}"] = r[k]
+            for k, q in enumerate(r["qn"]):
+                out[f"si_{tag}_{max_dim}_qn{k}"] = q
     np.savez_compressed(HERE / "sb_obs.npz", **out)
 
 

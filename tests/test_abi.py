@@ -44,7 +44,8 @@ def test_python_signatures_cover_headers():
 STRUCTS = ["CRS1", "BOX_CG", "BOX_II", "BOX_LAN", "DMRG_PARAMETER", "DMRG_TIME", "DMRG_BASIS", "DMRG_STATUS",
            "DMRG_BOX_LAN", "DMRG_BOX_CG", "DMRG_BOX_II", "EXACT_PARAMETER", "EXACT_TIME", "EXACT_HAM_INFO",
            "EXACT_BASIS_INFO", "EXACT_WHOLE_BASIS_Q1", "EXACT_WHOLE_BASIS_Q2", "EXACT_WHOLE_BASIS_Q3",
-           "DMRG_WHOLE_BASIS_Q1", "DMRG_WHOLE_BASIS_Q2", "DMRG_WHOLE_BASIS_Q3", "DMRG_WHOLE_BASIS_Q4"]
+           "DMRG_WHOLE_BASIS_Q1", "DMRG_WHOLE_BASIS_Q2", "DMRG_WHOLE_BASIS_Q3", "DMRG_WHOLE_BASIS_Q4", "CCS1",
+           "DMRG_SYSTEM_INFO"]
 
 
 def c_layout(tmp_path: Path, include_dirs, header):

@@ -290,3 +290,30 @@ def test_density_matrix_matches_reference_golden(oracle):
     got = np.concatenate([b.ravel() for b in blocks])
     assert np.array_equal(got.view(np.int64), g["dm_blocks"].view(np.int64))
     assert sum(b.shape[0] for b in blocks) == p.dim_LL * p.d
+
+
+def _golden_system_info(g, tag, max_dim):
+    pre = f"si_{tag}_{max_dim}_"
+    nq = 1 if tag == "q1" else 2
+    return dict(dim_renorm=int(g[pre + "dim_renorm"]), val=g[pre + "val"], sum_val=float(g[pre + "sum_val"]),
+                tr_error=float(g[pre + "tr_error"]), col_ptr=g[pre + "col_ptr"], rows=g[pre + "rows"], vals=g[pre + "vals"],
+                qn=[g[pre + f"qn{k}"] for k in range(nq)])
+
+
+def _system_info_qns(p, lllr, tag):
+    lab = lllr[3]
+    N = np.rint(lab / 1000).astype(np.int32)
+    return [lab.astype(np.int32)] if tag == "q1" else [N, (lab - N * 1000).astype(np.int32)]
+
+
+@pytest.mark.parametrize("tag", ["q1", "q2"])
+@pytest.mark.parametrize("max_dim", [20, 10000])
+def test_system_info_matches_reference_golden(oracle, tag, max_dim):
+    """DMRG_GET_SYSTEM_INFO_Q1 / _Q2 restated (numpy's eigensolver for LAPACK's): the same kept
+    dimension, quantum numbers and sparsity as the reference, spectra within 1e-13 * |v|^2 and
+    the same kept subspace in every block."""
+    p, g = _obs_problem()
+    st, inv0 = p.sectors[p.target], p.inv_sector(p.target)
+    lllr = oracle.lllr_list(p.q_LL, p.q_site, st)
+    got = oracle.system_info(_system_info_qns(p, lllr, tag), st, inv0, p.d, p.dim_RR, g["v_unit"], lllr, max_dim)
+    assert oracle.same_truncation(got, _golden_system_info(g, tag, max_dim)) == []
