@@ -25,14 +25,16 @@
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace dg {
 namespace {
 
-constexpr int kJacobiMaxN = 1024;    // largest density block
-constexpr int kJacobiSmemN = 160;    // blocks up to this size keep their matrix in shared memory
+constexpr int kJacobiMaxN = 1024;    // bound of the per-round rotation arrays
 constexpr int kJacobiSweeps = 60;    // cap on sweeps (convergence takes ~6-10)
+constexpr size_t kJacobiSmem = 200 * 1024;   // dynamic shared memory a CTA may take for its rows
 
 struct GramBlk {
   int64_t x_off, a_off;   // X_g (P x Q, row-major) and rho_g (P x P) offsets
@@ -76,47 +78,77 @@ struct EigBlk {
   int n;
 };
 
-// Cyclic Jacobi on every block: A_g -> diag (eigenvalues in W), V_g's columns the eigenvectors.
-// A sweep is m-1 rounds (m = n rounded up to even) of the round-robin pairing; the m/2 disjoint
-// rotations of a round are applied together: rows p, q of A, then columns p, q of A and V.  The
-// sweep loop stops when the off-diagonal part is below 1e-16 of the Frobenius norm, or after
-// max_sweeps (sweeps[g] reports the count).
-__global__ void __launch_bounds__(kThreads) k_jacobi(const EigBlk *__restrict__ blks, double *__restrict__ Ag, double *__restrict__ Vg,
-                                                    double *__restrict__ Wg, int smem_n, int max_sweeps, int *__restrict__ sweeps) {
-  extern __shared__ double sm_a[];
+// Cyclic Jacobi on every block, one thread-block cluster of cs CTAs a block: A_g -> diag
+// (eigenvalues in W), V_g's columns the eigenvectors.  CTA c keeps rows [c*rp, (c+1)*rp) of A_g and
+// V_g in its shared memory (rp = ceil(n / cs)), so a block's FP64 work spreads over cs SMs.  A sweep
+// is m-1 rounds (m = n rounded up to even) of the round-robin pairing; in a round the m/2 disjoint
+// rotations are applied together:
+//   1. every CTA computes every rotation from A[p][p], A[q][q], A[p][q] (read from their owners);
+//   2. rows p, q of A are rotated by the owner of row p (row q through distributed shared memory);
+//   3. columns p, q of A and V are rotated by every CTA in its own rows; A[p][q] = A[q][p] = 0.
+// Cluster barriers separate the steps.  The sweep loop stops when the off-diagonal part is below
+// 1e-16 of the Frobenius norm (the decision is taken by CTA 0 and broadcast, so every CTA leaves
+// together), or after max_sweeps (sweeps[g] reports the count).  Blocks are in descending size.
+__global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__restrict__ blks, const double *__restrict__ Ag,
+                                                            double *__restrict__ Vg, double *__restrict__ Wg, int max_sweeps,
+                                                            int *__restrict__ sweeps) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int cs = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ double sm_jac[];
   __shared__ double rc[kJacobiMaxN / 2], rs[kJacobiMaxN / 2];
-  __shared__ int rp[kJacobiMaxN / 2], rq[kJacobiMaxN / 2];
+  __shared__ int rp_[kJacobiMaxN / 2], rq_[kJacobiMaxN / 2], own[kJacobiMaxN / 2];
+  __shared__ int n_own;
+  __shared__ double s_part[2 * 16];
   __shared__ int s_done;
-  const EigBlk b = blks[blockIdx.x];
+  const EigBlk b = blks[blockIdx.x / cs];
   const int n = b.n;
-  if (n <= 0) {
-    if (threadIdx.x == 0) sweeps[blockIdx.x] = 0;
-    return;
+  if (n <= 0) return;   // the whole cluster sees the same block
+  const int rows = (n + cs - 1) / cs;
+  const int r0 = rank * rows, r1 = min(n, r0 + rows), nloc = max(0, r1 - r0);
+  double *A = sm_jac;                          // rows x n
+  double *V = sm_jac + (int64_t)rows * n;      // rows x n
+  for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
+    const int64_t i = r0 + e / n, j = e % n;
+    A[e] = Ag[b.off + i * n + j];
+    V[e] = i == j ? 1.0 : 0.0;
   }
-  const int64_t nn = (int64_t)n * n;
-  double *A = Ag + b.off;
-  if (n <= smem_n) {
-    for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) sm_a[e] = A[e];
-    A = sm_a;
-  }
-  double *V = Vg + b.off;
-  for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) V[e] = (e / n == e % n) ? 1.0 : 0.0;
-  __syncthreads();
+  auto row_ptr = [&](int i) -> double * {   // row i of A, in whichever CTA keeps it
+    double *base = cluster.map_shared_rank(sm_jac, i / rows);
+    return base + (int64_t)(i % rows) * n;
+  };
+  cluster.sync();
   const int m = n + (n & 1), half = m / 2;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     double off = 0.0, tot = 0.0;
-    for (int64_t e = threadIdx.x; e < nn; e += blockDim.x) {
+    for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
       const double a = A[e];
       tot += a * a;
-      if (e / n != e % n) off += a * a;
+      if (r0 + e / n != e % n) off += a * a;
     }
     off = block_sum(off);
     tot = block_sum(tot);
-    if (threadIdx.x == 0) s_done = off <= 1e-32 * tot;
-    __syncthreads();
+    if (threadIdx.x == 0) {
+      double *p0 = cluster.map_shared_rank(s_part, 0);
+      p0[2 * rank] = off;
+      p0[2 * rank + 1] = tot;
+    }
+    cluster.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+      double o = 0.0, t = 0.0;
+      for (int c = 0; c < cs; ++c) {
+        o += s_part[2 * c];
+        t += s_part[2 * c + 1];
+      }
+      const int done = o <= 1e-32 * t;
+      for (int c = 0; c < cs; ++c) *cluster.map_shared_rank(&s_done, c) = done;
+    }
+    cluster.sync();
     if (s_done) break;
     for (int r = 0; r < m - 1; ++r) {
+      // 1. the rotations of this round
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p, q;
         if (k == 0) {
@@ -133,9 +165,10 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const EigBlk *__restrict__ 
         }
         double c = 1.0, s = 0.0;
         if (q < n) {
-          const double apq = A[(int64_t)p * n + q];
+          const double *rowp = row_ptr(p), *rowq = row_ptr(q);
+          const double apq = rowp[q];
           if (apq != 0.0) {
-            const double th = (A[(int64_t)q * n + q] - A[(int64_t)p * n + p]) / (2.0 * apq);
+            const double th = (rowq[q] - rowp[p]) / (2.0 * apq);
             const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
             c = 1.0 / sqrt(t * t + 1.0);
             s = t * c;
@@ -143,27 +176,35 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const EigBlk *__restrict__ 
         }
         rc[k] = c;
         rs[k] = s;
-        rp[k] = p;
-        rq[k] = q;
+        rp_[k] = p;
+        rq_[k] = q;
       }
       __syncthreads();
-      for (int idx = threadIdx.x; idx < half * n; idx += blockDim.x) {   // rows p, q of A
-        const int k = idx / n, j = idx - k * n;
-        const double s = rs[k];
-        if (s == 0.0) continue;
-        const double c = rc[k];
-        double *ap = A + (int64_t)rp[k] * n + j, *aq = A + (int64_t)rq[k] * n + j;
+      if (threadIdx.x == 0) {   // the rotations whose row p this CTA keeps
+        int cnt = 0;
+        for (int k = 0; k < half; ++k)
+          if (rs[k] != 0.0 && rp_[k] >= r0 && rp_[k] < r1) own[cnt++] = k;
+        n_own = cnt;
+      }
+      cluster.sync();   // every CTA has read the old entries
+      // 2. rows p, q of A
+      for (int idx = threadIdx.x; idx < n_own * n; idx += blockDim.x) {
+        const int k = own[idx / n], j = idx % n;
+        const double c = rc[k], s = rs[k];
+        double *ap = A + (int64_t)(rp_[k] - r0) * n + j;
+        double *aq = row_ptr(rq_[k]) + j;
         const double x = *ap, y = *aq;
         *ap = c * x - s * y;
         *aq = s * x + c * y;
       }
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < half * n; idx += blockDim.x) {   // columns p, q of A and V
+      cluster.sync();   // rows done everywhere
+      // 3. columns p, q of A and V in this CTA's rows
+      for (int idx = threadIdx.x; idx < nloc * half; idx += blockDim.x) {
         const int i = idx / half, k = idx - i * half;
         const double s = rs[k];
         if (s == 0.0) continue;
         const double c = rc[k];
-        const int p = rp[k], q = rq[k];
+        const int p = rp_[k], q = rq_[k];
         double *a = A + (int64_t)i * n, *v = V + (int64_t)i * n;
         const double x = a[p], y = a[q];
         a[p] = c * x - s * y;
@@ -175,14 +216,16 @@ __global__ void __launch_bounds__(kThreads) k_jacobi(const EigBlk *__restrict__ 
       __syncthreads();
       for (int k = threadIdx.x; k < half; k += blockDim.x)
         if (rs[k] != 0.0) {
-          A[(int64_t)rp[k] * n + rq[k]] = 0.0;
-          A[(int64_t)rq[k] * n + rp[k]] = 0.0;
+          const int p = rp_[k], q = rq_[k];
+          if (p >= r0 && p < r1) A[(int64_t)(p - r0) * n + q] = 0.0;
+          if (q >= r0 && q < r1) A[(int64_t)(q - r0) * n + p] = 0.0;
         }
-      __syncthreads();
+      cluster.sync();   // the round is complete everywhere
     }
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) Wg[b.woff + i] = A[(int64_t)i * n + i];
-  if (threadIdx.x == 0) sweeps[blockIdx.x] = sweep;
+  for (int i = threadIdx.x; i < nloc; i += blockDim.x) Wg[b.woff + r0 + i] = A[(int64_t)i * n + r0 + i];
+  for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) Vg[b.off + (int64_t)r0 * n + e] = V[e];
+  if (rank == 0 && threadIdx.x == 0) sweeps[blockIdx.x / cs] = sweep;
 }
 
 [[noreturn]] void fatal(const char *who, const char *msg) {
@@ -241,7 +284,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
   std::vector<EigBlk> eb(nb);
   std::vector<int64_t> a_pre(nb + 1, 0);
   int64_t xs = 0, woff = 0;
-  int max_n = 0, max_small = 0;
+  int max_n = 0;
   for (int g = 0; g < nb; ++g) {
     const int P = blk_start[g + 1] - blk_start[g], Q = B->Sum_LLLR[blk_start[g]];
     gb[g] = GramBlk{xs, a_pre[g], P, Q};
@@ -250,7 +293,6 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     xs += (int64_t)P * Q;
     woff += P;
     max_n = std::max(max_n, P);
-    if (P <= kJacobiSmemN) max_small = std::max(max_small, P);
   }
   if (max_n > kJacobiMaxN) {
     snprintf(msg, sizeof(msg), "a density-matrix block of %d pairs exceeds %d", max_n, kJacobiMaxN);
@@ -296,7 +338,6 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     DevBuf<int> dsw(nb);
     DG_CUDA(cudaMemcpyAsync(dX.get(), X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemcpyAsync(dgb.get(), gb.data(), sizeof(GramBlk) * nb, cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(deb.get(), eb.data(), sizeof(EigBlk) * nb, cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemcpyAsync(dpre.get(), a_pre.data(), sizeof(int64_t) * (nb + 1), cudaMemcpyHostToDevice, st));
     const int64_t total = a_pre[nb];
     if (total > 0) {
@@ -305,17 +346,45 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
-    const size_t smem = sizeof(double) * (size_t)max_small * max_small;
-    DG_CUDA(cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_jacobi<<<nb, kThreads, smem, st>>>(deb.get(), dA.get(), dV.get(), dW.get(), kJacobiSmemN, kJacobiSweeps, dsw.get());
+    // one cluster a block, the largest blocks first; 8 CTAs a cluster (16 when a block's rows
+    // would not fit 8 CTAs' shared memory)
+    int cs = 8;
+    auto smem_for = [&](int c) { return 2 * sizeof(double) * (size_t)((max_n + c - 1) / c) * max_n; };
+    if (smem_for(cs) > kJacobiSmem) cs = 16;
+    DG_REQUIRE(smem_for(cs) <= kJacobiSmem, DG_ERR_ARG, "a density block of %d pairs is too large for the eigensolver", max_n);
+    const size_t smem = smem_for(cs);
+    std::vector<int> by_size(nb);
+    std::iota(by_size.begin(), by_size.end(), 0);
+    std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) { return eb[a].n > eb[b].n; });
+    std::vector<EigBlk> eb_sorted(nb);
+    for (int i = 0; i < nb; ++i) eb_sorted[i] = eb[by_size[i]];
+    DG_CUDA(cudaMemcpyAsync(deb.get(), eb_sorted.data(), sizeof(EigBlk) * nb, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemsetAsync(dsw.get(), 0, sizeof(int) * nb, st));
+    DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (cs > 8) DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)(nb * cs));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
+                               kJacobiSweeps, dsw.get()));
     count_launch();
     DG_CUDA(cudaGetLastError());
     DG_CUDA(cudaMemcpyAsync(W.data(), dW.get(), sizeof(double) * W.size(), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaMemcpyAsync(Vh.data(), dV.get(), sizeof(double) * Vh.size(), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaMemcpyAsync(sweeps.data(), dsw.get(), sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
-    for (int g = 0; g < nb; ++g)
-      DG_REQUIRE(sweeps[g] < kJacobiSweeps, DG_ERR_CUDA, "the Jacobi eigensolver did not converge on block %d", g);
+    for (int i = 0; i < nb; ++i)
+      DG_REQUIRE(sweeps[i] < kJacobiSweeps, DG_ERR_CUDA, "the Jacobi eigensolver did not converge on block %d", by_size[i]);
   });
   if (rc != DG_OK) {
     snprintf(msg, sizeof(msg), "GPU path failed (status %d): %s", rc, dg_last_error());
