@@ -21,6 +21,7 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -79,16 +80,20 @@ struct EigBlk {
 };
 
 // Cyclic Jacobi on every block, one thread-block cluster of cs CTAs a block: A_g -> diag
-// (eigenvalues in W), V_g's columns the eigenvectors.  CTA c keeps rows [c*rp, (c+1)*rp) of A_g and
-// V_g in its shared memory (rp = ceil(n / cs)), so a block's FP64 work spreads over cs SMs.  A sweep
-// is m-1 rounds (m = n rounded up to even) of the round-robin pairing; in a round the m/2 disjoint
-// rotations are applied together:
-//   1. every CTA computes every rotation from A[p][p], A[q][q], A[p][q] (read from their owners);
-//   2. rows p, q of A are rotated by the owner of row p (row q through distributed shared memory);
-//   3. columns p, q of A and V are rotated by every CTA in its own rows; A[p][q] = A[q][p] = 0.
-// Cluster barriers separate the steps.  The sweep loop stops when the off-diagonal part is below
-// 1e-16 of the Frobenius norm (the decision is taken by CTA 0 and broadcast, so every CTA leaves
-// together), or after max_sweeps (sweeps[g] reports the count).  Blocks are in descending size.
+// (eigenvalues in W), V_g's columns the eigenvectors.  CTA c keeps rows [c*rp, (c+1)*rp) of A_g (two
+// copies: the current one and the next) and of V_g in its shared memory (rp = ceil(n / cs)), so a
+// block's FP64 work spreads over cs SMs.  A sweep is m-1 rounds (m = n rounded up to even) of the
+// round-robin pairing; a round applies its m/2 disjoint rotations J at once, A' = J^T A J:
+//   1. every CTA computes every rotation of the round from the current A (A[p][p], A[q][q],
+//      A[p][q], read from the CTAs keeping those rows);
+//   2. every CTA writes its rows of A' into the next copy -- row i of A' needs row i and the row
+//      paired with i (read through distributed shared memory when another CTA keeps it) -- and
+//      rotates the columns of its rows of V in place;
+//   3. one cluster barrier, after which the copies swap.
+// Entries at or below 1e-18 of the Frobenius norm are not rotated away.  The sweep loop stops when
+// the off-diagonal part is below 1e-16 of the norm or a sweep found nothing to rotate (decided by
+// CTA 0 and broadcast, so every CTA leaves together), or after max_sweeps (sweeps[g] reports the
+// count).  Blocks are in descending size.
 __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__restrict__ blks, const double *__restrict__ Ag,
                                                             double *__restrict__ Vg, double *__restrict__ Wg, int max_sweeps,
                                                             int *__restrict__ sweeps) {
@@ -98,30 +103,34 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
   const int rank = (int)cluster.block_rank();
   extern __shared__ double sm_jac[];
   __shared__ double rc[kJacobiMaxN / 2], rs[kJacobiMaxN / 2];
-  __shared__ int rp_[kJacobiMaxN / 2], rq_[kJacobiMaxN / 2], own[kJacobiMaxN / 2];
-  __shared__ int n_own;
+  __shared__ int rp_[kJacobiMaxN / 2], rq_[kJacobiMaxN / 2];
+  __shared__ int pair_of[kJacobiMaxN];   // the round's pair of each index
   __shared__ double s_part[2 * 16];
-  __shared__ int s_done;
+  __shared__ int s_done, s_rot;
+  __shared__ double s_tol;
   const EigBlk b = blks[blockIdx.x / cs];
   const int n = b.n;
   if (n <= 0) return;   // the whole cluster sees the same block
   const int rows = (n + cs - 1) / cs;
   const int r0 = rank * rows, r1 = min(n, r0 + rows), nloc = max(0, r1 - r0);
-  double *A = sm_jac;                          // rows x n
-  double *V = sm_jac + (int64_t)rows * n;      // rows x n
+  const int64_t slab = (int64_t)rows * n;
+  double *V = sm_jac + 2 * slab;
   for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
     const int64_t i = r0 + e / n, j = e % n;
-    A[e] = Ag[b.off + i * n + j];
+    sm_jac[e] = Ag[b.off + i * n + j];
     V[e] = i == j ? 1.0 : 0.0;
   }
-  auto row_ptr = [&](int i) -> double * {   // row i of A, in whichever CTA keeps it
-    double *base = cluster.map_shared_rank(sm_jac, i / rows);
-    return base + (int64_t)(i % rows) * n;
+  int cur = 0;   // the copy holding the current A
+  auto row_ptr = [&](int i) -> const double * {   // row i of the current A, in whichever CTA keeps it
+    const double *base = cluster.map_shared_rank(sm_jac, i / rows);
+    return base + cur * slab + (int64_t)(i % rows) * n;
   };
+  if (threadIdx.x == 0) s_rot = 1;
   cluster.sync();
   const int m = n + (n & 1), half = m / 2;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
+    const double *A = sm_jac + cur * slab;
     double off = 0.0, tot = 0.0;
     for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
       const double a = A[e];
@@ -142,13 +151,21 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
         o += s_part[2 * c];
         t += s_part[2 * c + 1];
       }
-      const int done = o <= 1e-32 * t;
-      for (int c = 0; c < cs; ++c) *cluster.map_shared_rank(&s_done, c) = done;
+      // done when the off-diagonal part is negligible, or when the last sweep found nothing to
+      // rotate (every |A[p][q]| at or below 1e-18 of the norm; every CTA computes every rotation)
+      const int done = o <= 1e-32 * t || !s_rot;
+      const double tol = 1e-18 * sqrt(t);
+      for (int c = 0; c < cs; ++c) {
+        *cluster.map_shared_rank(&s_done, c) = done;
+        *cluster.map_shared_rank(&s_tol, c) = tol;
+      }
     }
     cluster.sync();
     if (s_done) break;
+    if (threadIdx.x == 0) s_rot = 0;   // each CTA flags the rotations it computes (all CTAs compute all)
+    __syncthreads();
     for (int r = 0; r < m - 1; ++r) {
-      // 1. the rotations of this round
+      // 1. the rotations of this round (every CTA computes all of them)
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p, q;
         if (k == 0) {
@@ -165,64 +182,68 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
         }
         double c = 1.0, s = 0.0;
         if (q < n) {
-          const double *rowp = row_ptr(p), *rowq = row_ptr(q);
+          const double *rowp = row_ptr(p);
           const double apq = rowp[q];
-          if (apq != 0.0) {
-            const double th = (rowq[q] - rowp[p]) / (2.0 * apq);
+          if (fabs(apq) > s_tol) {
+            const double th = (row_ptr(q)[q] - rowp[p]) / (2.0 * apq);
             const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
             c = 1.0 / sqrt(t * t + 1.0);
             s = t * c;
+            s_rot = 1;
           }
+          pair_of[q] = k;
         }
+        pair_of[p] = k;
         rc[k] = c;
         rs[k] = s;
         rp_[k] = p;
         rq_[k] = q;
       }
       __syncthreads();
-      if (threadIdx.x == 0) {   // the rotations whose row p this CTA keeps
-        int cnt = 0;
-        for (int k = 0; k < half; ++k)
-          if (rs[k] != 0.0 && rp_[k] >= r0 && rp_[k] < r1) own[cnt++] = k;
-        n_own = cnt;
-      }
-      cluster.sync();   // every CTA has read the old entries
-      // 2. rows p, q of A
-      for (int idx = threadIdx.x; idx < n_own * n; idx += blockDim.x) {
-        const int k = own[idx / n], j = idx % n;
-        const double c = rc[k], s = rs[k];
-        double *ap = A + (int64_t)(rp_[k] - r0) * n + j;
-        double *aq = row_ptr(rq_[k]) + j;
-        const double x = *ap, y = *aq;
-        *ap = c * x - s * y;
-        *aq = s * x + c * y;
-      }
-      cluster.sync();   // rows done everywhere
-      // 3. columns p, q of A and V in this CTA's rows
+      // 2. this CTA's rows of A' = J^T A J into the next copy; its rows of V rotated in place
+      const double *Acur = sm_jac + cur * slab;
+      double *Anext = sm_jac + (cur ^ 1) * slab;
       for (int idx = threadIdx.x; idx < nloc * half; idx += blockDim.x) {
-        const int i = idx / half, k = idx - i * half;
-        const double s = rs[k];
-        if (s == 0.0) continue;
-        const double c = rc[k];
-        const int p = rp_[k], q = rq_[k];
-        double *a = A + (int64_t)i * n, *v = V + (int64_t)i * n;
-        const double x = a[p], y = a[q];
-        a[p] = c * x - s * y;
-        a[q] = s * x + c * y;
-        const double u = v[p], w = v[q];
-        v[p] = c * u - s * w;
-        v[q] = s * u + c * w;
-      }
-      __syncthreads();
-      for (int k = threadIdx.x; k < half; k += blockDim.x)
-        if (rs[k] != 0.0) {
-          const int p = rp_[k], q = rq_[k];
-          if (p >= r0 && p < r1) A[(int64_t)(p - r0) * n + q] = 0.0;
-          if (q >= r0 && q < r1) A[(int64_t)(q - r0) * n + p] = 0.0;
+        const int li = idx / half, l = idx - li * half;
+        const int i = r0 + li;
+        const int k = pair_of[i];
+        const double ci = rc[k], si = rs[k];
+        const bool i_is_p = rp_[k] == i;
+        const int partner = i_is_p ? rq_[k] : rp_[k];
+        const double *ai = Acur + (int64_t)li * n;
+        const double *ap = (si != 0.0) ? row_ptr(partner) : ai;   // partner < n whenever si != 0
+        const int pl = rp_[l], ql = rq_[l];
+        const double cl = rc[l], sl = rs[l];
+        // row rotation of row i at columns pl (and ql)
+        auto rowrot = [&](int j) {
+          if (si == 0.0) return ai[j];
+          return i_is_p ? ci * ai[j] - si * ap[j] : si * ap[j] + ci * ai[j];
+        };
+        double *out = Anext + (int64_t)li * n;
+        const double xp = rowrot(pl);
+        if (ql >= n) {
+          out[pl] = xp;
+          continue;
         }
-      cluster.sync();   // the round is complete everywhere
+        const double xq = rowrot(ql);
+        if (sl == 0.0) {
+          out[pl] = xp;
+          out[ql] = xq;
+        } else {
+          out[pl] = cl * xp - sl * xq;
+          out[ql] = sl * xp + cl * xq;
+          if (k == l) out[i_is_p ? ql : pl] = 0.0;   // the entry this rotation annihilates
+          double *v = V + (int64_t)li * n;
+          const double u = v[pl], w = v[ql];
+          v[pl] = cl * u - sl * w;
+          v[ql] = sl * u + cl * w;
+        }
+      }
+      cluster.sync();   // every CTA has written its next rows and read the current ones
+      cur ^= 1;
     }
   }
+  const double *A = sm_jac + cur * slab;
   for (int i = threadIdx.x; i < nloc; i += blockDim.x) Wg[b.woff + r0 + i] = A[(int64_t)i * n + r0 + i];
   for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) Vg[b.off + (int64_t)r0 * n + e] = V[e];
   if (rank == 0 && threadIdx.x == 0) sweeps[blockIdx.x / cs] = sweep;
@@ -325,6 +346,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       }
     }
   }
+  const double t_gather = wall_s();
   // device: density matrices and their eigen-decompositions
   std::vector<double> W((size_t)std::max<int64_t>(woff, 1)), Vh((size_t)std::max<int64_t>(a_pre[nb], 1));
   std::vector<int> sweeps(nb);
@@ -348,11 +370,8 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     }
     // one cluster a block, the largest blocks first; 8 CTAs a cluster (16 when a block's rows
     // would not fit 8 CTAs' shared memory)
-    int cs = 8;
-    auto smem_for = [&](int c) { return 2 * sizeof(double) * (size_t)((max_n + c - 1) / c) * max_n; };
-    if (smem_for(cs) > kJacobiSmem) cs = 16;
-    DG_REQUIRE(smem_for(cs) <= kJacobiSmem, DG_ERR_ARG, "a density block of %d pairs is too large for the eigensolver", max_n);
-    const size_t smem = smem_for(cs);
+    auto smem_for = [&](int c) { return 3 * sizeof(double) * (size_t)((max_n + c - 1) / c) * max_n; };
+    DG_REQUIRE(smem_for(16) <= kJacobiSmem, DG_ERR_ARG, "a density block of %d pairs is too large for the eigensolver", max_n);
     std::vector<int> by_size(nb);
     std::iota(by_size.begin(), by_size.end(), 0);
     std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) { return eb[a].n > eb[b].n; });
@@ -360,23 +379,39 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     for (int i = 0; i < nb; ++i) eb_sorted[i] = eb[by_size[i]];
     DG_CUDA(cudaMemcpyAsync(deb.get(), eb_sorted.data(), sizeof(EigBlk) * nb, cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(dsw.get(), 0, sizeof(int) * nb, st));
-    DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (cs > 8) DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    cudaLaunchConfig_t cfg;
-    std::memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3((unsigned)(nb * cs));
-    cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)cs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
-                               kJacobiSweeps, dsw.get()));
+    // 16 CTAs a cluster (a non-portable size) when the largest block has 128 pairs or more and the
+    // device runs such clusters, else 8
+    int cs = 8;
+    DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
+    if (max_n >= 128 && cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+      cs = 16;
+    cudaGetLastError();
+    if (smem_for(8) > kJacobiSmem) cs = 16;
+    for (;;) {
+      cudaLaunchConfig_t cfg;
+      std::memset(&cfg, 0, sizeof(cfg));
+      cfg.gridDim = dim3((unsigned)(nb * cs));
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = smem_for(cs);
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&clusters, k_jacobi_cluster, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        DG_REQUIRE(cs == 16 && smem_for(8) <= kJacobiSmem, DG_ERR_CUDA, "the device runs no cluster of %d CTAs", cs);
+        cs = 8;   // try the portable size
+        continue;
+      }
+      DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
+                                 kJacobiSweeps, dsw.get()));
+      break;
+    }
     count_launch();
     DG_CUDA(cudaGetLastError());
     DG_CUDA(cudaMemcpyAsync(W.data(), dW.get(), sizeof(double) * W.size(), cudaMemcpyDeviceToHost, st));
@@ -390,6 +425,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     snprintf(msg, sizeof(msg), "GPU path failed (status %d): %s", rc, dg_last_error());
     fatal("DMRG_GET_SYSTEM_INFO", msg);
   }
+  const double t_device = wall_s();
   // per block: eigenpairs in ascending order (LAPACK's), as (value, column of V_g)
   std::vector<int> order_in_blk((size_t)std::max<int64_t>(woff, 1));
   for (int g = 0; g < nb; ++g) {
@@ -495,7 +531,16 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
   S->Trans_Matrix_Dagger = TD;
   S->dim_renorm = dim_renorm;
   S->dim_LLLR = dim_LLLR;
-  if (T) T->make_dens_mat = wall_s() - t0;
+  const double t_end = wall_s();
+  if (T) T->make_dens_mat = t_end - t0;
+  if (const char *e = std::getenv("DG_SB_TRUNC_TIMES")) {   // phase report for profiling
+    if (e[0] == '1') {
+      int mx = 0;
+      for (int sw : sweeps) mx = std::max(mx, sw);
+      fprintf(stderr, "truncation: gather %.2f ms, device %.2f ms (at most %d sweeps), host %.2f ms\n", (t_gather - t0) * 1e3,
+              (t_device - t_gather) * 1e3, mx, (t_end - t_device) * 1e3);
+    }
+  }
   return S;
 }
 

@@ -291,6 +291,7 @@ def truncation(repeats=3):
     import ctypes as C
     import time
     import numpy as np
+    import os
     from . import abi, sb_models, workloads
     libc = C.CDLL(None)
     libc.free.argtypes = [C.c_void_p]
@@ -324,6 +325,7 @@ def truncation(repeats=3):
         T = abi.DMRG_TIME()
         blocks = np.unique(lab, return_counts=True)[1]
         times = []
+        os.environ["DG_SB_TRUNC_TIMES"] = "1"
         for it in range(repeats + 1):
             t0 = time.perf_counter()
             S = lib.DMRG_GET_SYSTEM_INFO_Q2(abi.ptr(N, C.c_int), abi.ptr(sz, C.c_int), C.byref(B), abi.ptr(v, C.c_double), m, 1,
