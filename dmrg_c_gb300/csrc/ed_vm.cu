@@ -44,38 +44,64 @@ struct SiteOp {
   const double *val;
 };
 
+// Out[i] for output row i: the stored elements of the operator row of i's local state at `site`,
+// each adding Vec[j] * O (j: the input position of the code with that local state replaced),
+// summed in storage order and rounded as written, times the sign.  bits > 0: dim_onsite = 2^bits,
+// and digits come from shifts and masks instead of a 64-bit division per lower site (the same values).
+__device__ __forceinline__ double site_row(const int64_t *__restrict__ out_basis, long i, const int64_t *__restrict__ in_basis,
+                                           long dim_in, const SiteOp &op, int d, int bits, int site, int64_t dim_site,
+                                           const int *__restrict__ n_ele, int use_sign, const double *__restrict__ vec) {
+  const int64_t code = out_basis[i];
+  const int local = bits > 0 ? (int)((code >> (site * bits)) & (d - 1)) : digit_of(code, site, d);
+  int sign = 1;
+  if (use_sign) {
+    int ne = 0;
+    int64_t c = code;
+    for (int s = 0; s < site; ++s) {
+      if (bits > 0) {
+        ne += n_ele[(int)(c & (d - 1))];
+        c >>= bits;
+      } else {
+        ne += n_ele[(int)(c % d)];
+        c /= d;
+      }
+    }
+    sign = (ne % 2 == 0) ? 1 : -1;
+  }
+  double v = 0.0;
+  for (int64_t k = op.row[local]; k < op.row[local + 1]; ++k) {
+    const int64_t target = code - (int64_t)(local - op.col[k]) * dim_site;
+    const long j = find_code(in_basis, dim_in, target);
+    if (j >= 0) v = __dadd_rn(v, __dmul_rn(vec[j], op.val[k]));
+  }
+  return use_sign ? __dmul_rn(v, (double)sign) : v;
+}
+
 // One thread per output row (the grid covers the rows, so the binary searches of all rows are in
-// flight together).  bits > 0: dim_onsite = 2^bits, and digits come from shifts and masks instead of
-// a 64-bit division per lower site (the same values).
+// flight together).
 __global__ void k_site_apply(const int64_t *__restrict__ out_basis, long dim_out, const int64_t *__restrict__ in_basis, long dim_in,
                              SiteOp op, int d, int bits, int site, int64_t dim_site, const int *__restrict__ n_ele, int use_sign,
                              const double *__restrict__ vec, double *__restrict__ out) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < dim_out; i += (long)gridDim.x * blockDim.x) {
-    const int64_t code = out_basis[i];
-    const int local = bits > 0 ? (int)((code >> (site * bits)) & (d - 1)) : digit_of(code, site, d);
-    int sign = 1;
-    if (use_sign) {
-      int ne = 0;
-      int64_t c = code;
-      for (int s = 0; s < site; ++s) {
-        if (bits > 0) {
-          ne += n_ele[(int)(c & (d - 1))];
-          c >>= bits;
-        } else {
-          ne += n_ele[(int)(c % d)];
-          c /= d;
-        }
-      }
-      sign = (ne % 2 == 0) ? 1 : -1;
-    }
-    double v = 0.0;
-    for (int64_t k = op.row[local]; k < op.row[local + 1]; ++k) {
-      const int64_t target = code - (int64_t)(local - op.col[k]) * dim_site;
-      const long j = find_code(in_basis, dim_in, target);
-      if (j >= 0) v = v + vec[j] * op.val[k];
-    }
-    out[i] = (use_sign ? v * sign : v);
-  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < dim_out; i += (long)gridDim.x * blockDim.x)
+    out[i] = site_row(out_basis, i, in_basis, dim_in, op, d, bits, site, dim_site, n_ele, use_sign, vec);
+}
+
+// Block partials of sum_i w[i] (O_site Vec)[i] for every site of [site0, site0 + gridDim.y): one
+// launch for all sites (EXACT_EXPECTATION_ONSITE / _INTERSITE_Q0 without the per-site vectors).
+__global__ void k_site_expect(const int64_t *__restrict__ basis, long dim, SiteOp op, int d, int bits, int site0,
+                              const double *__restrict__ vec, const double *__restrict__ w, double *__restrict__ partials) {
+  const int site = site0 + blockIdx.y;
+  int64_t dim_site = 1;
+  for (int s = 0; s < site; ++s) dim_site *= d;
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < dim; i += (long)gridDim.x * blockDim.x)
+    acc += w[i] * site_row(basis, i, basis, dim, op, d, bits, site, dim_site, nullptr, 0, vec);
+  block_partial(acc, partials + (size_t)blockIdx.y * gridDim.x);
+}
+
+__global__ void k_site_expect_sum(const double *__restrict__ partials, int count, double *__restrict__ out) {
+  const double s = sum_partials(partials + (size_t)blockIdx.x * count, count);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
 // Host driver: uploads the tables and runs the kernel.
@@ -109,6 +135,78 @@ void site_apply(const CRS1 *M_On, const long *out_basis, long dim_out, const lon
                                                  site, dim_site, ne.get(), use_sign ? 1 : 0, x.get(), y.get()); ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
   DG_CUDA(cudaMemcpyAsync(out, y.get(), sizeof(double) * dim_out, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
+}
+
+// EXACT_EXPECTATION_ONSITE / _INTERSITE_Q0 on the Q0 basis: out[r] = <w|O_{site0+r}|Vec> for
+// r < count, with w = Vec (w_op null) or w = (w_op at site w_site) Vec, also written to w_out; the
+// last site's product is written to last_out (the reference leaves both in its work vectors).
+void site_expect(const CRS1 *M_w, int w_site, const CRS1 *M_On, int site0, int count, const long *basis, long dim, int d,
+                 const double *vec, double *out, double *w_out, double *last_out) {
+  require_device();
+  DG_REQUIRE(M_On && basis && vec, DG_ERR_ARG, "null argument");
+  DG_REQUIRE(d >= 2 && site0 >= 0 && count >= 0 && (!M_w || w_site >= 0), DG_ERR_ARG, "bad dim_onsite / sites");
+  DG_REQUIRE(count == 0 || out, DG_ERR_ARG, "null output");
+  cudaStream_t st = stream();
+  int bits = 0;
+  while ((1 << bits) < d) ++bits;
+  if ((1 << bits) != d) bits = 0;
+  auto upload_op = [&](const CRS1 *M, DevBuf<int64_t> &r, DevBuf<int> &c, DevBuf<double> &v) {
+    const long nnz = M->Row[d];
+    r.alloc(d + 1);
+    c.alloc(nnz);
+    v.alloc(nnz);
+    DG_CUDA(cudaMemcpyAsync(r.get(), M->Row, sizeof(int64_t) * (d + 1), cudaMemcpyHostToDevice, st));
+    if (nnz) {
+      DG_CUDA(cudaMemcpyAsync(c.get(), M->Col, sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
+      DG_CUDA(cudaMemcpyAsync(v.get(), M->Val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    }
+    return SiteOp{r.get(), c.get(), v.get()};
+  };
+  DevBuf<int64_t> b(dim), r1, r2;
+  DevBuf<int> c1, c2;
+  DevBuf<double> v1, v2, x(dim), w, last(dim);
+  DG_CUDA(cudaMemcpyAsync(b.get(), basis, sizeof(int64_t) * dim, cudaMemcpyHostToDevice, st));
+  DG_CUDA(cudaMemcpyAsync(x.get(), vec, sizeof(double) * dim, cudaMemcpyHostToDevice, st));
+  const SiteOp op = upload_op(M_On, r1, c1, v1);
+  const long blocks = std::max(1L, std::min((dim + kThreads - 1) / kThreads, (long)sm_count() * 64));
+  const double *wp = x.get();
+  auto pow_site = [&](int s) {
+    int64_t p = 1;
+    for (int k = 0; k < s; ++k) p *= d;
+    return p;
+  };
+  if (M_w) {
+    const SiteOp opw = upload_op(M_w, r2, c2, v2);
+    w.alloc(dim);
+    k_site_apply<<<(int)blocks, kThreads, 0, st>>>(b.get(), dim, b.get(), dim, opw, d, bits, w_site, pow_site(w_site), nullptr, 0,
+                                                   x.get(), w.get());
+    count_launch();
+    DG_CUDA(cudaGetLastError());
+    wp = w.get();
+    if (w_out) DG_CUDA(cudaMemcpyAsync(w_out, w.get(), sizeof(double) * dim, cudaMemcpyDeviceToHost, st));
+  }
+  if (count > 0) {
+    DG_REQUIRE(count <= 65535, DG_ERR_ARG, "at most 65535 sites");
+    const int gx = (int)std::max(1L, std::min(((long)sm_count() * 16 + count - 1) / count, (dim + kThreads - 1) / kThreads));
+    DevBuf<double> partials((size_t)gx * count), dout(count);
+    k_site_expect<<<dim3(gx, count), kThreads, 0, st>>>(b.get(), dim, op, d, bits, site0, x.get(), wp, partials.get());
+    count_launch();
+    DG_CUDA(cudaGetLastError());
+    k_site_expect_sum<<<count, kThreads, 0, st>>>(partials.get(), gx, dout.get());
+    count_launch();
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaMemcpyAsync(out, dout.get(), sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+    if (last_out) {
+      const int ls = site0 + count - 1;
+      k_site_apply<<<(int)blocks, kThreads, 0, st>>>(b.get(), dim, b.get(), dim, op, d, bits, ls, pow_site(ls), nullptr, 0, x.get(),
+                                                     last.get());
+      count_launch();
+      DG_CUDA(cudaGetLastError());
+      DG_CUDA(cudaMemcpyAsync(last_out, last.get(), sizeof(double) * dim, cudaMemcpyDeviceToHost, st));
+    }
+    DG_CUDA(cudaStreamSynchronize(st));   // partials and dout go out of scope
+  }
   DG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -188,6 +286,28 @@ void EXACT_V_M_Q3(CRS1 *M_On, int qn1_out, int qn2_out, int qn3_out, double *Vec
                        Vec, Out_Vec);
           }),
           "EXACT_V_M_Q3");
+}
+
+// include/exact.h:120 -- <Vec|O_site|Vec> for every site, one device pass; T_Vec receives the
+// last site's product (as the reference leaves it).
+void EXACT_EXPECTATION_ONSITE(CRS1 *M_On, double *Out, double *Vec, double *T_Vec, int dim_onsite, int tot_site, int,
+                              EXACT_BASIS_INFO *Basis_Info) {
+  vm_must(guarded([&] {
+            site_expect(nullptr, 0, M_On, 0, std::max(tot_site, 0), Basis_Info->Basis, Basis_Info->dim, dim_onsite, Vec, Out, nullptr,
+                        T_Vec);
+          }),
+          "EXACT_EXPECTATION_ONSITE");
+}
+
+// include/exact.h:121 -- <M_O(start) Vec | M_R(site) Vec> for start <= site < end; T_Vec1 receives
+// M_O(start) Vec and T_Vec2 the last site's product.
+void EXACT_EXPECTATION_INTERSITE_Q0(CRS1 *M_O, CRS1 *M_R, int start, int end, double *Out, double *Vec, double *T_Vec1,
+                                    double *T_Vec2, int dim_onsite, int, EXACT_BASIS_INFO *Basis_Info) {
+  vm_must(guarded([&] {
+            site_expect(M_O, start, M_R, start, std::max(end - start, 0), Basis_Info->Basis, Basis_Info->dim, dim_onsite, Vec, Out,
+                        T_Vec1, T_Vec2);
+          }),
+          "EXACT_EXPECTATION_INTERSITE_Q0");
 }
 
 }  // extern "C"

@@ -132,6 +132,9 @@ SIGNATURES = {
     "dg_sb_basis_upload": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_short), P(C.c_short), P(C.c_short),
                                      P(C.c_short), ip, P(vp)]),
     "dg_sb_ops_create": (C.c_int, [C.c_int, P(P(CRS1)), ip, P(vp)]),
+    "EXACT_EXPECTATION_ONSITE": (None, [P(CRS1), dp, dp, dp, C.c_int, C.c_int, C.c_int, P(abi.EXACT_BASIS_INFO)]),
+    "EXACT_EXPECTATION_INTERSITE_Q0": (None, [P(CRS1), P(CRS1), C.c_int, C.c_int, dp, dp, dp, dp, C.c_int, C.c_int,
+                                              P(abi.EXACT_BASIS_INFO)]),
     "dg_sb_density_info": (C.c_int, [vp, ip, ip, lp]),
     "dg_sb_density_layout": (C.c_int, [vp, ip, ip, ip]),
     "dg_sb_density_matrix": (C.c_int, [vp, vp, vp]),

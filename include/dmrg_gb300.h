@@ -84,6 +84,11 @@ void EXACT_V_M_Q0(CRS1 *M_On, double *Vec, double *Out_Vec, int dim_onsite, int 
 void EXACT_V_M_Q1(CRS1 *M_On, int qn_out, double *Vec, int qn_in, double *Out_Vec, int dim_onsite, int site, int p_threads, EXACT_WHOLE_BASIS_Q1 *W_Basis);
 void EXACT_V_M_Q2(CRS1 *M_On, int qn1_out, int qn2_out, double *Vec, int qn1_in, int qn2_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q2 *W_Basis);
 void EXACT_V_M_Q3(CRS1 *M_On, int qn1_out, int qn2_out, int qn3_out, double *Vec, int qn1_in, int qn2_in, int qn3_in, double *Out_Vec, char Sign_Flag[], int *N_Ele, int dim_onsite, int op_site, int p_threads, EXACT_WHOLE_BASIS_Q3 *W_Basis);
+/* <Vec|O_site|Vec> for every site / <O(start) Vec|O_R(site) Vec> for start <= site < end, every site
+ * in one device pass; the work vectors receive what the reference leaves in them; Out within 1e-12
+ * of the reference (the order of the final sums differs).  replace include/exact.h:120-121 */
+void EXACT_EXPECTATION_ONSITE(CRS1 *M_On, double *Out, double *Vec, double *T_Vec, int dim_onsite, int tot_site, int p_threads, EXACT_BASIS_INFO *Basis_Info);
+void EXACT_EXPECTATION_INTERSITE_Q0(CRS1 *M_O, CRS1 *M_R, int start, int end, double *Out, double *Vec, double *T_Vec1, double *T_Vec2, int dim_onsite, int p_threads, EXACT_BASIS_INFO *Basis_Info);
 
 /* Out = O V for a block operator on the superblock (one position of (LL, LR, RR, RL)); Q0 within
  * one sector, Q1..Q4 into the sector the quantum numbers name.  Out is bitwise the reference's.

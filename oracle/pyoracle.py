@@ -540,6 +540,24 @@ def same_truncation(a, b, tol_val=1e-13, tol_proj=1e-9):
     return bad
 
 
+def call_exact_expectation(lib, op_o, op_r, start, end, basis, vec, d):
+    """EXACT_EXPECTATION_ONSITE (op_o None: sites 0..end-1 of op_r) or _INTERSITE_Q0 of lib on a Q0
+    basis; returns (Out, work vector 1, work vector 2)."""
+    basis = np.ascontiguousarray(basis, np.int64)
+    vec = np.ascontiguousarray(vec, np.float64)
+    info = EXACT_BASIS_INFO(dim=len(basis), Basis=ptr(basis, C.c_long))
+    n = end - start
+    out = np.full(max(n, 1), np.nan)
+    t1, t2 = np.full(len(basis), np.nan), np.full(len(basis), np.nan)
+    if op_o is None:
+        lib.EXACT_EXPECTATION_ONSITE(op_r.ref, ptr(out, C.c_double), ptr(vec, C.c_double), ptr(t1, C.c_double), d, end, 1,
+                                     C.byref(info))
+    else:
+        lib.EXACT_EXPECTATION_INTERSITE_Q0(op_o.ref, op_r.ref, start, end, ptr(out, C.c_double), ptr(vec, C.c_double),
+                                           ptr(t1, C.c_double), ptr(t2, C.c_double), d, 1, C.byref(info))
+    return out[:max(n, 0)], t1, t2
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

@@ -225,6 +225,24 @@ def sb_obs_fixture():
     np.savez_compressed(HERE / "sb_obs.npz", **out)
 
 
+def ed_obs_fixture():
+    """The reference's EXACT_EXPECTATION_ONSITE / _INTERSITE_Q0 on the Hubbard L=6 basis: site
+    densities and density correlations."""
+    model = ed_models.hubbard_chain(6, t=-1.0, U=2.0, n_ele=6, twoSz=0)
+    basis, row, col, val = po.ed_build(model)
+    rng = np.random.default_rng(33)
+    vec = rng.standard_normal(len(basis))
+    dens = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 1.0, 2.0]))
+    nup = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 0.0, 1.0]))
+    ref = po.load_ref()
+    out = dict(basis=basis, vec=vec)
+    out["onsite"], out["onsite_t"], _ = po.call_exact_expectation(ref, None, dens, 0, 6, basis, vec, 4)
+    for start, end in ((0, 6), (2, 5), (3, 3)):
+        o, t1, t2 = po.call_exact_expectation(ref, nup, dens, start, end, basis, vec, 4)
+        out[f"inter_{start}_{end}"], out[f"inter_{start}_{end}_t1"], out[f"inter_{start}_{end}_t2"] = o, t1, t2
+    np.savez_compressed(HERE / "ed_obs_hubbard6.npz", **out)
+
+
 def obc_fixture():
     """The reference's matrix-free superblock product and OBC Lanczos on a seeded
     synthetic superblock (spin-1/2 sites, one block quantum number)."""
@@ -267,6 +285,7 @@ def main():
     sb_basis_fixture()
     vm_fixture()
     sb_obs_fixture()
+    ed_obs_fixture()
     obc_fixture()
     xxz_energy_fixture()
     for f in sorted(HERE.glob("*.npz")):

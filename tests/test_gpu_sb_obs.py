@@ -293,3 +293,26 @@ def test_density_matrix_device_api_vs_oracle(gpu, oracle, big):
         rd = torch.empty(ne.value, dtype=torch.float64, device="cuda")
         gpu.check(gpu.load().dg_sb_density_matrix(b.h, C.c_void_p(vd.data_ptr()), C.c_void_p(rd.data_ptr())))
         assert np.array_equal(_bits(rd.cpu().numpy()), _bits(rho))
+
+
+def test_ed_expectation_dropins_vs_reference_golden(gpu, oracle):
+    """EXACT_EXPECTATION_ONSITE / _INTERSITE_Q0 (every site in one device pass) against the
+    reference: values within 1e-12 of |v|^2, work vectors bit for bit, nothing written for an
+    empty site range."""
+    from dmrg_c_gb300 import abi
+    g = golden("ed_obs_hubbard6.npz")
+    basis, vec = g["basis"], g["vec"]
+    dens = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 1.0, 2.0]))
+    nup = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 0.0, 1.0]))
+    lib = gpu.load()
+    tol = 1e-12 * float(vec @ vec) * 4
+    out, t, _ = oracle.call_exact_expectation(lib, None, dens, 0, 6, basis, vec, 4)
+    assert np.allclose(out, g["onsite"], rtol=0, atol=tol)
+    assert np.array_equal(_bits(t), _bits(g["onsite_t"]))
+    for start, end in ((0, 6), (2, 5), (3, 3)):
+        out, t1, t2 = oracle.call_exact_expectation(lib, nup, dens, start, end, basis, vec, 4)
+        assert np.allclose(out, g[f"inter_{start}_{end}"], rtol=0, atol=tol)
+        assert np.array_equal(_bits(t1), _bits(g[f"inter_{start}_{end}_t1"]))
+        ref_t2 = g[f"inter_{start}_{end}_t2"]
+        assert np.array_equal(np.isnan(t2), np.isnan(ref_t2))
+        assert np.array_equal(_bits(t2[~np.isnan(t2)]), _bits(ref_t2[~np.isnan(ref_t2)]))

@@ -317,3 +317,22 @@ def test_system_info_matches_reference_golden(oracle, tag, max_dim):
     lllr = oracle.lllr_list(p.q_LL, p.q_site, st)
     got = oracle.system_info(_system_info_qns(p, lllr, tag), st, inv0, p.d, p.dim_RR, g["v_unit"], lllr, max_dim)
     assert oracle.same_truncation(got, _golden_system_info(g, tag, max_dim)) == []
+
+
+def test_ed_expectation_matches_reference_golden(oracle):
+    """EXACT_EXPECTATION_ONSITE / _INTERSITE_Q0: the oracle's site products dotted with the vector
+    (or with the origin's product) agree with the reference within 1e-12 of |v|^2; the work
+    vectors are the products themselves."""
+    g = golden("ed_obs_hubbard6.npz")
+    basis, vec = g["basis"], g["vec"]
+    dens = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 1.0, 2.0]))
+    nup = abi.Crs(np.arange(5), np.arange(4, dtype=np.int32), np.array([0.0, 1.0, 0.0, 1.0]))
+    tol = 1e-12 * float(vec @ vec) * 4
+    on = [vec @ oracle.site_apply(dens, basis, basis, 4, s, vec) for s in range(6)]
+    assert np.allclose(on, g["onsite"], rtol=0, atol=tol)
+    assert np.array_equal(oracle.site_apply(dens, basis, basis, 4, 5, vec), g["onsite_t"])
+    for start, end in ((0, 6), (2, 5), (3, 3)):
+        t1 = oracle.site_apply(nup, basis, basis, 4, start, vec)
+        assert np.array_equal(t1, g[f"inter_{start}_{end}_t1"])
+        got = [t1 @ oracle.site_apply(dens, basis, basis, 4, s, vec) for s in range(start, end)]
+        assert np.allclose(got, g[f"inter_{start}_{end}"], rtol=0, atol=tol)
