@@ -350,6 +350,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
   // device: density matrices and their eigen-decompositions
   std::vector<double> W((size_t)std::max<int64_t>(woff, 1)), Vh((size_t)std::max<int64_t>(a_pre[nb], 1));
   std::vector<int> sweeps(nb);
+  int cs_used = 0;
   const int rc = guarded([&] {
     require_device();
     cudaStream_t st = stream();
@@ -410,6 +411,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       }
       DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
                                  kJacobiSweeps, dsw.get()));
+      cs_used = cs;
       break;
     }
     count_launch();
@@ -537,8 +539,8 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     if (e[0] == '1') {
       int mx = 0;
       for (int sw : sweeps) mx = std::max(mx, sw);
-      fprintf(stderr, "truncation: gather %.2f ms, device %.2f ms (at most %d sweeps), host %.2f ms\n", (t_gather - t0) * 1e3,
-              (t_device - t_gather) * 1e3, mx, (t_end - t_device) * 1e3);
+      fprintf(stderr, "truncation: gather %.2f ms, device %.2f ms (clusters of %d CTAs, at most %d sweeps), host %.2f ms\n",
+              (t_gather - t0) * 1e3, (t_device - t_gather) * 1e3, cs_used, mx, (t_end - t_device) * 1e3);
     }
   }
   return S;
