@@ -190,37 +190,43 @@ __device__ __forceinline__ int find_block(const int64_t *__restrict__ off, int B
 }
 
 // rho_g[p][q] = sum_t w[row p][t] * v[row q][t] for every block, summed over t in order and rounded
-// as written (with w = v these are DMRG_GET_DENSITY_MATRIX's entries, bit for bit).
+// as written (with w = v these are DMRG_GET_DENSITY_MATRIX's entries, bit for bit).  sym (w = v):
+// only p <= q is computed and mirrored -- the products of (q, p) are those of (p, q), so the mirror
+// is the value the sum would give.
 __global__ void __launch_bounds__(kThreads) k_gram_rows(PairView P, const double *__restrict__ w, const double *__restrict__ v,
-                                                       double *__restrict__ rho) {
+                                                       int sym, double *__restrict__ rho) {
   const int64_t total = P.rho_off[P.B];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int g = find_block(P.rho_off, P.B, e);
     const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
     const int64_t loc = e - P.rho_off[g];
     const int p = (int)(loc / Pg), q = (int)(loc - (int64_t)p * Pg);
+    if (sym && p > q) continue;
     const double *__restrict__ x = w + P.blk_base[g] + (int64_t)p * Q;
     const double *__restrict__ y = v + P.blk_base[g] + (int64_t)q * Q;
     double acc = 0.0;
     for (int t = 0; t < Q; ++t) acc = __dadd_rn(acc, __dmul_rn(x[t], y[t]));
     rho[e] = acc;
+    if (sym) rho[P.rho_off[g] + (int64_t)q * Pg + p] = acc;
   }
 }
 
-// sigma_g[t][u] = sum_p w[row p][t] * v[row p][u] for every block.
+// sigma_g[t][u] = sum_p w[row p][t] * v[row p][u] for every block (sym: t <= u, mirrored).
 __global__ void __launch_bounds__(kThreads) k_gram_cols(PairView P, const double *__restrict__ w, const double *__restrict__ v,
-                                                       double *__restrict__ sig) {
+                                                       int sym, double *__restrict__ sig) {
   const int64_t total = P.sig_off[P.B];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int g = find_block(P.sig_off, P.B, e);
     const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
     const int64_t loc = e - P.sig_off[g];
     const int t = (int)(loc / Q), u = (int)(loc - (int64_t)t * Q);
+    if (sym && t > u) continue;
     const double *__restrict__ x = w + P.blk_base[g] + t;
     const double *__restrict__ y = v + P.blk_base[g] + u;
     double acc = 0.0;
     for (int p = 0; p < Pg; ++p) acc = __dadd_rn(acc, __dmul_rn(x[(int64_t)p * Q], y[(int64_t)p * Q]));
     sig[e] = acc;
+    if (sym) sig[P.sig_off[g] + (int64_t)u * Q + t] = acc;
   }
 }
 
@@ -229,17 +235,19 @@ struct TraceTerm {
   int pos, weight;
 };
 
-// out[term] = trace of the term's operator against rho (LL, LR) or sigma (RR, RL); one block a term.
+// Block partials of the trace of each term's operator against rho (LL, LR) or sigma (RR, RL):
+// blockIdx.y is the term, blockIdx.x a chunk of its runs / (RR, RL) positions.
 __global__ void __launch_bounds__(kThreads) k_sb_trace(PairView P, SbStates S, const TraceTerm *__restrict__ terms,
                                                       const int *__restrict__ col, const double *__restrict__ val,
                                                       const double *__restrict__ rho0, const double *__restrict__ rho1,
                                                       const double *__restrict__ sig0, const double *__restrict__ sig1,
-                                                      double *__restrict__ out) {
-  const TraceTerm t = terms[blockIdx.x];
+                                                      double *__restrict__ partials) {
+  const TraceTerm t = terms[blockIdx.y];
+  const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   double acc = 0.0;
   if (t.pos == DG_SB_LL || t.pos == DG_SB_LR) {
     const double *__restrict__ rho = t.weight ? rho1 : rho0;
-    for (int r = threadIdx.x; r < P.R; r += blockDim.x) {
+    for (int r = first; r < P.R; r += stride) {
       const int g = P.run_blk[r], r0 = P.blk_run0[g], Pg = P.blk_run0[g + 1] - r0;
       const int a = P.run_ll[r], lr = P.run_lr[r];
       const int s = t.pos == DG_SB_LL ? a : lr;
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_sb_trace(PairView P, SbStates S, c
     const double *__restrict__ sig = t.weight ? sig1 : sig0;
     const int64_t slots = P.q_off[P.B];
     const int64_t tab = (int64_t)P.dim_RR * P.d;
-    for (int64_t u = threadIdx.x; u < slots; u += blockDim.x) {
+    for (int64_t u = first; u < slots; u += stride) {
       const int g = find_block(P.q_off, P.B, u);
       const int Q = P.blk_Q[g];
       const int tt = (int)(u - P.q_off[g]);
@@ -270,8 +278,7 @@ __global__ void __launch_bounds__(kThreads) k_sb_trace(PairView P, SbStates S, c
       }
     }
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) out[blockIdx.x] = acc;
+  block_partial(acc, partials + (size_t)blockIdx.y * gridDim.x);
 }
 
 // Is inv exactly the sector's own table: Inv at every state's index is that index, and no other
@@ -478,25 +485,32 @@ void launch_trace(const dg_sb_basis *b, const std::vector<SbTerm> &terms, const 
   DevBuf<double> rho[2], sig[2];
   const double *w[2] = {w0, w1};
   for (int k = 0; k < 2; ++k) {
+    const int sym = w[k] == v;
     if (rows[k]) {
       const int64_t total = P.rho_off[P.B];
       rho[k].alloc(total);
-      k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, rho[k].get());
+      k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sym, rho[k].get());
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
     if (cols[k]) {
       const int64_t total = P.sig_off[P.B];
       sig[k].alloc(total);
-      k_gram_cols<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sig[k].get());
+      k_gram_cols<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sym, sig[k].get());
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
   }
   DevBuf<TraceTerm> dterms(tt.size());
   DG_CUDA(cudaMemcpyAsync(dterms.get(), tt.data(), sizeof(TraceTerm) * tt.size(), cudaMemcpyHostToDevice, st));
-  k_sb_trace<<<(int)tt.size(), kThreads, 0, st>>>(pv, states_of(b), dterms.get(), ops->col.get(), ops->val.get(), rho[0].get(),
-                                                 rho[1].get(), sig[0].get(), sig[1].get(), dout);
+  const int nt = (int)tt.size();
+  const int gx = (int)std::max(1L, std::min(8L, ((long)sm_count() * 4 + nt - 1) / nt));
+  DevBuf<double> partials((size_t)gx * nt);
+  k_sb_trace<<<dim3(gx, nt), kThreads, 0, st>>>(pv, states_of(b), dterms.get(), ops->col.get(), ops->val.get(), rho[0].get(),
+                                                rho[1].get(), sig[0].get(), sig[1].get(), partials.get());
+  count_launch();
+  DG_CUDA(cudaGetLastError());
+  k_sb_expect_sum<<<nt, kThreads, 0, st>>>(partials.get(), gx, dout);
   count_launch();
   DG_CUDA(cudaGetLastError());
   DG_CUDA(cudaStreamSynchronize(st));   // dterms and the density matrices go out of scope
@@ -1047,7 +1061,7 @@ int dg_sb_density_matrix(const dg_sb_basis *b, const double *v, double *rho) {
       ob.alloc(total);
       dr = ob.get();
     }
-    k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pair_view(P), dv, dv, dr);
+    k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pair_view(P), dv, dv, 1, dr);
     count_launch();
     DG_CUDA(cudaGetLastError());
     if (!out_dev) DG_CUDA(cudaMemcpyAsync(rho, dr, sizeof(double) * total, cudaMemcpyDeviceToHost, st));

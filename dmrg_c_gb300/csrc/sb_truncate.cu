@@ -380,11 +380,11 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     for (int i = 0; i < nb; ++i) eb_sorted[i] = eb[by_size[i]];
     DG_CUDA(cudaMemcpyAsync(deb.get(), eb_sorted.data(), sizeof(EigBlk) * nb, cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(dsw.get(), 0, sizeof(int) * nb, st));
-    // 16 CTAs a cluster (a non-portable size) when the largest block has 128 pairs or more and the
+    // 16 CTAs a cluster (a non-portable size) when the largest block has 64 pairs or more and the
     // device runs such clusters, else 8
     int cs = 8;
     DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
-    if (max_n >= 128 && cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+    if (max_n >= 64 && cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
       cs = 16;
     cudaGetLastError();
     if (smem_for(8) > kJacobiSmem) cs = 16;
