@@ -352,6 +352,32 @@ class Crs:
         return cls(A.indptr, A.indices, A.data, n=A.shape[0], ncol=A.shape[1])
 
 
+class Ccs:
+    """A CCS1 structure viewing numpy arrays (col offsets int64, row int32, val float64), kept alive
+    by this object; ``.ref`` points to it."""
+
+    def __init__(self, col, row, val, n_rows, n_cols, max_val=None):
+        self.col = np.ascontiguousarray(col, dtype=np.int64)
+        self.row = np.ascontiguousarray(row if len(row) else np.zeros(1), dtype=np.int32)
+        self.val = np.ascontiguousarray(val if len(val) else np.zeros(1), dtype=np.float64)
+        self.struct = CCS1(max_val=max_val if max_val is not None else max(len(val), 1), max_col=n_cols + 1, row_dim=n_rows,
+                           col_dim=n_cols, Col=ptr(self.col, C.c_long), Row=ptr(self.row, C.c_int), Val=ptr(self.val, C.c_double))
+        self.ref = C.pointer(self.struct)
+
+    @classmethod
+    def from_scipy(cls, A):
+        A = A.tocsc()
+        A.sort_indices()
+        return cls(A.indptr, A.indices, A.data, A.shape[0], A.shape[1])
+
+    @classmethod
+    def empty(cls, n_cols, max_val):
+        """An output CCS as GET_CCS1(n_cols, max_val) allocates it."""
+        c = cls(np.zeros(n_cols + 1, np.int64), np.zeros(max(max_val, 1), np.int32), np.zeros(max(max_val, 1)), 0, 0, max_val)
+        c.struct.max_col = n_cols + 1
+        return c
+
+
 def lower_diag_last(A) -> Crs:
     """Symmetric matrix -> the *_SYM layout: lower triangle, columns ascending, diagonal
     stored last in every row (explicitly, even when zero)."""

@@ -139,6 +139,7 @@ SIGNATURES = {
     "dg_sb_density_layout": (C.c_int, [vp, ip, ip, ip]),
     "dg_sb_density_matrix": (C.c_int, [vp, vp, vp]),
     "DMRG_GET_DENSITY_MATRIX": (P(dp), [C.c_int, ip, P(DMRG_BASIS), dp, C.c_int]),
+    "CRS_CRS_CCS_PRODUCT": (None, [P(CRS1), P(CRS1), P(abi.CCS1), P(CRS1), P(abi.CCS1), dp]),
     "DMRG_GET_SYSTEM_INFO_Q1": (P(abi.DMRG_SYSTEM_INFO), [ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),
     "DMRG_GET_SYSTEM_INFO_Q2": (P(abi.DMRG_SYSTEM_INFO), [ip, ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),
     "DMRG_GET_SYSTEM_INFO_Q3": (P(abi.DMRG_SYSTEM_INFO), [ip, ip, ip, P(DMRG_BASIS), dp, C.c_int, C.c_int, P(DMRG_TIME)]),

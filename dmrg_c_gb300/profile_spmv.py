@@ -342,6 +342,58 @@ def truncation(repeats=3):
               f"truncation error {tr:.3e}: {min(times[1:]) * 1e3:.2f} ms per call", flush=True)
 
 
+def renorm_operands(r3, c3, nblk, per_row, seed=0):
+    """T^dagger, O, T of one renormalisation: T (r3 x c3) with each column on one of nblk row blocks,
+    O conserving the blocks with per_row elements a row (the shape TRANSFORM_MATRIX sees)."""
+    import numpy as np
+    import scipy.sparse as sp
+    from . import abi
+    rng = np.random.default_rng(seed)
+    blocks = np.sort(rng.integers(0, nblk, r3))
+    rows_t, cols_t = [], []
+    for j in range(c3):
+        r = np.flatnonzero(blocks == j % nblk)
+        rows_t.append(r)
+        cols_t.append(np.full(len(r), j))
+    rt, ct = np.concatenate(rows_t), np.concatenate(cols_t)
+    T = sp.csc_matrix((rng.standard_normal(len(rt)), (rt, ct)), shape=(r3, c3))
+    ro, co = [], []
+    for b in range(nblk):
+        idx = np.flatnonzero(blocks == b)
+        if len(idx) == 0:
+            continue
+        k = min(per_row, len(idx))
+        for i in idx:
+            ro.append(np.full(k, i))
+            co.append(rng.choice(idx, size=k, replace=False))
+    ro, co = np.concatenate(ro), np.concatenate(co)
+    O = sp.csr_matrix((rng.standard_normal(len(ro)), (ro, co)), shape=(r3, r3))
+    return abi.Crs.from_scipy(T.T.tocsr()), abi.Crs.from_scipy(O), abi.Ccs.from_scipy(T)
+
+
+def renorm(repeats=5):
+    """CRS_CRS_CCS_PRODUCT (T^dagger O T) with the shapes of the KLM m=128 (LLLR 1024 -> 128) and
+    Hubbard m=512 (LLLR 2048 -> 512) renormalisations: wall time per drop-in call from host arrays."""
+    import ctypes as C
+    import time
+    import numpy as np
+    from . import abi
+    lib = L.load()
+    for name, r3, c3, nblk, per_row in (("klm m=128", 1024, 128, 47, 16), ("hubbard m=512", 2048, 512, 57, 24)):
+        M1, M2, M3 = renorm_operands(r3, c3, nblk, per_row)
+        work = abi.Ccs.empty(c3, r3 * c3)
+        out = abi.Crs(np.zeros(c3 + 1, np.int64), np.zeros(c3 * c3, np.int32), np.zeros(c3 * c3), n=c3)
+        wv = np.zeros(r3)
+        args = (M1.ref, M2.ref, M3.ref, out.ref, work.ref, abi.ptr(wv, C.c_double))
+        lib.CRS_CRS_CCS_PRODUCT(*args)
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            lib.CRS_CRS_CCS_PRODUCT(*args)
+        t = (time.perf_counter() - t0) / repeats
+        print(f"CRS_CRS_CCS_PRODUCT {name}: T {r3} x {c3} ({M3.col[-1]} stored), O {M2.nnz} stored -> W {int(work.col[c3])}, "
+              f"Out {int(out.row[c3])} stored: {t * 1e3:.2f} ms per call", flush=True)
+
+
 def solvers(name, repeats=5):
     """Whole ground-state solves on one device-resident matrix with the solver forms side by side:
     Lanczos + inverse iteration with CG or with MINRES inner solves (FP64), and the two
@@ -417,6 +469,7 @@ def main(argv=None):
     ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
     ap.add_argument("--obs", action="store_true", help="site expectation values on the Hubbard m=512 superblock")
     ap.add_argument("--trunc", action="store_true", help="DMRG_GET_SYSTEM_INFO_Q2 on the KLM m=128 and Hubbard m=512 superblocks")
+    ap.add_argument("--renorm", action="store_true", help="CRS_CRS_CCS_PRODUCT with the KLM m=128 and Hubbard m=512 shapes")
     ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES), default=None,
                     help="solve times of the solver forms on one matrix")
     a = ap.parse_args(argv)
@@ -428,6 +481,8 @@ def main(argv=None):
         observables()
     elif a.trunc:
         truncation()
+    elif a.renorm:
+        renorm()
     elif a.obc:
         obc_solve(a.obc)
     elif a.build:

@@ -37,6 +37,11 @@ extern "C" {
 
 /* y = M x on a full CRS matrix.                         replaces include/SML.h:291 */
 void MATRIX_VECTOR_PRODUCT(CRS1 *M, double *V1, double *Out, int p_threads);
+/* Out = M1 (M2 M3): M1, M2 CRS, M3 CCS (the renormalisation T^dagger O T of TRANSFORM_MATRIX and
+ * DMRG_EXTEND_AND_REDUCE); Work receives M2 M3 in CCS.  Entries with |v| > 1e-15 kept, in the
+ * reference's order and bitwise its values; the reference's capacity checks and messages.
+ *                                                       replaces include/SML.h:181 */
+void CRS_CRS_CCS_PRODUCT(CRS1 *M1, CRS1 *M2, CCS1 *M3, CRS1 *Out, CCS1 *Work, double *Work_Vec);
 /* y = M x on a lower-triangle CRS whose rows end with the diagonal; Temp is the
  * reference's per-thread scratch and is neither read nor written here.
  *                                                        replaces include/SML.h:292 */

@@ -558,6 +558,56 @@ def call_exact_expectation(lib, op_o, op_r, start, end, basis, vec, d):
     return out[:max(n, 0)], t1, t2
 
 
+def crs_crs_ccs(M1: abi.Crs, M2: abi.Crs, M3: abi.Ccs):
+    """CRS_CRS_CCS_PRODUCT restated with numpy (sml/CRS_CRS_CCS_PRODUCT.c:42-121): W = M2 M3 by
+    columns (each row of M2 summed in storage order against the dense column of M3), Out = M1 W by
+    rows (each column of W summed in its storage order against the dense row of M1), entries with
+    |v| > 1e-15 kept, every step rounded as the reference's loops round it.  Returns
+    (W_col, W_row, W_val, Out_row, Out_col, Out_val)."""
+    r1, r2 = M1.struct.row_dim, M2.struct.row_dim
+    r3, c3 = M3.struct.row_dim, M3.struct.col_dim
+    D3 = np.zeros((c3, r3))
+    for c in range(c3):
+        for e in range(M3.col[c], M3.col[c + 1]):
+            D3[c, M3.row[e]] = M3.val[e]
+    start, length = M2.row[:r2], M2.row[1:r2 + 1] - M2.row[:r2]
+    W = np.zeros((c3, r2))
+    for k in range(int(length.max()) if r2 else 0):
+        live = np.flatnonzero(length > k)
+        e = start[live] + k
+        W[:, live] = W[:, live] + D3[:, M2.col[e]] * M2.val[e][None, :]
+    keep = np.abs(W) > 1e-15
+    w_col = np.concatenate([[0], np.cumsum(keep.sum(axis=1))])
+    w_row = np.concatenate([np.flatnonzero(keep[c]) for c in range(c3)]) if c3 else np.zeros(0, int)
+    w_val = W[keep]
+    D1 = np.zeros((r1, r2))
+    for r in range(r1):
+        for e in range(M1.row[r], M1.row[r + 1]):
+            D1[r, M1.col[e]] = M1.val[e]
+    O = np.zeros((r1, c3))
+    for c in range(c3):
+        for e in range(w_col[c], w_col[c + 1]):
+            O[:, c] = O[:, c] + D1[:, w_row[e]] * w_val[e]
+    keep = np.abs(O) > 1e-15
+    o_row = np.concatenate([[0], np.cumsum(keep.sum(axis=1))])
+    o_col = np.concatenate([np.flatnonzero(keep[r]) for r in range(r1)]) if r1 else np.zeros(0, int)
+    return w_col, w_row, w_val, o_row, o_col, O[keep]
+
+
+def call_crs_crs_ccs(lib, M1: abi.Crs, M2: abi.Crs, M3: abi.Ccs, max_w, max_o):
+    """CRS_CRS_CCS_PRODUCT of lib into fresh outputs of the given capacities; returns the same tuple
+    as crs_crs_ccs and the work vector."""
+    r1, r2, r3, c3 = M1.struct.row_dim, M2.struct.row_dim, M3.struct.row_dim, M3.struct.col_dim
+    work = abi.Ccs.empty(c3, max_w)
+    out = abi.Crs(np.zeros(r1 + 1, np.int64), np.zeros(max(max_o, 1), np.int32), np.zeros(max(max_o, 1)), n=r1)
+    out.struct.max_val = max_o
+    wv = np.full(max(r2, r3), np.nan)
+    lib.CRS_CRS_CCS_PRODUCT(M1.ref, M2.ref, M3.ref, out.ref, work.ref, ptr(wv, C.c_double))
+    nw, no = int(work.col[c3]), int(out.row[r1])
+    return (work.col.copy(), work.row[:nw].copy(), work.val[:nw].copy(), out.row.copy(), out.col[:no].copy(), out.val[:no].copy(),
+            wv, (work.struct.row_dim, work.struct.col_dim, out.struct.row_dim, out.struct.col_dim))
+
+
 def site_apply(op: abi.Crs, out_basis, in_basis, d, site, vec, n_ele=None, threads=None):
     out_basis = np.ascontiguousarray(out_basis, np.int64)
     in_basis = np.ascontiguousarray(in_basis, np.int64)

@@ -60,6 +60,16 @@ def golden(name):
     return np.load(GOLDEN / name)
 
 
+def renorm_operands_from_golden(g):
+    """(M1, M2, M3) of the renormalisation fixture: T^dagger (CRS), O (CRS), T (CCS)."""
+    from dmrg_c_gb300 import abi
+    r1, r2, r3, c3 = (int(x) for x in g["dims"])
+    M1 = abi.Crs(g["m1_row"], g["m1_col"], g["m1_val"], n=r1, ncol=r2)
+    M2 = abi.Crs(g["m2_row"], g["m2_col"], g["m2_val"], n=r2, ncol=r3)
+    M3 = abi.Ccs(g["m3_col"], g["m3_row"], g["m3_val"], r3, c3)
+    return M1, M2, M3
+
+
 @pytest.fixture
 def rng():
     return np.random.default_rng(1234)

@@ -243,6 +243,38 @@ def ed_obs_fixture():
     np.savez_compressed(HERE / "ed_obs_hubbard6.npz", **out)
 
 
+def renorm_operands(seed=71, r3=60, c3=24, per_row=7):
+    """Operands of a renormalisation T^dagger O T: T (r3 x c3, CCS) with each column supported on one
+    block of rows, T^dagger as CRS, O (r3 x r3, CRS) with a row whose products cancel exactly."""
+    rng = np.random.default_rng(seed)
+    blocks = np.sort(rng.integers(0, 6, r3))
+    T = np.zeros((r3, c3))
+    for j in range(c3):
+        rows = np.flatnonzero(blocks == j % 6)
+        T[rows, j] = rng.standard_normal(len(rows))
+    O = sp.random(r3, r3, density=per_row / r3, random_state=seed, data_rvs=rng.standard_normal).toarray()
+    O[O == 0] = 0.0
+    # row 0: +x on row a and -x on row b of T, where T's rows a and b are equal -> exact zeros
+    a, b = 1, 2
+    T[b] = T[a]
+    O[0] = 0.0
+    O[0, a], O[0, b] = 0.75, -0.75
+    M3 = sp.csc_matrix(T)
+    return abi.Crs.from_scipy(sp.csr_matrix(T.T)), abi.Crs.from_scipy(sp.csr_matrix(O)), abi.Ccs.from_scipy(M3)
+
+
+def renorm_fixture():
+    """The reference's CRS_CRS_CCS_PRODUCT on seeded renormalisation operands."""
+    M1, M2, M3 = renorm_operands()
+    ref = po.load_ref()
+    r = po.call_crs_crs_ccs(ref, M1, M2, M3, 60 * 24, 24 * 24)
+    names = ("w_col", "w_row", "w_val", "o_row", "o_col", "o_val")
+    ops = dict(m1_row=M1.row, m1_col=M1.col[:M1.nnz], m1_val=M1.val[:M1.nnz], m2_row=M2.row, m2_col=M2.col[:M2.nnz],
+               m2_val=M2.val[:M2.nnz], m3_col=M3.col, m3_row=M3.row[:M3.col[-1]], m3_val=M3.val[:M3.col[-1]],
+               dims=np.array([M1.struct.row_dim, M2.struct.row_dim, M3.struct.row_dim, M3.struct.col_dim]))
+    np.savez_compressed(HERE / "renorm.npz", **dict(zip(names, r[:6])), shape=np.array(r[7]), **ops)
+
+
 def obc_fixture():
     """The reference's matrix-free superblock product and OBC Lanczos on a seeded
     synthetic superblock (spin-1/2 sites, one block quantum number)."""
@@ -286,6 +318,7 @@ def main():
     vm_fixture()
     sb_obs_fixture()
     ed_obs_fixture()
+    renorm_fixture()
     obc_fixture()
     xxz_energy_fixture()
     for f in sorted(HERE.glob("*.npz")):

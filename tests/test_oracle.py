@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
-from conftest import golden, klm_model_from_golden
+from conftest import golden, klm_model_from_golden, renorm_operands_from_golden
 from dmrg_c_gb300 import abi, ed_models, superblock
 
 
@@ -336,3 +336,17 @@ def test_ed_expectation_matches_reference_golden(oracle):
         assert np.array_equal(t1, g[f"inter_{start}_{end}_t1"])
         got = [t1 @ oracle.site_apply(dens, basis, basis, 4, s, vec) for s in range(start, end)]
         assert np.allclose(got, g[f"inter_{start}_{end}"], rtol=0, atol=tol)
+
+
+def test_renorm_product_matches_reference_golden(oracle):
+    """CRS_CRS_CCS_PRODUCT restated (numpy, the reference's summation order) equals the reference's
+    intermediate (CCS) and result (CRS) bit for bit, exact cancellations dropped."""
+    g = golden("renorm.npz")
+    M1, M2, M3 = renorm_operands_from_golden(g)
+    got = oracle.crs_crs_ccs(M1, M2, M3)
+    for a, name in zip(got, ("w_col", "w_row", "w_val", "o_row", "o_col", "o_val")):
+        a = np.asarray(a)
+        b = g[name]
+        assert a.shape == b.shape, name
+        assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a.astype(np.int64),
+                              b.view(np.int64) if b.dtype == np.float64 else b.astype(np.int64)), name
