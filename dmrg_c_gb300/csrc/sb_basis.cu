@@ -176,11 +176,15 @@ dg_sb_basis *sb_basis_build(const dg_sb_basis_spec *s) {
 void SbPairs::finish_and_upload() {
   rho_off.assign(B + 1, 0);
   sig_off.assign(B + 1, 0);
+  rho_tri.assign(B + 1, 0);
+  sig_tri.assign(B + 1, 0);
   q_off.assign(B + 1, 0);
   for (int g = 0; g < B; ++g) {
     const int64_t Pg = blk_run0[g + 1] - blk_run0[g], Q = blk_Q[g];
     rho_off[g + 1] = rho_off[g] + Pg * Pg;
     sig_off[g + 1] = sig_off[g] + Q * Q;
+    rho_tri[g + 1] = rho_tri[g] + Pg * (Pg + 1) / 2;
+    sig_tri[g + 1] = sig_tri[g] + Q * (Q + 1) / 2;
     q_off[g + 1] = q_off[g] + Q;
   }
   cudaStream_t st = stream();
@@ -194,6 +198,8 @@ void SbPairs::finish_and_upload() {
   upload(d_blk_base, blk_base, st);
   upload(d_rho_off, rho_off, st);
   upload(d_sig_off, sig_off, st);
+  upload(d_rho_tri, rho_tri, st);
+  upload(d_sig_tri, sig_tri, st);
   upload(d_q_off, q_off, st);
   DG_CUDA(cudaStreamSynchronize(st));   // the host vectors may change later
 }

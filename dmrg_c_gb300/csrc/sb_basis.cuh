@@ -23,11 +23,12 @@ struct SbPairs {
   std::vector<int> blk_Q;                     // [B]   states per run
   std::vector<int64_t> blk_base;              // [B]   first state of each block
   std::vector<int64_t> rho_off, sig_off, q_off;   // [B+1] prefix sums of P^2, Q^2, Q
+  std::vector<int64_t> rho_tri, sig_tri;          // [B+1] prefix sums of P(P+1)/2, Q(Q+1)/2
   std::vector<int> pair_run;                  // [dim_LL*d] run of each (LL, LR) pair, -1 if absent
   std::vector<int> rrrl_pos;                  // [B*dim_RR*d] position t of (RR, RL) in block g, -1 if absent
   // device copies
   DevBuf<int> d_run_ll, d_run_lr, d_run_blk, d_blk_run0, d_blk_Q, d_pair_run, d_rrrl_pos;
-  DevBuf<int64_t> d_blk_base, d_rho_off, d_sig_off, d_q_off;
+  DevBuf<int64_t> d_blk_base, d_rho_off, d_sig_off, d_q_off, d_rho_tri, d_sig_tri;
   void finish_and_upload();   // fills the prefix sums and the device copies
 };
 

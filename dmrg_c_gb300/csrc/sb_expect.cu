@@ -168,12 +168,13 @@ __global__ void __launch_bounds__(kThreads) k_sb_expect_sum(const double *__rest
 struct PairView {
   int R, B, dim_RR, d;
   const int *run_ll, *run_lr, *run_blk, *blk_run0, *blk_Q, *pair_run, *rrrl_pos;
-  const int64_t *blk_base, *rho_off, *sig_off, *q_off;
+  const int64_t *blk_base, *rho_off, *sig_off, *q_off, *rho_tri, *sig_tri;
 };
 
 PairView pair_view(const SbPairs &P) {
   return PairView{P.R, P.B, P.dim_RR, P.d, P.d_run_ll.get(), P.d_run_lr.get(), P.d_run_blk.get(), P.d_blk_run0.get(), P.d_blk_Q.get(),
-                  P.d_pair_run.get(), P.d_rrrl_pos.get(), P.d_blk_base.get(), P.d_rho_off.get(), P.d_sig_off.get(), P.d_q_off.get()};
+                  P.d_pair_run.get(), P.d_rrrl_pos.get(), P.d_blk_base.get(), P.d_rho_off.get(), P.d_sig_off.get(), P.d_q_off.get(),
+                  P.d_rho_tri.get(), P.d_sig_tri.get()};
 }
 
 // Largest g in [0, B) with off[g] <= e (off ascending, off[0] = 0).
@@ -189,44 +190,80 @@ __device__ __forceinline__ int find_block(const int64_t *__restrict__ off, int B
   return lo;
 }
 
-// rho_g[p][q] = sum_t w[row p][t] * v[row q][t] for every block, summed over t in order and rounded
-// as written (with w = v these are DMRG_GET_DENSITY_MATRIX's entries, bit for bit).  sym (w = v):
-// only p <= q is computed and mirrored -- the products of (q, p) are those of (p, q), so the mirror
-// is the value the sum would give.
+// (p, q), p <= q, of the loc-th entry of an n x n upper triangle taken row by row.
+__device__ __forceinline__ void tri_index(int64_t loc, int n, int &p, int &q) {
+  // row p starts at p*n - p*(p-1)/2; estimate p from the quadratic, then correct
+  const float b = 2.0f * n + 1.0f;
+  int r = (int)floorf((b - sqrtf(fmaxf(b * b - 8.0f * (float)loc, 0.0f))) * 0.5f);
+  r = max(0, min(r, n - 1));
+  auto start = [&](int x) { return (int64_t)x * n - (int64_t)x * (x - 1) / 2; };
+  while (r > 0 && start(r) > loc) --r;
+  while (r + 1 < n && start(r + 1) <= loc) ++r;
+  p = r;
+  q = r + (int)(loc - start(r));
+}
+
+// The sum of x[k*stride] * y[k*stride] over k < len, in k order: EXACT rounds every product and
+// sum as written (the reference's density-matrix entries, bitwise), else fused multiply-adds (half
+// the FP64 instructions; for the expectation values, which only need the value to 1e-16).
+template <bool EXACT>
+__device__ __forceinline__ double dot_strided(const double *__restrict__ x, const double *__restrict__ y, int len, int64_t stride) {
+  double acc = 0.0;
+  for (int k = 0; k < len; ++k) {
+    const double a = x[(int64_t)k * stride], b = y[(int64_t)k * stride];
+    acc = EXACT ? __dadd_rn(acc, __dmul_rn(a, b)) : fma(a, b, acc);
+  }
+  return acc;
+}
+
+// rho_g[p][q] = sum_t w[row p][t] * v[row q][t] for every block, summed over t in order (with
+// EXACT and w = v these are DMRG_GET_DENSITY_MATRIX's entries, bit for bit).  SYM (w = v): only the
+// upper triangles are enumerated (every thread has an entry) and mirrored -- the products of
+// (q, p) are those of (p, q), so the mirror is the value its own sum would give.
+template <bool SYM, bool EXACT>
 __global__ void __launch_bounds__(kThreads) k_gram_rows(PairView P, const double *__restrict__ w, const double *__restrict__ v,
-                                                       int sym, double *__restrict__ rho) {
-  const int64_t total = P.rho_off[P.B];
+                                                       double *__restrict__ rho) {
+  const int64_t *off = SYM ? P.rho_tri : P.rho_off;
+  const int64_t total = off[P.B];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int g = find_block(P.rho_off, P.B, e);
+    const int g = find_block(off, P.B, e);
     const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
-    const int64_t loc = e - P.rho_off[g];
-    const int p = (int)(loc / Pg), q = (int)(loc - (int64_t)p * Pg);
-    if (sym && p > q) continue;
-    const double *__restrict__ x = w + P.blk_base[g] + (int64_t)p * Q;
-    const double *__restrict__ y = v + P.blk_base[g] + (int64_t)q * Q;
-    double acc = 0.0;
-    for (int t = 0; t < Q; ++t) acc = __dadd_rn(acc, __dmul_rn(x[t], y[t]));
-    rho[e] = acc;
-    if (sym) rho[P.rho_off[g] + (int64_t)q * Pg + p] = acc;
+    const int64_t loc = e - off[g];
+    int p, q;
+    if (SYM) {
+      tri_index(loc, Pg, p, q);
+    } else {
+      p = (int)(loc / Pg);
+      q = (int)(loc - (int64_t)p * Pg);
+    }
+    const double acc = dot_strided<EXACT>(w + P.blk_base[g] + (int64_t)p * Q, v + P.blk_base[g] + (int64_t)q * Q, Q, 1);
+    double *blk = rho + P.rho_off[g];
+    blk[(int64_t)p * Pg + q] = acc;
+    if (SYM) blk[(int64_t)q * Pg + p] = acc;
   }
 }
 
-// sigma_g[t][u] = sum_p w[row p][t] * v[row p][u] for every block (sym: t <= u, mirrored).
+// sigma_g[t][u] = sum_p w[row p][t] * v[row p][u] for every block (SYM: upper triangles, mirrored).
+template <bool SYM>
 __global__ void __launch_bounds__(kThreads) k_gram_cols(PairView P, const double *__restrict__ w, const double *__restrict__ v,
-                                                       int sym, double *__restrict__ sig) {
-  const int64_t total = P.sig_off[P.B];
+                                                       double *__restrict__ sig) {
+  const int64_t *off = SYM ? P.sig_tri : P.sig_off;
+  const int64_t total = off[P.B];
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int g = find_block(P.sig_off, P.B, e);
+    const int g = find_block(off, P.B, e);
     const int Pg = P.blk_run0[g + 1] - P.blk_run0[g], Q = P.blk_Q[g];
-    const int64_t loc = e - P.sig_off[g];
-    const int t = (int)(loc / Q), u = (int)(loc - (int64_t)t * Q);
-    if (sym && t > u) continue;
-    const double *__restrict__ x = w + P.blk_base[g] + t;
-    const double *__restrict__ y = v + P.blk_base[g] + u;
-    double acc = 0.0;
-    for (int p = 0; p < Pg; ++p) acc = __dadd_rn(acc, __dmul_rn(x[(int64_t)p * Q], y[(int64_t)p * Q]));
-    sig[e] = acc;
-    if (sym) sig[P.sig_off[g] + (int64_t)u * Q + t] = acc;
+    const int64_t loc = e - off[g];
+    int t, u;
+    if (SYM) {
+      tri_index(loc, Q, t, u);
+    } else {
+      t = (int)(loc / Q);
+      u = (int)(loc - (int64_t)t * Q);
+    }
+    const double acc = dot_strided<false>(w + P.blk_base[g] + t, v + P.blk_base[g] + u, Pg, Q);
+    double *blk = sig + P.sig_off[g];
+    blk[(int64_t)t * Q + u] = acc;
+    if (SYM) blk[(int64_t)u * Q + t] = acc;
   }
 }
 
@@ -485,18 +522,24 @@ void launch_trace(const dg_sb_basis *b, const std::vector<SbTerm> &terms, const 
   DevBuf<double> rho[2], sig[2];
   const double *w[2] = {w0, w1};
   for (int k = 0; k < 2; ++k) {
-    const int sym = w[k] == v;
+    const bool sym = w[k] == v;
     if (rows[k]) {
-      const int64_t total = P.rho_off[P.B];
-      rho[k].alloc(total);
-      k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sym, rho[k].get());
+      rho[k].alloc(P.rho_off[P.B]);
+      const int64_t total = sym ? P.rho_tri[P.B] : P.rho_off[P.B];
+      if (sym)
+        k_gram_rows<true, false><<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, rho[k].get());
+      else
+        k_gram_rows<false, false><<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, rho[k].get());
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
     if (cols[k]) {
-      const int64_t total = P.sig_off[P.B];
-      sig[k].alloc(total);
-      k_gram_cols<<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sym, sig[k].get());
+      sig[k].alloc(P.sig_off[P.B]);
+      const int64_t total = sym ? P.sig_tri[P.B] : P.sig_off[P.B];
+      if (sym)
+        k_gram_cols<true><<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sig[k].get());
+      else
+        k_gram_cols<false><<<(int)state_grid(total), kThreads, 0, st>>>(pv, w[k], v, sig[k].get());
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
@@ -1061,7 +1104,7 @@ int dg_sb_density_matrix(const dg_sb_basis *b, const double *v, double *rho) {
       ob.alloc(total);
       dr = ob.get();
     }
-    k_gram_rows<<<(int)state_grid(total), kThreads, 0, st>>>(pair_view(P), dv, dv, 1, dr);
+    k_gram_rows<true, true><<<(int)state_grid(P.rho_tri[P.B]), kThreads, 0, st>>>(pair_view(P), dv, dv, dr);
     count_launch();
     DG_CUDA(cudaGetLastError());
     if (!out_dev) DG_CUDA(cudaMemcpyAsync(rho, dr, sizeof(double) * total, cudaMemcpyDeviceToHost, st));
