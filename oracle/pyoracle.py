@@ -454,6 +454,18 @@ def system_info(qns, states, inv, d, dim_RR, v, lllr, max_dim):
             if abs(val[i - 1] - val[i]) > zero and val[i - 1] > zero:
                 dim_renorm = i
                 break
+    # per block: the distance between its kept and its dropped eigenvalues, and its norm (the kept
+    # subspace of a block is determined to about 1e-16 * norm / gap)
+    kept_set = set(order[:dim_renorm])
+    gaps = {}
+    for g in range(len(blocks)):
+        if len(blocks[g]) == 0:
+            continue
+        es = [e for e in range(len(items)) if items[e][0] == g]
+        kv = [vals[g][items[e][1]] for e in es if e in kept_set]
+        dv = [vals[g][items[e][1]] for e in es if e not in kept_set]
+        gap = min((abs(a - b) for a in kv for b in dv), default=np.inf)
+        gaps[int(starts[g])] = (gap, float(np.abs(vals[g]).max()))
     kept = sorted(order[:dim_renorm], key=lambda e: tuple(int(q[starts[items[e][0]]]) for q in qns))
     cols, rows, qn_out = [], [], [[] for _ in qns]
     for e in kept:
@@ -463,6 +475,7 @@ def system_info(qns, states, inv, d, dim_RR, v, lllr, max_dim):
         for k, q in enumerate(qns):
             qn_out[k].append(int(q[starts[g]]))
     return dict(dim_renorm=dim_renorm, val=val, sum_val=float(np.sum(val)), tr_error=float(np.sum(val) - np.sum(val[:dim_renorm])),
+                gaps=gaps,
                 qn=[np.array(x, np.int32) for x in qn_out], col_ptr=np.concatenate([[0], np.cumsum([len(r) for r in rows])]),
                 rows=np.concatenate(rows) if rows else np.zeros(0, int), vals=np.concatenate(cols) if cols else np.zeros(0))
 
@@ -508,7 +521,10 @@ def same_truncation(a, b, tol_val=1e-13, tol_proj=1e-9):
     """Two system_info results describe the same truncation: the same kept dimension, quantum
     numbers and sparsity; spectra within tol_val; and, per block of equal quantum numbers, the
     same kept subspace (projectors within tol_proj -- eigenvectors are fixed only up to sign and,
-    inside a degenerate multiplet, up to rotation).  Returns a list of differences (empty: same)."""
+    inside a degenerate multiplet, up to rotation).  Where b carries the oracle's per-block gaps
+    between kept and dropped eigenvalues, a block's projector tolerance grows by 1e-13 * norm / gap:
+    two correct eigensolvers may differ by that much on a subspace whose cut falls into a narrow
+    gap.  Returns a list of differences (empty: same)."""
     bad = []
     tol_val = tol_val * max(1.0, abs(a["sum_val"]))
     if a["dim_renorm"] != b["dim_renorm"]:
@@ -534,7 +550,11 @@ def same_truncation(a, b, tol_val=1e-13, tol_proj=1e-9):
         dim = cp[j + 1] - cp[j]
         Ta = np.stack([a["vals"][cp[c]:cp[c + 1]] for c in range(j, j1)], axis=1)
         Tb = np.stack([b["vals"][cp[c]:cp[c + 1]] for c in range(j, j1)], axis=1)
-        if np.abs(Ta @ Ta.T - Tb @ Tb.T).max() > tol_proj or dim != Ta.shape[0]:
+        tol = tol_proj
+        if "gaps" in b and int(r0) in b["gaps"]:
+            gap, norm = b["gaps"][int(r0)]
+            tol = tol_proj + (1e-13 * norm / gap if gap > 0 else np.inf)
+        if np.abs(Ta @ Ta.T - Tb @ Tb.T).max() > tol or dim != Ta.shape[0]:
             bad.append(f"subspace of the block at row {r0}")
         j = j1
     return bad
