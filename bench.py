@@ -299,6 +299,16 @@ def run_gb300(args, ws, rank, local_rank):
     mixed_rec = mixed_leg(2)
     mixed_rec["form"] = "FP32 SpMV (compensated FP32 sums) + FP64 three-term recurrence, Jacobi-Davidson refinement"
 
+    # the steps after the solve on the solved vector: site expectation values, truncation to m
+    # states, renormalisation of a block operator (EXPECTATION_VALUES / RENORMALIZE / TRANSFORM_MATRIX)
+    try:
+        from dmrg_c_gb300 import dmrg_step, workloads
+        qb, qs, _target, m_keep = workloads.superblock_labels(args.workload, args.seed)
+        n_sites = {"klm_m128": 11, "hubbard_m512": 31, "xxz_m64": 15}[args.workload]
+        post = dmrg_step.post_solve(sb, qb, qs, eigvec, m_keep, n_sites)
+    except Exception as e:   # recorded, the solve measurement stands
+        post = {"error": f"{type(e).__name__}: {e}"}
+
     # roofline of the SpMV kernel
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
@@ -367,6 +377,7 @@ def run_gb300(args, ws, rank, local_rank):
         "clocks": clk.summary(),
         "mixed": mixed,
         "mixed_fp32_spmv": mixed_rec,
+        "post_solve": post,
     }
     if rank == 0 and not args.no_hbm_case:
         result["roofline_hbm_case"] = hbm_case_roofline(peak, peak_kind)

@@ -66,6 +66,18 @@ def hubbard_superblock_m512(seed=0):
                                            seed=seed + 1, with_sign=True)
 
 
+def superblock_labels(name, seed=0):
+    """(block labels, site labels, target, kept states m) of the synthetic superblock `name` (the
+    labels the generators above draw, so the sector and its order are the same)."""
+    if name == "klm_m128":
+        return _block_labels(128, 11, 5.0, 0.95, 0.85, seed), klm_site_labels(), 12 * QN_SCALE, 128
+    if name == "hubbard_m512":
+        return _block_labels(512, 31, 31.0, 1.25, 0.9, seed), hubbard_site_labels(), 64 * QN_SCALE, 512
+    if name == "xxz_m64":
+        return _block_labels(64, 15, 0, 0, 0.95, seed, fermions=False), np.array([1, -1]), 0, 64
+    raise KeyError(name)
+
+
 def xxz_ed_batch(count=256, seed=0):
     """Batched XXZ ED instances: L uniform in {12,...,22}, Jz ~ U[0,2], hz ~ U[0,1], Jxy = 1, 2Sz = 0, OBC."""
     rng = np.random.default_rng(seed)
