@@ -350,3 +350,16 @@ def test_renorm_product_matches_reference_golden(oracle):
         assert a.shape == b.shape, name
         assert np.array_equal(a.view(np.int64) if a.dtype == np.float64 else a.astype(np.int64),
                               b.view(np.int64) if b.dtype == np.float64 else b.astype(np.int64)), name
+
+
+def test_dmrg_step_lllr_list_is_the_oracles(oracle):
+    """The post-solve driver lays out the LLLR list exactly as the oracle (pinned to the reference)
+    does."""
+    from dmrg_c_gb300 import dmrg_step, superblock, workloads
+    qb = workloads._block_labels(48, 9, 9.0, 1.0, 0.9, 7)
+    qs = workloads.hubbard_site_labels()
+    sb = superblock.synthetic_superblock(48, 4, qb, qs, 20 * workloads.QN_SCALE, nnz_lllr=6, nnz_lrrl=2, seed=8)
+    states = (sb.LL, sb.LR, sb.RR, sb.RL)
+    a, b = dmrg_step.lllr_list(qb, qs, states), oracle.lllr_list(qb, qs, states)
+    for x, y in zip(a, b[:4]):
+        assert np.array_equal(x, y)
