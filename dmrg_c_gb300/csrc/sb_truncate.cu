@@ -96,7 +96,7 @@ struct EigBlk {
 // count).  Blocks are in descending size.
 __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__restrict__ blks, const double *__restrict__ Ag,
                                                             double *__restrict__ Vg, double *__restrict__ Wg, int max_sweeps,
-                                                            int *__restrict__ sweeps) {
+                                                            int *__restrict__ sweeps, double *gwork, int64_t gstride) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int cs = (int)cluster.num_blocks();
@@ -114,23 +114,31 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
   const int rows = (n + cs - 1) / cs;
   const int r0 = rank * rows, r1 = min(n, r0 + rows), nloc = max(0, r1 - r0);
   const int64_t slab = (int64_t)rows * n;
-  double *V = sm_jac + 2 * slab;
+  // this CTA's rows: in shared memory, or (gwork != null, blocks too large for it) in a global
+  // workspace of gstride doubles a CTA
+  double *const mine = gwork ? gwork + (int64_t)blockIdx.x * gstride : sm_jac;
+  double *V = mine + 2 * slab;
   for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
     const int64_t i = r0 + e / n, j = e % n;
-    sm_jac[e] = Ag[b.off + i * n + j];
+    mine[e] = Ag[b.off + i * n + j];
     V[e] = i == j ? 1.0 : 0.0;
   }
   int cur = 0;   // the copy holding the current A
   auto row_ptr = [&](int i) -> const double * {   // row i of the current A, in whichever CTA keeps it
-    const double *base = cluster.map_shared_rank(sm_jac, i / rows);
+    const int owner = i / rows;
+    const double *base =
+        gwork ? gwork + (int64_t)(blockIdx.x - rank + owner) * gstride : cluster.map_shared_rank(sm_jac, owner);
     return base + cur * slab + (int64_t)(i % rows) * n;
   };
+  // a value of another CTA's rows (global workspace: read from L2, where the writer's stores are
+  // visible after the cluster barrier)
+  auto rd = [&](const double *p) { return gwork ? __ldcg(p) : *p; };
   if (threadIdx.x == 0) s_rot = 1;
   cluster.sync();
   const int m = n + (n & 1), half = m / 2;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
-    const double *A = sm_jac + cur * slab;
+    const double *A = mine + cur * slab;
     double off = 0.0, tot = 0.0;
     for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
       const double a = A[e];
@@ -183,9 +191,9 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
         double c = 1.0, s = 0.0;
         if (q < n) {
           const double *rowp = row_ptr(p);
-          const double apq = rowp[q];
+          const double apq = rd(rowp + q);
           if (fabs(apq) > s_tol) {
-            const double th = (row_ptr(q)[q] - rowp[p]) / (2.0 * apq);
+            const double th = (rd(row_ptr(q) + q) - rd(rowp + p)) / (2.0 * apq);
             const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
             c = 1.0 / sqrt(t * t + 1.0);
             s = t * c;
@@ -201,8 +209,8 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
       }
       __syncthreads();
       // 2. this CTA's rows of A' = J^T A J into the next copy; its rows of V rotated in place
-      const double *Acur = sm_jac + cur * slab;
-      double *Anext = sm_jac + (cur ^ 1) * slab;
+      const double *Acur = mine + cur * slab;
+      double *Anext = mine + (cur ^ 1) * slab;
       for (int idx = threadIdx.x; idx < nloc * half; idx += blockDim.x) {
         const int li = idx / half, l = idx - li * half;
         const int i = r0 + li;
@@ -217,7 +225,8 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
         // row rotation of row i at columns pl (and ql)
         auto rowrot = [&](int j) {
           if (si == 0.0) return ai[j];
-          return i_is_p ? ci * ai[j] - si * ap[j] : si * ap[j] + ci * ai[j];
+          const double y = rd(ap + j);
+          return i_is_p ? ci * ai[j] - si * y : si * y + ci * ai[j];
         };
         double *out = Anext + (int64_t)li * n;
         const double xp = rowrot(pl);
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
       cur ^= 1;
     }
   }
-  const double *A = sm_jac + cur * slab;
+  const double *A = mine + cur * slab;
   for (int i = threadIdx.x; i < nloc; i += blockDim.x) Wg[b.woff + r0 + i] = A[(int64_t)i * n + r0 + i];
   for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) Vg[b.off + (int64_t)r0 * n + e] = V[e];
   if (rank == 0 && threadIdx.x == 0) sweeps[blockIdx.x / cs] = sweep;
@@ -369,10 +378,10 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       count_launch();
       DG_CUDA(cudaGetLastError());
     }
-    // one cluster a block, the largest blocks first; 8 CTAs a cluster (16 when a block's rows
-    // would not fit 8 CTAs' shared memory)
+    // one cluster a block, the largest blocks first
     auto smem_for = [&](int c) { return 3 * sizeof(double) * (size_t)((max_n + c - 1) / c) * max_n; };
-    DG_REQUIRE(smem_for(16) <= kJacobiSmem, DG_ERR_ARG, "a density block of %d pairs is too large for the eigensolver", max_n);
+    // blocks whose rows do not fit 16 CTAs' shared memory keep them in a global workspace instead
+    const bool gmem = smem_for(16) > kJacobiSmem;
     std::vector<int> by_size(nb);
     std::iota(by_size.begin(), by_size.end(), 0);
     std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) { return eb[a].n > eb[b].n; });
@@ -387,13 +396,14 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     if (max_n >= 64 && cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
       cs = 16;
     cudaGetLastError();
-    if (smem_for(8) > kJacobiSmem) cs = 16;
+    if (!gmem && smem_for(8) > kJacobiSmem) cs = 16;
+    DevBuf<double> gwork;
     for (;;) {
       cudaLaunchConfig_t cfg;
       std::memset(&cfg, 0, sizeof(cfg));
       cfg.gridDim = dim3((unsigned)(nb * cs));
       cfg.blockDim = dim3(kThreads);
-      cfg.dynamicSmemBytes = smem_for(cs);
+      cfg.dynamicSmemBytes = gmem ? 0 : smem_for(cs);
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -405,12 +415,14 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       int clusters = 0;
       if (cudaOccupancyMaxActiveClusters(&clusters, k_jacobi_cluster, &cfg) != cudaSuccess || clusters < 1) {
         cudaGetLastError();
-        DG_REQUIRE(cs == 16 && smem_for(8) <= kJacobiSmem, DG_ERR_CUDA, "the device runs no cluster of %d CTAs", cs);
+        DG_REQUIRE(cs == 16 && (gmem || smem_for(8) <= kJacobiSmem), DG_ERR_CUDA, "the device runs no cluster of %d CTAs", cs);
         cs = 8;   // try the portable size
         continue;
       }
+      const int64_t gstride = 3 * (int64_t)((max_n + cs - 1) / cs) * max_n;
+      if (gmem) gwork.alloc((size_t)nb * cs * gstride);
       DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
-                                 kJacobiSweeps, dsw.get()));
+                                 kJacobiSweeps, dsw.get(), gmem ? gwork.get() : (double *)nullptr, gstride));
       cs_used = cs;
       break;
     }

@@ -90,3 +90,21 @@ def test_system_info_hubbard_m512_vs_oracle(gpu, oracle):
     got = oracle.call_system_info(gpu.load(), qns, st, inv, 512, 512, d, v, lllr, 512, _free())
     assert oracle.same_truncation(got, want) == []
     assert got["time"] > 0
+
+
+def test_system_info_block_beyond_shared_memory(gpu, oracle):
+    """One density block of 400 pairs (every state with one label): too large for the CTAs' shared
+    memory, so the eigensolver keeps its rows in a global workspace."""
+    dim, d = 200, 2
+    qb, qs = np.zeros(dim, np.int64), np.zeros(d, np.int64)
+    st = sb_models.sector_states(qb, qb, qs, 0)
+    inv = -np.ones(dim * d * dim * d, np.int32)
+    inv[((st[0].astype(np.int64) * d + st[1]) * dim + st[2]) * d + st[3]] = np.arange(len(st[0]), dtype=np.int32)
+    lllr = oracle.lllr_list(qb, qs, st)
+    assert len(lllr[4]) == 1 and lllr[4][0] == 400
+    v = np.random.default_rng(23).standard_normal(len(st[0]))
+    v /= np.linalg.norm(v)
+    qns = [np.zeros(dim * d, np.int32)]
+    want = oracle.system_info(qns, st, inv, d, dim, v, lllr, 100)
+    got = oracle.call_system_info(gpu.load(), qns, st, inv, dim, dim, d, v, lllr, 100, _free())
+    assert oracle.same_truncation(got, want) == []
