@@ -94,6 +94,7 @@ struct EigBlk {
 // the off-diagonal part is below 1e-16 of the norm or a sweep found nothing to rotate (decided by
 // CTA 0 and broadcast, so every CTA leaves together), or after max_sweeps (sweeps[g] reports the
 // count).  Blocks are in descending size.
+template <bool GMEM>
 __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__restrict__ blks, const double *__restrict__ Ag,
                                                             double *__restrict__ Vg, double *__restrict__ Wg, int max_sweeps,
                                                             int *__restrict__ sweeps, double *gwork, int64_t gstride) {
@@ -114,9 +115,9 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
   const int rows = (n + cs - 1) / cs;
   const int r0 = rank * rows, r1 = min(n, r0 + rows), nloc = max(0, r1 - r0);
   const int64_t slab = (int64_t)rows * n;
-  // this CTA's rows: in shared memory, or (gwork != null, blocks too large for it) in a global
-  // workspace of gstride doubles a CTA
-  double *const mine = gwork ? gwork + (int64_t)blockIdx.x * gstride : sm_jac;
+  // this CTA's rows: in shared memory, or (GMEM, blocks too large for it) in the global workspace
+  // gwork, gstride doubles a CTA
+  double *const mine = GMEM ? gwork + (int64_t)blockIdx.x * gstride : sm_jac;
   double *V = mine + 2 * slab;
   for (int64_t e = threadIdx.x; e < (int64_t)nloc * n; e += blockDim.x) {
     const int64_t i = r0 + e / n, j = e % n;
@@ -127,12 +128,12 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
   auto row_ptr = [&](int i) -> const double * {   // row i of the current A, in whichever CTA keeps it
     const int owner = i / rows;
     const double *base =
-        gwork ? gwork + (int64_t)(blockIdx.x - rank + owner) * gstride : cluster.map_shared_rank(sm_jac, owner);
+        GMEM ? gwork + (int64_t)(blockIdx.x - rank + owner) * gstride : cluster.map_shared_rank(sm_jac, owner);
     return base + cur * slab + (int64_t)(i % rows) * n;
   };
   // a value of another CTA's rows (global workspace: read from L2, where the writer's stores are
   // visible after the cluster barrier)
-  auto rd = [&](const double *p) { return gwork ? __ldcg(p) : *p; };
+  auto rd = [&](const double *p) { return GMEM ? __ldcg(p) : *p; };
   if (threadIdx.x == 0) s_rot = 1;
   cluster.sync();
   const int m = n + (n & 1), half = m / 2;
@@ -392,8 +393,9 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     // 16 CTAs a cluster (a non-portable size) when the largest block has 64 pairs or more and the
     // device runs such clusters, else 8
     int cs = 8;
-    DG_CUDA(cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
-    if (max_n >= 64 && cudaFuncSetAttribute(k_jacobi_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
+    auto kernel = gmem ? k_jacobi_cluster<true> : k_jacobi_cluster<false>;
+    DG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
+    if (max_n >= 64 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
       cs = 16;
     cudaGetLastError();
     if (!gmem && smem_for(8) > kJacobiSmem) cs = 16;
@@ -413,7 +415,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       int clusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&clusters, k_jacobi_cluster, &cfg) != cudaSuccess || clusters < 1) {
+      if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess || clusters < 1) {
         cudaGetLastError();
         DG_REQUIRE(cs == 16 && (gmem || smem_for(8) <= kJacobiSmem), DG_ERR_CUDA, "the device runs no cluster of %d CTAs", cs);
         cs = 8;   // try the portable size
@@ -421,8 +423,8 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       }
       const int64_t gstride = 3 * (int64_t)((max_n + cs - 1) / cs) * max_n;
       if (gmem) gwork.alloc((size_t)nb * cs * gstride);
-      DG_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi_cluster, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(),
-                                 kJacobiSweeps, dsw.get(), gmem ? gwork.get() : (double *)nullptr, gstride));
+      DG_CUDA(cudaLaunchKernelEx(&cfg, kernel, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(), kJacobiSweeps,
+                                 dsw.get(), gmem ? gwork.get() : (double *)nullptr, gstride));
       cs_used = cs;
       break;
     }

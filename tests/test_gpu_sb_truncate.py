@@ -73,8 +73,8 @@ def test_system_info_q3_and_orthonormal_columns(gpu, oracle):
 
 
 def test_system_info_hubbard_m512_vs_oracle(gpu, oracle):
-    """The Hubbard m=512 superblock (L=64, half filling): 57 density blocks of up to 216 pairs, four
-    of them too large for shared memory; keep 512 states."""
+    """The Hubbard m=512 superblock (L=64, half filling): 57 density blocks of up to 216 pairs (16-CTA
+    clusters); keep 512 states."""
     qb = workloads._block_labels(512, 31, 31.0, 1.25, 0.9, 0)
     qs = workloads.hubbard_site_labels()
     st = sb_models.sector_states(qb, qb, qs, 64 * sb_models.QN_SCALE)
