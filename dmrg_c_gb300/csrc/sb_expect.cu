@@ -20,7 +20,6 @@
 // in one launch on a 2-D grid (state chunks x terms) without writing the per-site vectors, and a
 // second launch sums each term's block partials in a fixed order.
 #include <algorithm>
-#include <climits>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -703,12 +702,11 @@ Staged stage(const HostSector &h, const std::vector<HostOp> &ops, const int *ele
   return s;
 }
 
-int op_index(const Staged &s, const std::vector<HostOp> &ops, const CRS1 *M) {
-  // ops_upload kept the first appearance order of distinct pointers
+// Index of M in the operator set stage() uploaded (distinct pointers in first-appearance order).
+int op_index(const std::vector<HostOp> &ops, const CRS1 *M) {
   std::vector<const CRS1 *> uniq;
   for (const HostOp &o : ops)
     if (std::find(uniq.begin(), uniq.end(), o.M) == uniq.end()) uniq.push_back(o.M);
-  (void)s;
   return (int)(std::find(uniq.begin(), uniq.end(), M) - uniq.begin());
 }
 
@@ -795,10 +793,10 @@ void expect_host(const HostSector &h, const std::vector<HostOp> &terms_h, const 
   const SbStates S = states_of(s.b.get());
   const SbParity par = s.par.view();
   std::vector<SbTerm> terms;
-  for (const HostOp &o : terms_h) terms.push_back(term_of(s.ops.get(), op_index(s, all, o.M), o.pos, o.sign, o.weight));
+  for (const HostOp &o : terms_h) terms.push_back(term_of(s.ops.get(), op_index(all, o.M), o.pos, o.sign, o.weight));
   if (t1_op) {
     t1b.alloc(h.n);
-    launch_vm(S, s.b->inv.get(), s.g, term_of(s.ops.get(), op_index(s, all, t1_op->M), t1_op->pos, 0, 0), s.ops.get(), par, v, h.v_len,
+    launch_vm(S, s.b->inv.get(), s.g, term_of(s.ops.get(), op_index(all, t1_op->M), t1_op->pos, 0, 0), s.ops.get(), par, v, h.v_len,
               t1b.get(), bad.get(), st);
   }
   if (h.dim_LL > 0) s.b->pairs = sb_pairs_from_states(h.n, h.st, h.dim_LL, h.dim_RR, h.d);
