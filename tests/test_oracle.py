@@ -1,6 +1,8 @@
 """The oracle (CPU restatement) pinned against the reference: golden fixtures produced by
 the reference's own code (always), the live reference build (where its sources exist),
 and closed-form answers."""
+import ctypes as C
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -363,3 +365,54 @@ def test_dmrg_step_lllr_list_is_the_oracles(oracle):
     a, b = dmrg_step.lllr_list(qb, qs, states), oracle.lllr_list(qb, qs, states)
     for x, y in zip(a, b[:4]):
         assert np.array_equal(x, y)
+
+
+def test_live_reference_vm_whole_basis(ref):
+    """The reference's DMRG_V_M_*_Q1..Q4 on another seeded problem, called through the ctypes
+    DMRG_WHOLE_BASIS_Qk mirrors, equal the numpy restatement bit for bit (signs included)."""
+    from dmrg_c_gb300 import sb_models
+    p = sb_models.random_observable_problem(dim_LL=20, dim_RR=18, seed=13)
+    lib = ref.load_ref()
+    v = np.random.default_rng(5).standard_normal(len(p.sectors[p.target][0]))
+    q_out = p.target - 1001
+    shift = {0: p.ops["CdLL"][0], 1: p.ops["CdOn"], 2: p.ops["CdRR"][0], 3: p.ops["CdOn"]}
+    n = 0
+    for k in (1, 2, 3, 4):
+        wb = p.whole_basis(k)
+        for pos, op in shift.items():
+            if k == 4 and pos < 2:
+                continue
+            for sign in ((False,) if pos == 0 else (False, True)):
+                got = ref.call_vm_whole(lib, wb, p.index(q_out, k), op, pos, v, ele=p.ele, sign=sign)
+                want = ref.sb_vm(p.sectors[q_out], p.inv, p.dim_RR, p.d, op, pos, v, ele=p.ele if sign else None)
+                assert np.array_equal(got.view(np.int64), want.view(np.int64)), (k, pos, sign)
+                n += 1
+    assert n == 25
+
+
+def test_live_reference_truncation_and_renorm(ref):
+    """The reference's DMRG_GET_SYSTEM_INFO_Q2 and CRS_CRS_CCS_PRODUCT on a superblock ground state:
+    the restatements agree (the truncation as a truncation, the product bit for bit)."""
+    import scipy.sparse as sp
+    from dmrg_c_gb300 import superblock, workloads
+    qb = workloads._block_labels(40, 8, 8.0, 1.0, 0.9, 17)
+    qs = workloads.hubbard_site_labels()
+    sb = superblock.synthetic_superblock(40, 4, qb, qs, 18 * workloads.QN_SCALE, nnz_lllr=6, nnz_lrrl=2, seed=19)
+    w, V = np.linalg.eigh(sb.explicit().toarray())
+    psi = V[:, 0]
+    states = (sb.LL, sb.LR, sb.RR, sb.RL)
+    lllr = ref.lllr_list(qb, qs, states)
+    N = np.rint(lllr[3] / 1000).astype(np.int32)
+    qns = [N, (lllr[3] - N * 1000).astype(np.int32)]
+    libc = C.CDLL(None)
+    libc.free.argtypes = [C.c_void_p]
+    got = ref.call_system_info(ref.load_ref(), qns, states, sb.inv, 40, 40, 4, psi, lllr, 30, libc.free)
+    assert ref.same_truncation(got, ref.system_info(qns, states, sb.inv, 4, 40, psi, lllr, 30)) == []
+    nr, L = got["dim_renorm"], len(lllr[0])
+    T = sp.csc_matrix((got["vals"], got["rows"], got["col_ptr"]), shape=(L, nr))
+    O = sp.random(L, L, density=0.05, random_state=3, format="csr")
+    M1, M2, M3 = abi.Crs.from_scipy(sp.csr_matrix(T.T)), abi.Crs.from_scipy(O + O.T), abi.Ccs.from_scipy(T)
+    r = ref.call_crs_crs_ccs(ref.load_ref(), M1, M2, M3, L * nr, nr * nr)
+    for x, y in zip(r[:6], ref.crs_crs_ccs(M1, M2, M3)):
+        x, y = np.asarray(x), np.asarray(y)
+        assert np.array_equal(x.astype(np.float64).view(np.int64), y.astype(np.float64).view(np.int64))
