@@ -1,30 +1,35 @@
 #!/usr/bin/env python3
-"""Benchmark: superblock ground-state solves on GB300 (one JSON line on stdout).
+"""Benchmark: DMRG superblock ground-state solves on GB300 (one JSON line on stdout).
 
-Workload (default ``klm_m128``): the largest superblock of the Kondo-lattice DMRG
-configuration (klm_vf, L=24, N_e=12, 2Sz=0, m=128; d=8 sites) -- n = 56,612 states,
-3.69e6 stored entries of the full matrix -- built from seeded synthetic block operators
-(dmrg_c_gb300.workloads; no DMRG sweep runs).  One step = one ground-state solve exactly as
-DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: Lanczos (acc 1e-14, Normal) then inverse iteration
-(CG, ii_acc 1e-9), FP64.
+Workloads are superblocks of the reference's own DMRG runs (tests/golden/dmrg_<model>_sweep<k>.npz,
+recorded from main/dmrg/<model> at the configurations below; the term list is built into the
+superblock CRS on the device, bitwise the reference's GET_HAM_LLLRRRRL):
 
-* ``value``: solves/s with the matrix resident on the device, device time (CUDA events of
-  the library stream) summed over K steps; L2 is flushed (256 MiB rewrite) before every step.
-* ``mixed``: the same solve in the mixed-precision form (FP32 values and Krylov vectors, FP64
-  recurrence, reorthogonalisation and refinement), with its energy error and eigenvector
-  overlap against the FP64 result.
-* ``e2e``: solves/s through the drop-in C entry point DMRG_DIAGONALIZE_SUPERBLOCK_SYM from
-  host arrays (upload, device expansion, solve, eigenvector download inside the timing).
-* ``roofline``: the fused SpMV kernel (product + <x,y> epilogue), CUDA-event timed with L2
-  flushed before each launch (256 MiB rewritten, then another 256 MiB read, so the rewrite's dirty
-  lines are written back before the timed launch); algorithmic bytes nnz_full*12 + (n+1)*4 + 2*n*8.
+  hubbard_m512 (default)  Hubbard DMRG (hubbard_vf), OBC, L=64, t=1, U=4, N_e=64, 2Sz=0, m=512:
+                          the largest superblock of the 4th finite sweep
+  klm_m128                Kondo lattice DMRG (klm_vf), OBC, L=24, J=1, h_z=0.1, N_e=12, 2Sz=0, m=128
+  xxz_m64                 XXZ DMRG (xxz_vf), OBC, L=32, Jxy=Jz=1, 2Sz=0, m=64
+
+One step = one ground-state solve as DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: Lanczos (acc 1e-14,
+"Normal"; Lanczos_Slow for xxz_vf) then inverse iteration with CG (the driver's cg_acc), FP64.
+
+* ``value``: solves/s with the matrix resident on the device; the device time of each solve
+  (CUDA events on the library stream) summed over K steps.  Inputs larger than L2 (hubbard_m512:
+  0.69 GB of CRS) or L2 flushed (256 MiB rewrite) before every step (the smaller workloads).
+* ``e2e``: solves/s through the drop-in entry point DMRG_DIAGONALIZE_SUPERBLOCK_SYM from pinned
+  host arrays (lower-triangle CRS upload, device expansion, solve, eigenvector download), every
+  step timed on its own.
+* ``mixed`` / ``mixed_fp32_spmv``: the mixed-precision forms on the same superblock, with their
+  energy error against the reference's gs_val and the FP64 result.
+* ``sweeps``: every recorded sweep superblock of klm_vf and hubbard_vf solved FP64 and in both
+  mixed forms: |dE|/|E| against the reference's gs_val per sweep.
+* ``roofline``: the fused FP64 product kernel on the workload, CUDA-event timed, algorithmic bytes
+  nnz_full*12 + (n+1)*4 + 2*n*8 per launch; ``roofline_mixed`` the FP32-value product.
 * ``cpu_baseline``: the oracle's OpenMP restatement of the same solve on all host cores.
-* ``roofline_hbm_case``: the HBM-bound product (Hubbard m=512 superblock, 0.69 GB), FP64 with the
-  autotuned shape and the mixed-precision product, L2 flushed before every launch.
 
 ``--impl reference`` times the CPU path (the oracle port of the reference's LANCZOS_SYM +
-INVERSE_ITERATION_SYM; the reference itself cannot be built on the benchmark host) on the
-same workload.  Multi-GPU runs (torchrun) are independent replicas.
+INVERSE_ITERATION_SYM; the reference itself cannot be built on the benchmark host) on the same
+superblock.  Multi-GPU runs (torchrun) are independent replicas.
 """
 from __future__ import annotations
 
@@ -47,6 +52,20 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "ground-state solves/s and SpMV GB/s, mixed vs FP64 at |dE|<1e-10; p50/p99 ms"
 FLUSH_BYTES = 256 << 20
+L2_BYTES = 129 << 20
+GOLDEN = ROOT / "tests" / "golden"
+
+WORKLOADS = {
+    "hubbard_m512": ("dmrg_hubbard_vf_sweep4.npz",
+                     "hubbard_vf DMRG superblock (reference run, 4th sweep's largest): L=64 t=1 U=4 N_e=64 2Sz=0 m=512, "
+                     "FP64 Lanczos + inverse iteration"),
+    "klm_m128": ("dmrg_klm_vf_sweep4.npz",
+                 "klm_vf DMRG superblock (reference run, 4th sweep's largest): L=24 J=1 h_z=0.1 N_e=12 2Sz=0 m=128, "
+                 "FP64 Lanczos + inverse iteration"),
+    "xxz_m64": ("dmrg_xxz_vf_sweep4.npz",
+                "xxz_vf DMRG superblock (reference run, 4th sweep's largest): L=32 Jxy=Jz=1 2Sz=0 m=64, "
+                "FP64 Lanczos_Slow + inverse iteration"),
+}
 
 
 def dist_info():
@@ -78,19 +97,36 @@ def job_rate(steps, ws, max_ms):
     return ws * steps / (max_ms * 1e-3)
 
 
-def build_workload(name, seed):
-    from dmrg_c_gb300 import workloads
-    fn = {"klm_m128": workloads.klm_superblock_m128, "xxz_m64": workloads.xxz_superblock_m64,
-          "hubbard_m512": workloads.hubbard_superblock_m512}[name]
-    sb = fn(seed)
-    return sb, sb.explicit_lower()
+def load_workload(name):
+    from dmrg_c_gb300 import sb_models
+    return sb_models.load_dmrg_superblock(GOLDEN / WORKLOADS[name][0])
 
 
-WORKLOAD_DESC = {
-    "klm_m128": "klm_vf DMRG superblock, L=24 N_e=12 2Sz=0 m=128 (synthetic blocks), FP64 Lanczos + inverse iteration",
-    "xxz_m64": "xxz_vf DMRG superblock, L=32 2Sz=0 m=64 (synthetic blocks), FP64 Lanczos + inverse iteration",
-    "hubbard_m512": "hubbard_vf DMRG superblock, L=64 N_e=64 2Sz=0 m=512 (synthetic blocks), FP64 Lanczos + inverse iteration",
-}
+def solver_settings(name):
+    """The driver's settings (main/dmrg/<model>/src/main/main.c): Lanczos_Slow, cg_acc 1e-6 and
+    1000 steps for xxz_vf; Lanczos, 1e-7 and 2000 for klm_vf / hubbard_vf."""
+    xxz = name.startswith("xxz")
+    return dict(slow=xxz, cg_acc=1e-6 if xxz else 1e-7, cg_max_step=1000 if xxz else 2000)
+
+
+def config_dict(name, n, nnz_full):
+    """The workload description both arms print."""
+    s = solver_settings(name)
+    return {"workload": name, "desc": WORKLOADS[name][1], "source": f"tests/golden/{WORKLOADS[name][0]}", "n": int(n),
+            "nnz_full": int(nnz_full), "lanczos_acc": 1e-14, "ii_acc": 1e-9, "cg_acc": s["cg_acc"],
+            "l2": ("inputs larger than L2" if spmv_bytes(n, nnz_full) > 2 * L2_BYTES
+                   else "flushed (256 MiB rewrite) before every step")}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
 
 
 class ClockSampler:
@@ -174,25 +210,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def oracle_solve(low, seed, threads):
-    """The CPU path on one solve: oracle LANCZOS_SYM (Guess "No", same seeded start vector as
-    the GPU run) + INVERSE_ITERATION_SYM.  Returns (seconds, energy, vector)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import pyoracle
-    t0 = time.perf_counter()
-    rc, out, v = pyoracle.lanczos(low, True, seed=seed, threads=threads)
-    rc2, oi, v2 = pyoracle.inverse_iteration(low, True, out.eig_val, v, cg_acc=1e-7, threads=threads)
-    return time.perf_counter() - t0, out.eig_val, v2, out.steps, oi.cg_total
-
-
 def spmv_bytes(n, nnz_full, s_val=8, s_vec=8):
     return nnz_full * (s_val + 4) + (n + 1) * 4 + 2 * n * s_vec
 
 
-def traffic_from_profile(workload, mixed=False):
-    """DRAM bytes (read + write) per launch of the SpMV kernel, from the committed ncu summary
-    of this workload (profiles/k_apply_sell_[mixed_]<workload>.md), if present."""
-    f = ROOT / "profiles" / f"k_apply_sell_{'mixed_' if mixed else ''}{workload}.md"
+def traffic_from_profile(name, mixed=False):
+    """DRAM bytes (read + write) per launch of the product kernel, from the committed ncu summary of
+    this workload (profiles/k_apply_sell_[mixed_]<workload>.md, line traffic_bytes_per_launch)."""
+    f = ROOT / "profiles" / f"k_apply_sell_{'mixed_' if mixed else ''}{name}.md"
     if f.exists():
         for line in f.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
@@ -200,31 +225,69 @@ def traffic_from_profile(workload, mixed=False):
     return None
 
 
-def hbm_case_roofline(peak, peak_kind):
-    """The HBM-bound product: the Hubbard m=512 superblock (n = 227,652, 57.1 M stored, 0.69 GB),
-    FP64 with the autotuned shape and the mixed-precision product, CUDA-event timed with L2
-    flushed before every launch (the matrix is 5x the L2)."""
-    import torch
-    from dmrg_c_gb300 import lib as L
-    low = build_workload("hubbard_m512", 0)[1]
-    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH)
-    x = torch.randn(m.n, dtype=torch.float64, device="cuda")
-    y = torch.empty_like(x)
-    t_heur = m.profile_spmv(x, y, iters=20, flush_bytes=FLUSH_BYTES)
-    t32 = m.profile_spmv_mixed(x.float(), y, iters=20, flush_bytes=FLUSH_BYTES)   # heuristic shape
-    tune = m.autotune(iters=5)                                                    # FP64 shapes
-    t64 = m.profile_spmv(x, y, iters=20, flush_bytes=FLUSH_BYTES)
-    B64, B32 = spmv_bytes(m.n, m.nnz), spmv_bytes(m.n, m.nnz, 4, 4)
-    a64, a32 = B64 / (t64 * 1e-3) / 1e9, B32 / (t32 * 1e-3) / 1e9
-    out = {"workload": "hubbard_m512 superblock SpMV", "n": m.n, "nnz_full": m.nnz, "bound": "hbm", "unit": "GB/s",
-           "peak": peak, "peak_source": peak_kind,
-           "l2": "flushed before every launch: 256 MiB rewritten, then another 256 MiB read",
-           "fp64": {"kernel": f"k_apply_sell<double> (autotuned: WS={tune.shape} variant={tune.variant} window={tune.window})",
-                    "ms_per_launch": t64, "bytes_per_launch": B64, "achieved": a64, "frac": a64 / peak,
-                    "traffic": traffic_from_profile("hubbard_m512"), "heuristic_ms_per_launch": t_heur},
-           "mixed": {"kernel": "k_apply_sell<float> (compensated FP32 sums, heuristic shape)", "ms_per_launch": t32, "bytes_per_launch": B32,
-                     "achieved": a32, "frac": a32 / peak, "traffic": traffic_from_profile("hubbard_m512", mixed=True)}}
-    m.close()
+def oracle_superblock(sb, threads):
+    """The workload's lower-triangle CRS built on the host by the oracle (bitwise the device build)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    from dmrg_c_gb300 import abi
+    row, col, val = pyoracle.sb_build(sb.model, threads=threads)
+    return abi.Crs(row, col, val, n=sb.model.n)
+
+
+def oracle_solve(low, settings, seed, threads):
+    """The CPU path on one solve: oracle LANCZOS[_SLOW]_SYM (Guess "No", seeded start vector) +
+    INVERSE_ITERATION_SYM with CG.  Returns (seconds, energy, vector, Lanczos steps, CG steps)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    t0 = time.perf_counter()
+    rc, out, v = pyoracle.lanczos(low, True, seed=seed, slow=settings["slow"], threads=threads)
+    rc2, oi, v2 = pyoracle.inverse_iteration(low, True, out.eig_val, v, cg_acc=settings["cg_acc"],
+                                             cg_max_step=settings["cg_max_step"], threads=threads)
+    return time.perf_counter() - t0, out.eig_val, v2, out.steps, oi.cg_total
+
+
+def cpu_sample(low, settings, seed, threads, min_solves=5, budget_s=30.0):
+    """Times whole CPU solves: at least min_solves, more while under budget_s."""
+    times, E, v = [], None, None
+    while len(times) < min_solves or sum(times) < budget_s * 0.5:
+        s, E, v, st, cg = oracle_solve(low, settings, seed, threads)
+        times.append(s)
+        if sum(times) > budget_s and len(times) >= min_solves:
+            break
+    return times, E, v, st, cg
+
+
+def solve_params(L, name, seed, mixed=0):
+    s = solver_settings(name)
+    return L.default_params(lanczos_acc=1e-14, cg_acc=s["cg_acc"], cg_max_step=s["cg_max_step"],
+                            lanczos_slow=int(s["slow"]), seed=seed, mixed=mixed)
+
+
+def sweeps_leg(L, seed, models=("klm_vf", "hubbard_vf")):
+    """Every recorded sweep superblock of the models, FP64 and both mixed forms: |dE|/|E| against
+    the reference's gs_val of that superblock, and solve times."""
+    from dmrg_c_gb300 import sb_models
+    out = {}
+    for model in models:
+        name = {"klm_vf": "klm_m128", "hubbard_vf": "hubbard_m512", "xxz_vf": "xxz_m64"}[model]
+        rows = []
+        for path in sorted(GOLDEN.glob(f"dmrg_{model}_sweep*.npz")):
+            sb = sb_models.load_dmrg_superblock(path)
+            s = L.SuperblockCRS(sb.model)
+            m = s.matrix(L.DG_VALUES_BOTH)
+            row = {"sweep": sb.sweep, "n": sb.model.n, "gs_val_ref": sb.gs_val}
+            for mixed, tag in ((0, "fp64"), (1, "mixed1"), (2, "mixed2")):
+                v, info = L.ground_state(m, solve_params(L, name, seed, mixed))
+                ov = abs(v @ sb.gs_vec) / (np.linalg.norm(v) * np.linalg.norm(sb.gs_vec))
+                row[tag] = {"eig_val": info.eig_val, "dE_rel_vs_ref": abs(info.eig_val - sb.gs_val) / abs(sb.gs_val),
+                            "overlap_vs_ref": float(ov), "ms": info.ms_lanczos + info.ms_ii,
+                            "lanczos_steps": info.lanczos_steps}
+            for tag in ("mixed1", "mixed2"):
+                row[tag]["dE_rel_vs_fp64"] = abs(row[tag]["eig_val"] - row["fp64"]["eig_val"]) / abs(row["fp64"]["eig_val"])
+            rows.append(row)
+            m.close()
+            s.close()
+        out[model] = rows
     return out
 
 
@@ -233,17 +296,23 @@ def run_gb300(args, ws, rank, local_rank):
     from dmrg_c_gb300 import abi, lib as L
 
     torch.cuda.set_device(local_rank)
-    sb, low = build_workload(args.workload, args.seed)
+    sb = load_workload(args.workload)
+    settings = solver_settings(args.workload)
+    sbc = L.SuperblockCRS(sb.model)                      # the reference's CRS, built on the device
+    row_h, col_h, val_h = sbc.download()
+    low = abi.Crs(row_h, col_h, val_h, n=sb.model.n)
     n = low.n
     nnz_full = 2 * low.nnz - n
-    m = L.DeviceMatrix(low, L.DG_STORE_LOWER_DIAG_LAST, L.DG_VALUES_BOTH)
-    params = L.default_params(lanczos_acc=1e-14, cg_acc=1e-7, seed=args.seed + 1)
+    m = sbc.matrix(L.DG_VALUES_BOTH)
+    params = solve_params(L, args.workload, args.seed + 1)
     out = torch.empty(n, dtype=torch.float64, device="cuda")
+    small = spmv_bytes(n, nnz_full) <= 2 * L2_BYTES
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
 
     def one_solve(p=params, o=out):
-        flush.fill_(1)
-        torch.cuda.synchronize()
+        if small:
+            flush.fill_(1)
+            torch.cuda.synchronize()
         v, info = L.ground_state(m, p, guess=None, out=o)
         if not info.converged:
             raise RuntimeError("Lanczos did not converge")
@@ -271,10 +340,10 @@ def run_gb300(args, ws, rank, local_rank):
     total_ms = replica_time(float(sum(dev_ms)), ws)
     eigvec = out.cpu().numpy()
     E = infos[-1].eig_val
+    ov_ref = abs(eigvec @ sb.gs_vec) / (np.linalg.norm(eigvec) * np.linalg.norm(sb.gs_vec))
 
-    # mixed-precision forms on the same superblock and start vector
     def mixed_leg(form):
-        pm = L.default_params(lanczos_acc=1e-14, cg_acc=1e-7, seed=args.seed + 1, mixed=form)
+        pm = solve_params(L, args.workload, args.seed + 1, mixed=form)
         o = torch.empty(n, dtype=torch.float64, device="cuda")
         for _ in range(args.warmup):
             one_solve(pm, o)
@@ -287,8 +356,9 @@ def run_gb300(args, ws, rank, local_rank):
         Em = infs[-1].eig_val
         return {"value": ws * args.steps / (sum(ms) * 1e-3), "unit": "solves/s", "ms_per_step": sum(ms) / args.steps,
                 "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
-                "speedup_vs_fp64": total_ms / sum(ms), "eig_val": Em, "dE_rel_vs_fp64": abs(Em - E) / abs(E),
-                "overlap_vs_fp64": float(abs(v @ eigvec)), "lanczos_steps": infs[-1].lanczos_steps,
+                "speedup_vs_fp64": total_ms / sum(ms), "eig_val": Em, "dE_rel_vs_ref": abs(Em - sb.gs_val) / abs(sb.gs_val),
+                "dE_rel_vs_fp64": abs(Em - E) / abs(E), "overlap_vs_ref": float(abs(v @ sb.gs_vec) / np.linalg.norm(sb.gs_vec)),
+                "lanczos_steps": infs[-1].lanczos_steps,
                 "eig_lanczos_dE_rel": abs(infs[-1].eig_lanczos - E) / abs(E),
                 "refine_fp32_products": infs[-1].cg_steps, "refine_steps": infs[-1].ii_steps,
                 "residual_l1": infs[-1].error}
@@ -299,17 +369,7 @@ def run_gb300(args, ws, rank, local_rank):
     mixed_rec = mixed_leg(2)
     mixed_rec["form"] = "FP32 SpMV (compensated FP32 sums) + FP64 three-term recurrence, Jacobi-Davidson refinement"
 
-    # the steps after the solve on the solved vector: site expectation values, truncation to m
-    # states, renormalisation of a block operator (EXPECTATION_VALUES / RENORMALIZE / TRANSFORM_MATRIX)
-    try:
-        from dmrg_c_gb300 import dmrg_step, workloads
-        qb, qs, _target, m_keep = workloads.superblock_labels(args.workload, args.seed)
-        n_sites = {"klm_m128": 11, "hubbard_m512": 31, "xxz_m64": 15}[args.workload]
-        post = dmrg_step.post_solve(sb, qb, qs, eigvec, m_keep, n_sites)
-    except Exception as e:   # recorded, the solve measurement stands
-        post = {"error": f"{type(e).__name__}: {e}"}
-
-    # roofline of the SpMV kernel
+    # roofline of the product kernels
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
     fmt, _stored = m.format()
@@ -317,116 +377,134 @@ def run_gb300(args, ws, rank, local_rank):
               else "k_apply (CSR, lanes per row, fused <x,y> epilogue)")
     spmv_ms = m.profile_spmv(x, y, iters=30, flush_bytes=FLUSH_BYTES)
     spmv_warm_ms = m.profile_spmv(x, y, iters=30, flush_bytes=0)
-    B = spmv_bytes(n, nnz_full)
+    spmv32_ms = m.profile_spmv_mixed(x.float(), y, iters=30, flush_bytes=FLUSH_BYTES)
+    B, B32 = spmv_bytes(n, nnz_full), spmv_bytes(n, nnz_full, 4, 4)
     peak, peak_kind = peaks()
-    achieved = B / (spmv_ms * 1e-3) / 1e9
+    achieved, achieved32 = B / (spmv_ms * 1e-3) / 1e9, B32 / (spmv32_ms * 1e-3) / 1e9
 
     # end to end through the reference-facing entry point, from pinned host arrays (the CRS the
-    # caller holds and the eigenvector it receives)
+    # caller holds and the eigenvector it receives); every step timed on its own
     lib = L.load()
     pinned = [torch.from_numpy(a).pin_memory() for a in (low.row, low.col[:low.nnz], low.val[:low.nnz])]
     low_h = abi.Crs(*(t.numpy() for t in pinned), n=n)
     gs_t = torch.zeros(n, dtype=torch.float64).pin_memory()
     par = abi.DMRG_PARAMETER()
-    par.Diag_Method, par.Lan_Con, par.II_Type = b"Lanczos", b"Normal", b"CG"
+    par.Diag_Method = b"Lanczos_Slow" if settings["slow"] else b"Lanczos"
+    par.Lan_Con, par.II_Type, par.Initial_Guess = b"Normal", b"CG", b"No"
     par.diag_acc, par.diag_min_step, par.diag_max_step = 1e-14, 1, 800
-    par.cg_acc, par.cg_max_step = 1e-7, 1000
+    par.cg_acc, par.cg_max_step = settings["cg_acc"], settings["cg_max_step"]
     par.inv_iter_acc, par.inv_iter_diag_add, par.inv_iter_max_step = 1e-9, 1e-11, 3
     gs = gs_t.numpy()
     st = abi.DMRG_STATUS()
     st.GS_Vec = abi.ptr(gs, C.c_double)
     tm = abi.DMRG_TIME()
-    e2e_steps = max(1, min(args.steps, 10))
+    e2e_ms = []
     old = os.getcwd()
     with tempfile.TemporaryDirectory() as d:
         os.chdir(d)
         try:
-            lib.DMRG_DIAGONALIZE_SUPERBLOCK_SYM(low_h.ref, C.byref(tm), C.byref(par), C.byref(st), 1)   # warm
-            t0 = time.perf_counter()
-            for _ in range(e2e_steps):
-                flush.fill_(1)
-                torch.cuda.synchronize()
+            for _ in range(args.warmup):
                 lib.DMRG_DIAGONALIZE_SUPERBLOCK_SYM(low_h.ref, C.byref(tm), C.byref(par), C.byref(st), 1)
-            e2e_s = (time.perf_counter() - t0) / e2e_steps
+            for _ in range(args.steps):
+                if small:
+                    flush.fill_(1)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                lib.DMRG_DIAGONALIZE_SUPERBLOCK_SYM(low_h.ref, C.byref(tm), C.byref(par), C.byref(st), 1)
+                e2e_ms.append((time.perf_counter() - t0) * 1e3)
         finally:
             os.chdir(old)
+    e2e_max_ms = replica_time(float(sum(e2e_ms)), ws)
     h2d = (n + 1) * 8 + low.nnz * 4 + low.nnz * 8
     d2h = n * 8
 
     result = {
         "metric": METRIC, "value": job_rate(args.steps, ws, total_ms), "unit": "solves/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded block operators)",
-        "config": {"workload": args.workload, "desc": WORKLOAD_DESC[args.workload], "n": n, "nnz_full": nnz_full,
-                   "nnz_lower": low.nnz, "l2": "flushed (256 MiB) before every step", "parallelism": f"replicas x{ws}",
-                   "lanczos_acc": 1e-14, "ii_acc": 1e-9, "cg_acc": 1e-7},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "superblocks recorded from the reference's own DMRG run (tests/golden)",
+        "config": config_dict(args.workload, n, nnz_full),
+        "parallelism": f"replicas x{ws}",
         "wall_ms_per_step": wall * 1e3 / args.steps,
         "p50_ms": float(np.percentile(dev_ms, 50)), "p99_ms": float(np.percentile(dev_ms, 99)),
         "ms_lanczos_p50": float(np.percentile([i.ms_lanczos for i in infos], 50)),
         "ms_ii_p50": float(np.percentile([i.ms_ii for i in infos], 50)),
         "lanczos_steps": infos[-1].lanczos_steps, "cg_steps": infos[-1].cg_steps, "spmv_per_solve": infos[-1].spmv_count,
-        "ii_error": infos[-1].error, "eig_val": E,
-        "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "entry": "DMRG_DIAGONALIZE_SUPERBLOCK_SYM", "gs_val": st.gs_val},
+        "ii_error": infos[-1].error, "eig_val": E, "gs_val_ref": sb.gs_val,
+        "dE_rel_vs_ref": abs(E - sb.gs_val) / abs(sb.gs_val), "overlap_vs_ref": float(ov_ref),
+        "e2e": {"value": job_rate(args.steps, ws, e2e_max_ms), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "entry": "DMRG_DIAGONALIZE_SUPERBLOCK_SYM",
+                "p50_ms": float(np.percentile(e2e_ms, 50)), "p99_ms": float(np.percentile(e2e_ms, 99)),
+                "gs_val": st.gs_val, "dE_rel_vs_ref": abs(st.gs_val - sb.gs_val) / abs(sb.gs_val)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic_from_profile(args.workload), "peak_source": peak_kind,
-                     "kernel": kernel, "ms_per_launch": spmv_ms,
-                     "bytes_per_launch": B, "l2_warm_ms_per_launch": spmv_warm_ms,
-                     "l2_warm_gbs": B / (spmv_warm_ms * 1e-3) / 1e9},
+                     "kernel": kernel, "ms_per_launch": spmv_ms, "bytes_per_launch": B,
+                     "l2": "flushed before every launch: 256 MiB rewritten, then another 256 MiB read",
+                     "l2_warm_ms_per_launch": spmv_warm_ms, "l2_warm_gbs": B / (spmv_warm_ms * 1e-3) / 1e9},
+        "roofline_mixed": {"bound": "hbm", "achieved": achieved32, "peak": peak, "unit": "GB/s", "frac": achieved32 / peak,
+                           "traffic": traffic_from_profile(args.workload, mixed=True), "peak_source": peak_kind,
+                           "kernel": "k_apply_sell<float> (FP32 values and x, compensated FP32 sums)",
+                           "ms_per_launch": spmv32_ms, "bytes_per_launch": B32},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "mixed": mixed,
         "mixed_fp32_spmv": mixed_rec,
-        "post_solve": post,
     }
-    if rank == 0 and not args.no_hbm_case:
-        result["roofline_hbm_case"] = hbm_case_roofline(peak, peak_kind)
+    if rank == 0 and not args.no_sweeps:
+        result["sweeps"] = sweeps_leg(L, args.seed + 1)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        secs, E_cpu, v_cpu, st_cpu, cg_cpu = oracle_solve(low, args.seed + 1, threads)
-        result["cpu_baseline"] = {"value": 1.0 / secs, "unit": "solves/s", "cores": threads, "kind": "port",
-                                  "sample": "1 full solve (Lanczos + inverse iteration) of the same superblock",
+        times, E_cpu, v_cpu, st_cpu, cg_cpu = cpu_sample(low, settings, args.seed + 1, threads)
+        result["cpu_baseline"] = {"value": len(times) / sum(times), "unit": "solves/s", "cores": threads, "kind": "port",
+                                  "cpu": cpu_model(),
+                                  "sample": f"{len(times)} full solves (Lanczos + inverse iteration) of the same superblock",
                                   "lanczos_steps": st_cpu, "cg_steps": cg_cpu}
         result["dE_rel_vs_cpu"] = abs(E - E_cpu) / abs(E_cpu)
         result["overlap_vs_cpu"] = float(abs(eigvec @ v_cpu))
+    m.close()
+    sbc.close()
     return result
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
-    sb, low = build_workload(args.workload, args.seed)
+    sb = load_workload(args.workload)
+    settings = solver_settings(args.workload)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        oracle_solve(low, args.seed + 1, threads)
+    low = oracle_superblock(sb, threads)
+    for _ in range(min(args.warmup, 2)):
+        oracle_solve(low, settings, args.seed + 1, threads)
     times = []
     E = None
     for _ in range(args.steps):
-        s, E, v, st, cg = oracle_solve(low, args.seed + 1, threads)
+        s, E, v, st, cg = oracle_solve(low, settings, args.seed + 1, threads)
         times.append(s)
     value = args.steps / sum(times)
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded block operators)",
-            "config": {"workload": args.workload, "desc": WORKLOAD_DESC[args.workload], "n": low.n,
-                       "nnz_full": 2 * low.nnz - low.n},
-            "eig_val": E,
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "superblocks recorded from the reference's own DMRG run (tests/golden)",
+            "config": config_dict(args.workload, low.n, 2 * low.nnz - low.n),
+            "eig_val": E, "dE_rel_vs_ref": abs(E - sb.gs_val) / abs(sb.gs_val),
+            "p50_ms": float(np.percentile(times, 50)) * 1e3, "p99_ms": float(np.percentile(times, 99)) * 1e3,
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
                              "sample": f"{args.steps} full solves of the workload superblock (oracle restatement of "
-                                       "LANCZOS_SYM + INVERSE_ITERATION_SYM, OpenMP on all host cores)"},
+                                       f"LANCZOS{'_SLOW' if settings['slow'] else ''}_SYM + INVERSE_ITERATION_SYM, "
+                                       "OpenMP on all host cores), after min(W, 2) untimed solves"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=sorted(WORKLOAD_DESC), default="klm_m128")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hubbard_m512")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-hbm-case", action="store_true", help="skip the m=512 superblock product roofline")
+    ap.add_argument("--no-sweeps", action="store_true", help="skip the per-sweep energy errors")
     args = ap.parse_args(argv)
     ws, rank, local_rank = dist_info()
     if args.impl == "reference":

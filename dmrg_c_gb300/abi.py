@@ -228,6 +228,49 @@ class EXACT_WHOLE_BASIS_Q3(C.Structure):
                 ("max_dim", C.c_int)]
 
 
+class ExactWholeBasis:
+    """An EXACT_WHOLE_BASIS_Q1 / _Q2 / _Q3 over numpy arrays (include/exact.h:89-111): ``sectors``
+    maps a k-tuple of non-negative quantum-number indices to that sector's ascending int64 code
+    table, ``shape`` gives the extent of each index (absent sectors have dimension 0).  With
+    ``pad`` each table is followed by one sentinel larger than any code (the reference's binary
+    search may read one element past the table, exact/EXACT_V_M_Q1.c:29).  ``.ref`` points at the
+    struct; the arrays are kept alive by this object."""
+
+    def __init__(self, sectors: dict, shape: tuple, pad: bool = False):
+        k = len(shape)
+        assert 1 <= k <= 3
+        self.keep = []
+        empty = np.full(1, np.iinfo(np.int64).max, np.int64)
+        self.keep.append(empty)
+
+        def build(prefix, leaf, leaf_type):
+            depth = len(prefix)
+            if depth == k:
+                return leaf(prefix)
+            elem_t = leaf_type
+            for _ in range(k - depth - 1):
+                elem_t = C.POINTER(elem_t)
+            arr = (elem_t * shape[depth])(*[build(prefix + (i,), leaf, leaf_type) for i in range(shape[depth])])
+            self.keep.append(arr)
+            return C.cast(arr, C.POINTER(elem_t))
+
+        def table(prefix):
+            b = sectors.get(prefix)
+            if b is None or len(b) == 0:
+                return empty.ctypes.data_as(c_long_p)
+            a = np.ascontiguousarray(b, np.int64)
+            if pad:
+                a = np.concatenate([a, [np.iinfo(np.int64).max]])
+            self.keep.append(a)
+            return a.ctypes.data_as(c_long_p)
+
+        dim = build((), lambda prefix: len(sectors[prefix]) if prefix in sectors else 0, C.c_int)
+        basis = build((), table, c_long_p)
+        T = {1: EXACT_WHOLE_BASIS_Q1, 2: EXACT_WHOLE_BASIS_Q2, 3: EXACT_WHOLE_BASIS_Q3}[k]
+        self.struct = T(Dim=dim, Basis=basis, max_dim=max((len(v) for v in sectors.values()), default=0))
+        self.ref = C.pointer(self.struct)
+
+
 class MODEL_1DKLM_VF(C.Structure):
     """include/model.h:23-45"""
     _fields_ = [("BC", C.c_char * 1000), ("p_threads", C.c_int), ("spin_loc", C.c_int), ("tot_site", C.c_int),

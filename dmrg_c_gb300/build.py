@@ -5,7 +5,10 @@ Every CUDA translation unit under csrc/ is compiled in parallel with
 ``dmrg_c_gb300/libdmrg_gb300.so``.  Object files go to ``_build/`` at the repository
 root.  Rebuilds only what changed (timestamps of the sources and the headers).
 
-Usage: ``python -m dmrg_c_gb300.build [--force] [--debug-checks]``
+Usage: ``python -m dmrg_c_gb300.build [--force]``
+
+There is no separate bounds-check build: the input invariants (CRS layout, operator and basis
+ranges of the superblock and ED models) are checked on every call and reported as error codes.
 """
 from __future__ import annotations
 
@@ -48,9 +51,9 @@ def _compile(src: Path, obj: Path, extra: list[str]) -> None:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
 
 
-def build(force: bool = False, debug_checks: bool = False, verbose: bool = False) -> Path:
+def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(parents=True, exist_ok=True)
-    extra = ["-DDG_DEBUG_CHECKS=1"] if debug_checks else []
+    extra: list[str] = []
     sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     hdr_time = _newest_header()
     jobs = []
@@ -80,9 +83,8 @@ def build(force: bool = False, debug_checks: bool = False, verbose: bool = False
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--force", action="store_true")
-    ap.add_argument("--debug-checks", action="store_true")
     a = ap.parse_args(argv)
-    build(force=a.force, debug_checks=a.debug_checks, verbose=True)
+    build(force=a.force, verbose=True)
     return 0
 
 

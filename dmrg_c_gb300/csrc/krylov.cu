@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
   if (threadIdx.x == 0) *ticket = 0u;
 }
 
-__global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef_g,
-                                                    const float *__restrict__ y, int n, RedSlot out, Norm2 *r2) {
+__global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nvec, const float *__restrict__ coef_g,
+                                                    const float *y, int n, RedSlot out, Norm2 *r2) {
   pdl_wait();
   extern __shared__ float coef[];   // nvec entries
   for (int j = threadIdx.x; j < nvec; j += blockDim.x) coef[j] = coef_g[j];
@@ -233,11 +233,11 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long
     for (; j + 8 <= nvec; j += 8) {   // eight loads in flight per thread
       float v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = V[(long)(j + u) * ldv + i];
+      for (int u = 0; u < 8; ++u) v[u] = __ldg(V + (long)(j + u) * ldv + i);   // V_j, j < nvec: read-only here
 #pragma unroll
       for (int u = 0; u < 8; ++u) a.add(coef[j + u], v[u]);
     }
-    for (; j < nvec; ++j) a.add(coef[j], V[(long)j * ldv + i]);
+    for (; j < nvec; ++j) a.add(coef[j], __ldg(V + (long)j * ldv + i));
     const double w = a.get();
     vout[i] = (float)w;
     acc += w * w;

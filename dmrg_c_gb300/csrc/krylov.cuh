@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <limits>
 #include <thread>
@@ -311,9 +312,10 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
                                                        const float *__restrict__ y, double *D, double *hD, const double *O, int n,
                                                        const double *pp, int pcount, RedSlot out, Norm2 *r2);
 // w = y + sum_j coef_j V_j (compensated); V[nvec] = fl32(w); <w,w> into block partials (r2
-// null) or the Norm2 *r2.
-__global__ void __launch_bounds__(kThreads) k_mx_sub(float *__restrict__ V, long ldv, int nvec, const float *__restrict__ coef,
-                                                    const float *__restrict__ y, int n, RedSlot out, Norm2 *r2);
+// null) or the Norm2 *r2.  y may be V[nvec] itself (each element is read, then written, by
+// one thread).
+__global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nvec, const float *__restrict__ coef,
+                                                    const float *y, int n, RedSlot out, Norm2 *r2);
 // out_i = sum_{j<k} s_j sig_j V_j[i] (FP64, j order); *r2 = <out,out>.
 __global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
                                                      const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
@@ -616,12 +618,23 @@ struct LzStepsMixed {
                  r2);
       return;
     }
+    // Full reorthogonalisation: the three-term recurrence first (w = y - alpha_b v_b - beta_b v_{b-1},
+    // stored in V[b+1]), then one classical Gram-Schmidt pass of that w against every stored
+    // vector, in place.  Gram-Schmidt applied to y itself amplifies the basis' loss of
+    // orthogonality by ||y|| / ||w|| every step (|alpha| / beta: about 7 on a DMRG superblock whose
+    // energy is far from zero), which on FP32 vectors broke the recurrence within ten steps; on
+    // the three-term residual the ratio is about 1 and orthogonality stays at the FP32 level.
+    const RedSlot scratch{ws.partials3.get(), ws.ticket.get()};
+    launch_pdl(k_mx_update, ws.vgrid, kThreads, st, B.V, (long)n, b, (const double *)sig.get(), (const float *)y.get(), z.D.get(),
+               z.hD.d, (const double *)z.O.get(), n, (const double *)slot.partials, defer ? op.grid() : 0, scratch,
+               (Norm2 *)nullptr);
     const int nvec = b + 1;
-    launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec,
-               (const float *)y.get(), n, nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get(),
-               (const double *)slot.partials, defer ? op.grid() : 0, z.D.get(), z.hD.d, b);
+    const float *w3 = B.vec(b + 1);
+    launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec, w3, n,
+               nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get(), (const double *)nullptr, 0, z.D.get(),
+               z.hD.d, b);
     launch_pdl_smem(k_mx_sub, dim3(ws.vgrid), dim3(kThreads), sizeof(float) * nvec, st, B.V, (long)n, nvec,
-                    (const float *)coef.get(), (const float *)y.get(), n, r2slot, r2);
+                    (const float *)coef.get(), w3, n, r2slot, r2);
   }
   void combine(int k, const std::vector<double> &s, double *dst) {
     z.upload_s(k, s, ws.st);
@@ -651,6 +664,7 @@ LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, d
   int n_last = 0;             // order of the last tridiagonal solved
   std::vector<double> s_last;
   const int W = std::max(1, cfg.lookahead);
+  static const bool trace = std::getenv("DG_LANCZOS_TRACE") != nullptr;   // per-check report on stderr
 
   auto finish = [&](int k, const std::vector<double> &s) {
     steps.combine(k, s, out_dev);
@@ -726,6 +740,7 @@ LanczosResult lanczos_run(const Opl &op, const LanczosCfg &cfg, double *w_dev, d
         conv = std::fabs(E - lam) < cfg.acc;
       }
       if (!conv && cfg.mixed && E < 1e14) conv = std::fabs(E - lam) <= cfg.mixed_rel * std::fabs(lam);
+      if (trace) std::fprintf(stderr, "lanczos step %d lam %.17g dE %.3e beta %.3e\n", total_step, lam, std::fabs(E - lam), hO[bs]);
       if (!conv && cfg.accept_at_end && bs == nb_max) conv = true;
       n_last = nn;
       if (conv) {

@@ -282,6 +282,10 @@ __global__ void k_sell_fill(const int64_t *__restrict__ row, const int *__restri
 
 }  // namespace
 
+void launch_validate(const int64_t *row, const int *col, int n, long nnz, int lower, int *bad, cudaStream_t st) {
+  k_validate<<<warp_grid(n), kThreads, 0, st>>>(row, col, n, nnz, lower, bad); ::dg::count_launch();
+}
+
 void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   const int n = m->n;
   const int nwin = (n + kSellWindow - 1) / kSellWindow;

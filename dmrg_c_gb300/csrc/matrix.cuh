@@ -108,6 +108,11 @@ void matrix_apply32(const dg_matrix *m, const float *x, Scale sc, double sigma, 
 // Blocks needed by the current format (for sizing reduction partials).
 inline int matrix_grid(const dg_matrix *m) { return m->format == DG_FORMAT_SELL ? m->sell_grid : m->grid; }
 
+// Checks the CRS invariants of device arrays on stream st (row offsets non-decreasing within
+// [0, nnz]; columns in [0, n), or the lower-triangle layout when lower = 1).  *bad must hold
+// INT_MAX before the launch and receives the smallest offending row.
+void launch_validate(const int64_t *row, const int *col, int n, long nnz, int lower, int *bad, cudaStream_t st);
+
 // Build the sliced-ELL copy of a device CRS with the given row-sorting window.
 void build_sell(dg_matrix *m, cudaStream_t st, int window);
 

@@ -1,23 +1,31 @@
 // noalloc.cu -- conjugate-gradient solve that allocates nothing.
 //
-// Some callers cannot let a library allocate device memory: code that runs inside a CUDA
-// stream capture, an application whose memory pool owns the whole device, or an embedding
-// that forbids allocation on its solve path.  dg_cg_noalloc serves them: the caller passes
-// the matrix (full CRS) and the vectors in device memory, and every temporary the solve
-// needs (three work vectors, the reduction partials and the solver scalars) lives in one
-// file-scope static device array of fixed size.  No cudaMalloc, cudaFree, pinned-host or
-// library allocation happens on this path.
+// Some callers cannot let a library allocate device memory: an application whose own memory
+// pool owns the whole device (a cudaMalloc from here would fail or fragment it), or an
+// embedding whose solve path must not allocate (real-time or certified code that reserves all
+// memory up front).  dg_cg_noalloc serves them: the caller passes the matrix (full CRS) and the
+// vectors in device memory, and every temporary the solve needs (three work vectors, the
+// reduction partials, the validation word and the solver scalars) lives in one file-scope
+// static device array of fixed size.  No cudaMalloc, cudaFree, pinned-host or library
+// allocation happens on this path.
 //
 // Limits and sharing:
 //  * n <= kNoAllocMaxN rows (the array holds three vectors of that length); larger systems
 //    are rejected with DG_ERR_ARG before any device work;
+//  * the caller's CRS is checked on the device first (row offsets from 0 to row[n],
+//    non-decreasing; columns in [0, n)) and a malformed one is rejected with DG_ERR_MATRIX
+//    before any product reads through it;
 //  * the array is one per device and every call on that device shares it, keeping the last
-//    call's contents; the call clears what must start at zero (reduction ticket, solver
-//    state).  Calls from one process are serialised by a mutex, but any other device work
-//    that touches the array while a call runs would race with it;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current) and caches it, so make that first
-//    call before any stream capture begins.
+//    call's contents; the call clears what must start at zero (reduction ticket, validation
+//    word, solver state).  Calls from one process take one process-wide mutex, so calls on
+//    different devices also run one at a time; any other device work that touches the array
+//    while a call runs would race with it;
+//  * the call runs on the library's own per-thread stream and returns after that stream has
+//    finished (also on every error path, before the mutex is released); the inputs must
+//    already be complete on the device when it is called;
+//  * the first call on a device looks up the array's device address (cudaGetSymbolAddress,
+//    with that device current) and caches it, so make that first call before any stream
+//    capture begins.
 #include <mutex>
 
 #include "krylov.cuh"
@@ -35,7 +43,8 @@ constexpr size_t kOffPartials2 = kOffPartials + sizeof(double) * kNoAllocMaxGrid
 constexpr size_t kOffScalars = kOffPartials2 + sizeof(double) * kNoAllocMaxGrid;
 constexpr size_t kOffProgress = kOffScalars + ((sizeof(Scalars) + 255) / 256) * 256;
 constexpr size_t kOffTicket = kOffProgress + ((sizeof(Progress) + 255) / 256) * 256;
-constexpr size_t kScratchBytes = kOffTicket + 256;
+constexpr size_t kOffBad = kOffTicket + 256;         // validation: first malformed row
+constexpr size_t kScratchBytes = kOffBad + 256;
 
 // The scratch array: 3 x 8 MiB vectors + partials + state, about 24 MiB per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -56,6 +65,13 @@ unsigned char *scratch_for_current_device() {
   }
   return g_scratch_ptr[dev];
 }
+
+// Waits for the stream on every exit path, so that no kernel of this call is still running on
+// the shared array once the mutex is released.
+struct StreamDrain {
+  cudaStream_t st;
+  ~StreamDrain() { cudaStreamSynchronize(st); }
+};
 
 struct RawCrsLauncher {
   CrsOp<double> op;
@@ -87,6 +103,8 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
                    is_device_ptr(x_dev),
                DG_ERR_ARG, "dg_cg_noalloc takes device pointers only");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    cudaStream_t st = stream();
+    StreamDrain drain{st};
     unsigned char *base = scratch_for_current_device();
     double *r = reinterpret_cast<double *>(base + kOffR);
     double *p = reinterpret_cast<double *>(base + kOffP);
@@ -96,13 +114,22 @@ extern "C" int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, con
     Scalars *S = reinterpret_cast<Scalars *>(base + kOffScalars);
     Progress *prog = reinterpret_cast<Progress *>(base + kOffProgress);
     unsigned *ticket = reinterpret_cast<unsigned *>(base + kOffTicket);
-    cudaStream_t st = stream();
+    int *bad = reinterpret_cast<int *>(base + kOffBad);
 
     int64_t ends[2];
     DG_CUDA(cudaMemcpyAsync(&ends[0], row_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaMemcpyAsync(&ends[1], row_dev + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
-    DG_REQUIRE(ends[0] == 0 && ends[1] >= 0, DG_ERR_MATRIX, "CRS row offsets must start at 0");
+    DG_REQUIRE(ends[0] == 0 && ends[1] >= 0, DG_ERR_MATRIX, "CRS row offsets must run from 0 to row[n] >= 0");
+    // The CRS invariants, checked on the device before any product gathers through the columns.
+    const int big = 0x7fffffff;
+    int first_bad = 0;
+    DG_CUDA(cudaMemcpyAsync(bad, &big, sizeof(int), cudaMemcpyHostToDevice, st));
+    launch_validate(reinterpret_cast<const int64_t *>(row_dev), col_dev, n, (long)ends[1], 0, bad, st);
+    DG_CUDA(cudaGetLastError());
+    DG_CUDA(cudaMemcpyAsync(&first_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    DG_REQUIRE(first_bad == big, DG_ERR_MATRIX, "row %d has a column outside [0, n) or decreasing offsets", first_bad);
     RawCrsLauncher op;
     op.op = CrsOp<double>{reinterpret_cast<const int64_t *>(row_dev), col_dev, val_dev};
     op.n_ = n;

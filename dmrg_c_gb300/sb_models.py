@@ -275,3 +275,45 @@ def random_observable_problem(dim_LL=16, dim_RR=14, n_LL=3, n_RR=3, per_row=4, s
                CdRR=[_crs(_random_shift_op(qR, up, per_row, rng))],
                CdOn=_crs(sp.csr_matrix(cupd)))
     return ObservableProblem(qL, qR, qs, ops, (2 * n_sites + 2) * QN_SCALE)
+
+
+# ---------------------------------------------------------------------------------------
+# Superblocks recorded from the reference's own DMRG runs
+# ---------------------------------------------------------------------------------------
+@dataclass
+class DmrgSuperblock:
+    """One superblock of a reference DMRG run: the term list (``model``) and what the reference's
+    solve returned for it (``gs_val``, ``gs_error``, ``gs_vec``), with the dg64 checksums of the
+    reference's lower-triangle CRS (``crs_dg64``: Row, Col, Val) and its stored element count."""
+    name: str
+    model: SBModel
+    sweep: int
+    LL_site: int
+    RR_site: int
+    nnz: int
+    crs_dg64: tuple
+    gs_val: float
+    gs_error: float
+    gs_vec: np.ndarray
+
+
+def load_dmrg_superblock(path) -> DmrgSuperblock:
+    """Term list and reference results from a ``dmrg_<model>_sweep<k>.npz`` file (written by
+    the fixture generator that runs main/dmrg/<model>; the terms are in the order the model's
+    MAKE_ELEMENT_HAM_LLLRRRRL applies them, e.g. main/dmrg/hubbard_vf/src/main/
+    MAKE_ELEMENT_HAM_LLLRRRRL.c:16-45)."""
+    z = np.load(path)
+    n, d, dim_LL, dim_RR = int(z["n"]), int(z["dim_onsite"]), int(z["dim_LL"]), int(z["dim_RR"])
+    LL, LR, RR, RL = (np.ascontiguousarray(z["states"][k]) for k in range(4))
+    inv = -np.ones(dim_LL * d * dim_RR * d, np.int32)
+    sup = ((LL.astype(np.int64) * d + LR) * dim_RR + RR) * d + RL
+    inv[sup] = np.arange(n, dtype=np.int32)
+    ops = [Crs(z[f"op{k}_row"], z[f"op{k}_col"], z[f"op{k}_val"]) for k in range(int(z["n_ops"]))]
+    ti, tc = z["term_int"], z["term_coef"]
+    terms = [(int(a[0]), int(a[1]), int(a[2]), int(a[3]), float(c), int(a[4]), int(a[5])) for a, c in zip(ti, tc)]
+    ele = [np.asarray(z[f"ele{p}"]) if f"ele{p}" in z.files else None for p in range(4)]
+    model = SBModel(n, dim_LL, dim_RR, d, LL, LR, RR, RL, inv, ops, terms, ele)
+    name = f"{z['model']} sweep {int(z['sweep'])} ({int(z['LL_site']) + 1},1,1,{int(z['RR_site']) + 1})"
+    return DmrgSuperblock(name, model, int(z["sweep"]), int(z["LL_site"]), int(z["RR_site"]), int(z["nnz"]),
+                          (np.uint64(z["row_dg64"]), np.uint64(z["col_dg64"]), np.uint64(z["val_dg64"])),
+                          float(z["gs_val"]), float(z["gs_error"]), np.asarray(z["gs_vec"], np.float64))

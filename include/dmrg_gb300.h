@@ -301,14 +301,17 @@ int dg_linear_solve(dg_matrix *m, double sigma, const double *b, double *x, doub
 int dg_residual_l1(dg_matrix *m, const double *x, double lambda, double *out);
 
 /* Allocation-free CG (no counterpart in the reference; an addition for callers that cannot
- * let a library allocate device memory, e.g. code inside a stream capture or under an
- * application-owned memory pool).  Solves (M + sigma I) x = b like dg_linear_solve (CG,
- * x normalised first) for a full CRS whose row/col/val and b/x are all device pointers.
- * Every temporary lives in one static device array of about 24 MiB per device, so:
- * n <= 1,048,576 (larger n returns DG_ERR_ARG); calls share that array (serialised within a
- * process; other device work touching it concurrently would race); the first call on a
- * device looks up the array's address and should come before any stream capture.  Returns
- * DG_ERR_NOCONV if acc is not reached within max_step iterations (x holds the last iterate). */
+ * let a library allocate device memory: an application whose own memory pool owns the device,
+ * or a solve path that must not allocate).  Solves (M + sigma I) x = b like dg_linear_solve
+ * (CG, x normalised first) for a full CRS whose row/col/val and b/x are all device pointers;
+ * the inputs must already be complete on the device.  The CRS is validated on the device first
+ * (malformed offsets or columns: DG_ERR_MATRIX).  Every temporary lives in one static device
+ * array of about 24 MiB per device, so: n <= 1,048,576 (larger n returns DG_ERR_ARG); calls
+ * share that array and keep its last contents; calls are serialised by one process-wide mutex
+ * (also across devices) and return after their work has finished; other device work touching
+ * the array concurrently would race.  The first call on a device looks up the array's address
+ * and should come before any stream capture.  Returns DG_ERR_NOCONV if acc is not reached
+ * within max_step iterations (x holds the last iterate). */
 int dg_cg_noalloc(int n, const long *row_dev, const int *col_dev, const double *val_dev, double sigma, const double *b_dev,
                   double *x_dev, double acc, int max_step, int *iters);
 

@@ -192,6 +192,23 @@ def sb_build(model, threads=None):
     return row, col[:row[-1]], val[:row[-1]]
 
 
+def dg64(a: np.ndarray) -> np.uint64:
+    """Checksum of an array's bytes shared with ref_dmrg_dump.c: the bytes as little-endian 64-bit
+    words (the last zero-padded), word i contributing mix64(w_i + (i + 1) * 0x9E3779B97F4A7C15)
+    (the splitmix64 finaliser), summed modulo 2**64."""
+    b = np.ascontiguousarray(a).view(np.uint8).ravel()
+    pad = (-len(b)) % 8
+    if pad:
+        b = np.concatenate([b, np.zeros(pad, np.uint8)])
+    w = b.view("<u8").astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = w + (np.arange(1, len(w) + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+        return np.uint64(np.sum(z, dtype=np.uint64))
+
+
 def ref_sb_build(model, cap=None):
     """The same through the reference's own DMRG_MAKE_ELEM_*_LLLRRRRL builders (oracle/_ref)."""
     lib = load_ref()
@@ -856,6 +873,30 @@ def ref_site_apply(op: abi.Crs, basis, d, site, vec):
     out = np.zeros(len(basis))
     info = EXACT_BASIS_INFO(dim=len(basis), Basis=ptr(padded, C.c_long), tot_sz=0, tot_ele=0, tot_parity=0)
     lib.EXACT_V_M_Q0(op.ref, ptr(vec, C.c_double), ptr(out, C.c_double), d, site, 1, C.byref(info))
+    return out
+
+
+def ref_vm_q1(op: abi.Crs, sectors, shape, qn_out, qn_in, vec, d, site):
+    """The reference's EXACT_V_M_Q1 (exact/EXACT_V_M_Q1.c:8-38) between two sectors of a whole basis."""
+    lib = load_ref()
+    W = abi.ExactWholeBasis(sectors, shape, pad=True)
+    vec = np.ascontiguousarray(vec, np.float64)
+    out = np.zeros(len(sectors[(qn_out,)]))
+    lib.EXACT_V_M_Q1(op.ref, C.c_int(qn_out), ptr(vec, C.c_double), C.c_int(qn_in), ptr(out, C.c_double), C.c_int(d),
+                     C.c_int(site), C.c_int(1), W.ref)
+    return out
+
+
+def ref_vm_q3(op: abi.Crs, sectors, shape, q_out, q_in, vec, sign, n_ele, d, site):
+    """The reference's EXACT_V_M_Q3 (exact/EXACT_V_M_Q3.c:10-60) between two sectors (3-index labels)."""
+    lib = load_ref()
+    W = abi.ExactWholeBasis(sectors, shape, pad=True)
+    vec = np.ascontiguousarray(vec, np.float64)
+    ne = np.ascontiguousarray(n_ele, np.int32)
+    out = np.zeros(len(sectors[tuple(q_out)]))
+    lib.EXACT_V_M_Q3(op.ref, *(C.c_int(q) for q in q_out), ptr(vec, C.c_double), *(C.c_int(q) for q in q_in),
+                     ptr(out, C.c_double), b"Yes" if sign else b"No", ptr(ne, C.c_int), C.c_int(d), C.c_int(site), C.c_int(1),
+                     W.ref)
     return out
 
 

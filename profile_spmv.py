@@ -1,18 +1,18 @@
-"""SpMV rate survey of the library's operator kernels on the named superblock and ED matrices.
+"""Measurement harness (beside bench.py, not part of the package): SpMV rate survey of the library's operator kernels on the named superblock and ED matrices.
 
-    python -m dmrg_c_gb300.profile_spmv                      # heuristic and autotuned rates
-    python -m dmrg_c_gb300.profile_spmv --sweep              # every SELL shape / variant / window
-    python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --format sell --launches 3
+    python profile_spmv.py                      # heuristic and autotuned rates
+    python profile_spmv.py --sweep              # every SELL shape / variant / window
+    python profile_spmv.py --case hubbard_m512 --format sell --launches 3
                                                              # a few launches, for an ncu capture
-    python -m dmrg_c_gb300.profile_spmv --case hubbard_m512 --mixed --launches 3
+    python profile_spmv.py --case hubbard_m512 --mixed --launches 3
                                                              # the mixed-precision product
-    python -m dmrg_c_gb300.profile_spmv --sweep --cases xxz_ed22 hubbard_ed12
+    python profile_spmv.py --sweep --cases xxz_ed22 hubbard_ed12
                                                              # the ED Hamiltonians
-    python -m dmrg_c_gb300.profile_spmv --build ed_hubbard12 # device ED build (basis + CRS)
-    python -m dmrg_c_gb300.profile_spmv --obc klm_m128       # matrix-free OBC vs explicit Lanczos
-    python -m dmrg_c_gb300.profile_spmv --vm                 # EXACT_V_M_Q0 on the Hubbard L=12 basis
-    python -m dmrg_c_gb300.profile_spmv --solvers klm_m128   # CG / MINRES / mixed solve times
-    python -m dmrg_c_gb300.profile_spmv --build sb_m512      # device superblock CRS build
+    python profile_spmv.py --build ed_hubbard12 # device ED build (basis + CRS)
+    python profile_spmv.py --obc klm_m128       # matrix-free OBC vs explicit Lanczos
+    python profile_spmv.py --vm                 # EXACT_V_M_Q0 on the Hubbard L=12 basis
+    python profile_spmv.py --solvers klm_m128   # CG / MINRES / mixed solve times
+    python profile_spmv.py --build sb_m512      # device superblock CRS build
 
 Rates are CUDA-event timed on the library stream (dg_profile_spmv): "cold" rewrites a
 256 MiB buffer before every launch so the matrix is not L2-resident, "warm" does not.
@@ -24,9 +24,9 @@ import argparse
 import json
 import sys
 
-from . import ed_models
-from . import lib as L
-from . import workloads
+from dmrg_c_gb300 import ed_models
+from dmrg_c_gb300 import lib as L
+from dmrg_c_gb300 import workloads
 
 CASES = {
     "xxz_m64": workloads.xxz_superblock_m64,
@@ -149,7 +149,7 @@ def obc_solve(name, repeats=3):
     import tempfile
     import time
     import numpy as np
-    from . import abi
+    from dmrg_c_gb300 import abi
     sb = CASES[name](0)
     lib = L.load()
     guess = np.random.default_rng(3).standard_normal(sb.n)
@@ -190,7 +190,7 @@ def vm(repeats=10):
     import time
     import numpy as np
     import torch
-    from . import abi
+    from dmrg_c_gb300 import abi
     ed = L.EDSystem(ed_models.hubbard_chain(12, U=4.0, hz=0.2))
     basis = ed.download()[0]
     ed.close()
@@ -224,7 +224,7 @@ def observables(repeats=5, per_row=16):
     import numpy as np
     import scipy.sparse as sp
     import torch
-    from . import abi, sb_models, workloads
+    from dmrg_c_gb300 import abi, sb_models, workloads
     qb = workloads._block_labels(512, 31, 31.0, 1.25, 0.9, 0)
     qs = workloads.hubbard_site_labels()
     b = L.SuperblockBasis(512, 512, 4, qb, qb, qs, 64 * workloads.QN_SCALE)
@@ -292,7 +292,7 @@ def truncation(repeats=3):
     import time
     import numpy as np
     import os
-    from . import abi, sb_models, workloads
+    from dmrg_c_gb300 import abi, sb_models, workloads
     libc = C.CDLL(None)
     libc.free.argtypes = [C.c_void_p]
     lib = L.load()
@@ -347,7 +347,7 @@ def renorm_operands(r3, c3, nblk, per_row, seed=0):
     O conserving the blocks with per_row elements a row (the shape TRANSFORM_MATRIX sees)."""
     import numpy as np
     import scipy.sparse as sp
-    from . import abi
+    from dmrg_c_gb300 import abi
     rng = np.random.default_rng(seed)
     blocks = np.sort(rng.integers(0, nblk, r3))
     rows_t, cols_t = [], []
@@ -377,7 +377,7 @@ def renorm(repeats=5):
     import ctypes as C
     import time
     import numpy as np
-    from . import abi
+    from dmrg_c_gb300 import abi
     lib = L.load()
     for name, r3, c3, nblk, per_row in (("klm m=128", 1024, 128, 47, 16), ("hubbard m=512", 2048, 512, 57, 24)):
         M1, M2, M3 = renorm_operands(r3, c3, nblk, per_row)
@@ -420,7 +420,7 @@ def build(which, repeats=3):
     """Device builds: ED basis + Hamiltonian, the superblock CRS from host basis arrays, or the
     superblock basis and then the CRS on it (wall time per build)."""
     import time
-    from . import ed_models
+    from dmrg_c_gb300 import ed_models
     if which.startswith("ed_"):
         model = ed_models.hubbard_chain(12, U=4.0, hz=0.2) if which == "ed_hubbard12" else ed_models.xxz_chain(22, Jz=1.3)
         make = lambda: L.EDSystem(model)  # noqa: E731

@@ -101,3 +101,18 @@ def klm_driver_model(g, tag):
     m.dim_charge, m.dim_lspin, m.dim_onsite = 4, 2, 8
     m.t, m.J, m.D_z, m.I_xy, m.I_z, m.h_z, m.mu = t, J, D_z, I_xy, I_z, h_z, mu
     return m
+
+
+def vm_whole_sectors():
+    """The whole bases of vm_q13.npz (as tests/golden/make_golden.py builds them): spin-1/2 L=8 codes
+    by number of up spins (Q1 index k), Hubbard L=4 codes (local states empty, up, down, up+down)
+    by (N_up, N_down, 0) (Q3)."""
+    codes = np.arange(2 ** 8, dtype=np.int64)
+    ups = sum((codes >> s) & 1 for s in range(8))
+    q1 = {(k,): codes[ups == k] for k in range(9)}
+    codes = np.arange(4 ** 4, dtype=np.int64)
+    digits = [(codes // 4 ** s) % 4 for s in range(4)]
+    nu = sum((dg == 1) | (dg == 3) for dg in digits)
+    nd = sum((dg == 2) | (dg == 3) for dg in digits)
+    q3 = {(a, b, 0): codes[(nu == a) & (nd == b)] for a in range(5) for b in range(5)}
+    return q1, (9,), q3, (5, 5, 1)

@@ -166,6 +166,33 @@ def vm_fixture():
     np.savez_compressed(HERE / "vm_hubbard6.npz", **out)
 
 
+def vm_q13_fixture():
+    """The reference's EXACT_V_M_Q1 (spin-1/2 chain: a sector-raising and a diagonal site operator)
+    and EXACT_V_M_Q3 (Hubbard chain: c^dagger_up with and without the fermion sign)."""
+    sys.path.insert(0, str(HERE.parent))
+    from conftest import vm_whole_sectors
+    q1, s1, q3, s3 = vm_whole_sectors()
+    rng = np.random.default_rng(41)
+    out = {}
+    raise_op = abi.Crs(np.array([0, 0, 1]), np.array([0], np.int32), np.array([1.5]), n=2)   # row: output local state
+    diag_op = abi.Crs(np.array([0, 1, 2]), np.array([0, 1], np.int32), np.array([-0.5, 0.75]), n=2)
+    v3, v4 = rng.standard_normal(len(q1[(3,)])), rng.standard_normal(len(q1[(4,)]))
+    out.update(q1_v3=v3, q1_v4=v4)
+    for site in (0, 3, 7):
+        out[f"q1_raise_site{site}"] = po.ref_vm_q1(raise_op, q1, s1, 4, 3, v3, 2, site)
+        out[f"q1_diag_site{site}"] = po.ref_vm_q1(diag_op, q1, s1, 4, 4, v4, 2, site)
+    model = ed_models.hubbard_chain(4, t=-1.0, U=2.0, n_ele=2, twoSz=0)
+    cdu = model.ops[1]                                   # c^dagger_up (row: output local state)
+    out.update(q3_op_row=cdu.row, q3_op_col=cdu.col[:cdu.nnz], q3_op_val=cdu.val[:cdu.nnz])
+    vin = rng.standard_normal(len(q3[(1, 1, 0)]))
+    out["q3_v"] = vin
+    n_ele = np.array([0, 1, 1, 2], np.int32)
+    for site in (0, 2, 3):
+        for sign in (False, True):
+            out[f"q3_site{site}_sign{int(sign)}"] = po.ref_vm_q3(cdu, q3, s3, (2, 1, 0), (1, 1, 0), vin, sign, n_ele, 4, site)
+    np.savez_compressed(HERE / "vm_q13.npz", **out)
+
+
 def sb_obs_fixture():
     """The reference's DMRG_V_M_{LL,LR,RR,RL}_Q0..Q4 and DMRG_EXPECTATION_ONSITE /
     _INTERSITE_Q0 on a seeded Hubbard-type superblock with every sector laid out: block
@@ -316,6 +343,7 @@ def main():
     sb_fixture()
     sb_basis_fixture()
     vm_fixture()
+    vm_q13_fixture()
     sb_obs_fixture()
     ed_obs_fixture()
     renorm_fixture()

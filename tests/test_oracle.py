@@ -416,3 +416,23 @@ def test_live_reference_truncation_and_renorm(ref):
     for x, y in zip(r[:6], ref.crs_crs_ccs(M1, M2, M3)):
         x, y = np.asarray(x), np.asarray(y)
         assert np.array_equal(x.astype(np.float64).view(np.int64), y.astype(np.float64).view(np.int64))
+
+
+def test_oracle_site_apply_matches_reference_q1_q3_golden(oracle):
+    """The oracle's site-operator application against the reference's EXACT_V_M_Q1 / _Q3 (golden)."""
+    from conftest import vm_whole_sectors
+    g = golden("vm_q13.npz")
+    q1, _, q3, _ = vm_whole_sectors()
+    raise_op = abi.Crs(np.array([0, 0, 1]), np.array([0], np.int32), np.array([1.5]), n=2)
+    diag_op = abi.Crs(np.array([0, 1, 2]), np.array([0, 1], np.int32), np.array([-0.5, 0.75]), n=2)
+    for site in (0, 3, 7):
+        np.testing.assert_array_equal(oracle.site_apply(raise_op, q1[(4,)], q1[(3,)], 2, site, g["q1_v3"]),
+                                      g[f"q1_raise_site{site}"])
+        np.testing.assert_array_equal(oracle.site_apply(diag_op, q1[(4,)], q1[(4,)], 2, site, g["q1_v4"]),
+                                      g[f"q1_diag_site{site}"])
+    op = abi.Crs(g["q3_op_row"], g["q3_op_col"], g["q3_op_val"], n=4)
+    for site in (0, 2, 3):
+        for sign in (0, 1):
+            ne = np.array([0, 1, 1, 2], np.int32) if sign else None
+            np.testing.assert_array_equal(oracle.site_apply(op, q3[(2, 1, 0)], q3[(1, 1, 0)], 4, site, g["q3_v"], n_ele=ne),
+                                          g[f"q3_site{site}_sign{sign}"])

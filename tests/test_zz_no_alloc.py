@@ -1,9 +1,11 @@
 """The allocation-free CG entry point (dg_cg_noalloc), for callers that cannot let a library
-allocate device memory (inside a stream capture, under an application-owned memory pool).
+allocate device memory (an application whose own memory pool owns the device, or a solve path
+that must not allocate).
 
 It must give the same solution as the allocating entry point (dg_linear_solve) on the same
-system, on consecutive calls that share its static scratch array, and reject systems larger
-than the array holds.  Kept in its own file, collected last."""
+system, on consecutive calls that share its static scratch array, match the reference's own
+CONJUGATE_GRADIENT_SYM solution (golden cg_x), reject systems larger than the array holds and
+reject a malformed CRS before any product runs.  Kept in its own file, collected last."""
 import ctypes as C
 
 import numpy as np
@@ -65,6 +67,37 @@ def test_noalloc_cg_matches_allocating_entry_point_twice(gpu):
         assert rc == 0 and rc_ref == 0
         assert abs(it - it_ref) <= 2
         assert np.abs(x - x_ref).max() <= TOL * np.abs(x_ref).max()
+
+
+def test_noalloc_cg_matches_reference_golden(gpu):
+    """The first system is the golden fixture's B x = b from x0, solved by the reference's
+    CONJUGATE_GRADIENT_SYM to ||r||^2 < 1e-10 (sml/CONJUGATE_GRADIENT_SYM.c)."""
+    torch = pytest.importorskip("torch")
+    g = golden("sml_random1500.npz")
+    crs, b, x0, sigma = _systems()[0]
+    rc, it, x = _noalloc(gpu, torch, crs, b, x0, sigma, acc=1e-10, max_step=1000)
+    assert rc == 0
+    np.testing.assert_allclose(x, g["cg_x"], rtol=0, atol=1e-8)
+    assert abs(it - int(g["cg_iters"])) <= 2
+
+
+def test_noalloc_cg_rejects_malformed_crs(gpu):
+    """A column outside [0, n) and decreasing row offsets are refused (DG_ERR_MATRIX) by the
+    device-side check, before any product gathers through them; the next good call still works."""
+    torch = pytest.importorskip("torch")
+    crs, b, x0, sigma = _systems()[0]
+    for how in ("column", "offsets"):
+        row, col = crs.row.copy(), crs.col[:crs.nnz].copy()
+        if how == "column":
+            col[17] = crs.n + 100
+        else:
+            row[40] = row[42] + 1
+        bad = abi.Crs(row, col, crs.val[:crs.nnz].copy(), n=crs.n)
+        rc, it, x = _noalloc(gpu, torch, bad, b, x0, sigma)
+        assert rc == 7, (how, rc)
+        assert b"row" in gpu.load().dg_last_error()
+    rc, it, x = _noalloc(gpu, torch, crs, b, x0, sigma)
+    assert rc == 0
 
 
 def test_noalloc_cg_rejects_oversized_system(gpu):
