@@ -13,7 +13,8 @@ scratch directory and stores, for the largest superblock of every finite sweep:
   LANCZOS[_SLOW]_SYM + INVERSE_ITERATION_SYM);
 
 and, per run, every superblock solve (sweep, sites, dimension, stored elements, energy) and the
-model's own result/.../energy.txt lines.
+lines of the run's own result files: result/log.txt (PRINT_STATUS), result/SystemInfo/
+Energy_<sweep>.txt and result/[...]/AverageValues/energy.txt.
 
 Configurations (the workloads of the benchmark):
   xxz_vf      spin-1/2 XXZ chain, OBC, L=32, Jxy=Jz=1, hz=0, 2Sz=0, m=64, 4 sweeps, Lanczos_Slow
@@ -29,6 +30,7 @@ Needs the reference source tree (env DMRG_REF, default /root/reference) and abou
 from __future__ import annotations
 
 import argparse
+import json
 import os
 import subprocess
 import sys
@@ -40,6 +42,13 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 MODELS = ("xxz_vf", "klm_vf", "hubbard_vf")
+# the MODEL_* fields oracle/ref_dmrg_dump.c sets (and the drivers print in energy.txt)
+MODEL_PARAMS = {
+    "xxz_vf": dict(tot_site=32, spin=1, tot_sz=0, J_xy=1.0, J_z=1.0, D_z=0.0, h_z=0.0, m=64),
+    "klm_vf": dict(tot_site=24, tot_ele=12, spin_loc=1, tot_sz=0, t=-1.0, J=1.0, D_z=0.0, I_xy=0.0, I_z=0.0, h_z=0.1, mu=0.0,
+                   m=128),
+    "hubbard_vf": dict(tot_site=64, tot_ele=64, tot_sz=0, t1=-1.0, t2=0.0, U=4.0, V=0.0, h_z=0.0, mu=0.0, m=512),
+}
 # ground-state vectors above this many states are stored in float32 (the overlap test is
 # insensitive to it: rounding each component by 6e-8 moves the overlap by ~1e-15)
 F64_VECTOR_MAX = 100_000
@@ -109,9 +118,15 @@ def convert_run(model: str, run_dir: Path) -> list[Path]:
         for p in sorted(res.glob("*/AverageValues/energy.txt")):
             for line in p.read_text().splitlines():
                 energy_lines.append(f"{p.parent.parent.name}\t{line}")
+    log_lines = (res / "log.txt").read_text().splitlines() if (res / "log.txt").exists() else []
+    sweep_lines = []
+    for p in sorted((res / "SystemInfo").glob("Energy_*.txt")) if res.exists() else []:
+        k = int(p.stem.split("_")[1])
+        sweep_lines += [f"{k}\t{line}" for line in p.read_text().splitlines()]
     summary = dict(sweep=st[:, 0].astype(np.int32), LL_site=st[:, 1].astype(np.int32), RR_site=st[:, 2].astype(np.int32),
                    n=st[:, 3].astype(np.int64), nnz=st[:, 4].astype(np.int64), gs_val=st[:, 5].astype(np.float64),
-                   gs_error=st[:, 6].astype(np.float64), energy_txt=np.array(energy_lines))
+                   gs_error=st[:, 6].astype(np.float64), energy_txt=np.array(energy_lines), log_txt=np.array(log_lines),
+                   energy_sweep_txt=np.array(sweep_lines), model_params=np.array(json.dumps(MODEL_PARAMS[model])))
     p = HERE / f"dmrg_{model}_steps.npz"
     np.savez_compressed(p, **summary)
     written.append(p)

@@ -1,13 +1,18 @@
 """C-ABI checks that need no GPU: the library loads, exports every function the headers
 declare, and the ctypes mirrors have the C layouts (and, where the reference tree is
 present, the reference headers' layouts)."""
+import os
 import re
 import subprocess
+import sys
 from pathlib import Path
 
 import pytest
 
 from conftest import ROOT
+
+# the reference source tree, where it exists (its headers are compared with ours)
+REF = Path(os.environ.get("DMRG_REF", "/root/reference"))
 
 HEADERS = sorted((ROOT / "include").glob("*.h"))
 
@@ -84,7 +89,7 @@ def test_struct_layouts_match_our_header(tmp_path):
 
 
 def test_struct_layouts_match_reference_headers(tmp_path):
-    ref = Path("/root/reference/include")
+    ref = REF / "include"
     if not (ref / "SML.h").exists():
         pytest.skip("reference headers not present")
     (tmp_path / "both.h").write_text('#include "dmrg.h"\n#include "exact.h"\n')
@@ -93,7 +98,7 @@ def test_struct_layouts_match_reference_headers(tmp_path):
 
 def test_headers_compile_after_reference_headers(tmp_path):
     """A reference translation unit can include our header after its own."""
-    ref = Path("/root/reference/include")
+    ref = REF / "include"
     if not (ref / "SML.h").exists():
         pytest.skip("reference headers not present")
     src = tmp_path / "tu.c"
@@ -112,3 +117,58 @@ def test_native_api_without_device_reports_nodevice(lib):
     with pytest.raises(L.DgError) as e:
         L.DeviceMatrix(crs)
     assert e.value.code == 6
+
+
+def _link_trace(tmp_path, objs, symbols, out_name):
+    """Link objs against libdmrg_gb300.so ahead of the reference's archives (oracle/_ref) the way a
+    reference program is linked (LFLAGS = -ldmrg -lonsite_op -lsml, main/dmrg/xxz_vf/makefile:17,22);
+    returns {symbol: [file defining it]} from the linker's -y trace."""
+    openblas = subprocess.run([sys.executable, "-c", "import scipy, os, glob; d = os.path.join(os.path.dirname(scipy.__file__), "
+                               "os.pardir, 'scipy.libs'); print(os.path.abspath(sorted(glob.glob(os.path.join(d, "
+                               "'libscipy_openblas*.so')))[0]))"], capture_output=True, text=True, check=True).stdout.strip()
+    refdir = ROOT / "oracle" / "_ref"
+    cmd = ["gcc", "-fopenmp", "-o", str(tmp_path / out_name), *map(str, objs), str(refdir / "obj" / "lapack_shim.o"),
+           f"-L{ROOT / 'dmrg_c_gb300'}", "-ldmrg_gb300", f"-L{refdir}", "-ldmrg", "-lonsite_op", "-lsml", openblas, "-lm"]
+    cmd += [f"-Wl,-y,{s}" for s in symbols]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    defs = {}
+    for line in (r.stdout + r.stderr).splitlines():
+        m = re.match(r".*?([^\s:]+): definition of (\w+)", line)
+        if m:
+            defs.setdefault(m.group(2), []).append(Path(m.group(1)).name)
+    return defs
+
+
+def _ref_build(ref):
+    subprocess.run(["make", "-s", "-j8", "-C", str(ROOT / "oracle"), "archives", f"REF={ref.REF_SRC}"], check=True)
+
+
+def test_reference_dmrg_program_links_the_gpu_library(ref, lib, tmp_path):
+    """The reference's own Hubbard DMRG program (every object of main/dmrg/hubbard_vf, its main.c
+    included, compiled unchanged) links with libdmrg_gb300 ahead of the reference archives: the
+    superblock solve it calls (GET_GROUND_STATE.c:18) and the solvers resolve to the GPU library."""
+    _ref_build(ref)
+    objs = sorted((ROOT / "oracle" / "_ref" / "obj" / "main" / "dmrg" / "hubbard_vf").rglob("*.o"))
+    assert any(o.name == "main.o" for o in objs)
+    syms = ["DMRG_DIAGONALIZE_SUPERBLOCK_SYM", "LANCZOS_SYM", "INVERSE_ITERATION_SYM", "CONJUGATE_GRADIENT_SYM",
+            "DMRG_GET_SYSTEM_INFO_Q2", "CRS_CRS_CCS_PRODUCT"]
+    defs = _link_trace(tmp_path, objs, syms, "hubbard_vf_on_gb300")
+    assert defs["DMRG_DIAGONALIZE_SUPERBLOCK_SYM"] == ["libdmrg_gb300.so"], defs
+    for s in syms:
+        assert defs.get(s) == ["libdmrg_gb300.so"], (s, defs.get(s))
+
+
+def test_reference_solver_wrapper_links_the_gpu_solvers(ref, lib, tmp_path):
+    """A reference translation unit that calls the solvers -- dmrg/DMRG_DIAGONALIZE_SUPERBLOCK_SYM.c
+    itself, forced in as an object -- gets LANCZOS_SYM, LANCZOS_SLOW_SYM and INVERSE_ITERATION_SYM
+    from the GPU library, not from the reference's libsml.a."""
+    _ref_build(ref)
+    main = tmp_path / "main.c"
+    main.write_text('#include "dmrg.h"\nint main(void) { DMRG_DIAGONALIZE_SUPERBLOCK_SYM(0, 0, 0, 0, 1); return 0; }\n')
+    subprocess.run(["gcc", f"-I{ref.REF_SRC / 'include'}", "-c", str(main), "-o", str(tmp_path / "main.o")], check=True)
+    wrapper = ROOT / "oracle" / "_ref" / "obj" / "dmrg" / "DMRG_DIAGONALIZE_SUPERBLOCK_SYM.o"
+    syms = ["LANCZOS_SYM", "LANCZOS_SLOW_SYM", "INVERSE_ITERATION_SYM"]
+    defs = _link_trace(tmp_path, [tmp_path / "main.o", wrapper], syms, "wrapper_on_gb300")
+    for s in syms:
+        assert defs.get(s) == ["libdmrg_gb300.so"], (s, defs.get(s))

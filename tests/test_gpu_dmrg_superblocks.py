@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from dmrg_c_gb300 import abi, sb_models
+from dmrg_c_gb300 import abi, sb_models, status_files
 
 TOL_E = 1e-10
 TOL_OV = 1e-9
@@ -89,3 +89,15 @@ def test_dmrg_dropin_on_final_superblock(gpu, oracle, loaded, in_tmp, model):
     assert abs(st.gs_val - sb.gs_val) <= TOL_E * abs(sb.gs_val)
     assert st.gs_error < 1e-9 and tm.diag > 0 and tm.inv_iter > 0
     assert abs(gs @ sb.gs_vec) / (np.linalg.norm(gs) * np.linalg.norm(sb.gs_vec)) >= 1 - TOL_OV
+    # the step's line of result/SystemInfo/Energy_<sweep>.txt from what the drop-in filled, against
+    # the reference run's line: sizes and step counter identical, E and E/N within the tolerance
+    z = np.load(GOLDEN / f"dmrg_{model}_steps.npz")
+    i = int(np.flatnonzero((z["sweep"] == sb.sweep) & (z["LL_site"] == sb.LL_site) & (z["RR_site"] == sb.RR_site))[0])
+    ref_lines = [str(e).split("\t", 1)[1] for e in z["energy_sweep_txt"] if str(e).startswith(f"{sb.sweep}\t")]
+    ref_lines = [ln for ln in ref_lines if ln and not ln.startswith("###")]
+    k = i - int(np.flatnonzero(z["sweep"] == sb.sweep)[0])
+    mine = status_files.energy_sweep_line(sb.LL_site, sb.RR_site, i + 1, st.gs_val, st.gs_error).split()
+    ref = ref_lines[k].split()
+    assert mine[:3] == ref[:3]
+    assert abs(float(mine[3]) - float(ref[3])) <= TOL_E * abs(float(ref[3])) + 1e-15
+    assert abs(float(mine[4]) - float(ref[4])) <= TOL_E * abs(float(ref[4])) + 1e-15
