@@ -291,6 +291,122 @@ def sweeps_leg(L, seed, models=("klm_vf", "hubbard_vf")):
     return out
 
 
+def _engine_run(L, models, params, lanczos_batch, workers=8, arrivals=None):
+    """Every model through the engine (arrivals: submission times in s, else all at once); returns
+    (wall s, {index: dg_job_result})."""
+    eng = L.Engine(workers=workers, lanczos_batch=lanczos_batch)
+    res = {}
+    t0 = time.perf_counter()
+    for i, m in enumerate(models):
+        if arrivals is not None:
+            while True:
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt <= 0:
+                    break
+                for r, _ in eng.poll(256, wait_ms=0):
+                    res[r.id] = r
+                time.sleep(min(dt, 0.002))
+        eng.submit(m, params, i)
+    while len(res) < len(models):
+        for r, _ in eng.poll(256, wait_ms=50):
+            res[r.id] = r
+    wall = time.perf_counter() - t0
+    eng.close()
+    bad = [i for i, r in res.items() if r.status != 0 or not r.converged]
+    if bad:
+        raise RuntimeError(f"{len(bad)} engine jobs failed, e.g. {bad[:4]}")
+    return wall, res
+
+
+def oracle_ed_solve(model, threads):
+    """One ED instance on the CPU: the oracle's basis and CRS build, LANCZOS (Guess "No", seeded)
+    and INVERSE_ITERATION with CG.  Returns (seconds, energy)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+    from dmrg_c_gb300 import abi
+    t0 = time.perf_counter()
+    basis, row, col, val = pyoracle.ed_build(model, threads=threads)
+    H = abi.Crs(row, col, val, n=len(basis))
+    rc, out, v = pyoracle.lanczos(H, False, seed=7, threads=threads)
+    pyoracle.inverse_iteration(H, False, out.eig_val, v, threads=threads)
+    return time.perf_counter() - t0, out.eig_val
+
+
+def batched_leg(L, args):
+    """The batched form on the 256 XXZ chains of the batched-ED workload (L in {12..22}, Jz ~ U[0,2],
+    hz ~ U[0,1], seed 0): FP64 and mixed (mixed = 2) through the engine's lock-step Lanczos, beside
+    the engine without it, with every mixed energy against the FP64 one."""
+    from dmrg_c_gb300 import workloads
+    inst = workloads.xxz_ed_batch(256, seed=0)
+    models = [i["model"]() for i in inst]
+    out = {"workload": "256 XXZ chains, L in {12,...,22} (n 924 ... 705,432), Jz ~ U[0,2], hz ~ U[0,1], seed 0",
+           "unit": "solves/s"}
+    E = {}
+    for tag, mixed, lb in (("fp64", 0, True), ("mixed", 2, True), ("fp64_streams", 0, False), ("mixed_streams", 2, False)):
+        p = L.default_params(seed=7, mixed=mixed)
+        _engine_run(L, models[:16], p, lb)                      # warm-up
+        walls = []
+        for _ in range(2):
+            wall, res = _engine_run(L, models, p, lb)
+            walls.append(wall)
+        E[tag] = np.array([res[i].eig_val for i in range(len(models))])
+        out[tag] = {"value": len(models) / min(walls), "wall_ms": 1e3 * min(walls), "lanczos_batch": lb,
+                    "p50_ms_per_job": float(np.percentile([r.t_done_ms - r.t_submit_ms for r in res.values()], 50))}
+    out["mixed_speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["lanczos_batch_speedup_fp64"] = out["fp64"]["value"] / out["fp64_streams"]["value"]
+    out["max_dE_rel_mixed_vs_fp64"] = float(np.max(np.abs(E["mixed"] - E["fp64"]) / np.abs(E["fp64"])))
+    out["max_dE_rel_batch_vs_streams"] = float(np.max(np.abs(E["fp64"] - E["fp64_streams"]) / np.abs(E["fp64_streams"])))
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = [i for Lx in (12, 14, 16, 18, 20, 22) for i in range(len(inst)) if inst[i]["L"] == Lx][:0]
+        for Lx in (12, 14, 16, 18, 20, 22):
+            sample += [i for i in range(len(inst)) if inst[i]["L"] == Lx][:1]
+        secs = {}
+        for i in sample:
+            t, e = oracle_ed_solve(models[i], threads)
+            secs[inst[i]["L"]] = t
+        total = sum(secs[i["L"]] for i in inst)     # sequential FIFO over the whole batch
+        out["cpu_baseline"] = {"value": len(inst) / total, "unit": "solves/s", "cores": threads, "kind": "port",
+                               "cpu": cpu_model(), "sample": "one instance of each L solved by the oracle (ED build + "
+                               "LANCZOS + INVERSE_ITERATION), extrapolated to the batch's L mix, one after another",
+                               "sec_by_L": {int(k): v for k, v in secs.items()}}
+    return out
+
+
+def served_leg(L, args):
+    """The served form: the Hubbard request stream (L in {8,10,12}, U ~ U[0,8], h ~ U[0,0.5], half
+    filling, Poisson arrivals at 200/s, seed 1) replayed in real time for --served-seconds, FP64 and
+    mixed, through the engine's continuous lock-step batch; p50/p99 latency, solves/s, each mixed
+    energy against the FP64 one; and the capacity of each form on an 800/s stream."""
+    from dmrg_c_gb300 import workloads
+    trace = workloads.hubbard_request_trace(rate=200.0, duration=args.served_seconds, seed=1)
+    models = [r["model"]() for r in trace]
+    arr = [r["t"] for r in trace]
+    out = {"workload": f"Hubbard ED requests, Poisson 200/s for {args.served_seconds:g} s, L in {{8,10,12}}, seed 1",
+           "requests": len(trace)}
+    E = {}
+    for tag, mixed in (("fp64", 0), ("mixed", 2)):
+        p = L.default_params(seed=11, mixed=mixed)
+        _engine_run(L, models[:16], p, True)
+        wall, res = _engine_run(L, models, p, True, arrivals=arr)
+        lat = np.array([res[i].t_done_ms - res[i].t_submit_ms for i in range(len(models))])
+        first = min(r.t_submit_ms for r in res.values())
+        last = max(r.t_done_ms for r in res.values())
+        E[tag] = np.array([res[i].eig_val for i in range(len(models))])
+        out[tag] = {"solves_per_s": len(models) / ((last - first) * 1e-3), "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean())}
+        # capacity: the same requests offered at 800/s for 5 s
+        cap_trace = workloads.hubbard_request_trace(rate=800.0, duration=5.0, seed=2)
+        cap_models = [r["model"]() for r in cap_trace]
+        wall, res = _engine_run(L, cap_models, p, True, arrivals=[r["t"] for r in cap_trace])
+        first = min(r.t_submit_ms for r in res.values())
+        last = max(r.t_done_ms for r in res.values())
+        out[tag]["capacity_solves_per_s"] = len(cap_models) / ((last - first) * 1e-3)
+    out["mixed_capacity_speedup_vs_fp64"] = out["mixed"]["capacity_solves_per_s"] / out["fp64"]["capacity_solves_per_s"]
+    out["max_dE_rel_mixed_vs_fp64"] = float(np.max(np.abs(E["mixed"] - E["fp64"]) / np.abs(E["fp64"])))
+    return out
+
+
 def run_gb300(args, ws, rank, local_rank):
     import torch
     from dmrg_c_gb300 import abi, lib as L
@@ -452,6 +568,9 @@ def run_gb300(args, ws, rank, local_rank):
     }
     if rank == 0 and not args.no_sweeps:
         result["sweeps"] = sweeps_leg(L, args.seed + 1)
+    if rank == 0 and not args.no_ed:
+        result["batched"] = batched_leg(L, args)
+        result["served"] = served_leg(L, args)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         times, E_cpu, v_cpu, st_cpu, cg_cpu = cpu_sample(low, settings, args.seed + 1, threads)
@@ -505,6 +624,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweeps", action="store_true", help="skip the per-sweep energy errors")
+    ap.add_argument("--no-ed", action="store_true", help="skip the batched and served ED legs")
+    ap.add_argument("--served-seconds", type=float, default=20.0, help="length of the served request stream")
     args = ap.parse_args(argv)
     ws, rank, local_rank = dist_info()
     if args.impl == "reference":

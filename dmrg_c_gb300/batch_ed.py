@@ -1,11 +1,13 @@
 """Batched ED ground states: 256 XXZ chains of uneven size through the concurrent engine.
 
-    python -m dmrg_c_gb300.batch_ed [--count 256] [--workers 8] [--mixed] [--json out.json]
+    python -m dmrg_c_gb300.batch_ed [--count 256] [--workers 8] [--mixed] [--lanczos-batch] [--json out.json]
 
 Instances (dmrg_c_gb300.workloads.xxz_ed_batch, seed 0): L uniform in {12,...,22} (Sz = 0
 sector dimensions 924 ... 705,432), Jz ~ U[0,2], hz ~ U[0,1], Jxy = 1, OBC.  Each instance's
 basis and Hamiltonian are built on the device; solves run concurrently on the engine's
-worker streams.  Reports batch solves/s against the same batch run one instance at a time.
+worker streams; with --lanczos-batch their Lanczos phases run in the engine's lock-step batch
+(one launch of each kernel a step over all instances).  Reports batch solves/s against the same
+batch run one instance at a time.
 """
 from __future__ import annotations
 
@@ -20,9 +22,9 @@ from . import lib as L
 from . import workloads
 
 
-def run_batch(instances, params, workers, hbm_budget=0):
+def run_batch(instances, params, workers, hbm_budget=0, lanczos_batch=False):
     """Submit every instance, wait for all; returns (wall seconds, results by index)."""
-    eng = L.Engine(workers=workers, hbm_budget=hbm_budget)
+    eng = L.Engine(workers=workers, hbm_budget=hbm_budget, lanczos_batch=lanczos_batch)
     models = [inst["model"]() for inst in instances]
     t0 = time.perf_counter()
     for i, m in enumerate(models):
@@ -44,14 +46,16 @@ def main(argv=None):
     ap.add_argument("--count", type=int, default=256)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--lanczos-batch", action="store_true")
     ap.add_argument("--no-sequential", action="store_true")
     ap.add_argument("--json", default=None)
     a = ap.parse_args(argv)
     inst = workloads.xxz_ed_batch(a.count, seed=0)
     p = L.default_params(seed=7, mixed=2 if a.mixed else 0)
-    run_batch(inst[:8], p, a.workers)                       # warm-up (pool, kernels)
-    wall, res = run_batch(inst, p, a.workers)
+    run_batch(inst[:8], p, a.workers, lanczos_batch=a.lanczos_batch)   # warm-up (pool, kernels)
+    wall, res = run_batch(inst, p, a.workers, lanczos_batch=a.lanczos_batch)
     out = {"instances": a.count, "workers": a.workers, "form": "mixed" if a.mixed else "fp64",
+           "lanczos_batch": a.lanczos_batch,
            "wall_s": wall, "solves_per_s": a.count / wall,
            "sum_dim": int(sum(r.dim for r in res.values())), "sum_nnz": int(sum(r.nnz for r in res.values()))}
     if not a.no_sequential:

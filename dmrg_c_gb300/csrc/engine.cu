@@ -9,6 +9,12 @@
 // posts the result.  Kernels of different jobs overlap on the device; each job's Krylov
 // state lives on the device for the whole solve.
 //
+// With lanczos_batch, a worker hands an eligible job, once built, to the engine's lock-step
+// Lanczos (batch.cuh: every Lanczos step of all such jobs is one launch of each of four kernels)
+// and takes the next job; when the job's Lanczos phase converges, a worker runs its inverse
+// iteration or refinement on its own stream and posts the result.  Jobs join and leave the
+// lock-step batch at any step, so requests that arrive while others iterate start at once.
+//
 // Admission: a job starts only when a worker is idle and its device-memory estimate fits the
 // engine's budget next to the jobs already running (a job larger than the whole budget runs
 // alone).  Jobs start in submission order.  Every job's result is the same as when it runs
@@ -25,6 +31,9 @@
 
 #include <cuda_runtime.h>
 
+#include <unordered_map>
+
+#include "batch.cuh"
 #include "common.cuh"
 #include "dmrg_gb300_ed.h"
 
@@ -102,6 +111,14 @@ size_t estimate_bytes(const dg_ed_model &m, long dim, const dg_solver_params &p)
 
 }  // namespace
 
+// A job whose Lanczos phase runs in the lock-step batch, between its build and its post phase.
+struct Parked {
+  Job job;
+  dg_job_result r{};
+  dg_matrix *mat = nullptr;
+  cudaEvent_t built = nullptr;
+};
+
 struct dg_engine {
   dg_engine_config cfg{};
   int device = 0;
@@ -115,6 +132,58 @@ struct dg_engine {
   int running = 0;
   bool stop = false;
   std::vector<std::thread> workers;
+  // lock-step batch (one per form: FP64, mixed = 2), created on first use
+  std::unique_ptr<dg::BatchLanczos> batch[3];
+  std::unordered_map<long, Parked> parked;   // by internal sequence number
+  std::deque<dg::BatchDone> posts;           // converged Lanczos phases awaiting their post phase
+  long seq = 0;
+
+  dg::BatchLanczos &batcher(int mixed) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!batch[mixed])
+      batch[mixed] = std::make_unique<dg::BatchLanczos>(device, mixed, [this](dg::BatchDone &d) {
+        {
+          std::lock_guard<std::mutex> lk2(mu);
+          posts.push_back(d);
+        }
+        cv_job.notify_all();
+      });
+    return *batch[mixed];
+  }
+
+  void finish_job(const Job &j, const dg_job_result &r) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      used -= j.bytes;
+      --running;
+      done.push_back(r);
+    }
+    cv_done.notify_all();
+    cv_job.notify_all();
+  }
+
+  // The post phase of a parked job whose Lanczos phase has left the batch.
+  void run_post(dg::BatchDone &d) {
+    Parked pk;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      auto it = parked.find(d.tag);
+      pk = std::move(it->second);
+      parked.erase(it);
+    }
+    dg_solve_info info{};
+    const int rc = dg::batch_post(d, pk.job.params, pk.job.out_vec, &info);
+    pk.r.eig_val = info.eig_val;
+    pk.r.error = info.error;
+    pk.r.lanczos_steps = info.lanczos_steps;
+    pk.r.cg_steps = info.cg_steps;
+    pk.r.converged = (rc == DG_OK) && info.converged;
+    pk.r.status = rc;
+    pk.r.t_done_ms = now_ms();
+    if (pk.built) cudaEventDestroy(pk.built);
+    dg_matrix_free(pk.mat);
+    finish_job(pk.job, pk.r);
+  }
 
   double now_ms() const { return std::chrono::duration<double, std::milli>(clock_type::now() - t0).count(); }
 
@@ -135,6 +204,31 @@ struct dg_engine {
       ed = nullptr;
     }
     r.t_built_ms = now_ms();
+    if (rc == DG_OK && cfg.lanczos_batch && dg::batch_eligible(mat, j.params)) {
+      // park the job; its Lanczos phase joins the lock-step batch
+      cudaEvent_t ev = nullptr;
+      rc = dg::guarded([&] {
+        DG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        DG_CUDA(cudaEventRecord(ev, dg::stream()));
+      });
+      if (rc == DG_OK) {
+        dg::BatchLanczos &bl = batcher(j.params.mixed);
+        long tag;
+        const dg_solver_params params = j.params;
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          tag = seq++;
+          Parked &pk = parked[tag];
+          pk.job = std::move(j);
+          pk.r = r;
+          pk.mat = mat;
+          pk.built = ev;
+        }
+        bl.add(tag, mat, params, ev);
+        r.status = -1;   // no result yet
+        return;
+      }
+    }
     if (rc == DG_OK) {
       // The eigenvector stays on the device (stream-ordered pool memory: no device-wide
       // synchronisation that would stall the other workers' streams).
@@ -164,29 +258,36 @@ struct dg_engine {
     cudaSetDevice(device);
     while (true) {
       Job j;
+      dg::BatchDone post;
+      bool is_post = false;
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_job.wait(lk, [&] {
           if (stop) return true;
+          if (!posts.empty()) return true;
           if (queue.empty()) return false;
           return running == 0 || used + queue.front().bytes <= budget;
         });
         if (stop) return;
-        j = std::move(queue.front());
-        queue.pop_front();
-        used += j.bytes;
-        ++running;
+        if (!posts.empty()) {   // finishing jobs first keeps their latency down
+          post = posts.front();
+          posts.pop_front();
+          is_post = true;
+        } else {
+          j = std::move(queue.front());
+          queue.pop_front();
+          used += j.bytes;
+          ++running;
+        }
+      }
+      if (is_post) {
+        run_post(post);
+        continue;
       }
       dg_job_result r{};
       run_job(j, r);
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        used -= j.bytes;
-        --running;
-        done.push_back(r);
-      }
-      cv_done.notify_all();
-      cv_job.notify_all();
+      if (r.status == -1) continue;   // parked in the lock-step batch
+      finish_job(j, r);
     }
   }
 };
@@ -270,6 +371,17 @@ void dg_engine_destroy(dg_engine *e) {
   }
   e->cv_job.notify_all();
   for (auto &t : e->workers) t.join();
+  // the batches finish the Lanczos phases in flight; their post phases are dropped
+  for (auto &b : e->batch) b.reset();
+  for (auto &d : e->posts) {
+    if (d.psi) dg::pool_free(d.psi, dg::stream());
+    if (d.ready) cudaEventDestroy(d.ready);
+  }
+  for (auto &kv : e->parked) {
+    if (kv.second.built) cudaEventDestroy(kv.second.built);
+    dg_matrix_free(kv.second.mat);
+  }
+  cudaStreamSynchronize(dg::stream());
   delete e;
 }
 

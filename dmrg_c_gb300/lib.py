@@ -117,6 +117,7 @@ SIGNATURES = {
     "dg_lanczos": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
     "dg_inverse_iteration": (C.c_int, [vp, P(dg_solver_params), C.c_double, vp, P(dg_solve_info)]),
     "dg_ground_state": (C.c_int, [vp, P(dg_solver_params), vp, vp, P(dg_solve_info)]),
+    "dg_batch_ground_state": (C.c_int, [C.c_int, P(vp), P(dg_solver_params), P(vp), P(dg_solve_info), P(C.c_int)]),
     "dg_linear_solve": (C.c_int, [vp, C.c_double, vp, vp, C.c_double, C.c_int, C.c_int, ip]),
     "dg_residual_l1": (C.c_int, [vp, vp, C.c_double, dp]),
     "dg_cg_noalloc": (C.c_int, [C.c_int, vp, vp, vp, C.c_double, vp, vp, C.c_double, C.c_int, ip]),
@@ -508,8 +509,8 @@ class SuperblockCRS:
 class Engine:
     """Concurrent ED ground-state engine (dg_engine): submit models, poll results."""
 
-    def __init__(self, workers: int = 0, hbm_budget: int = 0):
-        cfg = abi.dg_engine_config(workers=workers, hbm_budget=hbm_budget)
+    def __init__(self, workers: int = 0, hbm_budget: int = 0, lanczos_batch: bool = False):
+        cfg = abi.dg_engine_config(workers=workers, hbm_budget=hbm_budget, lanczos_batch=int(lanczos_batch))
         h = C.c_void_p()
         check(load().dg_engine_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -573,6 +574,22 @@ def ground_state(m: DeviceMatrix, params: dg_solver_params | None = None, guess=
     fn = load().dg_lanczos if lanczos_only else load().dg_ground_state
     check(fn(m.h, C.byref(p), as_ptr(guess), as_ptr(out), C.byref(info)))
     return out, info
+
+
+def batch_ground_state(mats, params: dg_solver_params | None = None, want_vectors=True):
+    """Ground states of several DeviceMatrix solved together (dg_batch_ground_state); returns
+    ([eigvec or None], [dg_solve_info]).  Raises DgError if any instance failed."""
+    p = params or default_params()
+    k = len(mats)
+    handles = (vp * max(k, 1))(*[m.h for m in mats])
+    outs = [np.empty(m.n, np.float64) for m in mats] if want_vectors else []
+    vecs = (vp * max(k, 1))(*[as_ptr(o) for o in outs]) if want_vectors else None
+    infos = (dg_solve_info * max(k, 1))()
+    st = (C.c_int * max(k, 1))()
+    check(load().dg_batch_ground_state(k, handles, C.byref(p), vecs, infos, st))
+    for i in range(k):
+        check(st[i])
+    return (outs if want_vectors else [None] * k), [infos[i] for i in range(k)]
 
 
 def linear_solve(m: DeviceMatrix, b, x, sigma=0.0, acc=1e-7, max_step=1000, minres=False):

@@ -1,6 +1,6 @@
 """Served ED ground states: a Poisson request stream replayed in real time against the engine.
 
-    python -m dmrg_c_gb300.serve [--rate 200] [--seconds 60] [--workers 8] [--mixed]
+    python -m dmrg_c_gb300.serve [--rate 200] [--seconds 60] [--workers 8] [--mixed] [--lanczos-batch]
 
 Requests (dmrg_c_gb300.workloads.hubbard_request_trace, seed 1): 1D Hubbard chains, OBC,
 half filling, 2Sz = 0, L in {8,10,12} (dimensions 4,900 / 63,504 / 853,776), t = 1,
@@ -22,9 +22,9 @@ from . import lib as L
 from . import workloads
 
 
-def serve(trace, params, workers, hbm_budget=0):
+def serve(trace, params, workers, hbm_budget=0, lanczos_batch=False):
     models = [req["model"]() for req in trace]
-    eng = L.Engine(workers=workers, hbm_budget=hbm_budget)
+    eng = L.Engine(workers=workers, hbm_budget=hbm_budget, lanczos_batch=lanczos_batch)
     res = {}
     max_queue = 0
     t0 = time.perf_counter()
@@ -65,13 +65,15 @@ def main(argv=None):
     ap.add_argument("--seconds", type=float, default=60.0)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--lanczos-batch", action="store_true")
     a = ap.parse_args(argv)
     trace = workloads.hubbard_request_trace(rate=a.rate, duration=a.seconds, seed=1)
     p = L.default_params(seed=11, mixed=2 if a.mixed else 0)
-    serve(trace[:16], p, a.workers)                          # warm-up
-    res, max_queue = serve(trace, p, a.workers)
+    serve(trace[:16], p, a.workers, lanczos_batch=a.lanczos_batch)   # warm-up
+    res, max_queue = serve(trace, p, a.workers, lanczos_batch=a.lanczos_batch)
     out = summarize(trace, res)
     out.update({"offered_rate": a.rate, "seconds": a.seconds, "workers": a.workers, "max_queue": max_queue,
+                "lanczos_batch": a.lanczos_batch,
                 "form": "mixed" if a.mixed else "fp64"})
     print(json.dumps(out))
     return 0

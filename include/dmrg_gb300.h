@@ -294,6 +294,17 @@ int dg_lanczos(dg_matrix *m, const dg_solver_params *p, const double *guess, dou
 int dg_inverse_iteration(dg_matrix *m, const dg_solver_params *p, double eig_val, double *eigvec, dg_solve_info *info);
 /* Lanczos + inverse iteration (the DMRG_DIAGONALIZE_SUPERBLOCK body). */
 int dg_ground_state(dg_matrix *m, const dg_solver_params *p, const double *guess, double *eigvec, dg_solve_info *info);
+/* Ground states of count operators solved together (no counterpart in the reference; the
+ * batched form of dg_ground_state).  The Lanczos phases of all eligible instances advance in
+ * lock-step, each step one launch of each of four kernels over every instance still iterating
+ * (SELL format, mixed = 0 or 2, no restart before lanczos_max_step, n >= dense_below); their
+ * inverse iteration (mixed = 0) or refinement (mixed = 2) then runs per instance on worker
+ * threads, and ineligible instances take dg_ground_state.  eigvecs may be NULL or hold count
+ * host or device pointers (entries may be NULL); statuses[i] is instance i's DG_* code (the
+ * call itself returns DG_OK with the first failure's message in dg_last_error).  The energies
+ * equal the one-at-a-time solve's within rounding (the sums run in another order). */
+int dg_batch_ground_state(int count, dg_matrix *const *mats, const dg_solver_params *p, double *const *eigvecs,
+                          dg_solve_info *infos, int *statuses);
 /* CG on (M + sigma I) x = b from x (in/out; normalised first, as the reference does).
  * minres = 1 runs MINRES instead (x not normalised, as the reference's MINIMUM_RESIDUAL). */
 int dg_linear_solve(dg_matrix *m, double sigma, const double *b, double *x, double acc, int max_step, int minres, int *iters);

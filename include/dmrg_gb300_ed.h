@@ -94,6 +94,9 @@ typedef struct dg_engine dg_engine;
 typedef struct {
    int workers;            /* jobs in flight at once (0 = 8)                           */
    size_t hbm_budget;      /* device bytes jobs may hold together (0 = 80% of free)   */
+   int lanczos_batch;      /* 1: the Lanczos phases of eligible jobs (mixed = 0 or 2) run
+                              in the engine's lock-step batch (one launch of each kernel a
+                              step over all of them); 0: every job solves on its worker   */
 } dg_engine_config;
 
 typedef struct {

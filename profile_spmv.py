@@ -40,9 +40,26 @@ ED_CASES = {
 }
 
 
+# superblocks of the reference's own DMRG runs (tests/golden), built on the device from their term lists
+DMRG_CASES = {
+    "dmrg_hubbard_m512": "dmrg_hubbard_vf_sweep4.npz",
+    "dmrg_klm_m128": "dmrg_klm_vf_sweep4.npz",
+    "dmrg_xxz_m64": "dmrg_xxz_vf_sweep4.npz",
+}
+
+
 def _matrix(name, values=None):
-    """Device matrix of a named case (superblock: host lower CRS uploaded; ED: built on the device)."""
+    """Device matrix of a named case (synthetic superblock: host lower CRS uploaded; ED and recorded
+    DMRG superblocks: built on the device)."""
     values = L.DG_VALUES_F64 if values is None else values
+    if name in DMRG_CASES:
+        from pathlib import Path
+        from dmrg_c_gb300 import sb_models
+        sb = sb_models.load_dmrg_superblock(Path(__file__).resolve().parent / "tests" / "golden" / DMRG_CASES[name])
+        s = L.SuperblockCRS(sb.model)
+        m = s.matrix(values)
+        s.close()
+        return m
     if name in ED_CASES:
         ed = L.EDSystem(ED_CASES[name]())
         m = ed.matrix(values)
@@ -456,11 +473,11 @@ def build(which, repeats=3):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
-    ap.add_argument("--cases", nargs="*", default=list(CASES), choices=list(CASES) + list(ED_CASES))
+    ap.add_argument("--cases", nargs="*", default=list(CASES), choices=list(CASES) + list(ED_CASES) + list(DMRG_CASES))
     ap.add_argument("--sweep", action="store_true")
     ap.add_argument("--iters", type=int, default=10)
     ap.add_argument("--json", default=None)
-    ap.add_argument("--case", choices=list(CASES) + list(ED_CASES), default=None)
+    ap.add_argument("--case", choices=list(CASES) + list(ED_CASES) + list(DMRG_CASES), default=None)
     ap.add_argument("--format", choices=["sell", "csr"], default="sell")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--mixed", action="store_true")
@@ -470,7 +487,7 @@ def main(argv=None):
     ap.add_argument("--obs", action="store_true", help="site expectation values on the Hubbard m=512 superblock")
     ap.add_argument("--trunc", action="store_true", help="DMRG_GET_SYSTEM_INFO_Q2 on the KLM m=128 and Hubbard m=512 superblocks")
     ap.add_argument("--renorm", action="store_true", help="CRS_CRS_CCS_PRODUCT with the KLM m=128 and Hubbard m=512 shapes")
-    ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES), default=None,
+    ap.add_argument("--solvers", choices=list(CASES) + list(ED_CASES) + list(DMRG_CASES), default=None,
                     help="solve times of the solver forms on one matrix")
     a = ap.parse_args(argv)
     if a.solvers:

@@ -8,8 +8,8 @@ from dmrg_c_gb300 import ed_models, workloads
 TOL_E = 1e-10
 
 
-def _run(gpu, models, params, workers, budget=0):
-    eng = gpu.Engine(workers=workers, hbm_budget=budget)
+def _run(gpu, models, params, workers, budget=0, lanczos_batch=False):
+    eng = gpu.Engine(workers=workers, hbm_budget=budget, lanczos_batch=lanczos_batch)
     for i, m in enumerate(models):
         eng.submit(m, params, i)
     res = {}
@@ -32,6 +32,37 @@ def test_results_same_alone_and_in_the_mix(gpu, mixed):
         a, b = alone[i].eig_val, mix[i].eig_val
         assert alone[i].status == 0 and mix[i].status == 0
         assert abs(a - b) <= TOL_E * abs(a), (a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [0, 2])
+def test_lanczos_batch_same_alone_and_in_the_mix(gpu, mixed):
+    """Continuous batching: jobs admitted while others iterate join the lock-step Lanczos; each
+    result equals the same job run alone (also through the lock-step batch) and the plain engine."""
+    trace = workloads.hubbard_request_trace(rate=200.0, duration=0.2, seed=1)
+    probe = [ed_models.hubbard_chain(8, U=3.1, hz=0.2), ed_models.hubbard_chain(10, U=6.4, hz=0.05)]
+    p = gpu.default_params(seed=3, mixed=mixed)
+    alone = _run(gpu, probe, p, workers=1, lanczos_batch=True)
+    plain = _run(gpu, probe, p, workers=1)
+    mix = _run(gpu, probe + [req["model"]() for req in trace], p, workers=8, lanczos_batch=True)
+    assert all(r.status == 0 and r.converged for r in mix.values())
+    for i in range(len(probe)):
+        a, b, c = alone[i].eig_val, mix[i].eig_val, plain[i].eig_val
+        assert abs(a - b) <= TOL_E * abs(a), (a, b)
+        assert abs(a - c) <= TOL_E * abs(c), (a, c)
+
+
+@pytest.mark.gpu
+def test_lanczos_batch_energies_match_oracle(gpu, oracle):
+    inst = [m for m in workloads.xxz_ed_batch(40, seed=0) if m["L"] in (14, 16)][:8]
+    models = [m["model"]() for m in inst]
+    res = _run(gpu, models, gpu.default_params(seed=9), workers=4, lanczos_batch=True)
+    from dmrg_c_gb300 import abi
+    for i, m in enumerate(models):
+        basis, row, col, val = oracle.ed_build(m)
+        rc, out, v = oracle.lanczos(abi.Crs(row, col, val, n=len(basis)), False, seed=9)
+        assert res[i].status == 0
+        assert abs(res[i].eig_val - out.eig_val) <= TOL_E * abs(out.eig_val)
 
 
 @pytest.mark.gpu
