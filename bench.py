@@ -358,7 +358,7 @@ def batched_leg(L, args):
     out["max_dE_rel_batch_vs_streams"] = float(np.max(np.abs(E["fp64"] - E["fp64_streams"]) / np.abs(E["fp64_streams"])))
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        sample = [i for Lx in (12, 14, 16, 18, 20, 22) for i in range(len(inst)) if inst[i]["L"] == Lx][:0]
+        sample = []
         for Lx in (12, 14, 16, 18, 20, 22):
             sample += [i for i in range(len(inst)) if inst[i]["L"] == Lx][:1]
         secs = {}

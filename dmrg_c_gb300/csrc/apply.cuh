@@ -45,13 +45,15 @@ __device__ __forceinline__ void set_norm2(Norm2 *p, double t) {
 //   NORM2     s = rs of the Norm2 at p      (NORMALIZE: 1/sqrt(<w,w>)), r2 = its v
 //   PARTIALS  r2 = sum of count block partials at p, s = 1/sqrt(r2)
 struct Scale {
-  enum Mode : int { ONE = 0, MUL = 1, NORM2 = 2, PARTIALS = 3 };
+  // PAIRS: as PARTIALS, the partials being FP32 pairs (float2, sum_partials_pair; the mixed form)
+  enum Mode : int { ONE = 0, MUL = 1, NORM2 = 2, PARTIALS = 3, PAIRS = 4 };
   const double *p = nullptr;
   int mode = ONE;
   int count = 0;
   static Scale mul(const double *q) { return Scale{q, MUL, 0}; }
   static Scale norm2(const Norm2 *q) { return Scale{reinterpret_cast<const double *>(q), NORM2, 0}; }
   static Scale partials(const double *q, int c) { return Scale{q, PARTIALS, c}; }
+  static Scale pairs(const double *q, int c) { return Scale{q, PAIRS, c}; }
 };
 
 struct ScaleVal {
@@ -69,6 +71,18 @@ __device__ __forceinline__ ScaleVal load_scale(const Scale &sc) {
     if (threadIdx.x == 0) s_rs = 1.0 / sqrt(r2);
     __syncthreads();
     return ScaleVal{s_rs, r2};
+  }
+  if (sc.mode == Scale::PAIRS) {
+    // FP32 merges in every thread; the FP64 square root and division once, in thread 0
+    __shared__ double s_rs2, s_r22;
+    const AccDot2 a = sum_partials_pair(reinterpret_cast<const float2 *>(sc.p), sc.count);
+    if (threadIdx.x == 0) {
+      const double r2 = a.get();
+      s_r22 = r2;
+      s_rs2 = 1.0 / sqrt(r2);
+    }
+    __syncthreads();
+    return ScaleVal{s_rs2, s_r22};
   }
   return ScaleVal{1.0, 0.0};
 }
@@ -146,7 +160,9 @@ k_apply(Op op, int n, const XT *__restrict__ x, Scale sc, double sigma,
   }
   pdl_trigger();
   if constexpr (Epi::kReduce) {
-    if constexpr (is_deferred<Epi>::value)
+    if constexpr (is_deferred<Epi>::value && has_pair_partials<Epi>::value)
+      block_partial_split(acc, reinterpret_cast<float2 *>(slot.partials));
+    else if constexpr (is_deferred<Epi>::value)
       block_partial(acc, slot.partials);
     else
       grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });

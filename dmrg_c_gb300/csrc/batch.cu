@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "batch.cuh"
 #include "refine.cuh"
@@ -33,8 +34,14 @@ struct BLzDesc {
   int *step;            // b: the step the next iteration computes
   double *D, *O;        // alpha_b, beta_b = ||w_b|| (O[0] = ||w_0||)
   double *rs;           // 1 / ||w_b||
+  float *sc;            // mixed form: the FP32 scalars of the step (kSc*), null in the FP64 form
   double *hD, *hO;      // mapped host mirrors of D and O
 };
+
+// The mixed form's per-step scalars in FP32, formed once per instance by the one-warp kernels so
+// that the row and element kernels execute no FP64 instruction: 1/beta_b, and alpha_b and
+// beta_b each split into two floats (hi + lo carries the double to ~2^-48).
+enum { kScRs = 0, kScAhi, kScAlo, kScBhi, kScBlo, kScCount = 8 };
 
 constexpr int kBlzLookahead = 2;   // iterations the device runs ahead of the host's checks
 
@@ -46,25 +53,43 @@ __global__ void __launch_bounds__(kThreads) k_blz_apply(const BLzDesc *__restric
   const int2 m = bmap[blockIdx.x];
   const BLzDesc &d = desc[m.x];
   const int b = *d.step;
-  const double s = *d.rs;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int sl = m.y * kWarps + wib;
   const VT *__restrict__ w = static_cast<const VT *>(d.w);
   double acc = 0.0;
+  AccDot2 a2;
   if (sl < d.nslices && b < d.cap - 1) {
     const SellOp<VT> op{d.off, d.width, d.perm, d.col, static_cast<const VT *>(d.val), d.nslices, 1, 0};
-    double sum = sell_row_sum<1, U, false, false, VT, VT>(op, d.off[sl] + lane, d.width[sl], 0, w);
-    sum *= s;
     const int row = d.perm[(long)sl * kSellC + lane];
-    if (row >= 0) {
-      const double xi = (double)w[row] * s;
-      static_cast<VT *>(d.V)[(size_t)b * d.n + row] = (VT)xi;
-      static_cast<VT *>(d.y)[row] = (VT)sum;
-      acc = sum * xi;
+    if constexpr (std::is_same<VT, float>::value) {
+      // mixed form: the row in FP32, no FP64 instruction (see sell.cuh has_row32)
+      const float sf = d.sc[kScRs];
+      const AccDot2 r = sell_row_acc<1, U, false, false, VT, VT>(op, d.off[sl] + lane, d.width[sl], 0, w);
+      const float sum = __fmul_rn(__fadd_rn(r.p, r.c), sf);
+      if (row >= 0) {
+        const float xi = __fmul_rn(w[row], sf);
+        static_cast<float *>(d.V)[(size_t)b * d.n + row] = xi;
+        static_cast<float *>(d.y)[row] = sum;
+        a2.add(sum, xi);
+      }
+    } else {
+      const double s = *d.rs;
+      double sum = sell_row_sum<1, U, false, false, VT, VT>(op, d.off[sl] + lane, d.width[sl], 0, w);
+      sum *= s;
+      if (row >= 0) {
+        const double xi = (double)w[row] * s;
+        static_cast<VT *>(d.V)[(size_t)b * d.n + row] = (VT)xi;
+        static_cast<VT *>(d.y)[row] = (VT)sum;
+        acc = sum * xi;
+      }
     }
   }
   pdl_trigger();
-  const double t = block_sum(acc);
+  double t;
+  if constexpr (std::is_same<VT, float>::value)
+    t = block_sum_pair(a2);
+  else
+    t = block_sum(acc);
   if (threadIdx.x == 0) d.part_p[m.y] = t;
 }
 
@@ -81,6 +106,11 @@ __global__ void __launch_bounds__(kThreads) k_blz_alpha(const BLzDesc *__restric
     if (lane == 0 && b < d.cap - 1) {
       d.D[b] = s;
       *(volatile double *)(d.hD + b) = s;
+      if (d.sc) {
+        const float hi = (float)s;
+        d.sc[kScAhi] = hi;
+        d.sc[kScAlo] = (float)(s - (double)hi);
+      }
     }
   }
   pdl_trigger();
@@ -95,16 +125,39 @@ __global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restri
   const int b = *d.step;
   const int i = m.y * kThreads + threadIdx.x;
   double acc = 0.0;
+  AccDot2 a2;
   if (i < d.n && b < d.cap - 1) {
     const VT *V = static_cast<const VT *>(d.V);
-    const double a = d.D[b];
-    double wi = (double)static_cast<const VT *>(d.y)[i] - a * (double)V[(size_t)b * d.n + i];
-    if (b > 0) wi -= d.O[b] * (double)V[(size_t)(b - 1) * d.n + i];
-    static_cast<VT *>(d.w)[i] = (VT)wi;
-    acc = wi * wi;
+    if constexpr (std::is_same<VT, float>::value) {
+      // compensated FP32 with alpha and beta as two floats each (as k_mx_update); no FP64
+      // instruction per element
+      AccDot2 t;
+      t.p = static_cast<const float *>(d.y)[i];
+      const float vb = V[(size_t)b * d.n + i];
+      t.add(-d.sc[kScAhi], vb);
+      t.add(-d.sc[kScAlo], vb);
+      if (b > 0) {
+        const float vp = V[(size_t)(b - 1) * d.n + i];
+        t.add(-d.sc[kScBhi], vp);
+        t.add(-d.sc[kScBlo], vp);
+      }
+      const float wi = __fadd_rn(t.p, t.c);
+      static_cast<float *>(d.w)[i] = wi;
+      a2.add(wi, wi);
+    } else {
+      const double a = d.D[b];
+      double wi = (double)static_cast<const VT *>(d.y)[i] - a * (double)V[(size_t)b * d.n + i];
+      if (b > 0) wi -= d.O[b] * (double)V[(size_t)(b - 1) * d.n + i];
+      static_cast<VT *>(d.w)[i] = (VT)wi;
+      acc = wi * wi;
+    }
   }
   pdl_trigger();
-  const double t = block_sum(acc);
+  double t;
+  if constexpr (std::is_same<VT, float>::value)
+    t = block_sum_pair(a2);
+  else
+    t = block_sum(acc);
   if (threadIdx.x == 0) d.part_v[m.y] = t;
 }
 
@@ -119,10 +172,16 @@ __global__ void __launch_bounds__(kThreads) k_blz_beta(const BLzDesc *__restrict
     s = warp_sum(s);
     const int b = *d.step;
     if (lane == 0 && b < d.cap - 1) {
-      const double be = sqrt(s);
+      const double be = sqrt(s), r = 1.0 / be;
       d.O[b + 1] = be;
       *(volatile double *)(d.hO + b + 1) = be;
-      *d.rs = 1.0 / be;
+      *d.rs = r;
+      if (d.sc) {
+        const float hi = (float)be;
+        d.sc[kScRs] = (float)r;
+        d.sc[kScBhi] = hi;
+        d.sc[kScBlo] = (float)(be - (double)hi);
+      }
       *d.step = b + 1;
     }
   }
@@ -144,7 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_blz_start(VT *w, const double *w64
 }
 
 // One block: step 0, O[0] = ||w_0||, rs, mirrors.
-__global__ void k_blz_start_norm(const double *part, int count, int *step, double *O, double *hO, double *rs) {
+__global__ void k_blz_start_norm(const double *part, int count, int *step, double *O, double *hO, double *rs, float *sc) {
   double s = 0.0;
   for (int k = threadIdx.x; k < count; k += blockDim.x) s += part[k];
   s = block_sum(s);
@@ -154,6 +213,7 @@ __global__ void k_blz_start_norm(const double *part, int count, int *step, doubl
     O[0] = be;
     *(volatile double *)hO = be;
     *rs = 1.0 / be;
+    if (sc) sc[kScRs] = (float)(1.0 / be);
   }
 }
 
@@ -171,6 +231,42 @@ __global__ void __launch_bounds__(kThreads) k_blz_ritz(const VT *__restrict__ V,
   }
   const double t = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Mixed form: psi = sum_{j<k} z_j v_j with z_j as float pairs (hi + lo) and compensated FP32
+// sums (FP64 result, one conversion per element); block partials of ||psi||^2 (the pair's
+// square, p^2 + 2pc).  Dynamic shared memory: k float2.
+__global__ void __launch_bounds__(kThreads) k_blz_ritz32(const float *__restrict__ V, int n, int k, const float2 *__restrict__ zp,
+                                                        double *__restrict__ psi, double *part) {
+  extern __shared__ float2 zs[];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) zs[j] = zp[j];
+  __syncthreads();
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  AccDot2 nrm;
+  if (i < n) {
+    AccDot2 t;
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {   // eight loads in flight per thread
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(j + u) * n + i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        t.add(zs[j + u].x, v[u]);
+        t.add(zs[j + u].y, v[u]);
+      }
+    }
+    for (; j < k; ++j) {
+      const float v = V[(size_t)j * n + i];
+      t.add(zs[j].x, v);
+      t.add(zs[j].y, v);
+    }
+    psi[i] = t.get();
+    nrm.add(t.p, t.p);
+    nrm.add(__fmul_rn(2.0f, t.c), t.p);
+  }
+  const double b = block_sum_pair(nrm);
+  if (threadIdx.x == 0) part[blockIdx.x] = b;
 }
 
 // psi /= ||psi|| (every block sums the partials; used once per instance).
@@ -204,8 +300,23 @@ struct BatchLanczosImpl {
     size_t esz = 8;
     void *V = nullptr, *w = nullptr, *y = nullptr;
     double *part_p = nullptr, *part_v = nullptr, *D = nullptr, *O = nullptr, *rs = nullptr;
+    float *sc = nullptr;
     int *step = nullptr;
-    std::unique_ptr<Mapped<double>> hD, hO;
+    // One pool allocation holds everything but the basis, the Ritz vector psi at its base: a
+    // converged instance hands psi (and so the allocation) to the post phase, which frees it.
+    // A departure then costs a handful of CUDA calls: allocation calls on the batch thread
+    // contend with the post-phase workers' launches.
+    char *mem = nullptr;
+    double *psi = nullptr, *zd = nullptr;
+    // mapped host mirrors of D and O: a slot of the batch's mirror arena (or own memory when the
+    // instance needs more steps than a slot holds)
+    double *hDh = nullptr, *hOh = nullptr, *hDd = nullptr, *hOd = nullptr;
+    int slot = -1;
+    std::unique_ptr<Mapped<double>> own;
+    int leave = 0;      // set by the checks: 1 converged, 2 step limit, 3 wait failed (err, err_msg)
+    int leave_k = 0, leave_bs = 0, err = DG_OK;
+    std::string err_msg;
+    double leave_lam = 0.0;
     int enq = 0;        // iterations launched with this instance (its device step after them)
     int next = 1;       // next step to check
     double E = 1e15;
@@ -226,11 +337,26 @@ struct BatchLanczosImpl {
   std::atomic<long> iters{0};
   bool stop = false;
   std::thread th;
+  // Mirror arena: blocks of kSlots slots of 2 * slot_len mapped doubles (hD then hO).  Pinned
+  // memory is allocated once per block and reused by later instances: freeing pinned memory
+  // synchronises the device, which stalled the lock-step pipeline every time instances left.
+  static constexpr int kSlots = 64;
+  int slot_len = 0;
+  std::vector<std::unique_ptr<Mapped<double>>> arena;
+  std::vector<int> free_slots;
+  // Pinned staging of the table uploads, kept until the copy has run and then recycled: a copy
+  // from pageable memory may wait for the stream, and allocating or freeing pinned memory
+  // synchronises the device, either of which drains the lookahead.
+  std::deque<std::pair<cudaEvent_t, std::unique_ptr<Mapped<char>>>> staging;
+  std::vector<std::unique_ptr<Mapped<char>>> pinned_free;
   // device table
   BLzDesc *t_desc = nullptr;
   int2 *t_pmap = nullptr, *t_vmap = nullptr;
   int t_pgrid = 0, t_vgrid = 0, t_count = 0;
   bool dirty = true;
+  // DG_BATCH_TRACE: a line per iteration on stderr (host time of the checks, split by part)
+  const bool trace = std::getenv("DG_BATCH_TRACE") != nullptr;
+  double t_tri = 0.0, t_leave = 0.0;
 
   BatchLanczosImpl(int dev, int mx, std::function<void(BatchDone &)> cb) : device(dev), mixed(mx), on_done(std::move(cb)) {
     th = std::thread([this] { loop(); });
@@ -242,6 +368,7 @@ struct BatchLanczosImpl {
     }
     cv.notify_all();
     th.join();
+    stop_helpers();
   }
 
   void finish(Inst &in, int status, const char *msg, double *psi, cudaEvent_t ev, double E, int steps, bool conv) {
@@ -259,12 +386,15 @@ struct BatchLanczosImpl {
     inflight.fetch_sub(1);
   }
 
+  // Frees the basis, and the instance's allocation unless psi took it to the post phase.
   void release(Inst &in, cudaStream_t st) {
-    for (void *p : {in.V, in.w, in.y, (void *)in.part_p, (void *)in.part_v, (void *)in.D, (void *)in.O, (void *)in.rs,
-                    (void *)in.step})
-      if (p) pool_free(p, st);
+    if (in.V) pool_free(in.V, st);
+    if (in.mem) pool_free(in.mem, st);
     in.V = in.w = in.y = nullptr;
+    in.mem = nullptr;
+    in.psi = in.zd = nullptr;
     in.part_p = in.part_v = in.D = in.O = in.rs = nullptr;
+    in.sc = nullptr;
     in.step = nullptr;
   }
 
@@ -279,19 +409,33 @@ struct BatchLanczosImpl {
     in.vcap = std::min(in.cap, 64);
     if (in.built) DG_CUDA(cudaStreamWaitEvent(st, in.built, 0));
     in.V = pool_alloc(in.esz * (size_t)in.vcap * in.n, st);
-    in.w = pool_alloc(in.esz * (size_t)in.n, st);
-    in.y = pool_alloc(in.esz * (size_t)in.n, st);
-    in.part_p = static_cast<double *>(pool_alloc(sizeof(double) * in.pblk, st));
-    in.part_v = static_cast<double *>(pool_alloc(sizeof(double) * std::max(in.vblk, in.pblk), st));
-    in.D = static_cast<double *>(pool_alloc(sizeof(double) * in.cap, st));
-    in.O = static_cast<double *>(pool_alloc(sizeof(double) * in.cap, st));
-    in.rs = static_cast<double *>(pool_alloc(sizeof(double), st));
-    in.step = static_cast<int *>(pool_alloc(sizeof(int), st));
-    in.hD = std::make_unique<Mapped<double>>(in.cap);
-    in.hO = std::make_unique<Mapped<double>>(in.cap);
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+      const size_t o = off;
+      off += (bytes + 255) & ~(size_t)255;
+      return o;
+    };
+    const size_t o_psi = carve(sizeof(double) * (size_t)in.n), o_w = carve(in.esz * (size_t)in.n),
+                 o_y = carve(in.esz * (size_t)in.n), o_pp = carve(sizeof(double) * in.pblk),
+                 o_pv = carve(sizeof(double) * std::max(in.vblk, in.pblk)), o_D = carve(sizeof(double) * in.cap),
+                 o_O = carve(sizeof(double) * in.cap), o_z = carve(sizeof(double) * in.cap), o_rs = carve(sizeof(double)),
+                 o_sc = carve(sizeof(float) * kScCount), o_st = carve(sizeof(int));
+    in.mem = static_cast<char *>(pool_alloc(off, st));
+    in.psi = reinterpret_cast<double *>(in.mem + o_psi);
+    in.w = in.mem + o_w;
+    in.y = in.mem + o_y;
+    in.part_p = reinterpret_cast<double *>(in.mem + o_pp);
+    in.part_v = reinterpret_cast<double *>(in.mem + o_pv);
+    in.D = reinterpret_cast<double *>(in.mem + o_D);
+    in.O = reinterpret_cast<double *>(in.mem + o_O);
+    in.zd = reinterpret_cast<double *>(in.mem + o_z);
+    in.rs = reinterpret_cast<double *>(in.mem + o_rs);
+    in.sc = mixed ? reinterpret_cast<float *>(in.mem + o_sc) : nullptr;
+    in.step = reinterpret_cast<int *>(in.mem + o_st);
+    take_mirrors(in);
     for (int j = 0; j < in.cap; ++j) {
-      std::memcpy((void *)(in.hD->h + j), &kLzSentinel, sizeof(double));
-      std::memcpy((void *)(in.hO->h + j), &kLzSentinel, sizeof(double));
+      std::memcpy((void *)(in.hDh + j), &kLzSentinel, sizeof(double));
+      std::memcpy((void *)(in.hOh + j), &kLzSentinel, sizeof(double));
     }
     double *w64 = static_cast<double *>(pool_alloc(sizeof(double) * (size_t)in.n, st));
     k_random_start<<<vector_grid(in.n), kThreads, 0, st>>>(w64, in.n, (unsigned long long)in.p.seed); ::dg::count_launch();
@@ -300,7 +444,7 @@ struct BatchLanczosImpl {
     else
       k_blz_start<double><<<in.vblk, kThreads, 0, st>>>(static_cast<double *>(in.w), w64, in.n, in.part_v);
     ::dg::count_launch();
-    k_blz_start_norm<<<1, kThreads, 0, st>>>(in.part_v, in.vblk, in.step, in.O, in.hO->d, in.rs); ::dg::count_launch();
+    k_blz_start_norm<<<1, kThreads, 0, st>>>(in.part_v, in.vblk, in.step, in.O, in.hOd, in.rs, in.sc); ::dg::count_launch();
     DG_CUDA(cudaGetLastError());
     pool_free(w64, st);
   }
@@ -344,8 +488,9 @@ struct BatchLanczosImpl {
       d.D = in.D;
       d.O = in.O;
       d.rs = in.rs;
-      d.hD = in.hD->d;
-      d.hO = in.hO->d;
+      d.sc = in.sc;
+      d.hD = in.hDd;
+      d.hO = in.hOd;
       ds.push_back(d);
       for (int b = 0; b < in.pblk; ++b) pm.push_back(int2{(int)k, b});
       for (int b = 0; b < in.vblk; ++b) vm.push_back(int2{(int)k, b});
@@ -356,9 +501,15 @@ struct BatchLanczosImpl {
     t_desc = static_cast<BLzDesc *>(pool_alloc(sizeof(BLzDesc) * ds.size(), st));
     t_pmap = static_cast<int2 *>(pool_alloc(sizeof(int2) * pm.size(), st));
     t_vmap = static_cast<int2 *>(pool_alloc(sizeof(int2) * vm.size(), st));
-    DG_CUDA(cudaMemcpyAsync(t_desc, ds.data(), sizeof(BLzDesc) * ds.size(), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(t_pmap, pm.data(), sizeof(int2) * pm.size(), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(t_vmap, vm.data(), sizeof(int2) * vm.size(), cudaMemcpyHostToDevice, st));
+    const size_t b0 = sizeof(BLzDesc) * ds.size(), b1 = sizeof(int2) * pm.size(), b2 = sizeof(int2) * vm.size();
+    auto buf = take_pinned(b0 + b1 + b2);
+    std::memcpy(buf->h, ds.data(), b0);
+    std::memcpy(buf->h + b0, pm.data(), b1);
+    std::memcpy(buf->h + b0 + b1, vm.data(), b2);
+    DG_CUDA(cudaMemcpyAsync(t_desc, buf->h, b0, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(t_pmap, buf->h + b0, b1, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(t_vmap, buf->h + b0 + b1, b2, cudaMemcpyHostToDevice, st));
+    staged(std::move(buf), st);
     t_pgrid = (int)pm.size();
     t_vgrid = (int)vm.size();
     t_count = (int)ds.size();
@@ -368,7 +519,7 @@ struct BatchLanczosImpl {
   void launch_iteration(cudaStream_t st) {
     const int cgrid = blocks_of(t_count, kWarps);
     if (mixed)
-      launch_pdl(k_blz_apply<float, 16>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_pmap);
+      launch_pdl(k_blz_apply<float, 8>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_pmap);
     else
       launch_pdl(k_blz_apply<double, 16>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_pmap);
     launch_pdl(k_blz_alpha, dim3(cgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, t_count);
@@ -381,19 +532,76 @@ struct BatchLanczosImpl {
     iters.fetch_add(1);
   }
 
-  // Destroys retired instances whose last iterations have finished (all of them when wait).
+  // Mirror slots of the arena (own memory when an instance needs more steps than a slot holds).
+  void take_mirrors(Inst &in) {
+    if (slot_len == 0) slot_len = in.cap;
+    if (in.cap > slot_len) {
+      in.own = std::make_unique<Mapped<double>>(2 * (size_t)in.cap);
+      in.hDh = in.own->h;
+      in.hDd = in.own->d;
+      in.hOh = in.own->h + in.cap;
+      in.hOd = in.own->d + in.cap;
+      return;
+    }
+    if (free_slots.empty()) {
+      arena.push_back(std::make_unique<Mapped<double>>((size_t)kSlots * 2 * slot_len));
+      const int b = (int)arena.size() - 1;
+      for (int k = kSlots - 1; k >= 0; --k) free_slots.push_back(b * kSlots + k);
+    }
+    in.slot = free_slots.back();
+    free_slots.pop_back();
+    Mapped<double> &blk = *arena[in.slot / kSlots];
+    const size_t o = (size_t)(in.slot % kSlots) * 2 * slot_len;
+    in.hDh = blk.h + o;
+    in.hDd = blk.d + o;
+    in.hOh = blk.h + o + slot_len;
+    in.hOd = blk.d + o + slot_len;
+  }
+
+  // A pinned upload buffer of at least `bytes` from the recycled ones (allocated when none fits).
+  std::unique_ptr<Mapped<char>> take_pinned(size_t bytes) {
+    for (size_t i = 0; i < pinned_free.size(); ++i)
+      if (pinned_free[i]->bytes >= bytes) {
+        std::unique_ptr<Mapped<char>> b = std::move(pinned_free[i]);
+        pinned_free.erase(pinned_free.begin() + (long)i);
+        return b;
+      }
+    return std::make_unique<Mapped<char>>(std::max<size_t>(bytes, 1) * 2);
+  }
+
+  // Keeps a pinned upload buffer until the copies enqueued from it have run.
+  void staged(std::unique_ptr<Mapped<char>> buf, cudaStream_t st) {
+    cudaEvent_t ev;
+    DG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    DG_CUDA(cudaEventRecord(ev, st));
+    staging.emplace_back(ev, std::move(buf));
+  }
+
+  // Destroys retired instances whose last iterations have finished (all of them when wait),
+  // returning their mirror slots, and drops staging buffers whose copies have run.
   void reap(bool wait) {
     while (!retired.empty()) {
       cudaEvent_t ev = retired.front().first;
       if (wait)
         cudaEventSynchronize(ev);
       else if (cudaEventQuery(ev) != cudaSuccess)
-        return;
+        break;
       while (!retired.empty() && retired.front().first == ev) {
         const bool owner = !retired.front().second;
+        if (!owner && retired.front().second->slot >= 0) free_slots.push_back(retired.front().second->slot);
         retired.pop_front();
         if (owner) cudaEventDestroy(ev);
       }
+    }
+    while (!staging.empty()) {
+      cudaEvent_t ev = staging.front().first;
+      if (wait)
+        cudaEventSynchronize(ev);
+      else if (cudaEventQuery(ev) != cudaSuccess)
+        break;
+      cudaEventDestroy(ev);
+      pinned_free.push_back(std::move(staging.front().second));
+      staging.pop_front();
     }
   }
 
@@ -403,10 +611,13 @@ struct BatchLanczosImpl {
     return v != kLzSentinel;
   }
 
-  // Checks step bs of an instance (its iteration bs has landed).  Returns 0 to continue,
-  // 1 when the instance leaves (converged or failed; finish() called).
-  int check(Inst &in, int bs, cudaStream_t st) {
-    const volatile double *hD = in.hD->h, *hO = in.hO->h;
+  // Host part of the check of step bs of an instance (its iteration bs has landed): the
+  // tridiagonal eigenvalue, the convergence test (the reference's "Normal" criterion, as
+  // lanczos_run) and, when the instance leaves, the Ritz coefficients.  Touches only the
+  // instance, so the instances' checks run on several threads.  Returns 0 to continue, 1 when
+  // the instance leaves (in.leave set).
+  int decide(Inst &in, int bs) {
+    const volatile double *hD = in.hDh, *hO = in.hOh;
     const int nn = bs + 1;
     // breakdown: w_bs vanished, the Ritz pair of T_bs is exact (as lanczos_run)
     double scale = 0.0;
@@ -426,38 +637,159 @@ struct BatchLanczosImpl {
     if (conv) {
       in.z.assign(k, 0.0);
       tridiag_eigenvector(in.d.data(), in.e.data(), k, lam, in.z.data());
-      double *zd = static_cast<double *>(pool_alloc(sizeof(double) * k, st));
-      DG_CUDA(cudaMemcpyAsync(zd, in.z.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
-      double *psi = static_cast<double *>(pool_alloc(sizeof(double) * (size_t)in.n, st));
-      if (mixed)
-        k_blz_ritz<float><<<in.vblk, kThreads, 0, st>>>(static_cast<const float *>(in.V), in.n, k, zd, psi, in.part_v);
-      else
-        k_blz_ritz<double><<<in.vblk, kThreads, 0, st>>>(static_cast<const double *>(in.V), in.n, k, zd, psi, in.part_v);
-      ::dg::count_launch();
-      k_blz_normalise<<<in.vblk, kThreads, 0, st>>>(psi, in.n, in.part_v, in.vblk); ::dg::count_launch();
-      DG_CUDA(cudaGetLastError());
-      pool_free(zd, st);
-      cudaEvent_t ev;
-      DG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-      DG_CUDA(cudaEventRecord(ev, st));
-      release(in, st);
-      finish(in, DG_OK, nullptr, psi, ev, lam, bs, true);
+      in.leave = 1;
+      in.leave_k = k;
+      in.leave_bs = bs;
+      in.leave_lam = lam;
       return 1;
     }
     in.E = lam;
     if (bs + 1 >= in.p.lanczos_max_step) {
-      release(in, st);
-      finish(in, DG_ERR_NOCONV, "Lanczos did not converge", nullptr, nullptr, lam, bs, false);
+      in.leave = 2;
+      in.leave_bs = bs;
+      in.leave_lam = lam;
       return 1;
     }
     return 0;
   }
 
+  // Checks every step of the instance that lags kBlzLookahead iterations behind its launches.
+  // Returns 1 when it leaves.  A failed wait (time-out, device error) sets in.leave = 3 with the
+  // error, which the loop thread raises (this may run on a helper thread).
+  int check_lagging(Inst &in, cudaStream_t st) {
+    try {
+      while (in.next <= in.enq - 1 - kBlzLookahead) {
+        const int bs = in.next;
+        if (!host_wait(st, [&] { return landed(in.hDh + bs) && landed(in.hOh + bs); })) {
+          char buf[96];
+          std::snprintf(buf, sizeof buf, "batched Lanczos: timed out waiting for step %d", bs);
+          in.err = DG_ERR_TIMEOUT;
+          in.err_msg = buf;
+          in.leave = 3;
+          return 1;
+        }
+        ++in.next;
+        if (decide(in, bs)) return 1;
+      }
+    } catch (const Error &e) {
+      in.err = e.code;
+      in.err_msg = last_error();
+      in.leave = 3;
+      return 1;
+    }
+    return 0;
+  }
+
+  // Device part of a departure (loop thread, batch stream order): the Ritz vector of a converged
+  // instance, its release, and the hand-off.
+  void depart(Inst &in, cudaStream_t st) {
+    if (in.leave == 2) {
+      release(in, st);
+      finish(in, DG_ERR_NOCONV, "Lanczos did not converge", nullptr, nullptr, in.leave_lam, in.leave_bs, false);
+      return;
+    }
+    const int k = in.leave_k;
+    // the coefficients go up from the instance's own pinned mirror: entries 0..bs of hD have
+    // been read, the iterations still in flight write entries above bs, and the slot is
+    // recycled only after the retire event recorded behind this copy
+    double *zd = in.zd, *psi = in.psi;
+    if (mixed) {
+      // the coefficients as float pairs (8 bytes each, as a double)
+      float2 *zp = reinterpret_cast<float2 *>((void *)in.hDh);
+      for (int j = 0; j < k; ++j) {
+        const float hi = (float)in.z[j];
+        zp[j] = make_float2(hi, (float)(in.z[j] - (double)hi));
+      }
+    } else {
+      std::memcpy((void *)in.hDh, in.z.data(), sizeof(double) * k);
+    }
+    DG_CUDA(cudaMemcpyAsync(zd, (const void *)in.hDh, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+    if (mixed)
+      k_blz_ritz32<<<in.vblk, kThreads, sizeof(float2) * k, st>>>(static_cast<const float *>(in.V), in.n, k,
+                                                                 reinterpret_cast<const float2 *>(zd), psi, in.part_v);
+    else
+      k_blz_ritz<double><<<in.vblk, kThreads, 0, st>>>(static_cast<const double *>(in.V), in.n, k, zd, psi, in.part_v);
+    ::dg::count_launch();
+    k_blz_normalise<<<in.vblk, kThreads, 0, st>>>(psi, in.n, in.part_v, in.vblk); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    in.mem = nullptr;   // psi (the allocation's base) goes to the post phase
+    cudaEvent_t ev;
+    DG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    DG_CUDA(cudaEventRecord(ev, st));
+    release(in, st);
+    finish(in, DG_OK, nullptr, psi, ev, in.leave_lam, in.leave_bs, true);
+  }
+
+  // Helper threads for the checks: the loop thread and kHelpers threads take instances from a
+  // shared counter.  Each iteration's checks cost ~6 us of Sturm bisection per instance at
+  // k ~ 40 steps, which on one core exceeded the device's time per lock-step iteration once a
+  // batch held a few hundred instances.
+  static constexpr int kHelpers = 3;
+  static constexpr size_t kParallelChecks = 32;   // fewer active instances: the loop thread alone
+  std::vector<std::thread> helpers;
+  std::mutex hmu;
+  std::condition_variable hcv, hdone;
+  long hgen = 0;
+  int hbusy = 0;
+  bool hstop = false;
+  std::atomic<size_t> hnext{0};
+  cudaStream_t hstream = nullptr;
+
+  void check_share() {
+    for (size_t i; (i = hnext.fetch_add(1)) < active.size();) check_lagging(*active[i], hstream);
+  }
+  void helper_main() {
+    cudaSetDevice(device);
+    long seen = 0;
+    while (true) {
+      {
+        std::unique_lock<std::mutex> lk(hmu);
+        hcv.wait(lk, [&] { return hstop || hgen != seen; });
+        if (hstop) return;
+        seen = hgen;
+      }
+      check_share();
+      {
+        std::lock_guard<std::mutex> lk(hmu);
+        --hbusy;
+      }
+      hdone.notify_all();
+    }
+  }
+  void check_all(cudaStream_t st) {
+    hnext.store(0);
+    if (active.size() < kParallelChecks) {
+      hstream = st;
+      check_share();
+      return;
+    }
+    if (helpers.empty())
+      for (int h = 0; h < kHelpers; ++h) helpers.emplace_back([this] { helper_main(); });
+    {
+      std::lock_guard<std::mutex> lk(hmu);
+      hstream = st;
+      hbusy = kHelpers;
+      ++hgen;
+    }
+    hcv.notify_all();
+    check_share();
+    std::unique_lock<std::mutex> lk(hmu);
+    hdone.wait(lk, [&] { return hbusy == 0; });
+  }
+  void stop_helpers() {
+    {
+      std::lock_guard<std::mutex> lk(hmu);
+      hstop = true;
+    }
+    hcv.notify_all();
+    for (auto &t : helpers) t.join();
+    helpers.clear();
+  }
+
   void loop() {
     cudaSetDevice(device);
     cudaStream_t st = stream();
-    static const bool trace = std::getenv("DG_BATCH_TRACE") != nullptr;   // per-iteration report on stderr
-    double t_last = now_ms(), t_checks = 0.0;
+    double t_last = now_ms();
     while (true) {
       {
         std::unique_lock<std::mutex> lk(mu);
@@ -489,26 +821,28 @@ struct BatchLanczosImpl {
         if (dirty) rebuild(st);
         launch_iteration(st);
         for (auto &in : active) ++in->enq;
-        // checks lag kBlzLookahead iterations behind the launches
+        // checks lag kBlzLookahead iterations behind the launches: the host part on the
+        // helpers, then the departures' device work here, in order
         const double tc0 = now_ms();
+        check_all(st);
+        if (trace) t_tri += now_ms() - tc0;
+        for (auto &up : active)
+          if (up->leave == 3) {
+            set_error("%s", up->err_msg.c_str());
+            throw Error{up->err};
+          }
         std::vector<std::unique_ptr<Inst>> keep;
         bool changed = false;
         for (auto &up : active) {
           Inst &in = *up;
-          int left = 0;
-          while (!left && in.next <= in.enq - 1 - kBlzLookahead) {
-            const int bs = in.next;
-            if (!host_wait(st, [&] { return landed(in.hD->h + bs) && landed(in.hO->h + bs); })) {
-              set_error("batched Lanczos: timed out waiting for step %d", bs);
-              throw Error{DG_ERR_TIMEOUT};
-            }
-            left = check(in, bs, st);
-            ++in.next;
-          }
-          if (left)
+          if (in.leave) {
+            const double tl0 = trace ? now_ms() : 0.0;
+            depart(in, st);
+            if (trace) t_leave += now_ms() - tl0;
             changed = true;
-          else
+          } else {
             keep.push_back(std::move(up));
+          }
         }
         if (changed) {
           cudaEvent_t ev;
@@ -520,12 +854,15 @@ struct BatchLanczosImpl {
           dirty = true;
         }
         active.swap(keep);
+        const double t_reap0 = trace ? now_ms() : 0.0;
         reap(false);
         if (trace) {
+          // ms: since the previous line; checks: waits + tridiagonal work (all threads);
+          // depart: the departures' device work; reap: retired instances and staging
           const double t = now_ms();
-          t_checks = t - tc0;
-          std::fprintf(stderr, "batch iteration %ld active %zu rows %d ms %.3f checks_ms %.3f\n", iters.load(), keep.size(),
-                       t_vgrid * kThreads, t - t_last, t_checks);
+          std::fprintf(stderr, "batch iteration %ld active %zu rows %d ms %.3f checks_ms %.3f depart_ms %.3f reap_ms %.3f\n",
+                       iters.load(), keep.size(), t_vgrid * kThreads, t - t_last, t_tri, t_leave, t - t_reap0);
+          t_tri = t_leave = 0.0;
           t_last = t;
         }
       } catch (const Error &e) {

@@ -222,9 +222,15 @@ struct RedSlot {
 // Reduce v over the grid.  The last block to finish sums the per-block partials in block
 // order and calls fin(total) from thread 0, then re-arms the ticket.
 template <class Fin>
+__device__ __forceinline__ void grid_reduce_block(double b, RedSlot slot, Fin fin);
+template <class Fin>
 __device__ __forceinline__ void grid_reduce(double v, RedSlot slot, Fin fin) {
+  grid_reduce_block(block_sum(v), slot, fin);
+}
+// The same from the block's sum b (valid in thread 0).
+template <class Fin>
+__device__ __forceinline__ void grid_reduce_block(double b, RedSlot slot, Fin fin) {
   __shared__ bool s_last;
-  double b = block_sum(v);
   if (threadIdx.x == 0) {
     slot.partials[blockIdx.x] = b;
     __threadfence();
@@ -264,6 +270,116 @@ __device__ __forceinline__ double sum_partials(const double *partials, int count
   if (threadIdx.x == 0) s_total = s;
   __syncthreads();
   return s_total;
+}
+
+// ---------------------------------------------------------------------------------
+// Compensated FP32 sums (the mixed-precision form).  The exact product and compensated sum of
+// Ogita, Rump & Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2):
+// the product's rounding error comes from an FMA, the sum's from Knuth's TwoSum, and both are
+// carried in a second float, so a sum is as accurate as if accumulated in twice the working
+// precision -- on the FP32 pipes, which GB300 has ~60x more of than FP64 pipes.  The explicitly
+// rounded intrinsics keep the compiler from contracting the error terms away.
+// ---------------------------------------------------------------------------------
+struct AccDot2 {
+  float p = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float v, float x) {
+    const float h = __fmul_rn(v, x);
+    const float r = __fmaf_rn(v, x, -h);            // v x = h + r exactly
+    const float t = __fadd_rn(p, h);
+    const float z = __fsub_rn(t, p);
+    const float q = __fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z));   // p + h = t + q exactly
+    p = t;
+    c = __fadd_rn(c, __fadd_rn(q, r));
+  }
+  __device__ __forceinline__ double get() const { return (double)p + (double)c; }
+  // Adds another compensated sum: the two leading parts through TwoSum, the corrections and
+  // the TwoSum error into c.  Symmetric bit for bit in (this, o), so both lanes of an
+  // xor-shuffle pair hold the same result.
+  __device__ __forceinline__ void merge(float op, float oc) {
+    const float t = __fadd_rn(p, op);
+    const float z = __fsub_rn(t, p);
+    const float q = __fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(op, z));
+    p = t;
+    c = __fadd_rn(__fadd_rn(c, oc), q);
+  }
+};
+
+// Sum over a block of kThreads threads of compensated FP32 sums, valid in thread 0.  All the
+// adds are FP32 TwoSum merges.  Order: each lane of warp 0 merges its column of kWarps values
+// (warps in index order), then an xor-shuffle tree, as block_sum.  On GB300 a warp-wide FP64
+// instruction occupies a sub-partition's FP64 pipe for ~64 cycles, so the per-thread
+// (double)p + (double)c of get() and a double block_sum cost more than the FP32 row or element
+// work of the mixed form.
+__device__ __forceinline__ AccDot2 block_merge(AccDot2 a) {
+  static_assert(kWarps == 8, "column merge below is written for 8 warps");
+  __shared__ float2 smp[kThreads];
+  __syncthreads();   // an earlier call's readers are done with smp
+  smp[threadIdx.x] = make_float2(a.p, a.c);
+  __syncthreads();
+  AccDot2 s;
+  if (threadIdx.x < 32) {
+    s.p = smp[threadIdx.x].x;
+    s.c = smp[threadIdx.x].y;
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) s.merge(smp[threadIdx.x + 32 * w].x, smp[threadIdx.x + 32 * w].y);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float op = __shfl_xor_sync(0xffffffffu, s.p, o);
+      const float oc = __shfl_xor_sync(0xffffffffu, s.c, o);
+      s.merge(op, oc);
+    }
+  }
+  return s;
+}
+
+// The same as a double in thread 0 (one conversion a block).
+__device__ __forceinline__ double block_sum_pair(AccDot2 a) {
+  const AccDot2 s = block_merge(a);
+  return threadIdx.x == 0 ? s.get() : 0.0;
+}
+
+// Block partial of a compensated sum as an FP32 pair (consumer: sum_partials_pair).
+__device__ __forceinline__ void block_partial_pair(AccDot2 a, float2 *partials) {
+  const AccDot2 s = block_merge(a);
+  if (threadIdx.x == 0) partials[blockIdx.x] = make_float2(s.p, s.c);
+}
+
+// Sum of count pair partials written by the previous kernel, valid in every thread: each thread
+// merges a strided share, then block_merge; the same fixed order in every block.
+__device__ __forceinline__ AccDot2 sum_partials_pair(const float2 *partials, int count) {
+  __shared__ float2 s_total;
+  AccDot2 a;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) {
+    const float2 v = __ldcg(partials + i);
+    a.merge(v.x, v.y);
+  }
+  const AccDot2 s = block_merge(a);
+  if (threadIdx.x == 0) s_total = make_float2(s.p, s.c);
+  __syncthreads();
+  AccDot2 r;
+  r.p = s_total.x;
+  r.c = s_total.y;
+  return r;
+}
+
+// Epilogue trait: kPairPartials deferred epilogues take their block partials as FP32 pairs
+// (float2 in the partial slots, summed by sum_partials_pair).
+template <class E, class = void>
+struct has_pair_partials {
+  static constexpr bool value = false;
+};
+template <class E>
+struct has_pair_partials<E, decltype((void)E::kPairPartials)> {
+  static constexpr bool value = E::kPairPartials;
+};
+
+// A double block sum stored as a pair partial (hi + lo; thread 0 converts once).
+__device__ __forceinline__ void block_partial_split(double v, float2 *partials) {
+  const double b = block_sum(v);
+  if (threadIdx.x == 0) {
+    const float hi = (float)b;
+    partials[blockIdx.x] = make_float2(hi, (float)(b - (double)hi));
+  }
 }
 
 // Epilogue trait: kDeferred epilogues leave their reduction to the consumer (block partials

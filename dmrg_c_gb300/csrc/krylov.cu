@@ -162,17 +162,9 @@ __global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__r
 // ---- mixed-precision Lanczos ----------------------------------------------------------
 
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
-                                                    int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket, const double *pp, int pcount,
-                                                    double *D, double *hD, int bstep) {
+                                                    int n, int nchunk, float2 *__restrict__ partials, const double *__restrict__ sig,
+                                                    float *__restrict__ coef, unsigned *ticket) {
   pdl_wait();
-  if (pcount > 0 && blockIdx.x == 0 && blockIdx.y == 0) {   // block-uniform
-    const double d = sum_partials(pp, pcount);
-    if (threadIdx.x == 0) {
-      D[bstep] = d;
-      hD[bstep] = d;
-    }
-  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.y * kWarps + warp;
   const int chunk = blockIdx.x;
@@ -193,8 +185,13 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
       for (int u = 0; u < 4; ++u) acc.add(a[u], b[u]);
     }
     for (; i < r1; i += 32) acc.add(vj[i], y[i]);
-    const double t = warp_sum(acc.get());
-    if (lane == 0) partials[(long)j * nchunk + chunk] = t;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float op = __shfl_xor_sync(0xffffffffu, acc.p, o);
+      const float oc = __shfl_xor_sync(0xffffffffu, acc.c, o);
+      acc.merge(op, oc);
+    }
+    if (lane == 0) partials[(long)j * nchunk + chunk] = make_float2(acc.p, acc.c);
   }
   pdl_trigger();
   // The last block sums the chunk partials of every vector (one warp per vector, fixed
@@ -210,10 +207,18 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
   if (!s_last) return;
   __threadfence();
   for (int jj = warp; jj < nvec; jj += kWarps) {
-    double c = 0.0;
-    for (int ch = lane; ch < nchunk; ch += 32) c += __ldcg(partials + (long)jj * nchunk + ch);
-    c = warp_sum(c);
-    if (lane == 0) coef[jj] = (float)(-c * sig[jj] * sig[jj]);
+    AccDot2 c;
+    for (int ch = lane; ch < nchunk; ch += 32) {
+      const float2 v = __ldcg(partials + (long)jj * nchunk + ch);
+      c.merge(v.x, v.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float op = __shfl_xor_sync(0xffffffffu, c.p, o);
+      const float oc = __shfl_xor_sync(0xffffffffu, c.c, o);
+      c.merge(op, oc);
+    }
+    if (lane == 0) coef[jj] = (float)(-c.get() * sig[jj] * sig[jj]);
   }
   if (threadIdx.x == 0) *ticket = 0u;
 }
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nve
   for (int j = threadIdx.x; j < nvec; j += blockDim.x) coef[j] = coef_g[j];
   __syncthreads();
   float *vout = V + (long)nvec * ldv;
-  double acc = 0.0;
+  AccDot2 acc2;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     AccDot2 a;
     a.p = y[i];
@@ -238,15 +243,15 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nve
       for (int u = 0; u < 8; ++u) a.add(coef[j + u], v[u]);
     }
     for (; j < nvec; ++j) a.add(coef[j], __ldg(V + (long)j * ldv + i));
-    const double w = a.get();
-    vout[i] = (float)w;
-    acc += w * w;
+    const float w = __fadd_rn(a.p, a.c);
+    vout[i] = w;
+    acc2.add(w, w);
   }
   pdl_trigger();
   if (r2)
-    grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });
+    grid_reduce_block(block_sum_pair(acc2), out, [&](double t) { set_norm2(r2, t); });
   else
-    block_partial(acc, out.partials);
+    block_partial_pair(acc2, reinterpret_cast<float2 *>(out.partials));   // consumer: the next product (Scale::PAIRS)
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
@@ -264,45 +269,99 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
     b0 = vb[i0];
     q0 = vp[i0];
   }
-  double d;
-  if (pcount > 0) {
-    d = sum_partials(pp, pcount);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      D[b] = d;
-      hD[b] = d;
+  // The product's pair partials of <y, v_b> merged in FP32 by every thread; the FP64 scalars
+  // formed once by thread 0 and split into two floats each; the element arithmetic in
+  // compensated FP32 (Dot2): as accurate as FP64 arithmetic on the FP32 operands, without an
+  // FP64 instruction per element (GB300's scarce FP64 pipe).
+  __shared__ float s_sc[4];
+  AccDot2 pd;
+  if (pcount > 0) pd = sum_partials_pair(reinterpret_cast<const float2 *>(pp), pcount);
+  if (threadIdx.x == 0) {
+    double d;
+    if (pcount > 0) {
+      d = pd.get();
+      if (blockIdx.x == 0) {
+        D[b] = d;
+        hD[b] = d;
+      }
+    } else {
+      d = D[b];
     }
-  } else {
-    d = D[b];
+    const double a = d * sig[b];
+    const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
+    const float a_hi = (float)a, c_hi = (float)c;
+    s_sc[0] = a_hi;
+    s_sc[1] = (float)(a - (double)a_hi);
+    s_sc[2] = c_hi;
+    s_sc[3] = (float)(c - (double)c_hi);
   }
-  const double a = d * sig[b];
-  const double c = (b > 0) ? O[b] * sig[b - 1] : 0.0;
-  double acc = 0.0;
+  __syncthreads();
+  const float a_hi = s_sc[0], a_lo = s_sc[1], c_hi = s_sc[2], c_lo = s_sc[3];
+  AccDot2 acc2;
   auto step = [&](int i, float yi, float bi, float qi) {
-    double w = (double)yi - a * (double)bi;
-    if (b > 0) w -= c * (double)qi;
-    vn[i] = (float)w;
-    acc += w * w;
+    AccDot2 t;
+    t.p = yi;
+    t.add(-a_hi, bi);
+    t.add(-a_lo, bi);
+    if (b > 0) {
+      t.add(-c_hi, qi);
+      t.add(-c_lo, qi);
+    }
+    const float w = __fadd_rn(t.p, t.c);
+    vn[i] = w;
+    acc2.add(w, w);
   };
   if (i0 < n) step(i0, y0, b0, q0);
   for (int i = i0 + stride; i < n; i += stride) step(i, y[i], vb[i], vp[i]);
   pdl_trigger();
   if (r2)
-    grid_reduce(acc, out, [&](double t) { set_norm2(r2, t); });
+    grid_reduce_block(block_sum_pair(acc2), out, [&](double t) { set_norm2(r2, t); });
   else
-    block_partial(acc, out.partials);
+    block_partial_pair(acc2, reinterpret_cast<float2 *>(out.partials));   // consumer: the next product (Scale::PAIRS)
 }
 
-__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
-                                                     const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
-                                                     RedSlot slot) {
-  double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    double t = 0.0;
-    for (int j = 0; j < k; ++j) t = t + (s[j] * sig[j]) * (double)V[(long)j * ldv + i];
-    out[i] = t;
-    acc += t * t;
+__global__ void k_mx_ritz_coef(const double *__restrict__ s, const double *__restrict__ sig, int k, float2 *__restrict__ cp) {
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    const double c = s[j] * sig[j];
+    const float hi = (float)c;
+    cp[j] = make_float2(hi, (float)(c - (double)hi));
   }
-  grid_reduce(acc, slot, [&](double t) { set_norm2(r2, t); });
+}
+
+// The FP32 Krylov basis combined on the FP32 pipes: with FP64 coefficients each (element,
+// vector) term took three FP64 instructions (a 49-vector combination of the XXZ L=22 basis
+// ran 221 us, FP64-issue bound); here the FP64 work is one conversion per element.
+__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const float2 *__restrict__ cp,
+                                                     double *__restrict__ out, int n, Norm2 *r2, RedSlot slot) {
+  extern __shared__ float2 cs[];   // k entries
+  for (int j = threadIdx.x; j < k; j += blockDim.x) cs[j] = cp[j];
+  __syncthreads();
+  AccDot2 nrm;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    AccDot2 t;
+    int j = 0;
+    for (; j + 8 <= k; j += 8) {   // eight loads in flight per thread
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldg(V + (long)(j + u) * ldv + i);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        t.add(cs[j + u].x, v[u]);
+        t.add(cs[j + u].y, v[u]);
+      }
+    }
+    for (; j < k; ++j) {
+      const float v = __ldg(V + (long)j * ldv + i);
+      t.add(cs[j].x, v);
+      t.add(cs[j].y, v);
+    }
+    out[i] = t.get();
+    // (p + c)^2 = p^2 + 2pc + c^2: the square of the pair, not of its FP32 rounding (which
+    // would leave the norm ~1e-10 off); c^2 is below the sum's resolution
+    nrm.add(t.p, t.p);
+    nrm.add(__fmul_rn(2.0f, t.c), t.p);
+  }
+  grid_reduce_block(block_sum_pair(nrm), slot, [&](double tot) { set_norm2(r2, tot); });
 }
 
 }  // namespace dg

@@ -22,9 +22,11 @@
 #include <cstdlib>
 #include <limits>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "apply.cuh"
+#include "sell.cuh"
 #include "common.cuh"
 #include "tridiag.h"
 
@@ -40,6 +42,7 @@ struct Scalars {
   double inv_gamma0;    // MINRES: 1/gamma0, the scale of the next product
   double thr;           // refinement CG: stopping threshold on <res,res>
   double rrs_ref[2];    // refinement CG: <res,res> entering iteration it is rrs_ref[it & 1]
+  float rr32[2];        // the same in FP32 (the correction solve's coefficients are FP32)
   int done;         // 0 running, 1 converged, 2 iteration limit
   int iters;
 };
@@ -189,6 +192,15 @@ struct EpiLanczos {
     if (vout) vout[i] = (VT)xi;
     acc += yi * xi;
   }
+  // The mixed form's FP32 rows (sell.cuh, has_row32): the same with the dot as a Dot2 pair, and
+  // the deferred block partials as FP32 pairs (consumer: k_mx_update).
+  static constexpr bool kRow32 = std::is_same<YT, float>::value && std::is_same<VT, float>::value;
+  static constexpr bool kPairPartials = kRow32;
+  __device__ void row32(int i, float xi, float yi, AccDot2 &acc) const {
+    y[i] = (YT)yi;
+    if (vout) vout[i] = (VT)xi;
+    acc.add(yi, xi);
+  }
   __device__ void finalize(double t) const {
     D[b] = t;
     hD[b] = t;
@@ -298,16 +310,15 @@ constexpr int kMxChunk = 512;
 
 // partials[j * nchunk + chunk] = <V_j, y> over the chunk's rows, one warp per vector; the
 // last block reduces them (fixed order) to coef_j = -sig_j^2 <V_j, y> = -c_j sig_j with
-// c_j = <v_j, y>.  ticket: zero between uses.  With pcount > 0, block (0, 0) also sums the
-// product's pcount block partials into D[bstep] = <y, v_bstep> and its host mirror.
+// coef_j = -sig_j^2 <v_j, y> for j < nvec: per-chunk pair partials, summed by the last block.
+// ticket: zero between uses.
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
-                                                    int n, int nchunk, double *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket, const double *pp, int pcount,
-                                                    double *D, double *hD, int bstep);
-// Three-term recurrence of the mixed form without reorthogonalisation:
-// w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} (FP64); V[b+1] = fl32(w).  D[b] as in
-// k_lz_update (summed from the product's pcount partials, or as its last block recorded it);
-// <w,w> into block partials (r2 null) or the Norm2 *r2.
+                                                    int n, int nchunk, float2 *__restrict__ partials, const double *__restrict__ sig,
+                                                    float *__restrict__ coef, unsigned *ticket);
+// Three-term recurrence of the mixed form: w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} in
+// compensated FP32 with the scalars as float pairs; V[b+1] = w.  D[b] summed from the
+// product's pcount pair partials, or, with pcount 0, as its last block recorded it; <w,w> into
+// pair partials (r2 null; consumer Scale::PAIRS) or the Norm2 *r2.
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, long ldv, int b, const double *__restrict__ sig,
                                                        const float *__restrict__ y, double *D, double *hD, const double *O, int n,
                                                        const double *pp, int pcount, RedSlot out, Norm2 *r2);
@@ -316,10 +327,12 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ V, l
 // one thread).
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nvec, const float *__restrict__ coef,
                                                     const float *y, int n, RedSlot out, Norm2 *r2);
-// out_i = sum_{j<k} s_j sig_j V_j[i] (FP64, j order); *r2 = <out,out>.
-__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const double *__restrict__ s,
-                                                     const double *__restrict__ sig, double *__restrict__ out, int n, Norm2 *r2,
-                                                     RedSlot slot);
+// cp_j = s_j sig_j as two floats (hi + lo), j < k; one block.
+__global__ void k_mx_ritz_coef(const double *__restrict__ s, const double *__restrict__ sig, int k, float2 *__restrict__ cp);
+// out_i = sum_{j<k} cp_j V_j[i] in compensated FP32 (Dot2, j order; FP64 result), *r2 = <out,out>.
+// Dynamic shared memory: k float2.
+__global__ void __launch_bounds__(kThreads) k_mx_ritz(const float *__restrict__ V, long ldv, int k, const float2 *__restrict__ cp,
+                                                     double *__restrict__ out, int n, Norm2 *r2, RedSlot slot);
 
 // ---- CG ------------------------------------------------------------------------------
 
@@ -495,14 +508,26 @@ struct KrylovBasis {
   T *vec(int j) const { return V + (size_t)j * n; }
 };
 
-// Stored elements a product block needs before Lanczos leaves its reductions to the consumer
-// (LzSteps64, LzStepsMixed).  DG_DEFER_REDUCTIONS=0 / =1 forces the last-block / consumer form
-// (both give bitwise the same values); unset, the work per block decides.
+// Stored elements a product block needs before the FP64 Lanczos (LzSteps64) leaves its
+// reductions to the consumer.  DG_DEFER_REDUCTIONS=0 / =1 forces the last-block / consumer form
+// (in the FP64 form both give bitwise the same values); unset, the work per block decides.
 constexpr long kLzDeferWork = 6144;
-inline bool lz_defer(long nnz, int grid) {
+inline int defer_override() {
   const char *e = std::getenv("DG_DEFER_REDUCTIONS");
   if (e && e[0] && !e[1] && (e[0] == '0' || e[0] == '1')) return e[0] == '1';
-  return nnz >= kLzDeferWork * (long)grid;
+  return -1;
+}
+inline bool lz_defer(long nnz, int grid) {
+  const int o = defer_override();
+  return o >= 0 ? o == 1 : nnz >= kLzDeferWork * (long)grid;
+}
+// The mixed form (LzStepsMixed) leaves them to the consumer at every size unless forced: its
+// partials are FP32 pairs that every consumer block merges on the FP32 pipes, which costs less
+// than the serial tail of the last-block form (FP64 partials would cost each consumer block
+// FP64 adds, hence the work threshold above).
+inline bool lz_defer_mixed() {
+  const int o = defer_override();
+  return o >= 0 ? o == 1 : true;
 }
 
 // FP64 form (the reference's LANCZOS*): the product normalises w on the fly and stores v_b
@@ -576,7 +601,7 @@ struct LzStepsMixed {
   Workspace &ws;
   LzState &z;
   double *w;             // FP64 start / restart vector
-  DevBuf<float> y, coef;
+  DevBuf<float> y, coef, rcoef;
   DevBuf<double> sig, partials;
   DevBuf<unsigned> ticket;
   KrylovBasis<float> B;
@@ -600,8 +625,8 @@ struct LzStepsMixed {
     const RedSlot slot = ws.slot();
     B.ensure(b + 2, z.cap_max);
     // as LzSteps64: reductions finished by the consumer on products with enough work a block
-    const bool defer = lz_defer(op.nnz(), op.grid());
-    const Scale sc = (b > 0 && defer) ? Scale::partials(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
+    const bool defer = lz_defer_mixed();
+    const Scale sc = (b > 0 && defer) ? Scale::pairs(ws.partials2.get(), ws.vgrid) : Scale::norm2(&S->r2);
     if (defer) {
       EpiLanczos<float, float, true> epi{y.get(), (float *)nullptr, z.D.get(), z.O.get(), z.hD.d, z.hO.d, b, sig.get()};
       op.apply(B.vec(b), sc, 0.0, (const int *)nullptr, epi, slot, st);
@@ -631,14 +656,17 @@ struct LzStepsMixed {
     const int nvec = b + 1;
     const float *w3 = B.vec(b + 1);
     launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec, w3, n,
-               nchunk, partials.get(), (const double *)sig.get(), coef.get(), ticket.get(), (const double *)nullptr, 0, z.D.get(),
-               z.hD.d, b);
+               nchunk, reinterpret_cast<float2 *>(partials.get()), (const double *)sig.get(), coef.get(), ticket.get());
     launch_pdl_smem(k_mx_sub, dim3(ws.vgrid), dim3(kThreads), sizeof(float) * nvec, st, B.V, (long)n, nvec,
                     (const float *)coef.get(), w3, n, r2slot, r2);
   }
   void combine(int k, const std::vector<double> &s, double *dst) {
     z.upload_s(k, s, ws.st);
-    k_mx_ritz<<<ws.vgrid, kThreads, 0, ws.st>>>(B.V, z.n, k, z.s_dev.get(), sig.get(), dst, z.n, &ws.S()->r2, ws.slot()); ::dg::count_launch();
+    if (!rcoef.get()) rcoef.alloc(2 * (size_t)(z.cap_max + 1));
+    float2 *cp = reinterpret_cast<float2 *>(rcoef.get());
+    k_mx_ritz_coef<<<1, kThreads, 0, ws.st>>>(z.s_dev.get(), sig.get(), k, cp); ::dg::count_launch();
+    k_mx_ritz<<<ws.vgrid, kThreads, sizeof(float2) * k, ws.st>>>(B.V, z.n, k, (const float2 *)cp, dst, z.n, &ws.S()->r2,
+                                                                ws.slot()); ::dg::count_launch();
     DG_CUDA(cudaGetLastError());
   }
 };

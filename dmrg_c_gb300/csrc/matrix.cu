@@ -325,11 +325,6 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   // pipelined form, which has no second group to overlap, is the slowest (12-14 % behind).
   const double per_row = (double)total / ((double)nslices * kSellC);
   m->sell_variant = (m->sell_ws >= 4 || per_row < 24.0) ? V_U16 : V_PIPE8;
-  // The FP32 product takes 8-element groups on the long superblock rows (16 cost it 30 % on the
-  // m=512 superblock); a short ED row fits one 16-element group, while with 8 its remaining
-  // elements run one dependent column -> x chain at a time (XXZ L=22: 40 us FP32 against 44 us
-  // FP64).
-  m->sell_variant32 = per_row < 24.0 ? V_U16 : V_U8;
   DG_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -3,61 +3,64 @@
 
 namespace dg {
 
-__global__ void __launch_bounds__(kThreads) k_refine_update(int n, const float *__restrict__ p32, const double *__restrict__ q,
-                                                           const double *__restrict__ psi, double *__restrict__ t,
-                                                           double *__restrict__ res, const Scalars *S, int it, const double *pp,
-                                                           int pcount, const double *gpp, int gcount, double *up) {
+__global__ void __launch_bounds__(kThreads) k_refine32_update(int n, const float *__restrict__ p32, const float *__restrict__ q32,
+                                                             const float *__restrict__ psi32, float *__restrict__ t32,
+                                                             float *__restrict__ res32, const Scalars *S, int it, const float2 *pp,
+                                                             int pcount, const float2 *gpp, int gcount, float2 *up) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
   // first element's operands in flight before the partial sums (see k_lz_update)
   const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
-  double t0 = 0.0, r0 = 0.0, q0 = 0.0, s0 = 0.0;
-  float f0 = 0.0f;
+  float t0 = 0.0f, f0 = 0.0f, r0 = 0.0f, q0 = 0.0f, s0 = 0.0f;
   if (i0 < n) {
-    t0 = t[i0];
+    t0 = t32[i0];
     f0 = p32[i0];
-    r0 = res[i0];
-    q0 = q[i0];
-    s0 = psi[i0];
+    r0 = res32[i0];
+    q0 = q32[i0];
+    s0 = psi32[i0];
   }
-  __shared__ double s_a;
-  const double pq = sum_partials(pp, pcount);
-  const double gp = sum_partials(gpp, gcount);
-  if (threadIdx.x == 0) s_a = S->rrs_ref[it & 1] / pq;   // one division per block
+  __shared__ float s_a, s_g;
+  const AccDot2 pq = sum_partials_pair(pp, pcount);
+  const AccDot2 gp = sum_partials_pair(gpp, gcount);
+  if (threadIdx.x == 0) {
+    s_a = __fdiv_rn(S->rr32[it & 1], __fadd_rn(pq.p, pq.c));
+    s_g = __fadd_rn(gp.p, gp.c);
+  }
   __syncthreads();
-  const double a = s_a;
-  double acc = 0.0;
-  auto step = [&](int i, double ti, float fi, double ri, double qi, double si) {
-    t[i] = ti + a * (double)fi;
-    const double rn = ri - a * (qi - gp * si);
-    res[i] = rn;
-    acc += rn * rn;
+  const float a = s_a, g = s_g;
+  AccDot2 acc;
+  auto step = [&](int i, float ti, float fi, float ri, float qi, float si) {
+    t32[i] = __fmaf_rn(a, fi, ti);
+    const float rn = __fmaf_rn(-a, __fmaf_rn(-g, si, qi), ri);
+    res32[i] = rn;
+    acc.add(rn, rn);
   };
   if (i0 < n) step(i0, t0, f0, r0, q0, s0);
-  for (int i = i0 + stride; i < n; i += stride) step(i, t[i], p32[i], res[i], q[i], psi[i]);
+  for (int i = i0 + stride; i < n; i += stride) step(i, t32[i], p32[i], res32[i], q32[i], psi32[i]);
   pdl_trigger();
-  block_partial(acc, up);
+  block_partial_pair(acc, up);
 }
 
-__global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const double *__restrict__ res, double *__restrict__ p,
-                                                              float *__restrict__ p32, const double *__restrict__ g, Scalars *S,
-                                                              int it, int max_step, const double *up, int ucount, double *gout,
-                                                              Progress *prog) {
+__global__ void __launch_bounds__(kThreads) k_refine32_direction(int n, const float *__restrict__ res32, float *__restrict__ p32,
+                                                                const float *__restrict__ g32, Scalars *S, int it, int max_step,
+                                                                const float2 *up, int ucount, float2 *gout, Progress *prog) {
   pdl_wait();
   if (*((volatile const int *)&S->done)) return;
   // first element's operands in flight before the partial sums (see k_lz_update)
   const int i0 = blockIdx.x * kThreads + threadIdx.x, stride = gridDim.x * kThreads;
-  double r0 = 0.0, p0 = 0.0, g0 = 0.0;
+  float r0 = 0.0f, p0 = 0.0f, g0 = 0.0f;
   if (i0 < n) {
-    r0 = res[i0];
-    p0 = p[i0];
-    g0 = g[i0];
+    r0 = res32[i0];
+    p0 = p32[i0];
+    g0 = g32[i0];
   }
-  __shared__ double s_b;
+  __shared__ float s_b;
+  __shared__ int s_stop;
   if (it > 0) {
-    const double tot = sum_partials(up, ucount);
-    const bool converged = tot < S->thr, last = it >= max_step;
+    const AccDot2 tot = sum_partials_pair(up, ucount);
     if (threadIdx.x == 0) {
+      const double td = tot.get();   // one conversion a block
+      const bool converged = td < S->thr, last = it >= max_step;
       if (blockIdx.x == 0) {
         if (converged) {
           S->done = 1;
@@ -66,44 +69,38 @@ __global__ void __launch_bounds__(kThreads) k_refine_direction(int n, const doub
           S->done = 2;
           S->iters = max_step;
         }
-        S->rrs_ref[(it + 1) & 1] = tot;   // the other slot: this kernel's blocks read rrs_ref[it & 1]
+        // the other slot: this kernel's blocks read slot it & 1
+        S->rrs_ref[(it + 1) & 1] = td;
+        S->rr32[(it + 1) & 1] = (float)td;
         prog->done = S->done;
         prog->stamp = it;
       }
-      s_b = tot / S->rrs_ref[it & 1];
+      s_b = __fdiv_rn(__fadd_rn(tot.p, tot.c), S->rr32[it & 1]);
+      s_stop = (converged || last) ? 1 : 0;
     }
     __syncthreads();
-    if (converged || last) return;   // the same decision in every block
+    if (s_stop) return;   // the same decision in every block
   } else {
-    if (threadIdx.x == 0) s_b = 0.0;
+    if (threadIdx.x == 0) s_b = 0.0f;
     __syncthreads();
   }
-  const double b = s_b;
-  double acc = 0.0;
-  auto step = [&](int i, double ri, double pi0, double gi) {
-    const double pi = ri + b * pi0;
-    p[i] = pi;
-    const float pf = (float)pi;
-    p32[i] = pf;
-    acc += gi * (double)pf;
+  const float b = s_b;
+  AccDot2 acc;
+  auto step = [&](int i, float ri, float pi0, float gi) {
+    const float pi = it > 0 ? __fmaf_rn(b, pi0, ri) : ri;   // p32 holds no direction before iteration 1
+    p32[i] = pi;
+    acc.add(gi, pi);
   };
   if (i0 < n) step(i0, r0, p0, g0);
-  for (int i = i0 + stride; i < n; i += stride) step(i, res[i], p[i], g[i]);
+  for (int i = i0 + stride; i < n; i += stride) step(i, res32[i], p32[i], g32[i]);
   pdl_trigger();
-  block_partial(acc, gout);
+  block_partial_pair(acc, gout);
 }
 
 __global__ void __launch_bounds__(kThreads) k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out,
                                                   RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) acc += x[i] * y[i];
-  grid_reduce(acc, slot, [&](double tot) { *out = tot; });
-}
-
-__global__ void __launch_bounds__(kThreads) k_vdot_df(const double *__restrict__ g, const float *__restrict__ p32, int n,
-                                                     double *out, RedSlot slot) {
-  double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) acc += g[i] * (double)p32[i];
   grid_reduce(acc, slot, [&](double tot) { *out = tot; });
 }
 

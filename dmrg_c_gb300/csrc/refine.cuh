@@ -12,7 +12,11 @@
 //     with the FP32 operator (the projected operator is positive definite on psi's
 //     complement, with the spectral gap as its smallest eigenvalue) to the relative residual
 //     tau the step needs (the residual shrinks by about tau per step, down to the FP32
-//     operator's ||H - H32|| / gap): the step's accuracy is set by the FP64 residual;
+//     operator's ||H - H32|| / gap): the step's accuracy is set by the FP64 residual.
+//     tau >= 1e-4, so the solve runs in FP32 throughout (vectors, coefficients, compensated
+//     reductions with FP32 pair partials): on GB300 a warp-wide FP64 instruction occupies a
+//     sub-partition's FP64 pipe for ~64 cycles, and FP64 vector updates cost more than the
+//     FP32 products they sit between;
 //   * Rayleigh-Ritz in span{psi, t} with one FP64 product H t.
 // H psi is carried along (y), so a step costs one FP64 and k FP32 products.
 #pragma once
@@ -23,35 +27,40 @@ namespace dg {
 
 constexpr double kMixedRes = 1e-8;    // accept when ||H psi - theta psi||_2 <= kMixedRes |theta|
 
-// q = (H32 - theta) p32 (row sums from the product kernel) with block partials of <p32, q>
-// (summed by every block of the update kernel).
-struct EpiRefineDot {
+// q32 = (H32 - theta) p32 with pair partials of <p32, q32> (the FP32 correction solve).
+struct EpiRefineDot32 {
   static constexpr bool kReduce = true;
   static constexpr bool kDeferred = true;
-  double *q;
+  static constexpr bool kPairPartials = true;
+  static constexpr bool kRow32 = true;
+  float *q;
   __device__ void row(int i, double xi, double yi, double &acc) const {
-    q[i] = yi;
+    q[i] = (float)yi;
     acc += xi * yi;
+  }
+  __device__ void row32(int i, float xi, float yi, AccDot2 &acc) const {
+    q[i] = yi;
+    acc.add(xi, yi);
   }
   __device__ void finalize(double) const {}
 };
 
-// Iteration it of the projected correction CG.  <p32,q> from the product's pcount partials,
-// <g,p32> from the previous direction kernel's gcount partials; a = rrs_ref[it&1] / <p32,q>;
-// t += a p32; res -= a (q - <g,p32> psi); block partials of <res,res> into up.
-__global__ void k_refine_update(int n, const float *__restrict__ p32, const double *__restrict__ q, const double *__restrict__ psi,
-                                double *__restrict__ t, double *__restrict__ res, const Scalars *S, int it, const double *pp,
-                                int pcount, const double *gpp, int gcount, double *up);
-// Iteration it: <res,res> from the update's ucount partials; convergence (< S->thr) or the
-// iteration limit ends the solve (block 0 records it); otherwise p = res + beta p.  it = 0:
-// the start, p = res (beta 0, no test).  Then p32 = fl32(p) and block partials of <g,p32> into gout.
-__global__ void k_refine_direction(int n, const double *__restrict__ res, double *__restrict__ p, float *__restrict__ p32,
-                                   const double *__restrict__ g, Scalars *S, int it, int max_step, const double *up, int ucount,
-                                   double *gout, Progress *prog);
+// Iteration it of the FP32 correction CG: a = rr32[it&1] / <p32,q32> (the product's pcount
+// pair partials), gp = <g32,p32> (the previous direction kernel's gcount pair partials);
+// t32 += a p32; res32 -= a (q32 - gp psi32); pair partials of <res32,res32> into up.
+__global__ void k_refine32_update(int n, const float *__restrict__ p32, const float *__restrict__ q32,
+                                  const float *__restrict__ psi32, float *__restrict__ t32, float *__restrict__ res32,
+                                  const Scalars *S, int it, const float2 *pp, int pcount, const float2 *gpp, int gcount,
+                                  float2 *up);
+// Iteration it: <res32,res32> from the update's ucount pair partials; convergence (< S->thr) or
+// the iteration limit ends the solve (block 0 records it); otherwise p32 = res32 + beta p32.
+// it = 0: the start, p32 = res32.  Then pair partials of <g32,p32> into gout.
+__global__ void k_refine32_direction(int n, const float *__restrict__ res32, float *__restrict__ p32,
+                                     const float *__restrict__ g32, Scalars *S, int it, int max_step, const float2 *up,
+                                     int ucount, float2 *gout, Progress *prog);
+
 // *out = sum_i x_i y_i
 __global__ void k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out, RedSlot slot);
-// *out = sum_i g_i p32_i
-__global__ void k_vdot_df(const double *__restrict__ g, const float *__restrict__ p32, int n, double *out, RedSlot slot);
 // y = a x + b y
 __global__ void k_axpby(int n, double a, const double *__restrict__ x, double b, double *__restrict__ y);
 // r = y - theta psi; *out = sum_i |r_i|
@@ -77,8 +86,8 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
   Scalars *S = ws.S();
   const RedSlot slot = ws.slot();
   const int vg = ws.vgrid;
-  DevBuf<double> y(n), r(n), g(n), t(n), res(n), p(n), q(n), z(n), out1(1);
-  DevBuf<float> p32(n), psi32(n);
+  DevBuf<double> y(n), r(n), t(n), res(n), z(n), out1(1);
+  DevBuf<float> p32(n), psi32(n), g32(n), q32(n), t32(n), res32(n);
   RefineResult R;
   auto fetch = [&](const double *dptr) {
     double h = 0.0;
@@ -106,44 +115,48 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
   auto accepted = [&] { return l1 < acc || rn <= kMixedRes * std::fabs(theta); };
   for (int outer = 0; outer < max_outer && !accepted(); ++outer) {
     const double tau = std::min(1e-1, std::max(1e-4, 0.5 * kMixedRes * std::fabs(theta) / rn));
-    // g = (H32 - theta) fl32(psi): makes <psi, q> = <g, p32> available without a second reduction
+    // g32 = (H32 - theta) fl32(psi): makes <psi, q32> = <g32, p32> available without a second
+    // reduction
     k_copy<double, float><<<vg, kThreads, 0, st>>>(psi, psi32.get(), n); ::dg::count_launch();
-    op.apply(psi32.get(), Scale{}, -theta, (const int *)nullptr, EpiStore<double>{g.get()}, slot, st);
+    op.apply(psi32.get(), Scale{}, -theta, (const int *)nullptr, EpiStore<float>{g32.get()}, slot, st);
     ++R.inner;
-    // res = -(r - <psi,r> psi), t = 0, p = res
+    // res = -(r - <psi,r> psi) in FP64, then res32 = fl32(res), t32 = 0
     const double c = dot(psi, r.get());
     DG_CUDA(cudaMemsetAsync(res.get(), 0, sizeof(double) * n, st));
     axpby(-1.0, r.get(), 0.0, res.get());
     axpby(c, psi, 1.0, res.get());
-    DG_CUDA(cudaMemsetAsync(t.get(), 0, sizeof(double) * n, st));
-    DG_CUDA(cudaMemsetAsync(p.get(), 0, sizeof(double) * n, st));
+    k_copy<double, float><<<vg, kThreads, 0, st>>>(res.get(), res32.get(), n); ::dg::count_launch();
+    DG_CUDA(cudaMemsetAsync(t32.get(), 0, sizeof(float) * n, st));
     const double rr0 = dot(res.get(), res.get());
     if (!(rr0 > 0.0)) break;
-    // p = res (beta = 0), p32, <g,p32>
+    // p32 = res32 (beta = 0), <g32,p32>
     Scalars init{};
     init.rrs_ref[1] = rr0;   // enters iteration 1
+    init.rr32[1] = (float)rr0;
     init.thr = tau * tau * rr0;
     DG_CUDA(cudaMemcpyAsync(&S->rrs_ref[1], &init.rrs_ref[1], sizeof(double), cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(&S->rr32[1], &init.rr32[1], sizeof(float), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemcpyAsync(&S->thr, &init.thr, sizeof(double), cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(&S->done, 0, sizeof(int), st));
     DG_CUDA(cudaMemsetAsync(&S->iters, 0, sizeof(int), st));
-    // Partials: the product's <p32,q> in slot.partials, the update's <res,res> in partials2,
-    // the direction's <g,p32> in partials3; each is summed by every block of its consumer.
-    double *up = ws.partials2.get(), *gpp = ws.partials3.get();
+    // Pair partials: the product's <p32,q32> in slot.partials, the update's <res32,res32> in
+    // partials2, the direction's <g32,p32> in partials3; each summed by every block of its consumer.
+    float2 *up = reinterpret_cast<float2 *>(ws.partials2.get()), *gpp = reinterpret_cast<float2 *>(ws.partials3.get());
     const int pgrid = op.grid();
-    k_refine_direction<<<vg, kThreads, 0, st>>>(n, res.get(), p.get(), p32.get(), g.get(), S, 0, max_inner, (const double *)up, 0,
-                                                gpp, ws.prog.d); ::dg::count_launch();
+    k_refine32_direction<<<vg, kThreads, 0, st>>>(n, res32.get(), p32.get(), g32.get(), S, 0, max_inner, (const float2 *)up, 0,
+                                                  gpp, ws.prog.d); ::dg::count_launch();
     ws.prog.h->done = 0;
     ws.prog.h->stamp = 0;
     const int chunk = 8;
     int enq = 0, checked = 0;
     auto enqueue_to = [&](int last) {
       for (int it = enq + 1; it <= last; ++it) {
-        op.apply(p32.get(), Scale{}, -theta, &S->done, EpiRefineDot{q.get()}, slot, st);
-        launch_pdl(k_refine_update, vg, kThreads, st, n, (const float *)p32.get(), (const double *)q.get(), (const double *)psi,
-                   t.get(), res.get(), (const Scalars *)S, it, (const double *)slot.partials, pgrid, (const double *)gpp, vg, up);
-        launch_pdl(k_refine_direction, vg, kThreads, st, n, (const double *)res.get(), p.get(), p32.get(),
-                   (const double *)g.get(), S, it, max_inner, (const double *)up, vg, gpp, ws.prog.d);
+        op.apply(p32.get(), Scale{}, -theta, &S->done, EpiRefineDot32{q32.get()}, slot, st);
+        launch_pdl(k_refine32_update, vg, kThreads, st, n, (const float *)p32.get(), (const float *)q32.get(),
+                   (const float *)psi32.get(), t32.get(), res32.get(), (const Scalars *)S, it,
+                   (const float2 *)slot.partials, pgrid, (const float2 *)gpp, vg, up);
+        launch_pdl(k_refine32_direction, vg, kThreads, st, n, (const float *)res32.get(), p32.get(), (const float *)g32.get(), S,
+                   it, max_inner, (const float2 *)up, vg, gpp, ws.prog.d);
       }
       enq = std::max(enq, last);
     };
@@ -164,6 +177,7 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     DG_CUDA(cudaMemcpyAsync(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
     R.inner += hs.done ? hs.iters : max_inner;
+    k_copy<float, double><<<vg, kThreads, 0, st>>>(t32.get(), t.get(), n); ::dg::count_launch();
     // t_hat = (t - <psi,t> psi) / ||.||
     const double ct = dot(psi, t.get());
     axpby(-ct, psi, 1.0, t.get());

@@ -20,6 +20,8 @@
 // order.  Either way the order is fixed, so the product is bitwise reproducible.
 #pragma once
 
+#include <type_traits>
+
 #include "apply.cuh"
 
 namespace dg {
@@ -60,29 +62,11 @@ __device__ __forceinline__ T ld_vec(const T *p) {
 }
 
 // Row accumulators.  FP64 values or vectors: one DFMA per element.  FP32 values and FP32
-// vectors (the mixed-precision form): the exact product and compensated sum of Ogita, Rump
-// & Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2): the
-// product's rounding error comes from an FMA, the sum's from Knuth's TwoSum, and both are
-// carried in a second float, so the row sum is as accurate as if accumulated in twice the
-// working precision -- on the FP32 pipes, which GB300 has ~60x more of than FP64 pipes.
-// The explicitly rounded intrinsics keep the compiler from contracting the error terms away.
+// vectors (the mixed-precision form): AccDot2, the Dot2 pair of common.cuh.
 struct AccF64 {
   double s = 0.0;
   __device__ __forceinline__ void add(double v, double x) { s += v * x; }
   __device__ __forceinline__ double get() const { return s; }
-};
-struct AccDot2 {
-  float p = 0.0f, c = 0.0f;
-  __device__ __forceinline__ void add(float v, float x) {
-    const float h = __fmul_rn(v, x);
-    const float r = __fmaf_rn(v, x, -h);            // v x = h + r exactly
-    const float t = __fadd_rn(p, h);
-    const float z = __fsub_rn(t, p);
-    const float q = __fadd_rn(__fsub_rn(p, __fsub_rn(t, z)), __fsub_rn(h, z));   // p + h = t + q exactly
-    p = t;
-    c = __fadd_rn(c, __fadd_rn(q, r));
-  }
-  __device__ __forceinline__ double get() const { return (double)p + (double)c; }
 };
 template <class VT, class XT>
 struct AccFor {
@@ -93,10 +77,25 @@ struct AccFor<float, float> {
   using type = AccDot2;
 };
 
+// Epilogue trait: kRow32 epilogues (FP32 outputs of the mixed form) have
+// row32(i, xi, yi, AccDot2 &acc), called with FP32 row values so that a row of a few elements
+// (ED Hamiltonians) costs no FP64 instruction: on GB300 the per-row FP64 conversions, scalings
+// and dot accumulation of the double-valued epilogue kept the FP64 pipe 46 % busy in the FP32
+// product of the XXZ L=22 Hamiltonian (12 elements a row).
+template <class E, class = void>
+struct has_row32 {
+  static constexpr bool value = false;
+};
+template <class E>
+struct has_row32<E, decltype((void)E::kRow32)> {
+  static constexpr bool value = E::kRow32;
+};
+
 // Sum of this warp's share of one slice row.  WS warps share a slice: warp `sub` takes the
 // row elements k = sub, sub + WS, sub + 2 WS, ...; each lane owns one row.
 template <int WS, int U, bool PIPE, bool STREAM, class VT, class XT>
-__device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t base, int w, int sub, const XT *__restrict__ x) {
+__device__ __forceinline__ typename AccFor<VT, XT>::type sell_row_acc(const SellOp<VT> &op, int64_t base, int w, int sub,
+                                                                     const XT *__restrict__ x) {
   const int cnt = (w > sub) ? (w - sub + WS - 1) / WS : 0;   // elements of this warp
   const int G = cnt / U;
   const int64_t step = (int64_t)WS * kSellC;
@@ -141,7 +140,12 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
     const int64_t p = p0 + (int64_t)j * step;
     acc.add(ld_mat<STREAM>(op.val + p), ld_vec<STREAM>(x + ld_mat<STREAM>(op.col + p)));
   }
-  return acc.get();
+  return acc;
+}
+
+template <int WS, int U, bool PIPE, bool STREAM, class VT, class XT>
+__device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t base, int w, int sub, const XT *__restrict__ x) {
+  return sell_row_acc<WS, U, PIPE, STREAM, VT, XT>(op, base, w, sub, x).get();
 }
 
 template <int WS, int VAR, class VT, class XT, class Epi>
@@ -160,7 +164,31 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, co
   constexpr int GROUPS = kWarps / WS;        // slices per block per trip
   __shared__ double part[WS > 1 ? kWarps : 1][kSellC];
   double acc = 0.0;
-  if (WS == 1) {
+  AccDot2 acc2;
+  constexpr bool kF32Row = WS == 1 && std::is_same<VT, float>::value && std::is_same<XT, float>::value && has_row32<Epi>::value;
+  if constexpr (kF32Row) {
+    // mixed form, one warp per slice: the row sum, its scaling, the epilogue and the block
+    // reduction in FP32 (compensated: the product partial <y, x> is a Dot2 pair)
+    __shared__ float s_f[2];   // the scale and shift in FP32, converted once a block
+    if (threadIdx.x == 0) {
+      s_f[0] = (float)s;
+      s_f[1] = (float)sigma;
+    }
+    __syncthreads();
+    const float sf = s_f[0], sg = s_f[1];
+    const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
+    for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
+      const int row = op.perm[sl * kSellC + lane];
+      const AccDot2 r = sell_row_acc<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x);
+      float sum = __fadd_rn(r.p, r.c);
+      if (sf != 1.0f) sum = __fmul_rn(sum, sf);
+      if (row >= 0) {
+        const float xi = (sf == 1.0f) ? x[row] : __fmul_rn(x[row], sf);
+        const float yi = (sg == 0.0f) ? sum : __fmaf_rn(sg, xi, sum);
+        epi.row32(row, xi, yi, acc2);
+      }
+    }
+  } else if (WS == 1) {
     // warps advance independently (no block barrier)
     const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
     for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
@@ -198,10 +226,23 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, co
   }
   pdl_trigger();
   if constexpr (Epi::kReduce) {
-    if constexpr (is_deferred<Epi>::value)
-      block_partial(acc, slot.partials);
-    else
-      grid_reduce(acc, slot, [&](double total) { epi.finalize(total); });
+    if constexpr (is_deferred<Epi>::value && has_pair_partials<Epi>::value) {
+      if constexpr (kF32Row)
+        block_partial_pair(acc2, reinterpret_cast<float2 *>(slot.partials));
+      else
+        block_partial_split(acc, reinterpret_cast<float2 *>(slot.partials));
+    } else {
+      double b;   // the block's sum, valid in thread 0
+      if constexpr (kF32Row)
+        b = block_sum_pair(acc2);
+      else
+        b = block_sum(acc);
+      if constexpr (is_deferred<Epi>::value) {
+        if (threadIdx.x == 0) slot.partials[blockIdx.x] = b;
+      } else {
+        grid_reduce_block(b, slot, [&](double total) { epi.finalize(total); });
+      }
+    }
   }
 }
 
