@@ -291,10 +291,10 @@ def sweeps_leg(L, seed, models=("klm_vf", "hubbard_vf")):
     return out
 
 
-def _engine_run(L, models, params, lanczos_batch, workers=8, arrivals=None):
+def _engine_run(eng, models, params, arrivals=None):
     """Every model through the engine (arrivals: submission times in s, else all at once); returns
-    (wall s, {index: dg_job_result})."""
-    eng = L.Engine(workers=workers, lanczos_batch=lanczos_batch)
+    (wall s, {index: dg_job_result}).  One engine serves the warm-up and the timed runs, as a
+    serving process would."""
     res = {}
     t0 = time.perf_counter()
     for i, m in enumerate(models):
@@ -311,7 +311,6 @@ def _engine_run(L, models, params, lanczos_batch, workers=8, arrivals=None):
         for r, _ in eng.poll(256, wait_ms=50):
             res[r.id] = r
     wall = time.perf_counter() - t0
-    eng.close()
     bad = [i for i, r in res.items() if r.status != 0 or not r.converged]
     if bad:
         raise RuntimeError(f"{len(bad)} engine jobs failed, e.g. {bad[:4]}")
@@ -344,11 +343,13 @@ def batched_leg(L, args):
     E = {}
     for tag, mixed, lb in (("fp64", 0, True), ("mixed", 2, True), ("fp64_streams", 0, False), ("mixed_streams", 2, False)):
         p = L.default_params(seed=7, mixed=mixed)
-        _engine_run(L, models[:16], p, lb)                      # warm-up
+        eng = L.Engine(workers=8, lanczos_batch=lb)
+        _engine_run(eng, models[:16], p)                        # warm-up
         walls = []
         for _ in range(2):
-            wall, res = _engine_run(L, models, p, lb)
+            wall, res = _engine_run(eng, models, p)
             walls.append(wall)
+        eng.close()
         E[tag] = np.array([res[i].eig_val for i in range(len(models))])
         out[tag] = {"value": len(models) / min(walls), "wall_ms": 1e3 * min(walls), "lanczos_batch": lb,
                     "p50_ms_per_job": float(np.percentile([r.t_done_ms - r.t_submit_ms for r in res.values()], 50))}
@@ -387,8 +388,9 @@ def served_leg(L, args):
     E = {}
     for tag, mixed in (("fp64", 0), ("mixed", 2)):
         p = L.default_params(seed=11, mixed=mixed)
-        _engine_run(L, models[:16], p, True)
-        wall, res = _engine_run(L, models, p, True, arrivals=arr)
+        eng = L.Engine(workers=8, lanczos_batch=True)
+        _engine_run(eng, models[:16], p)
+        wall, res = _engine_run(eng, models, p, arrivals=arr)
         lat = np.array([res[i].t_done_ms - res[i].t_submit_ms for i in range(len(models))])
         first = min(r.t_submit_ms for r in res.values())
         last = max(r.t_done_ms for r in res.values())
@@ -398,7 +400,8 @@ def served_leg(L, args):
         # capacity: the same requests offered at 800/s for 5 s
         cap_trace = workloads.hubbard_request_trace(rate=800.0, duration=5.0, seed=2)
         cap_models = [r["model"]() for r in cap_trace]
-        wall, res = _engine_run(L, cap_models, p, True, arrivals=[r["t"] for r in cap_trace])
+        wall, res = _engine_run(eng, cap_models, p, arrivals=[r["t"] for r in cap_trace])
+        eng.close()
         first = min(r.t_submit_ms for r in res.values())
         last = max(r.t_done_ms for r in res.values())
         out[tag]["capacity_solves_per_s"] = len(cap_models) / ((last - first) * 1e-3)

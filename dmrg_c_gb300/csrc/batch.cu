@@ -45,12 +45,35 @@ enum { kScRs = 0, kScAhi, kScAlo, kScBhi, kScBlo, kScCount = 8 };
 
 constexpr int kBlzLookahead = 2;   // iterations the device runs ahead of the host's checks
 
+// The block's instance and its block within the instance: cum[k] is the first block of
+// instance k (cum[count] = the grid), searched by thread 0 and broadcast.  A per-instance table
+// instead of a per-block map keeps a rebuild of the launch tables O(instances): a per-block map
+// of a batch of 200 ED chains was ~170k entries, rebuilt and uploaded (3 MB) every time an
+// instance joined or left.
+__device__ __forceinline__ int2 blz_block(const int *__restrict__ cum, int count) {
+  __shared__ int2 s_m;
+  if (threadIdx.x == 0) {
+    const int b = (int)blockIdx.x;
+    int lo = 0, hi = count - 1;   // largest k with cum[k] <= b
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(cum + mid) <= b)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_m = make_int2(lo, b - __ldg(cum + lo));
+  }
+  __syncthreads();
+  return s_m;
+}
+
 // y = H v_b with v_b = rs w stored into V[b]; block partials of <y, v_b>.  One warp per slice,
 // one lane per row (sell.cuh); x gathered from w and scaled once per row.
 template <class VT, int U>
-__global__ void __launch_bounds__(kThreads) k_blz_apply(const BLzDesc *__restrict__ desc, const int2 *__restrict__ bmap) {
+__global__ void __launch_bounds__(kThreads) k_blz_apply(const BLzDesc *__restrict__ desc, const int *__restrict__ pcum, int count) {
   pdl_wait();
-  const int2 m = bmap[blockIdx.x];
+  const int2 m = blz_block(pcum, count);
   const BLzDesc &d = desc[m.x];
   const int b = *d.step;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -118,9 +141,9 @@ __global__ void __launch_bounds__(kThreads) k_blz_alpha(const BLzDesc *__restric
 
 // w_{b+1} = y - alpha_b v_b - beta_b v_{b-1} (FP64 arithmetic); block partials of ||w||^2.
 template <class VT>
-__global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restrict__ desc, const int2 *__restrict__ vmap) {
+__global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restrict__ desc, const int *__restrict__ vcum, int count) {
   pdl_wait();
-  const int2 m = vmap[blockIdx.x];
+  const int2 m = blz_block(vcum, count);
   const BLzDesc &d = desc[m.x];
   const int b = *d.step;
   const int i = m.y * kThreads + threadIdx.x;
@@ -291,6 +314,8 @@ bool batch_eligible(const dg_matrix *m, const dg_solver_params &p) {
 }
 
 struct BatchLanczosImpl {
+  // the pool keeps its memory while the batch lives (declared first: released last)
+  PoolHold hold;
   struct Inst {
     long tag = 0;
     const dg_matrix *m = nullptr;
@@ -351,14 +376,15 @@ struct BatchLanczosImpl {
   std::vector<std::unique_ptr<Mapped<char>>> pinned_free;
   // device table
   BLzDesc *t_desc = nullptr;
-  int2 *t_pmap = nullptr, *t_vmap = nullptr;
+  int *t_pcum = nullptr, *t_vcum = nullptr;   // first product / vector block of each instance
   int t_pgrid = 0, t_vgrid = 0, t_count = 0;
   bool dirty = true;
   // DG_BATCH_TRACE: a line per iteration on stderr (host time of the checks, split by part)
   const bool trace = std::getenv("DG_BATCH_TRACE") != nullptr;
   double t_tri = 0.0, t_leave = 0.0;
 
-  BatchLanczosImpl(int dev, int mx, std::function<void(BatchDone &)> cb) : device(dev), mixed(mx), on_done(std::move(cb)) {
+  BatchLanczosImpl(int dev, int mx, std::function<void(BatchDone &)> cb)
+      : hold(dev), device(dev), mixed(mx), on_done(std::move(cb)) {
     th = std::thread([this] { loop(); });
   }
   ~BatchLanczosImpl() {
@@ -464,7 +490,8 @@ struct BatchLanczosImpl {
 
   void rebuild(cudaStream_t st) {
     std::vector<BLzDesc> ds;
-    std::vector<int2> pm, vm;
+    std::vector<int> pc, vc;
+    int pgrid = 0, vgrid = 0;
     for (size_t k = 0; k < active.size(); ++k) {
       Inst &in = *active[k];
       const dg_matrix *m = in.m;
@@ -492,26 +519,30 @@ struct BatchLanczosImpl {
       d.hD = in.hDd;
       d.hO = in.hOd;
       ds.push_back(d);
-      for (int b = 0; b < in.pblk; ++b) pm.push_back(int2{(int)k, b});
-      for (int b = 0; b < in.vblk; ++b) vm.push_back(int2{(int)k, b});
+      pc.push_back(pgrid);
+      vc.push_back(vgrid);
+      pgrid += in.pblk;
+      vgrid += in.vblk;
     }
     if (t_desc) pool_free(t_desc, st);
-    if (t_pmap) pool_free(t_pmap, st);
-    if (t_vmap) pool_free(t_vmap, st);
+    if (t_pcum) pool_free(t_pcum, st);
+    if (t_vcum) pool_free(t_vcum, st);
     t_desc = static_cast<BLzDesc *>(pool_alloc(sizeof(BLzDesc) * ds.size(), st));
-    t_pmap = static_cast<int2 *>(pool_alloc(sizeof(int2) * pm.size(), st));
-    t_vmap = static_cast<int2 *>(pool_alloc(sizeof(int2) * vm.size(), st));
-    const size_t b0 = sizeof(BLzDesc) * ds.size(), b1 = sizeof(int2) * pm.size(), b2 = sizeof(int2) * vm.size();
+    pc.push_back(pgrid);
+    vc.push_back(vgrid);
+    t_pcum = static_cast<int *>(pool_alloc(sizeof(int) * pc.size(), st));
+    t_vcum = static_cast<int *>(pool_alloc(sizeof(int) * vc.size(), st));
+    const size_t b0 = sizeof(BLzDesc) * ds.size(), b1 = sizeof(int) * pc.size(), b2 = sizeof(int) * vc.size();
     auto buf = take_pinned(b0 + b1 + b2);
     std::memcpy(buf->h, ds.data(), b0);
-    std::memcpy(buf->h + b0, pm.data(), b1);
-    std::memcpy(buf->h + b0 + b1, vm.data(), b2);
+    std::memcpy(buf->h + b0, pc.data(), b1);
+    std::memcpy(buf->h + b0 + b1, vc.data(), b2);
     DG_CUDA(cudaMemcpyAsync(t_desc, buf->h, b0, cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(t_pmap, buf->h + b0, b1, cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(t_vmap, buf->h + b0 + b1, b2, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(t_pcum, buf->h + b0, b1, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaMemcpyAsync(t_vcum, buf->h + b0 + b1, b2, cudaMemcpyHostToDevice, st));
     staged(std::move(buf), st);
-    t_pgrid = (int)pm.size();
-    t_vgrid = (int)vm.size();
+    t_pgrid = pgrid;
+    t_vgrid = vgrid;
     t_count = (int)ds.size();
     dirty = false;
   }
@@ -519,14 +550,14 @@ struct BatchLanczosImpl {
   void launch_iteration(cudaStream_t st) {
     const int cgrid = blocks_of(t_count, kWarps);
     if (mixed)
-      launch_pdl(k_blz_apply<float, 8>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_pmap);
+      launch_pdl(k_blz_apply<float, 8>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int *)t_pcum, t_count);
     else
-      launch_pdl(k_blz_apply<double, 16>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_pmap);
+      launch_pdl(k_blz_apply<double, 16>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int *)t_pcum, t_count);
     launch_pdl(k_blz_alpha, dim3(cgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, t_count);
     if (mixed)
-      launch_pdl(k_blz_update<float>, dim3(t_vgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_vmap);
+      launch_pdl(k_blz_update<float>, dim3(t_vgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int *)t_vcum, t_count);
     else
-      launch_pdl(k_blz_update<double>, dim3(t_vgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int2 *)t_vmap);
+      launch_pdl(k_blz_update<double>, dim3(t_vgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int *)t_vcum, t_count);
     launch_pdl(k_blz_beta, dim3(cgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, t_count);
     DG_CUDA(cudaGetLastError());
     iters.fetch_add(1);
@@ -879,8 +910,8 @@ struct BatchLanczosImpl {
       }
     }
     if (t_desc) pool_free(t_desc, st);
-    if (t_pmap) pool_free(t_pmap, st);
-    if (t_vmap) pool_free(t_vmap, st);
+    if (t_pcum) pool_free(t_pcum, st);
+    if (t_vcum) pool_free(t_vcum, st);
     cudaStreamSynchronize(st);
     reap(true);
   }

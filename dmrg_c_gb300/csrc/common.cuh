@@ -73,6 +73,15 @@ int sm_count();
 // stream before returning, so a buffer is never in use on another stream when it is freed.
 // ---------------------------------------------------------------------------------
 cudaMemPool_t device_pool();
+// Keep (acquire) / stop keeping (release) every byte the device's pool has mapped; counted.
+void pool_hold(int device, bool acquire);
+struct PoolHold {
+  int device;
+  explicit PoolHold(int d) : device(d) { pool_hold(device, true); }
+  ~PoolHold() { pool_hold(device, false); }
+  PoolHold(const PoolHold &) = delete;
+  PoolHold &operator=(const PoolHold &) = delete;
+};
 void *pool_alloc(size_t bytes, cudaStream_t st);
 void pool_free(void *p, cudaStream_t st);
 

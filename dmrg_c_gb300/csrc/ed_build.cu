@@ -12,12 +12,23 @@
 // One thread per basis row generates the row's elements from the model's term list in the
 // reference order, merging a repeated target code by summation in generation order into a
 // code-sorted row buffer (exactly the accumulation EXACT_MAKE_ELEM_*.c perform), then maps
-// each code to its basis index by binary search and keeps it when |v| > 1e-15 or it is the
-// diagonal (GET_HAM.c:33-35).  Pass 1 counts, a device scan turns counts into row offsets,
-// pass 2 fills.  Products and sums use explicitly rounded intrinsics (no FMA contraction),
-// so every value is bitwise the one the reference computes.
+// each code to its basis index and keeps it when |v| > 1e-15 or it is the diagonal
+// (GET_HAM.c:33-35).  Pass 1 counts, a device scan turns counts into row offsets, pass 2 fills.
+// Products and sums use explicitly rounded intrinsics (no FMA contraction), so every value is
+// bitwise the one the reference computes.
+//
+// Ranking a target.  The reference searches the sorted basis for each generated code.  Here the
+// row's own index b is its rank, and a term that changes the digits of sites lo <= hi changes
+// only the rank terms of sites lo..hi (the rank of a code is sum_s T_s, T_s counting the sector
+// codes that agree above site s and have a smaller digit at s, from the digit-count table and the
+// quantum-number sum of sites 0..s).  A target whose quantum numbers leave the sector has no
+// rank: the reference's search does not find it and drops it; it is skipped here.  So each
+// element costs a few table reads instead of a ~20-step dependent search, with the same columns.
+// The fermion sign of a hopping term reads a per-row prefix count of electrons instead of
+// summing sites.  Models with a two-site term whose sites coincide keep the search.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "dmrg_gb300_ed.h"
@@ -30,6 +41,7 @@ namespace {
 struct EdTermDev {
   int kind, site1, site2, op1, op2, sign_mode;
   double coef;
+  int voff, nnz2;   // the term's element values in EdDev::tval: [voff + i1 * nnz2 + i2] (ranked rows)
 };
 
 // Everything the row kernel reads, in device memory.
@@ -44,16 +56,46 @@ struct EdDev {
   const double *op_val;
   const int *n_ele;          // d entries, or null
   double zero;               // drop threshold, 10^-15
+  // the sector's digit-count table (plan_model's cnt) and quantum numbers, for ranking targets
+  const int64_t *cnt;
+  const int *a1, *a2;
+  int R1, R2, off1, off2;
+  // ranked rows: each term's element values before the fermion sign, coef * v1 (on-site) and
+  // (coef * v1) * v2 (inter-site), rounded as the row loop rounds them; a sign of -1 only flips
+  // the sign bit, so the products are exact to the reference's and need no FP64 multiply per
+  // element
+  const double *tval;
 };
+
+__device__ __forceinline__ double flip_sign(double v, bool neg) {
+  return __longlong_as_double(__double_as_longlong(v) ^ (neg ? (long long)0x8000000000000000ull : 0ll));
+}
+
+// |v| > z for finite v and z >= 0, on the integer pipe.
+__device__ __forceinline__ bool abs_above(double v, double z) {
+  return (unsigned long long)(__double_as_longlong(v) & 0x7fffffffffffffffll) > (unsigned long long)__double_as_longlong(z);
+}
+
+// T_s for digit `dig` at site s with quantum-number sums (b1, b2) over sites 0..s: the sector
+// codes that agree with it above s and have a smaller digit at s (k_ed_unrank's walk, summed).
+__device__ __forceinline__ int rank_term(const EdDev &m, int s, int dig, int b1, int b2) {
+  long t = 0;
+  for (int l = 0; l < dig; ++l) {
+    const int q1 = b1 - __ldg(m.a1 + l) + m.off1, q2 = b2 - __ldg(m.a2 + l) + m.off2;
+    if (q1 >= 0 && q1 < m.R1 && q2 >= 0 && q2 < m.R2) t += __ldg(m.cnt + ((long)s * m.R1 + q1) * m.R2 + q2);
+  }
+  return (int)t;   // < dim <= 2^31 - 1
+}
 
 __device__ __forceinline__ int digit(const EdDev &m, int64_t code, int site) {
   if (m.shift >= 0) return (int)((code >> (m.shift * site)) & (m.d - 1));
   return (int)((code / m.pw[site]) % m.d);
 }
 
-// Generation-order accumulation into a code-sorted buffer (cf. acc in EXACT_MAKE_ELEM_ON.c:19-28).
-template <int CAP>
-__device__ __forceinline__ bool acc_add(int64_t *code, double *val, int &n, int64_t c, double v) {
+// Generation-order accumulation into a key-sorted buffer (cf. acc in EXACT_MAKE_ELEM_ON.c:19-28);
+// the key is the target's code, or its rank (the same order).
+template <int CAP, class K>
+__device__ __forceinline__ bool acc_add(K *code, double *val, int &n, K c, double v) {
   int lo = 0, hi = n - 1;
   while (lo <= hi) {
     const int mid = (lo + hi) >> 1;
@@ -121,7 +163,7 @@ __device__ bool ed_row(const EdDev &m, int64_t code, int64_t *rc, double *rv, in
       const int *orow = m.op_row + t.op1 * d1;
       for (int it = orow[l]; it < orow[l + 1]; ++it) {
         const int64_t target = code + (int64_t)(m.op_col[f + it] - l) * ds;
-        if (!acc_add<CAP>(rc, rv, n, target, __dmul_rn(t.coef, m.op_val[f + it]))) return false;
+        if (!acc_add<CAP, int64_t>(rc, rv, n, target, __dmul_rn(t.coef, m.op_val[f + it]))) return false;
       }
     } else {
       const int l1 = digit(m, code, t.site1), l2 = digit(m, code, t.site2);
@@ -134,12 +176,134 @@ __device__ bool ed_row(const EdDev &m, int64_t code, int64_t *rc, double *rv, in
         const int64_t c1 = code + (int64_t)(m.op_col[f1 + i1] - l1) * p1;
         for (int i2 = r2[l2]; i2 < r2[l2 + 1]; ++i2) {
           const int64_t target = c1 + (int64_t)(m.op_col[f2 + i2] - l2) * p2;
-          if (!acc_add<CAP>(rc, rv, n, target, __dmul_rn(a, m.op_val[f2 + i2]))) return false;
+          if (!acc_add<CAP, int64_t>(rc, rv, n, target, __dmul_rn(a, m.op_val[f2 + i2]))) return false;
         }
       }
     }
   }
   return true;
+}
+
+// Row b's merged off-diagonal elements into (rank, val), rank-sorted, and its diagonal into
+// (diag, has_diag), all generated in ed_row's order (every target's sum in generation order);
+// returns false on buffer overflow.  LM >= L.
+template <int CAP, int LM>
+__device__ bool ed_row_ranked(const EdDev &m, int b, int64_t code, int *rc, double *rv, int &n, double &diag, bool &has_diag) {
+  n = 0;
+  diag = 0.0;
+  has_diag = false;
+  auto add = [&](int target, double v) {
+    if (target == b) {
+      diag = has_diag ? __dadd_rn(diag, v) : v;
+      has_diag = true;
+      return true;
+    }
+    return acc_add<CAP, int>(rc, rv, n, target, v);
+  };
+  signed char dg[LM];
+  unsigned char nep[LM + 1];   // electrons on sites [0, s)
+  int b1[LM], b2[LM], T[LM];
+  {
+    int p1 = 0, p2 = 0, ne = 0;
+    for (int s = 0; s < m.L; ++s) {
+      const int l = digit(m, code, s);
+      dg[s] = (signed char)l;
+      nep[s] = (unsigned char)ne;
+      if (m.n_ele) ne += __ldg(m.n_ele + l);
+      p1 += __ldg(m.a1 + l);
+      p2 += __ldg(m.a2 + l);
+      b1[s] = p1;
+      b2[s] = p2;
+      T[s] = rank_term(m, s, l, p1, p2);
+    }
+    nep[m.L] = (unsigned char)ne;
+  }
+  const int d1 = m.d + 1;
+  for (int k = 0; k < m.n_terms; ++k) {
+    const EdTermDev t = m.terms[k];
+    if (t.kind == DG_ED_ONSITE) {
+      const int s1 = t.site1, l = dg[s1];
+      const int f = m.op_first[t.op1];
+      const int *orow = m.op_row + t.op1 * d1;
+      const int al1 = __ldg(m.a1 + l), al2 = __ldg(m.a2 + l);
+      for (int it = orow[l]; it < orow[l + 1]; ++it) {
+        const int nl = m.op_col[f + it];
+        if (__ldg(m.a1 + nl) != al1 || __ldg(m.a2 + nl) != al2) continue;   // leaves the sector
+        const int target = b + rank_term(m, s1, nl, b1[s1], b2[s1]) - T[s1];
+        if (!add(target, __ldg(m.tval + t.voff + it))) return false;
+      }
+    } else {
+      const int s1 = t.site1, s2 = t.site2, l1 = dg[s1], l2 = dg[s2];
+      bool neg = false;
+      if (t.sign_mode != DG_ED_SIGN_NONE && m.n_ele) {
+        const int ne = (t.sign_mode == DG_ED_SIGN_SITE1 || t.sign_mode == DG_ED_SIGN_SITE1_NEG) ? __ldg(m.n_ele + l1) : nep[s2];
+        neg = (ne % 2 != 1);   // sign -1 when the count is even
+        if (t.sign_mode == DG_ED_SIGN_SITE1_NEG || t.sign_mode == DG_ED_SIGN_RANGE_NEG) neg = !neg;
+      }
+      const int f1 = m.op_first[t.op1], f2 = m.op_first[t.op2];
+      const int *r1 = m.op_row + t.op1 * d1, *r2 = m.op_row + t.op2 * d1;
+      const bool s1lo = s1 < s2;
+      const int lo = s1lo ? s1 : s2, hi = s1lo ? s2 : s1;
+      for (int i1 = r1[l1]; i1 < r1[l1 + 1]; ++i1) {
+        const int n1 = m.op_col[f1 + i1];
+        const int e1 = __ldg(m.a1 + n1) - __ldg(m.a1 + l1), e2 = __ldg(m.a2 + n1) - __ldg(m.a2 + l1);
+        for (int i2 = r2[l2]; i2 < r2[l2 + 1]; ++i2) {
+          const int n2 = m.op_col[f2 + i2];
+          const int g1 = __ldg(m.a1 + n2) - __ldg(m.a1 + l2), g2 = __ldg(m.a2 + n2) - __ldg(m.a2 + l2);
+          if (e1 + g1 != 0 || e2 + g2 != 0) continue;   // leaves the sector
+          // the lower site's change shifts the sums of sites lo..hi-1; at hi they are restored
+          const int nlo = s1lo ? n1 : n2, nhi = s1lo ? n2 : n1;
+          const int dl1 = s1lo ? e1 : g1, dl2 = s1lo ? e2 : g2;
+          int target = b + rank_term(m, lo, nlo, b1[lo] + dl1, b2[lo] + dl2) - T[lo];
+          for (int s = lo + 1; s < hi; ++s) target += rank_term(m, s, dg[s], b1[s] + dl1, b2[s] + dl2) - T[s];
+          target += rank_term(m, hi, nhi, b1[hi], b2[hi]) - T[hi];
+          if (!add(target, flip_sign(__ldg(m.tval + t.voff + i1 * t.nnz2 + i2), neg))) return false;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+// Pass 1 (row != null: pass 2), ranked rows (LM > 0: sites <= LM) or searched codes (LM = 0).
+// err: 1 row buffer overflow, 2 count mismatch.
+template <int CAP, int LM>
+__global__ void __launch_bounds__(128) k_ed_rows_ranked(EdDev m, const int64_t *__restrict__ basis, long dim,
+                                                        long long *__restrict__ counts, const int64_t *__restrict__ row,
+                                                        int *__restrict__ col, double *__restrict__ val, int *err) {
+  int rc[CAP];
+  double rv[CAP];
+  for (long b = blockIdx.x * (long)blockDim.x + threadIdx.x; b < dim; b += (long)gridDim.x * blockDim.x) {
+    int n = 0;
+    double diag;
+    bool has_diag;
+    if (!ed_row_ranked<CAP, LM>(m, (int)b, basis[b], rc, rv, n, diag, has_diag)) {
+      atomicExch(err, 1);
+      if (counts) counts[b] = 0;
+      continue;
+    }
+    long long cnt = 0;
+    const int64_t start = row ? row[b] : 0, end = row ? row[b + 1] : 0;
+    auto put = [&](int c, double v) {
+      if (row) {
+        const int64_t pos = start + cnt;
+        if (pos < end) {
+          col[pos] = c;
+          val[pos] = v;
+        }
+      }
+      ++cnt;
+    };
+    // column order: the off-diagonals below b, the diagonal (always kept when generated), the rest
+    int i = 0;
+    for (; i < n && rc[i] < (int)b; ++i)
+      if (abs_above(rv[i], m.zero)) put(rc[i], rv[i]);
+    if (has_diag) put((int)b, diag);
+    for (; i < n; ++i)
+      if (abs_above(rv[i], m.zero)) put(rc[i], rv[i]);
+    if (counts) counts[b] = cnt;
+    if (row && start + cnt != end) atomicExch(err, 2);
+  }
 }
 
 // Pass 1 (row != null: pass 2).  err: 1 row buffer overflow, 2 count mismatch.
@@ -215,6 +379,7 @@ struct EdPlan {
   std::vector<int64_t> pw;          // L + 1
   long dim = 0;
   int cap = 0;                      // row buffer needed
+  bool ranked = true;               // targets ranked from the row's index (no two-site term on one site)
 };
 
 void plan_model(const dg_ed_model *m, EdPlan &p) {
@@ -298,12 +463,17 @@ void plan_model(const dg_ed_model *m, EdPlan &p) {
       DG_REQUIRE(t.site2 >= 0 && t.site2 < L, DG_ERR_ARG, "term %d: site2 out of range", k);
       DG_REQUIRE(t.op2 >= 0 && t.op2 < m->n_ops, DG_ERR_ARG, "term %d: op2 out of range", k);
       DG_REQUIRE(t.sign_mode == DG_ED_SIGN_NONE || m->n_ele, DG_ERR_ARG, "term %d: fermion sign without n_ele", k);
+      if (t.site1 == t.site2) p.ranked = false;
       cap += (long)width(t.op1) * width(t.op2);
     } else {
       cap += width(t.op1);
     }
   }
   p.cap = (int)std::min(cap, 1L << 20);
+  if (L > 64) p.ranked = false;
+  if (m->n_ele)
+    for (int l = 0; l < d; ++l)
+      if (m->n_ele[l] < 0 || m->n_ele[l] * L > 255) p.ranked = false;   // per-row prefix counts are bytes
 }
 
 }  // namespace
@@ -321,23 +491,29 @@ namespace dg {
 namespace {
 
 template <int CAP>
-void launch_rows(const EdDev &m, const int64_t *basis, long dim, long long *counts, const int64_t *row, int *col,
+void launch_rows(const EdDev &m, bool ranked, const int64_t *basis, long dim, long long *counts, const int64_t *row, int *col,
                  double *val, int *err, cudaStream_t st) {
-  const long blocks = std::min<long>((dim + 127) / 128, (long)sm_count() * 16);
-  k_ed_rows<CAP><<<(int)std::max(1L, blocks), 128, 0, st>>>(m, basis, dim, counts, row, col, val, err); ::dg::count_launch();
+  const long blocks = std::max(1L, std::min<long>((dim + 127) / 128, (long)sm_count() * 16));
+  if (ranked && m.L <= 32)
+    k_ed_rows_ranked<CAP, 32><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
+  else if (ranked)
+    k_ed_rows_ranked<CAP, 64><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
+  else
+    k_ed_rows<CAP><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
+  ::dg::count_launch();
   DG_CUDA(cudaGetLastError());
 }
 
-void rows_pass(int cap, const EdDev &m, const int64_t *basis, long dim, long long *counts, const int64_t *row, int *col,
-               double *val, int *err, cudaStream_t st) {
+void rows_pass(int cap, const EdDev &m, bool ranked, const int64_t *basis, long dim, long long *counts, const int64_t *row,
+               int *col, double *val, int *err, cudaStream_t st) {
   if (cap <= 32)
-    launch_rows<32>(m, basis, dim, counts, row, col, val, err, st);
+    launch_rows<32>(m, ranked, basis, dim, counts, row, col, val, err, st);
   else if (cap <= 64)
-    launch_rows<64>(m, basis, dim, counts, row, col, val, err, st);
+    launch_rows<64>(m, ranked, basis, dim, counts, row, col, val, err, st);
   else if (cap <= 128)
-    launch_rows<128>(m, basis, dim, counts, row, col, val, err, st);
+    launch_rows<128>(m, ranked, basis, dim, counts, row, col, val, err, st);
   else
-    launch_rows<256>(m, basis, dim, counts, row, col, val, err, st);
+    launch_rows<256>(m, ranked, basis, dim, counts, row, col, val, err, st);
 }
 
 dg_ed *ed_build(const dg_ed_model *model) {
@@ -350,12 +526,31 @@ dg_ed *ed_build(const dg_ed_model *model) {
   const int L = p.L, d = p.d;
 
   // device copies of the model
+  // Each term's element values before the fermion sign, rounded as ed_row rounds them: coef * v1
+  // (on-site); (coef * v1) * v2 (inter-site; ed_row forms (sign * coef) * v1 first, and a
+  // sign of +-1 commutes exactly with rounded products).  Plain IEEE double multiplies.
   std::vector<EdTermDev> terms(model->n_terms);
+  std::vector<double> tval;
   for (int k = 0; k < model->n_terms; ++k) {
     const dg_ed_term &t = model->terms[k];
-    terms[k] = EdTermDev{t.kind, t.site1, t.kind == DG_ED_INTER ? t.site2 : 0, t.op1,
-                         t.kind == DG_ED_INTER ? t.op2 : 0, t.sign_mode, t.coef};
+    const CRS1 &O1 = model->ops[t.op1];
+    const int inter = t.kind == DG_ED_INTER;
+    const long n1 = O1.Row[d], n2 = inter ? model->ops[t.op2].Row[d] : 1;
+    terms[k] = EdTermDev{t.kind, t.site1, inter ? t.site2 : 0, t.op1, inter ? t.op2 : 0, t.sign_mode, t.coef,
+                         (int)tval.size(), (int)n2};
+    for (long i1 = 0; i1 < n1; ++i1) {
+      const double a = t.coef * O1.Val[i1];   // products only: nothing for FMA contraction
+      if (!inter) {
+        tval.push_back(a);
+        continue;
+      }
+      const CRS1 &O2 = model->ops[t.op2];
+      for (long i2 = 0; i2 < n2; ++i2) {
+        tval.push_back(a * O2.Val[i2]);
+      }
+    }
   }
+  if (tval.empty()) tval.push_back(0.0);
   std::vector<int> op_row((size_t)model->n_ops * (d + 1)), op_first(model->n_ops), op_col;
   std::vector<double> op_val;
   for (int o = 0; o < model->n_ops; ++o) {
@@ -376,7 +571,7 @@ dg_ed *ed_build(const dg_ed_model *model) {
 
   DevBuf<int64_t> cnt(p.cnt.size()), pw(p.pw.size());
   DevBuf<int> a1(d), a2(d), orow(op_row.size()), ofirst(op_first.size()), ocol(op_col.size()), ne(std::max(d, 1)), err(1);
-  DevBuf<double> oval(op_val.size());
+  DevBuf<double> oval(op_val.size()), tv(tval.size());
   DevBuf<EdTermDev> tdev(std::max<size_t>(terms.size(), 1));
   DG_CUDA(cudaMemcpyAsync(cnt.get(), p.cnt.data(), sizeof(int64_t) * p.cnt.size(), cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemcpyAsync(pw.get(), p.pw.data(), sizeof(int64_t) * p.pw.size(), cudaMemcpyHostToDevice, st));
@@ -389,6 +584,7 @@ dg_ed *ed_build(const dg_ed_model *model) {
   if (!terms.empty())
     DG_CUDA(cudaMemcpyAsync(tdev.get(), terms.data(), sizeof(EdTermDev) * terms.size(), cudaMemcpyHostToDevice, st));
   if (!n_ele.empty()) DG_CUDA(cudaMemcpyAsync(ne.get(), n_ele.data(), sizeof(int) * d, cudaMemcpyHostToDevice, st));
+  DG_CUDA(cudaMemcpyAsync(tv.get(), tval.data(), sizeof(double) * tval.size(), cudaMemcpyHostToDevice, st));
   DG_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(int), st));
 
   dg_ed *e = new dg_ed();
@@ -405,10 +601,12 @@ dg_ed *ed_build(const dg_ed_model *model) {
     int shift = -1;
     for (int k = 0; k < 7; ++k)
       if ((1 << k) == d) shift = k;
-    EdDev m{L, d, model->n_terms, shift, pw.get(), tdev.get(), orow.get(), ofirst.get(), ocol.get(), oval.get(),
-            n_ele.empty() ? nullptr : ne.get(), std::pow(10.0, -15.0)};
+    EdDev m{L,         d,          model->n_terms, shift,     pw.get(),  tdev.get(),
+            orow.get(), ofirst.get(), ocol.get(),     oval.get(), n_ele.empty() ? nullptr : ne.get(),
+            std::pow(10.0, -15.0), cnt.get(), a1.get(), a2.get(), p.R1, p.R2, p.off1, p.off2, tv.get()};
+    const bool ranked = p.ranked && std::getenv("DG_ED_SEARCH") == nullptr;
     DevBuf<long long> counts(dim), tmp((dim + kScanTile - 1) / kScanTile + 2);
-    rows_pass(p.cap, m, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
+    rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
     e->row.alloc(dim + 1);
     exclusive_scan(counts.get(), dim, e->row.get(), tmp.get(), st);
     int64_t total = 0;
@@ -420,7 +618,7 @@ dg_ed *ed_build(const dg_ed_model *model) {
     e->nnz = total;
     e->col.alloc(total);
     e->val.alloc(total);
-    rows_pass(p.cap, m, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
+    rows_pass(p.cap, m, ranked, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
     DG_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
     DG_REQUIRE(herr == 0, DG_ERR_INTERNAL, "ED fill pass disagreed with the count pass (%d)", herr);
@@ -483,7 +681,7 @@ int dg_ed_matrix(const dg_ed *e, int values, dg_matrix **out) {
     require_device();
     DG_REQUIRE(e && out, DG_ERR_ARG, "null argument");
     *out = matrix_from_device((int)e->dim, e->nnz, reinterpret_cast<const long *>(e->row.get()), e->col.get(), e->val.get(),
-                              DG_STORE_FULL, values, stream());
+                              DG_STORE_FULL, values, stream(), true);
   });
 }
 

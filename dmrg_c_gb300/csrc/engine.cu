@@ -120,6 +120,8 @@ struct Parked {
 };
 
 struct dg_engine {
+  // the pool keeps its memory while the engine lives (jobs allocate and free per request)
+  std::unique_ptr<dg::PoolHold> hold;
   dg_engine_config cfg{};
   int device = 0;
   size_t budget = 0;
@@ -304,6 +306,7 @@ int dg_engine_create(const dg_engine_config *cfg, dg_engine **out) {
     if (e->cfg.workers <= 0) e->cfg.workers = 8;
     DG_REQUIRE(e->cfg.workers <= 256, DG_ERR_ARG, "at most 256 workers");
     DG_CUDA(cudaGetDevice(&e->device));
+    e->hold = std::make_unique<dg::PoolHold>(e->device);
     size_t free_b = 0, total_b = 0;
     DG_CUDA(cudaMemGetInfo(&free_b, &total_b));
     e->budget = e->cfg.hbm_budget ? e->cfg.hbm_budget : (size_t)(0.8 * (double)free_b);

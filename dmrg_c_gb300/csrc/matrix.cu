@@ -348,7 +348,7 @@ void choose_sell_shape(int nslices, long stored, int *ws, int *grid) {
 }
 
 dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *col_d, const double *val_d, int storage,
-                              int values, cudaStream_t st) {
+                              int values, cudaStream_t st, bool trusted) {
   DG_REQUIRE(n > 0, DG_ERR_ARG, "matrix dimension must be positive (n=%d)", n);
   DG_REQUIRE(storage == DG_STORE_FULL || storage == DG_STORE_LOWER_DIAG_LAST, DG_ERR_ARG, "unknown storage %d", storage);
   DG_REQUIRE(values >= DG_VALUES_F64 && values <= DG_VALUES_BOTH, DG_ERR_ARG, "unknown values flag %d", values);
@@ -356,23 +356,25 @@ dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *
   const int lower = storage == DG_STORE_LOWER_DIAG_LAST;
   const int g = vector_grid(n), gw = warp_grid(n);
 
-  DevBuf<int> bad(1);
-  int big = 0x7fffffff;
-  DG_CUDA(cudaMemcpyAsync(bad.get(), &big, sizeof(int), cudaMemcpyHostToDevice, st));
-  k_validate<<<gw, kThreads, 0, st>>>(row, col_d, n, nnz_in, lower, bad.get()); ::dg::count_launch();
-  DG_CUDA(cudaGetLastError());
-  int first_bad = 0;
-  int64_t ends[2];
-  DG_CUDA(cudaMemcpyAsync(&first_bad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
-  DG_CUDA(cudaMemcpyAsync(&ends[0], row, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  DG_CUDA(cudaMemcpyAsync(&ends[1], row + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  DG_CUDA(cudaStreamSynchronize(st));
-  DG_REQUIRE(ends[0] == 0 && ends[1] == nnz_in, DG_ERR_MATRIX, "CRS row offsets must run from 0 to nnz (got %lld..%lld, nnz=%ld)",
-             (long long)ends[0], (long long)ends[1], nnz_in);
-  DG_REQUIRE(first_bad == big, DG_ERR_MATRIX,
-             lower ? "row %d violates the lower-triangle layout (non-empty row, increasing columns < row, diagonal last)"
-                   : "row %d has a column outside [0, n) or decreasing offsets",
-             first_bad);
+  if (!trusted) {
+    DevBuf<int> bad(1);
+    int big = 0x7fffffff;
+    DG_CUDA(cudaMemcpyAsync(bad.get(), &big, sizeof(int), cudaMemcpyHostToDevice, st));
+    k_validate<<<gw, kThreads, 0, st>>>(row, col_d, n, nnz_in, lower, bad.get()); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    int first_bad = 0;
+    int64_t ends[2];
+    DG_CUDA(cudaMemcpyAsync(&first_bad, bad.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaMemcpyAsync(&ends[0], row, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaMemcpyAsync(&ends[1], row + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    DG_REQUIRE(ends[0] == 0 && ends[1] == nnz_in, DG_ERR_MATRIX,
+               "CRS row offsets must run from 0 to nnz (got %lld..%lld, nnz=%ld)", (long long)ends[0], (long long)ends[1], nnz_in);
+    DG_REQUIRE(first_bad == big, DG_ERR_MATRIX,
+               lower ? "row %d violates the lower-triangle layout (non-empty row, increasing columns < row, diagonal last)"
+                     : "row %d has a column outside [0, n) or decreasing offsets",
+               first_bad);
+  }
 
   dg_matrix *m = new dg_matrix();
   m->n = n;

@@ -116,8 +116,11 @@ void launch_validate(const int64_t *row, const int *col, int n, long nnz, int lo
 // Build the sliced-ELL copy of a device CRS with the given row-sorting window.
 void build_sell(dg_matrix *m, cudaStream_t st, int window);
 
-// Build a dg_matrix from device arrays (copied / expanded).  Throws on error.
+// Build a dg_matrix from device arrays (copied / expanded).  Throws on error.  trusted: the
+// arrays come from this library's own builders (ED, superblock), valid by construction, and the
+// device check of the layout (a kernel and a host synchronisation) is skipped; arrays from a
+// caller are always checked.
 dg_matrix *matrix_from_device(int n, long nnz_in, const long *row_d, const int *col_d, const double *val_d, int storage,
-                              int values, cudaStream_t st);
+                              int values, cudaStream_t st, bool trusted = false);
 
 }  // namespace dg

@@ -441,7 +441,7 @@ int dg_sb_matrix(const dg_sb *s, int values, dg_matrix **out) {
     require_device();
     DG_REQUIRE(s && out, DG_ERR_ARG, "null argument");
     *out = matrix_from_device(s->n, s->nnz, reinterpret_cast<const long *>(s->row.get()), s->col.get(), s->val.get(),
-                              DG_STORE_LOWER_DIAG_LAST, values, stream());
+                              DG_STORE_LOWER_DIAG_LAST, values, stream(), true);
   });
 }
 

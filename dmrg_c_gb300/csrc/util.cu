@@ -78,6 +78,34 @@ cudaMemPool_t device_pool() {
   return g_pools[dev];
 }
 
+// Pool holds: while any is active on a device, its pool keeps all the memory it has mapped
+// across synchronisations (release threshold unbounded), so that allocations of a batch or an
+// engine whose working set exceeds the default keep do not unmap and map physical memory each
+// time another thread synchronises.  The last hold restores the keep and trims to it.
+namespace {
+int g_pool_holds[kMaxPoolDevices] = {0};
+}
+void pool_hold(int device, bool acquire) {
+  if (device < 0 || device >= kMaxPoolDevices) return;
+  int prev = 0;
+  DG_CUDA(cudaGetDevice(&prev));
+  DG_CUDA(cudaSetDevice(device));
+  cudaMemPool_t pool = device_pool();
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  int &h = g_pool_holds[device];
+  if (acquire) {
+    if (h++ == 0) {
+      uint64_t all = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &all);
+    }
+  } else if (h > 0 && --h == 0) {
+    uint64_t keep = pool_keep_bytes();
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaMemPoolTrimTo(pool, keep);
+  }
+  cudaSetDevice(prev);
+}
+
 void *pool_alloc(size_t bytes, cudaStream_t st) {
   void *p = nullptr;
   DG_CUDA(cudaMallocFromPoolAsync(&p, bytes ? bytes : 1, device_pool(), st));

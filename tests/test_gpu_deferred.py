@@ -1,10 +1,13 @@
-"""Reductions finished by the consuming kernel give bitwise the values of the last-block form.
+"""Reductions finished by the consuming kernel against the last-block form.
 
 The Lanczos step can leave <y,v> and <w,w> to the kernels that consume them (every consumer
 block sums the producer's block partials in the same fixed order); DG_DEFER_REDUCTIONS=0 / =1
-forces either form at the same launch grid, so energies, vectors and step counts must match
-bit for bit.  CG and the refinement always use the consumer form; their parity against the
-reference is covered by the golden tests.
+forces either form at the same launch grid.  In the FP64 form both sum the same double partials
+in the same order, so energies, vectors and step counts must match bit for bit.  The mixed form's
+consumer sums compensated FP32 pairs (the last-block form converts each block's pair to double
+first), so there the step counts must match and the energies agree to rounding.  CG and the
+refinement always use the consumer form; their parity against the reference is covered by the
+golden tests.
 """
 import numpy as np
 import pytest
@@ -29,8 +32,12 @@ def test_deferred_lanczos_bitwise(gpu, monkeypatch, mixed):
     e0, v0, l0, c0 = _solve(gpu, low, mixed, g["guess"], monkeypatch, "0")
     e1, v1, l1, c1 = _solve(gpu, low, mixed, g["guess"], monkeypatch, "1")
     assert (l0, c0) == (l1, c1)
-    assert e0 == e1
-    assert np.array_equal(v0, v1)
+    if mixed == 0:
+        assert e0 == e1
+        assert np.array_equal(v0, v1)
+    else:
+        assert abs(e0 - e1) <= 1e-13 * abs(e0)
+        assert abs(v0 @ v1) >= 1 - 1e-12
 
 
 def test_deferred_superblock_bitwise(gpu, monkeypatch):
