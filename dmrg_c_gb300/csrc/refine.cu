@@ -97,26 +97,127 @@ __global__ void __launch_bounds__(kThreads) k_refine32_direction(int n, const fl
   block_partial_pair(acc, gout);
 }
 
+__global__ void __launch_bounds__(kThreads) k_refine_resid(int n, const double *__restrict__ y, const double *__restrict__ psi,
+                                                           double *__restrict__ r, double *rs, double *pa, double *pb,
+                                                           unsigned *ticket) {
+  const double theta = rs[kRsTheta];
+  double a1 = 0.0, a2 = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double ri = y[i] - theta * psi[i];
+    r[i] = ri;
+    a1 += fabs(ri);
+    a2 += ri * ri;
+  }
+  // two sums: block partials of each, then the last block sums both in block order
+  __shared__ bool s_last;
+  const double b1 = block_sum(a1);
+  const double b2 = block_sum(a2);
+  if (threadIdx.x == 0) {
+    pa[blockIdx.x] = b1;
+    pb[blockIdx.x] = b2;
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double t1 = 0.0, t2 = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+    t1 += __ldcg(pa + i);
+    t2 += __ldcg(pb + i);
+  }
+  t1 = block_sum(t1);
+  t2 = block_sum(t2);
+  if (threadIdx.x == 0) {
+    rs[kRsL1] = t1;
+    rs[kRsRn2] = t2;
+    *ticket = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_refine32_start(int n, const double *__restrict__ r, const double *__restrict__ psi,
+                                                            float *__restrict__ res32, float *__restrict__ t32, double tau2,
+                                                            Scalars *S, Progress *prog, double *rs, RedSlot slot) {
+  const double c = rs[kRsC];
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double v = c * psi[i] - r[i];
+    res32[i] = (float)v;
+    t32[i] = 0.0f;
+    acc += v * v;
+  }
+  grid_reduce(acc, slot, [&](double rr0) {
+    S->rrs_ref[1] = rr0;   // enters iteration 1
+    S->rr32[1] = (float)rr0;
+    S->thr = tau2 * rr0;
+    S->iters = 0;
+    rs[kRsDegen] = 0.0;   // the step's flag: set below, or by k_refine_orth / k_refine_rr
+    if (rr0 > 0.0) {
+      S->done = 0;
+    } else {
+      S->done = 1;   // no correction to solve for: the CG kernels return at once
+      rs[kRsDegen] = 1.0;
+      prog->done = 1;
+    }
+  });
+}
+
+__global__ void __launch_bounds__(kThreads) k_refine_orth(int n, double *__restrict__ t, const double *__restrict__ psi, double *rs,
+                                                         RedSlot slot) {
+  const double ct = rs[kRsCt];
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double v = t[i] - ct * psi[i];
+    t[i] = v;
+    acc += v * v;
+  }
+  grid_reduce(acc, slot, [&](double nt2) {
+    if (nt2 > 0.0) {
+      rs[kRsInv] = 1.0 / sqrt(nt2);
+    } else {
+      rs[kRsInv] = 0.0;
+      rs[kRsDegen] = 1.0;
+    }
+  });
+}
+
+__global__ void __launch_bounds__(kThreads) k_scale_by(int n, const double *s, double *__restrict__ x) {
+  const double v = *s;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) x[i] *= v;
+}
+
+__global__ void k_refine_rr(double *rs) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double a11 = rs[kRsTheta], a22 = rs[kRsA22], a12 = rs[kRsA12];
+  const double half = 0.5 * (a11 - a22);
+  const double lam = 0.5 * (a11 + a22) - sqrt(half * half + a12 * a12);
+  double c1 = a12, c2 = lam - a11;                 // (A - lam) [c1 c2]^T = 0, first row
+  if (fabs(lam - a22) > fabs(c2)) {                // better conditioned second row
+    c1 = lam - a22;
+    c2 = a12;
+  }
+  const double nc = sqrt(c1 * c1 + c2 * c2);
+  if (rs[kRsDegen] != 0.0 || !(nc > 0.0)) {
+    rs[kRsC1] = 1.0;
+    rs[kRsC2] = 0.0;
+    rs[kRsDegen] = 1.0;
+    return;
+  }
+  rs[kRsC1] = c1 / nc;
+  rs[kRsC2] = c2 / nc;
+  rs[kRsTheta] = lam;
+}
+
+__global__ void __launch_bounds__(kThreads) k_refine_combine(int n, const double *rs, const double *__restrict__ x,
+                                                            double *__restrict__ y) {
+  const double c1 = rs[kRsC1], c2 = rs[kRsC2];
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) y[i] = c2 * x[i] + c1 * y[i];
+}
+
 __global__ void __launch_bounds__(kThreads) k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out,
                                                   RedSlot slot) {
   double acc = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) acc += x[i] * y[i];
-  grid_reduce(acc, slot, [&](double tot) { *out = tot; });
-}
-
-__global__ void __launch_bounds__(kThreads) k_axpby(int n, double a, const double *__restrict__ x, double b, double *__restrict__ y) {
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) y[i] = a * x[i] + b * y[i];
-}
-
-__global__ void __launch_bounds__(kThreads) k_resid_l1(int n, const double *__restrict__ y, double theta,
-                                                      const double *__restrict__ psi, double *__restrict__ r, double *out,
-                                                      RedSlot slot) {
-  double acc = 0.0;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const double ri = y[i] - theta * psi[i];
-    r[i] = ri;
-    acc += fabs(ri);
-  }
   grid_reduce(acc, slot, [&](double tot) { *out = tot; });
 }
 

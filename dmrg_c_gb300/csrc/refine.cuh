@@ -18,7 +18,11 @@
 //     sub-partition's FP64 pipe for ~64 cycles, and FP64 vector updates cost more than the
 //     FP32 products they sit between;
 //   * Rayleigh-Ritz in span{psi, t} with one FP64 product H t.
-// H psi is carried along (y), so a step costs one FP64 and k FP32 products.
+// H psi is carried along (y), so a step costs one FP64 and k FP32 products.  The step's scalars
+// (theta, the residual norms, the projections, the 2 x 2 Rayleigh-Ritz) stay on the device,
+// formed by small kernels in stream order: the host reads one packed state per step.  With a
+// host read per dot product (about a dozen per step) the refinement of an ED instance spent
+// more time in synchronisations than in kernels once several solves shared the device.
 #pragma once
 
 #include "krylov.cuh"
@@ -59,13 +63,40 @@ __global__ void k_refine32_direction(int n, const float *__restrict__ res32, flo
                                      const float *__restrict__ g32, Scalars *S, int it, int max_step, const float2 *up,
                                      int ucount, float2 *gout, Progress *prog);
 
+// The refinement's device state (refine_core): slots of a double array.
+enum RefineSlot : int {
+  kRsTheta = 0,   // theta = <psi, H psi>
+  kRsL1,          // ||H psi - theta psi||_1
+  kRsRn2,         // ||H psi - theta psi||_2^2
+  kRsDegen,       // 1: the step had nothing to add (zero correction or Rayleigh-Ritz vector)
+  kRsC,           // <psi, r>
+  kRsCt,          // <psi, t>
+  kRsInv,         // 1 / ||t - <psi,t> psi||
+  kRsA22,         // <t_hat, H t_hat>
+  kRsA12,         // <y, t_hat>
+  kRsC1,          // psi <- c1 psi + c2 t_hat
+  kRsC2,
+  kRsCount
+};
+// r = y - rs[theta] psi; rs[L1] = sum |r_i|, rs[Rn2] = sum r_i^2 (two reductions, last block).
+__global__ void k_refine_resid(int n, const double *__restrict__ y, const double *__restrict__ psi, double *__restrict__ r,
+                               double *rs, double *pa, double *pb, unsigned *ticket);
+// res32 = fl32(c psi - r) with c = rs[C], t32 = 0, and the correction CG's start: rr0 = ||c psi - r||^2
+// into S (rrs_ref[1], rr32[1], thr = tau2 * rr0, done, iters); rr0 <= 0 marks the step
+// degenerate and the solve done (also in the host progress mirror).
+__global__ void k_refine32_start(int n, const double *__restrict__ r, const double *__restrict__ psi, float *__restrict__ res32,
+                                 float *__restrict__ t32, double tau2, Scalars *S, Progress *prog, double *rs, RedSlot slot);
+// t -= rs[Ct] psi, rs[Inv] = 1 / ||t|| (0 and degenerate when ||t|| = 0).
+__global__ void k_refine_orth(int n, double *__restrict__ t, const double *__restrict__ psi, double *rs, RedSlot slot);
+// x *= *s
+__global__ void k_scale_by(int n, const double *s, double *__restrict__ x);
+// The 2 x 2 Rayleigh-Ritz on span{psi, t_hat}: theta <- the lower eigenvalue, (c1, c2) its vector
+// (c1 = 1, c2 = 0 and degenerate when there is none).  One thread.
+__global__ void k_refine_rr(double *rs);
+// y = rs[C2] x + rs[C1] y
+__global__ void k_refine_combine(int n, const double *rs, const double *__restrict__ x, double *__restrict__ y);
 // *out = sum_i x_i y_i
 __global__ void k_vdot(const double *__restrict__ x, const double *__restrict__ y, int n, double *out, RedSlot slot);
-// y = a x + b y
-__global__ void k_axpby(int n, double a, const double *__restrict__ x, double b, double *__restrict__ y);
-// r = y - theta psi; *out = sum_i |r_i|
-__global__ void k_resid_l1(int n, const double *__restrict__ y, double theta, const double *__restrict__ psi,
-                           double *__restrict__ r, double *out, RedSlot slot);
 
 struct RefineResult {
   double eig_val = 0.0;
@@ -86,32 +117,25 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
   Scalars *S = ws.S();
   const RedSlot slot = ws.slot();
   const int vg = ws.vgrid;
-  DevBuf<double> y(n), r(n), t(n), res(n), z(n), out1(1);
+  DevBuf<double> y(n), r(n), t(n), z(n), rs(kRsCount);
   DevBuf<float> p32(n), psi32(n), g32(n), q32(n), t32(n), res32(n);
   RefineResult R;
-  auto fetch = [&](const double *dptr) {
-    double h = 0.0;
-    DG_CUDA(cudaMemcpyAsync(&h, dptr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  double hs[4];   // theta, L1, Rn2, degenerate
+  int hdi[2];     // S->done, S->iters
+  DG_CUDA(cudaMemsetAsync(rs.get(), 0, sizeof(double) * kRsCount, st));
+  // r = y - theta psi with its norms, then one read of the packed state
+  auto check = [&](bool with_cg) {
+    k_refine_resid<<<vg, kThreads, 0, st>>>(n, y.get(), psi, r.get(), rs.get(), ws.partials2.get(), ws.partials3.get(),
+                                            ws.ticket.get()); ::dg::count_launch();
+    DG_CUDA(cudaMemcpyAsync(hs, rs.get(), sizeof(hs), cudaMemcpyDeviceToHost, st));
+    if (with_cg) DG_CUDA(cudaMemcpyAsync(hdi, &S->done, sizeof(hdi), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
-    return h;
-  };
-  auto dot = [&](const double *a, const double *b) {
-    k_vdot<<<vg, kThreads, 0, st>>>(a, b, n, out1.get(), slot); ::dg::count_launch();
-    return fetch(out1.get());
-  };
-  auto axpby = [&](double a, const double *x, double b, double *yy) {
-    k_axpby<<<vg, kThreads, 0, st>>>(n, a, x, b, yy); ::dg::count_launch();
-  };
-  auto resid = [&](double theta) {
-    k_resid_l1<<<vg, kThreads, 0, st>>>(n, y.get(), theta, psi, r.get(), out1.get(), slot); ::dg::count_launch();
-    return fetch(out1.get());
   };
   // y = H psi, theta = <psi, y>
-  op.apply(psi, Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), &S->res}, slot, st);
+  op.apply(psi, Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{y.get(), rs.get() + kRsTheta}, slot, st);
   ++R.spmv64;
-  double theta = fetch(&S->res);
-  double l1 = resid(theta);
-  double rn = std::sqrt(dot(r.get(), r.get()));
+  check(false);
+  double theta = hs[0], l1 = hs[1], rn = std::sqrt(hs[2]);
   auto accepted = [&] { return l1 < acc || rn <= kMixedRes * std::fabs(theta); };
   for (int outer = 0; outer < max_outer && !accepted(); ++outer) {
     const double tau = std::min(1e-1, std::max(1e-4, 0.5 * kMixedRes * std::fabs(theta) / rn));
@@ -120,33 +144,18 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
     k_copy<double, float><<<vg, kThreads, 0, st>>>(psi, psi32.get(), n); ::dg::count_launch();
     op.apply(psi32.get(), Scale{}, -theta, (const int *)nullptr, EpiStore<float>{g32.get()}, slot, st);
     ++R.inner;
-    // res = -(r - <psi,r> psi) in FP64, then res32 = fl32(res), t32 = 0
-    const double c = dot(psi, r.get());
-    DG_CUDA(cudaMemsetAsync(res.get(), 0, sizeof(double) * n, st));
-    axpby(-1.0, r.get(), 0.0, res.get());
-    axpby(c, psi, 1.0, res.get());
-    k_copy<double, float><<<vg, kThreads, 0, st>>>(res.get(), res32.get(), n); ::dg::count_launch();
-    DG_CUDA(cudaMemsetAsync(t32.get(), 0, sizeof(float) * n, st));
-    const double rr0 = dot(res.get(), res.get());
-    if (!(rr0 > 0.0)) break;
-    // p32 = res32 (beta = 0), <g32,p32>
-    Scalars init{};
-    init.rrs_ref[1] = rr0;   // enters iteration 1
-    init.rr32[1] = (float)rr0;
-    init.thr = tau * tau * rr0;
-    DG_CUDA(cudaMemcpyAsync(&S->rrs_ref[1], &init.rrs_ref[1], sizeof(double), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(&S->rr32[1], &init.rr32[1], sizeof(float), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemcpyAsync(&S->thr, &init.thr, sizeof(double), cudaMemcpyHostToDevice, st));
-    DG_CUDA(cudaMemsetAsync(&S->done, 0, sizeof(int), st));
-    DG_CUDA(cudaMemsetAsync(&S->iters, 0, sizeof(int), st));
+    // res32 = fl32(-(r - <psi,r> psi)), t32 = 0, the CG's start on the device
+    k_vdot<<<vg, kThreads, 0, st>>>(psi, r.get(), n, rs.get() + kRsC, slot); ::dg::count_launch();
+    ws.prog.h->done = 0;
+    ws.prog.h->stamp = 0;
+    k_refine32_start<<<vg, kThreads, 0, st>>>(n, r.get(), psi, res32.get(), t32.get(), tau * tau, S, ws.prog.d, rs.get(), slot);
+    ::dg::count_launch();
     // Pair partials: the product's <p32,q32> in slot.partials, the update's <res32,res32> in
     // partials2, the direction's <g32,p32> in partials3; each summed by every block of its consumer.
     float2 *up = reinterpret_cast<float2 *>(ws.partials2.get()), *gpp = reinterpret_cast<float2 *>(ws.partials3.get());
     const int pgrid = op.grid();
     k_refine32_direction<<<vg, kThreads, 0, st>>>(n, res32.get(), p32.get(), g32.get(), S, 0, max_inner, (const float2 *)up, 0,
                                                   gpp, ws.prog.d); ::dg::count_launch();
-    ws.prog.h->done = 0;
-    ws.prog.h->stamp = 0;
     const int chunk = 8;
     int enq = 0, checked = 0;
     auto enqueue_to = [&](int last) {
@@ -172,42 +181,26 @@ RefineResult refine_core(const Opl &op, double acc, int max_outer, int max_inner
       checked = target;
       if (checked >= max_inner) break;
     }
-    DG_CUDA(cudaStreamSynchronize(st));
-    Scalars hs;
-    DG_CUDA(cudaMemcpyAsync(&hs, S, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-    DG_CUDA(cudaStreamSynchronize(st));
-    R.inner += hs.done ? hs.iters : max_inner;
+    // t_hat = (t - <psi,t> psi) / ||.||, z = H t_hat, a22 = <t_hat, z>, a12 = <y, t_hat>; the
+    // 2 x 2 Rayleigh-Ritz and psi = c1 psi + c2 t_hat, y = c1 y + c2 z, all on the device
     k_copy<float, double><<<vg, kThreads, 0, st>>>(t32.get(), t.get(), n); ::dg::count_launch();
-    // t_hat = (t - <psi,t> psi) / ||.||
-    const double ct = dot(psi, t.get());
-    axpby(-ct, psi, 1.0, t.get());
-    const double nt2 = dot(t.get(), t.get());
-    if (!(nt2 > 0.0)) break;
-    axpby(0.0, psi, 1.0 / std::sqrt(nt2), t.get());
-    // z = H t_hat; Rayleigh-Ritz on span{psi, t_hat}
-    op.apply((const double *)t.get(), Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{z.get(), &S->res},
-             slot, st);
+    k_vdot<<<vg, kThreads, 0, st>>>(psi, t.get(), n, rs.get() + kRsCt, slot); ::dg::count_launch();
+    k_refine_orth<<<vg, kThreads, 0, st>>>(n, t.get(), psi, rs.get(), slot); ::dg::count_launch();
+    k_scale_by<<<vg, kThreads, 0, st>>>(n, rs.get() + kRsInv, t.get()); ::dg::count_launch();
+    op.apply((const double *)t.get(), Scale{}, 0.0, (const int *)nullptr, EpiDot<double>{z.get(), rs.get() + kRsA22}, slot, st);
     ++R.spmv64;
-    const double a22 = fetch(&S->res);
-    const double a12 = dot(y.get(), t.get());
-    const double a11 = theta;
-    const double half = 0.5 * (a11 - a22);
-    const double lam = 0.5 * (a11 + a22) - std::sqrt(half * half + a12 * a12);
-    double c1 = a12, c2 = lam - a11;                 // (A - lam) [c1 c2]^T = 0, first row
-    if (std::fabs(lam - a22) > std::fabs(c2)) {      // better conditioned second row
-      c1 = lam - a22;
-      c2 = a12;
-    }
-    const double nc = std::sqrt(c1 * c1 + c2 * c2);
-    if (!(nc > 0.0)) break;
-    c1 /= nc;
-    c2 /= nc;
-    axpby(c2, t.get(), c1, psi);      // psi = c1 psi + c2 t_hat
-    axpby(c2, z.get(), c1, y.get());  // y = H psi
-    theta = lam;
+    k_vdot<<<vg, kThreads, 0, st>>>(y.get(), t.get(), n, rs.get() + kRsA12, slot); ::dg::count_launch();
+    k_refine_rr<<<1, 32, 0, st>>>(rs.get()); ::dg::count_launch();
+    k_refine_combine<<<vg, kThreads, 0, st>>>(n, rs.get(), t.get(), psi); ::dg::count_launch();
+    k_refine_combine<<<vg, kThreads, 0, st>>>(n, rs.get(), z.get(), y.get()); ::dg::count_launch();
+    DG_CUDA(cudaGetLastError());
+    check(true);
+    R.inner += hdi[0] ? hdi[1] : max_inner;
+    if (hs[3] != 0.0) break;   // nothing to add: the pair stays as it was
+    theta = hs[0];
+    l1 = hs[1];
+    rn = std::sqrt(hs[2]);
     ++R.outer;
-    l1 = resid(theta);
-    rn = std::sqrt(dot(r.get(), r.get()));
   }
   R.eig_val = theta;
   R.error = l1;
