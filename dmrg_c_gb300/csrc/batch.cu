@@ -24,7 +24,8 @@ struct BLzDesc {
   const int *col;
   const void *val;      // FP64 (FP64 form) or FP32 (mixed form) values
   int nslices, n;
-  int pblk, vblk;       // blocks of this instance in the product / in the vector kernels
+  int pblk, vblk;       // blocks of this instance in the product / in the one-element vector kernels
+  int ublk;             // blocks of this instance in k_blz_update (kUpd elements a thread)
   int cap;              // entries of D, O and their mirrors; steps b >= cap - 1 are not written
   void *V;              // Krylov basis: v_j at V + j n (element type of the form)
   void *w;              // unnormalised next vector
@@ -44,6 +45,7 @@ struct BLzDesc {
 enum { kScRs = 0, kScAhi, kScAlo, kScBhi, kScBlo, kScCount = 8 };
 
 constexpr int kBlzLookahead = 2;   // iterations the device runs ahead of the host's checks
+constexpr int kUpd = 4;            // elements a thread in k_blz_update
 
 // The block's instance and its block within the instance: cum[k] is the first block of
 // instance k (cum[count] = the grid), searched by thread 0 and broadcast.  A per-instance table
@@ -116,17 +118,17 @@ __global__ void __launch_bounds__(kThreads) k_blz_apply(const BLzDesc *__restric
   if (threadIdx.x == 0) d.part_p[m.y] = t;
 }
 
-// One warp per instance: alpha_b = the product partials summed in order.
+// One block per instance: alpha_b = the product partials summed in a fixed order (strided per
+// thread, then block_sum): a warp alone waited out one L2 round trip per 32 partials.
 __global__ void __launch_bounds__(kThreads) k_blz_alpha(const BLzDesc *__restrict__ desc, int count) {
   pdl_wait();
-  const int i = blockIdx.x * kWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i < count) {
-    const BLzDesc &d = desc[i];
+  {
+    const BLzDesc &d = desc[blockIdx.x];
     double s = 0.0;
-    for (int k = lane; k < d.pblk; k += 32) s += __ldcg(d.part_p + k);
-    s = warp_sum(s);
+    for (int k = threadIdx.x; k < d.pblk; k += kThreads) s += __ldcg(d.part_p + k);
+    s = block_sum(s);
     const int b = *d.step;
-    if (lane == 0 && b < d.cap - 1) {
+    if (threadIdx.x == 0 && b < d.cap - 1) {
       d.D[b] = s;
       *(volatile double *)(d.hD + b) = s;
       if (d.sc) {
@@ -139,40 +141,65 @@ __global__ void __launch_bounds__(kThreads) k_blz_alpha(const BLzDesc *__restric
   pdl_trigger();
 }
 
-// w_{b+1} = y - alpha_b v_b - beta_b v_{b-1} (FP64 arithmetic); block partials of ||w||^2.
+// w_{b+1} = y - alpha_b v_b - beta_b v_{b-1} (FP64 arithmetic, or compensated FP32 in the mixed
+// form); block partials of ||w||^2.  kUpd elements a thread, their loads issued before the
+// arithmetic: with one element a thread the kernel waited out one dependent L2/HBM round trip
+// per wave of blocks.
 template <class VT>
-__global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restrict__ desc, const int *__restrict__ vcum, int count) {
+__global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restrict__ desc, const int *__restrict__ ucum, int count) {
   pdl_wait();
-  const int2 m = blz_block(vcum, count);
+  const int2 m = blz_block(ucum, count);
   const BLzDesc &d = desc[m.x];
   const int b = *d.step;
-  const int i = m.y * kThreads + threadIdx.x;
+  const int i0 = m.y * (kThreads * kUpd) + threadIdx.x;
   double acc = 0.0;
   AccDot2 a2;
-  if (i < d.n && b < d.cap - 1) {
+  if (b < d.cap - 1) {
     const VT *V = static_cast<const VT *>(d.V);
+    const VT *vb = V + (size_t)b * d.n, *vp = V + (size_t)(b > 0 ? b - 1 : 0) * d.n;
+    const VT *y = static_cast<const VT *>(d.y);
+    VT ye[kUpd], be[kUpd], pe[kUpd];
+#pragma unroll
+    for (int e = 0; e < kUpd; ++e) {
+      const int i = i0 + e * kThreads;
+      ye[e] = be[e] = pe[e] = VT(0);
+      if (i < d.n) {
+        ye[e] = y[i];
+        be[e] = vb[i];
+        if (b > 0) pe[e] = vp[i];
+      }
+    }
     if constexpr (std::is_same<VT, float>::value) {
       // compensated FP32 with alpha and beta as two floats each (as k_mx_update); no FP64
       // instruction per element
-      AccDot2 t;
-      t.p = static_cast<const float *>(d.y)[i];
-      const float vb = V[(size_t)b * d.n + i];
-      t.add(-d.sc[kScAhi], vb);
-      t.add(-d.sc[kScAlo], vb);
-      if (b > 0) {
-        const float vp = V[(size_t)(b - 1) * d.n + i];
-        t.add(-d.sc[kScBhi], vp);
-        t.add(-d.sc[kScBlo], vp);
+      const float ahi = d.sc[kScAhi], alo = d.sc[kScAlo], bhi = d.sc[kScBhi], blo = d.sc[kScBlo];
+#pragma unroll
+      for (int e = 0; e < kUpd; ++e) {
+        const int i = i0 + e * kThreads;
+        if (i >= d.n) break;
+        AccDot2 t;
+        t.p = ye[e];
+        t.add(-ahi, be[e]);
+        t.add(-alo, be[e]);
+        if (b > 0) {
+          t.add(-bhi, pe[e]);
+          t.add(-blo, pe[e]);
+        }
+        const float wi = __fadd_rn(t.p, t.c);
+        static_cast<float *>(d.w)[i] = wi;
+        a2.add(wi, wi);
       }
-      const float wi = __fadd_rn(t.p, t.c);
-      static_cast<float *>(d.w)[i] = wi;
-      a2.add(wi, wi);
     } else {
-      const double a = d.D[b];
-      double wi = (double)static_cast<const VT *>(d.y)[i] - a * (double)V[(size_t)b * d.n + i];
-      if (b > 0) wi -= d.O[b] * (double)V[(size_t)(b - 1) * d.n + i];
-      static_cast<VT *>(d.w)[i] = (VT)wi;
-      acc = wi * wi;
+      const double a = d.D[b], o = b > 0 ? d.O[b] : 0.0;
+#pragma unroll
+      for (int e = 0; e < kUpd; ++e) {
+        const int i = i0 + e * kThreads;
+        if (i >= d.n) break;
+        double wi = (double)ye[e] - a * (double)be[e];
+        if (b > 0) wi -= o * (double)pe[e];
+        static_cast<VT *>(d.w)[i] = (VT)wi;
+        acc += wi * wi;
+      }
     }
   }
   pdl_trigger();
@@ -184,17 +211,17 @@ __global__ void __launch_bounds__(kThreads) k_blz_update(const BLzDesc *__restri
   if (threadIdx.x == 0) d.part_v[m.y] = t;
 }
 
-// One warp per instance: beta_{b+1} = ||w_{b+1}||, its reciprocal, and the step counter.
+// One block per instance: beta_{b+1} = ||w_{b+1}|| from the update's partials, its reciprocal,
+// and the step counter.
 __global__ void __launch_bounds__(kThreads) k_blz_beta(const BLzDesc *__restrict__ desc, int count) {
   pdl_wait();
-  const int i = blockIdx.x * kWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i < count) {
-    const BLzDesc &d = desc[i];
+  {
+    const BLzDesc &d = desc[blockIdx.x];
     double s = 0.0;
-    for (int k = lane; k < d.vblk; k += 32) s += __ldcg(d.part_v + k);
-    s = warp_sum(s);
+    for (int k = threadIdx.x; k < d.ublk; k += kThreads) s += __ldcg(d.part_v + k);
+    s = block_sum(s);
     const int b = *d.step;
-    if (lane == 0 && b < d.cap - 1) {
+    if (threadIdx.x == 0 && b < d.cap - 1) {
       const double be = sqrt(s), r = 1.0 / be;
       d.O[b + 1] = be;
       *(volatile double *)(d.hO + b + 1) = be;
@@ -321,7 +348,7 @@ struct BatchLanczosImpl {
     const dg_matrix *m = nullptr;
     dg_solver_params p{};
     cudaEvent_t built = nullptr;
-    int n = 0, pblk = 0, vblk = 0, cap = 0, vcap = 0;
+    int n = 0, pblk = 0, vblk = 0, ublk = 0, cap = 0, vcap = 0;
     size_t esz = 8;
     void *V = nullptr, *w = nullptr, *y = nullptr;
     double *part_p = nullptr, *part_v = nullptr, *D = nullptr, *O = nullptr, *rs = nullptr;
@@ -431,6 +458,7 @@ struct BatchLanczosImpl {
     in.esz = mixed ? sizeof(float) : sizeof(double);
     in.pblk = blocks_of(m->nslices, kWarps);
     in.vblk = blocks_of(in.n, kThreads);
+    in.ublk = blocks_of(in.n, kThreads * kUpd);
     in.cap = in.p.lanczos_max_step + kBlzLookahead + 3;
     in.vcap = std::min(in.cap, 64);
     if (in.built) DG_CUDA(cudaStreamWaitEvent(st, in.built, 0));
@@ -505,6 +533,7 @@ struct BatchLanczosImpl {
       d.n = in.n;
       d.pblk = in.pblk;
       d.vblk = in.vblk;
+      d.ublk = in.ublk;
       d.cap = std::min(in.cap, in.vcap + 1);   // the basis bounds the steps that may be written
       d.V = in.V;
       d.w = in.w;
@@ -522,7 +551,7 @@ struct BatchLanczosImpl {
       pc.push_back(pgrid);
       vc.push_back(vgrid);
       pgrid += in.pblk;
-      vgrid += in.vblk;
+      vgrid += in.ublk;
     }
     if (t_desc) pool_free(t_desc, st);
     if (t_pcum) pool_free(t_pcum, st);
@@ -548,7 +577,7 @@ struct BatchLanczosImpl {
   }
 
   void launch_iteration(cudaStream_t st) {
-    const int cgrid = blocks_of(t_count, kWarps);
+    const int cgrid = t_count;   // k_blz_alpha / k_blz_beta: one block per instance
     if (mixed)
       launch_pdl(k_blz_apply<float, 8>, dim3(t_pgrid), dim3(kThreads), st, (const BLzDesc *)t_desc, (const int *)t_pcum, t_count);
     else
@@ -892,7 +921,7 @@ struct BatchLanczosImpl {
           // depart: the departures' device work; reap: retired instances and staging
           const double t = now_ms();
           std::fprintf(stderr, "batch iteration %ld active %zu rows %d ms %.3f checks_ms %.3f depart_ms %.3f reap_ms %.3f\n",
-                       iters.load(), keep.size(), t_vgrid * kThreads, t - t_last, t_tri, t_leave, t - t_reap0);
+                       iters.load(), keep.size(), t_vgrid * kThreads * kUpd, t - t_last, t_tri, t_leave, t - t_reap0);
           t_tri = t_leave = 0.0;
           t_last = t;
         }

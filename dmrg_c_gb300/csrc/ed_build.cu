@@ -265,12 +265,14 @@ __device__ bool ed_row_ranked(const EdDev &m, int b, int64_t code, int *rc, doub
   return true;
 }
 
-// Pass 1 (row != null: pass 2), ranked rows (LM > 0: sites <= LM) or searched codes (LM = 0).
-// err: 1 row buffer overflow, 2 count mismatch.
+// Ranked rows, LM >= L sites.  Count pass (counts, row null, stride 0); fill pass (row set); or the
+// single pass (stride > 0): row b's kept elements go to col/val[b * stride ...] (a scratch of
+// stride >= the row's generated elements, so nothing overflows) and their number to counts[b],
+// for k_ed_compact.  err: 1 row buffer overflow, 2 count mismatch.
 template <int CAP, int LM>
 __global__ void __launch_bounds__(128) k_ed_rows_ranked(EdDev m, const int64_t *__restrict__ basis, long dim,
                                                         long long *__restrict__ counts, const int64_t *__restrict__ row,
-                                                        int *__restrict__ col, double *__restrict__ val, int *err) {
+                                                        int *__restrict__ col, double *__restrict__ val, int *err, long stride) {
   int rc[CAP];
   double rv[CAP];
   for (long b = blockIdx.x * (long)blockDim.x + threadIdx.x; b < dim; b += (long)gridDim.x * blockDim.x) {
@@ -283,9 +285,9 @@ __global__ void __launch_bounds__(128) k_ed_rows_ranked(EdDev m, const int64_t *
       continue;
     }
     long long cnt = 0;
-    const int64_t start = row ? row[b] : 0, end = row ? row[b + 1] : 0;
+    const int64_t start = stride ? b * stride : (row ? row[b] : 0), end = stride ? start + stride : (row ? row[b + 1] : 0);
     auto put = [&](int c, double v) {
-      if (row) {
+      if (row || stride) {
         const int64_t pos = start + cnt;
         if (pos < end) {
           col[pos] = c;
@@ -302,7 +304,24 @@ __global__ void __launch_bounds__(128) k_ed_rows_ranked(EdDev m, const int64_t *
     for (; i < n; ++i)
       if (abs_above(rv[i], m.zero)) put(rc[i], rv[i]);
     if (counts) counts[b] = cnt;
-    if (row && start + cnt != end) atomicExch(err, 2);
+    if (row && !stride && start + cnt != end) atomicExch(err, 2);
+  }
+}
+
+// The single pass's compaction: row b's elements from the scratch (stride entries a row) to
+// col/val[row[b] ...].  One warp a row.
+__global__ void __launch_bounds__(kThreads) k_ed_compact(long dim, long stride, const int64_t *__restrict__ row,
+                                                        const int *__restrict__ scol, const double *__restrict__ sval,
+                                                        int *__restrict__ col, double *__restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  const long nw = (long)gridDim.x * kWarps;
+  for (long b = blockIdx.x * (long)kWarps + (threadIdx.x >> 5); b < dim; b += nw) {
+    const int64_t o = row[b], cnt = row[b + 1] - o;
+    const long src = b * stride;
+    for (int64_t k = lane; k < cnt; k += 32) {
+      col[o + k] = scol[src + k];
+      val[o + k] = sval[src + k];
+    }
   }
 }
 
@@ -492,12 +511,12 @@ namespace {
 
 template <int CAP>
 void launch_rows(const EdDev &m, bool ranked, const int64_t *basis, long dim, long long *counts, const int64_t *row, int *col,
-                 double *val, int *err, cudaStream_t st) {
+                 double *val, int *err, long stride, cudaStream_t st) {
   const long blocks = std::max(1L, std::min<long>((dim + 127) / 128, (long)sm_count() * 16));
   if (ranked && m.L <= 32)
-    k_ed_rows_ranked<CAP, 32><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
+    k_ed_rows_ranked<CAP, 32><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err, stride);
   else if (ranked)
-    k_ed_rows_ranked<CAP, 64><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
+    k_ed_rows_ranked<CAP, 64><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err, stride);
   else
     k_ed_rows<CAP><<<(int)blocks, 128, 0, st>>>(m, basis, dim, counts, row, col, val, err);
   ::dg::count_launch();
@@ -505,16 +524,19 @@ void launch_rows(const EdDev &m, bool ranked, const int64_t *basis, long dim, lo
 }
 
 void rows_pass(int cap, const EdDev &m, bool ranked, const int64_t *basis, long dim, long long *counts, const int64_t *row,
-               int *col, double *val, int *err, cudaStream_t st) {
+               int *col, double *val, int *err, cudaStream_t st, long stride = 0) {
   if (cap <= 32)
-    launch_rows<32>(m, ranked, basis, dim, counts, row, col, val, err, st);
+    launch_rows<32>(m, ranked, basis, dim, counts, row, col, val, err, stride, st);
   else if (cap <= 64)
-    launch_rows<64>(m, ranked, basis, dim, counts, row, col, val, err, st);
+    launch_rows<64>(m, ranked, basis, dim, counts, row, col, val, err, stride, st);
   else if (cap <= 128)
-    launch_rows<128>(m, ranked, basis, dim, counts, row, col, val, err, st);
+    launch_rows<128>(m, ranked, basis, dim, counts, row, col, val, err, stride, st);
   else
-    launch_rows<256>(m, ranked, basis, dim, counts, row, col, val, err, st);
+    launch_rows<256>(m, ranked, basis, dim, counts, row, col, val, err, stride, st);
 }
+
+// Scratch of the single-pass build: at most this many bytes (else count and fill passes).
+constexpr size_t kEdScratchBytes = size_t(2) << 30;
 
 dg_ed *ed_build(const dg_ed_model *model) {
   EdPlan p;
@@ -606,7 +628,19 @@ dg_ed *ed_build(const dg_ed_model *model) {
             std::pow(10.0, -15.0), cnt.get(), a1.get(), a2.get(), p.R1, p.R2, p.off1, p.off2, tv.get()};
     const bool ranked = p.ranked && std::getenv("DG_ED_SEARCH") == nullptr;
     DevBuf<long long> counts(dim), tmp((dim + kScanTile - 1) / kScanTile + 2);
-    rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
+    // Ranked rows that fit the scratch are generated once (kept elements into a per-row slot of
+    // p.cap entries, then compacted); otherwise a count pass and a fill pass regenerate them.
+    const long stride = p.cap;
+    const bool single = ranked && (size_t)dim * (size_t)stride * (sizeof(int) + sizeof(double)) <= kEdScratchBytes;
+    DevBuf<int> scol;
+    DevBuf<double> sval;
+    if (single) {
+      scol.alloc((size_t)dim * stride);
+      sval.alloc((size_t)dim * stride);
+      rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, scol.get(), sval.get(), err.get(), st, stride);
+    } else {
+      rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
+    }
     e->row.alloc(dim + 1);
     exclusive_scan(counts.get(), dim, e->row.get(), tmp.get(), st);
     int64_t total = 0;
@@ -618,10 +652,17 @@ dg_ed *ed_build(const dg_ed_model *model) {
     e->nnz = total;
     e->col.alloc(total);
     e->val.alloc(total);
-    rows_pass(p.cap, m, ranked, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
-    DG_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
-    DG_CUDA(cudaStreamSynchronize(st));
-    DG_REQUIRE(herr == 0, DG_ERR_INTERNAL, "ED fill pass disagreed with the count pass (%d)", herr);
+    if (single) {
+      const long blocks = std::max(1L, std::min<long>((dim + kWarps - 1) / kWarps, (long)sm_count() * 16));
+      k_ed_compact<<<(int)blocks, kThreads, 0, st>>>(dim, stride, e->row.get(), scol.get(), sval.get(), e->col.get(),
+                                                     e->val.get()); ::dg::count_launch();
+      DG_CUDA(cudaGetLastError());
+    } else {
+      rows_pass(p.cap, m, ranked, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
+      DG_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+      DG_CUDA(cudaStreamSynchronize(st));
+      DG_REQUIRE(herr == 0, DG_ERR_INTERNAL, "ED fill pass disagreed with the count pass (%d)", herr);
+    }
   } catch (...) {
     delete e;
     throw;
