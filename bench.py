@@ -333,8 +333,10 @@ def oracle_ed_solve(model, threads):
 
 def batched_leg(L, args):
     """The batched form on the 256 XXZ chains of the batched-ED workload (L in {12..22}, Jz ~ U[0,2],
-    hz ~ U[0,1], seed 0): FP64 and mixed (mixed = 2) through the engine's lock-step Lanczos, beside
-    the engine without it, with every mixed energy against the FP64 one."""
+    hz ~ U[0,1], seed 0): FP64 and mixed (mixed = 2) through the engine (device build + solve per
+    chain) with its lock-step Lanczos, beside the engine without it, and through the lock-step API
+    (dg_batch_ground_state) on the matrices built once and kept resident; every mixed energy against
+    the FP64 one."""
     from dmrg_c_gb300 import workloads
     inst = workloads.xxz_ed_batch(256, seed=0)
     models = [i["model"]() for i in inst]
@@ -353,6 +355,25 @@ def batched_leg(L, args):
         E[tag] = np.array([res[i].eig_val for i in range(len(models))])
         out[tag] = {"value": len(models) / min(walls), "wall_ms": 1e3 * min(walls), "lanczos_batch": lb,
                     "p50_ms_per_job": float(np.percentile([r.t_done_ms - r.t_submit_ms for r in res.values()], 50))}
+    # the lock-step API on the same chains, matrices built once and resident (solves only)
+    eds = [L.EDSystem(m) for m in models]
+    mats = [e.matrix(L.DG_VALUES_BOTH) for e in eds]
+    for e in eds:
+        e.close()
+    for tag, mixed in (("fp64_api", 0), ("mixed_api", 2)):
+        p = L.default_params(seed=7, mixed=mixed)
+        L.batch_ground_state(mats[:16], p, want_vectors=False)   # warm-up
+        walls = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            _, infos = L.batch_ground_state(mats, p, want_vectors=False)
+            walls.append(time.perf_counter() - t0)
+        E[tag] = np.array([i.eig_val for i in infos])
+        out[tag] = {"value": len(mats) / min(walls), "wall_ms": 1e3 * min(walls),
+                    "entry": "dg_batch_ground_state, matrices resident (build excluded)"}
+    del mats
+    out["mixed_speedup_vs_fp64_api"] = out["mixed_api"]["value"] / out["fp64_api"]["value"]
+    out["max_dE_rel_mixed_vs_fp64_api"] = float(np.max(np.abs(E["mixed_api"] - E["fp64_api"]) / np.abs(E["fp64_api"])))
     out["mixed_speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
     out["lanczos_batch_speedup_fp64"] = out["fp64"]["value"] / out["fp64_streams"]["value"]
     out["max_dE_rel_mixed_vs_fp64"] = float(np.max(np.abs(E["mixed"] - E["fp64"]) / np.abs(E["fp64"])))
@@ -407,6 +428,18 @@ def served_leg(L, args):
         out[tag]["capacity_solves_per_s"] = len(cap_models) / ((last - first) * 1e-3)
     out["mixed_capacity_speedup_vs_fp64"] = out["mixed"]["capacity_solves_per_s"] / out["fp64"]["capacity_solves_per_s"]
     out["max_dE_rel_mixed_vs_fp64"] = float(np.max(np.abs(E["mixed"] - E["fp64"]) / np.abs(E["fp64"])))
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        secs = {}
+        for Lx in (8, 10, 12):
+            i = next(k for k in range(len(trace)) if trace[k]["L"] == Lx)
+            secs[Lx], _ = oracle_ed_solve(models[i], threads)
+        total = sum(secs[r["L"]] for r in trace)     # sequential FIFO over the stream's requests
+        out["cpu_baseline"] = {"value": len(trace) / total, "unit": "solves/s", "cores": threads, "kind": "port",
+                               "cpu": cpu_model(), "sample": "one request of each L solved by the oracle (ED build + "
+                               "LANCZOS + INVERSE_ITERATION), extrapolated to the stream's L mix, one after another: "
+                               "the capacity of a sequential FIFO server",
+                               "sec_by_L": {int(k): v for k, v in secs.items()}}
     return out
 
 
