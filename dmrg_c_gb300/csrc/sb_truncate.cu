@@ -380,9 +380,7 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
       DG_CUDA(cudaGetLastError());
     }
     // one cluster a block, the largest blocks first
-    auto smem_for = [&](int c) { return 3 * sizeof(double) * (size_t)((max_n + c - 1) / c) * max_n; };
-    // blocks whose rows do not fit 16 CTAs' shared memory keep them in a global workspace instead
-    const bool gmem = smem_for(16) > kJacobiSmem;
+    auto smem_for = [&](int c, int mn) { return 3 * sizeof(double) * (size_t)((mn + c - 1) / c) * mn; };
     std::vector<int> by_size(nb);
     std::iota(by_size.begin(), by_size.end(), 0);
     std::stable_sort(by_size.begin(), by_size.end(), [&](int a, int b) { return eb[a].n > eb[b].n; });
@@ -390,45 +388,56 @@ DMRG_SYSTEM_INFO *system_info(int nq, const int *const *qn, DMRG_BASIS *B, const
     for (int i = 0; i < nb; ++i) eb_sorted[i] = eb[by_size[i]];
     DG_CUDA(cudaMemcpyAsync(deb.get(), eb_sorted.data(), sizeof(EigBlk) * nb, cudaMemcpyHostToDevice, st));
     DG_CUDA(cudaMemsetAsync(dsw.get(), 0, sizeof(int) * nb, st));
-    // 16 CTAs a cluster (a non-portable size) when the largest block has 64 pairs or more and the
-    // device runs such clusters, else 8
-    int cs = 8;
-    auto kernel = gmem ? k_jacobi_cluster<true> : k_jacobi_cluster<false>;
-    DG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
-    if (max_n >= 64 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess)
-      cs = 16;
-    cudaGetLastError();
-    if (!gmem && smem_for(8) > kJacobiSmem) cs = 16;
+    // Blocks whose rows do not fit 16 CTAs' shared memory (a prefix of the sorted list) keep them in
+    // a global workspace sized for them alone; the others run from shared memory in a second launch,
+    // so one large block does not send every block to global memory.
+    int n_gmem = 0;
+    while (n_gmem < nb && smem_for(16, eb_sorted[n_gmem].n) > kJacobiSmem) ++n_gmem;
     DevBuf<double> gwork;
-    for (;;) {
-      cudaLaunchConfig_t cfg;
-      std::memset(&cfg, 0, sizeof(cfg));
-      cfg.gridDim = dim3((unsigned)(nb * cs));
-      cfg.blockDim = dim3(kThreads);
-      cfg.dynamicSmemBytes = gmem ? 0 : smem_for(cs);
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = (unsigned)cs;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      int clusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess || clusters < 1) {
-        cudaGetLastError();
-        DG_REQUIRE(cs == 16 && (gmem || smem_for(8) <= kJacobiSmem), DG_ERR_CUDA, "the device runs no cluster of %d CTAs", cs);
-        cs = 8;   // try the portable size
-        continue;
+    auto launch_part = [&](int first, int count, bool gmem) {
+      if (count <= 0) return;
+      const int mn = eb_sorted[first].n;
+      // 16 CTAs a cluster (a non-portable size) when the part's largest block has 64 pairs or
+      // more and the device runs such clusters, else 8
+      int cs = 8;
+      auto kernel = gmem ? k_jacobi_cluster<true> : k_jacobi_cluster<false>;
+      DG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kJacobiSmem));
+      if (mn >= 64 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) cs = 16;
+      cudaGetLastError();
+      if (!gmem && smem_for(8, mn) > kJacobiSmem) cs = 16;
+      for (;;) {
+        cudaLaunchConfig_t cfg;
+        std::memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)(count * cs));
+        cfg.blockDim = dim3(kThreads);
+        cfg.dynamicSmemBytes = gmem ? 0 : smem_for(cs, mn);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess || clusters < 1) {
+          cudaGetLastError();
+          DG_REQUIRE(cs == 16 && (gmem || smem_for(8, mn) <= kJacobiSmem), DG_ERR_CUDA, "the device runs no cluster of %d CTAs",
+                     cs);
+          cs = 8;   // try the portable size
+          continue;
+        }
+        const int64_t gstride = 3 * (int64_t)((mn + cs - 1) / cs) * mn;
+        if (gmem) gwork.alloc((size_t)count * cs * gstride);
+        DG_CUDA(cudaLaunchKernelEx(&cfg, kernel, (const EigBlk *)(deb.get() + first), (const double *)dA.get(), dV.get(), dW.get(),
+                                   kJacobiSweeps, dsw.get() + first, gmem ? gwork.get() : (double *)nullptr, gstride));
+        count_launch();
+        cs_used = std::max(cs_used, cs);
+        break;
       }
-      const int64_t gstride = 3 * (int64_t)((max_n + cs - 1) / cs) * max_n;
-      if (gmem) gwork.alloc((size_t)nb * cs * gstride);
-      DG_CUDA(cudaLaunchKernelEx(&cfg, kernel, (const EigBlk *)deb.get(), (const double *)dA.get(), dV.get(), dW.get(), kJacobiSweeps,
-                                 dsw.get(), gmem ? gwork.get() : (double *)nullptr, gstride));
-      cs_used = cs;
-      break;
-    }
-    count_launch();
+    };
+    launch_part(0, n_gmem, true);
+    launch_part(n_gmem, nb - n_gmem, false);
     DG_CUDA(cudaGetLastError());
     DG_CUDA(cudaMemcpyAsync(W.data(), dW.get(), sizeof(double) * W.size(), cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaMemcpyAsync(Vh.data(), dV.get(), sizeof(double) * Vh.size(), cudaMemcpyDeviceToHost, st));

@@ -108,3 +108,26 @@ def test_system_info_block_beyond_shared_memory(gpu, oracle):
     want = oracle.system_info(qns, st, inv, d, dim, v, lllr, 100)
     got = oracle.call_system_info(gpu.load(), qns, st, inv, dim, dim, d, v, lllr, 100, _free())
     assert oracle.same_truncation(got, want) == []
+
+
+def test_system_info_mixed_block_sizes_with_global_workspace(gpu, oracle):
+    """One density block beyond the CTAs' shared memory (400 pairs) beside small blocks, several
+    with fewer pairs than a cluster has CTAs (2 and 6 pairs), in one call: the large block runs
+    from the global workspace and the small ones from shared memory."""
+    d = 2
+    qb = np.array([0] * 200 + [1] * 3 + [-1] * 3 + [2] + [-2], np.int64)
+    dim = len(qb)
+    qs = np.zeros(d, np.int64)
+    st = sb_models.sector_states(qb, qb, qs, 0)
+    inv = -np.ones(dim * d * dim * d, np.int32)
+    inv[((st[0].astype(np.int64) * d + st[1]) * dim + st[2]) * d + st[3]] = np.arange(len(st[0]), dtype=np.int32)
+    lllr = oracle.lllr_list(qb, qs, st)
+    sizes = sorted(int(x) for x in lllr[4])
+    assert sizes[-1] == 400 and sizes[0] < 8 and len(sizes) >= 4
+    v = np.random.default_rng(29).standard_normal(len(st[0]))
+    v /= np.linalg.norm(v)
+    qns = [(np.repeat(qb, d) + np.tile(qs, dim)).astype(np.int32)]
+    for keep in (30, 404):
+        want = oracle.system_info(qns, st, inv, d, dim, v, lllr, keep)
+        got = oracle.call_system_info(gpu.load(), qns, st, inv, dim, dim, d, v, lllr, keep, _free())
+        assert oracle.same_truncation(got, want) == []
