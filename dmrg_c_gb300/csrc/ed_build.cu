@@ -200,9 +200,13 @@ __device__ bool ed_row_ranked(const EdDev &m, int b, int64_t code, int *rc, doub
     }
     return acc_add<CAP, int>(rc, rv, n, target, v);
   };
+  // per-site state of the row (local memory, so kept small: it spills out of L1 with a row
+  // buffer a thread): digits, electrons below each site, quantum-number sums of sites 0..s
+  // (16 bits, checked on the host), rank terms
   signed char dg[LM];
   unsigned char nep[LM + 1];   // electrons on sites [0, s)
-  int b1[LM], b2[LM], T[LM];
+  short b1[LM], b2[LM];
+  int T[LM];
   {
     int p1 = 0, p2 = 0, ne = 0;
     for (int s = 0; s < m.L; ++s) {
@@ -212,8 +216,8 @@ __device__ bool ed_row_ranked(const EdDev &m, int b, int64_t code, int *rc, doub
       if (m.n_ele) ne += __ldg(m.n_ele + l);
       p1 += __ldg(m.a1 + l);
       p2 += __ldg(m.a2 + l);
-      b1[s] = p1;
-      b2[s] = p2;
+      b1[s] = (short)p1;
+      b2[s] = (short)p2;
       T[s] = rank_term(m, s, l, p1, p2);
     }
     nep[m.L] = (unsigned char)ne;
@@ -397,7 +401,8 @@ struct EdPlan {
   std::vector<int64_t> cnt;         // (L + 1) * R1 * R2
   std::vector<int64_t> pw;          // L + 1
   long dim = 0;
-  int cap = 0;                      // row buffer needed
+  int cap = 0;                      // row buffer needed (searched rows: every generated element)
+  int cap_ranked = 0;               // ranked rows: off-diagonal elements a row can generate, + 1
   bool ranked = true;               // targets ranked from the row's index (no two-site term on one site)
 };
 
@@ -470,7 +475,13 @@ void plan_model(const dg_ed_model *m, EdPlan &p) {
     for (int l = 0; l < d; ++l) w = std::max(w, (int)(m->ops[o].Row[l + 1] - m->ops[o].Row[l]));
     return w;
   };
-  long cap = 1;
+  auto diagonal = [&](int o) {   // every entry on the diagonal: the operator keeps the digit
+    for (int l = 0; l < d; ++l)
+      for (long it = m->ops[o].Row[l]; it < m->ops[o].Row[l + 1]; ++it)
+        if (m->ops[o].Col[it] != l) return false;
+    return true;
+  };
+  long cap = 1, cap_off = 0;
   for (int k = 0; k < m->n_terms; ++k) {
     const dg_ed_term &t = m->terms[k];
     DG_REQUIRE(t.kind == DG_ED_ONSITE || t.kind == DG_ED_INTER, DG_ERR_ARG, "term %d: unknown kind", k);
@@ -484,12 +495,21 @@ void plan_model(const dg_ed_model *m, EdPlan &p) {
       DG_REQUIRE(t.sign_mode == DG_ED_SIGN_NONE || m->n_ele, DG_ERR_ARG, "term %d: fermion sign without n_ele", k);
       if (t.site1 == t.site2) p.ranked = false;
       cap += (long)width(t.op1) * width(t.op2);
+      if (!diagonal(t.op1) || !diagonal(t.op2)) cap_off += (long)width(t.op1) * width(t.op2);
     } else {
       cap += width(t.op1);
+      if (!diagonal(t.op1)) cap_off += width(t.op1);
     }
   }
   p.cap = (int)std::min(cap, 1L << 20);
+  p.cap_ranked = (int)std::min(cap_off + 1, 1L << 20);
   if (L > 64) p.ranked = false;
+  // the ranked rows keep per-site quantum-number sums in 16 bits
+  {
+    int amax = 0;
+    for (int l = 0; l < d; ++l) amax = std::max(amax, std::max(std::abs(p.a1[l]), std::abs(p.a2[l])));
+    if ((long)L * amax > 32767) p.ranked = false;
+  }
   if (m->n_ele)
     for (int l = 0; l < d; ++l)
       if (m->n_ele[l] < 0 || m->n_ele[l] * L > 255) p.ranked = false;   // per-row prefix counts are bytes
@@ -543,7 +563,8 @@ dg_ed *ed_build(const dg_ed_model *model) {
   plan_model(model, p);
   DG_REQUIRE(p.dim > 0, DG_ERR_ARG, "the symmetry sector is empty");
   DG_REQUIRE(p.dim <= 0x7fffffffL, DG_ERR_ARG, "sector dimension %ld exceeds the int32 column range", p.dim);
-  DG_REQUIRE(p.cap <= 256, DG_ERR_ARG, "a row can generate %d elements; at most 256 are supported", p.cap);
+  DG_REQUIRE((p.ranked ? p.cap_ranked : p.cap) <= 256, DG_ERR_ARG, "a row can generate %d elements; at most 256 are supported",
+             p.ranked ? p.cap_ranked : p.cap);
   cudaStream_t st = stream();
   const int L = p.L, d = p.d;
 
@@ -630,16 +651,17 @@ dg_ed *ed_build(const dg_ed_model *model) {
     DevBuf<long long> counts(dim), tmp((dim + kScanTile - 1) / kScanTile + 2);
     // Ranked rows that fit the scratch are generated once (kept elements into a per-row slot of
     // p.cap entries, then compacted); otherwise a count pass and a fill pass regenerate them.
-    const long stride = p.cap;
+    const int cap = ranked ? p.cap_ranked : p.cap;
+    const long stride = cap;
     const bool single = ranked && (size_t)dim * (size_t)stride * (sizeof(int) + sizeof(double)) <= kEdScratchBytes;
     DevBuf<int> scol;
     DevBuf<double> sval;
     if (single) {
       scol.alloc((size_t)dim * stride);
       sval.alloc((size_t)dim * stride);
-      rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, scol.get(), sval.get(), err.get(), st, stride);
+      rows_pass(cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, scol.get(), sval.get(), err.get(), st, stride);
     } else {
-      rows_pass(p.cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
+      rows_pass(cap, m, ranked, e->basis.get(), dim, counts.get(), nullptr, nullptr, nullptr, err.get(), st);
     }
     e->row.alloc(dim + 1);
     exclusive_scan(counts.get(), dim, e->row.get(), tmp.get(), st);
@@ -658,7 +680,7 @@ dg_ed *ed_build(const dg_ed_model *model) {
                                                      e->val.get()); ::dg::count_launch();
       DG_CUDA(cudaGetLastError());
     } else {
-      rows_pass(p.cap, m, ranked, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
+      rows_pass(cap, m, ranked, e->basis.get(), dim, nullptr, e->row.get(), e->col.get(), e->val.get(), err.get(), st);
       DG_CUDA(cudaMemcpyAsync(&herr, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
       DG_CUDA(cudaStreamSynchronize(st));
       DG_REQUIRE(herr == 0, DG_ERR_INTERNAL, "ED fill pass disagreed with the count pass (%d)", herr);

@@ -126,7 +126,7 @@ def test_system_info_mixed_block_sizes_with_global_workspace(gpu, oracle):
     assert sizes[-1] == 400 and sizes[0] < 8 and len(sizes) >= 4
     v = np.random.default_rng(29).standard_normal(len(st[0]))
     v /= np.linalg.norm(v)
-    qns = [(np.repeat(qb, d) + np.tile(qs, dim)).astype(np.int32)]
+    qns = _qns(lllr[3], 1)   # the LLLR labels in the basis' ascending order
     for keep in (30, 404):
         want = oracle.system_info(qns, st, inv, d, dim, v, lllr, keep)
         got = oracle.call_system_info(gpu.load(), qns, st, inv, dim, dim, d, v, lllr, keep, _free())
