@@ -334,7 +334,7 @@ bool batch_eligible(const dg_matrix *m, const dg_solver_params &p) {
   if (!m || m->format != DG_FORMAT_SELL || m->nslices <= 0) return false;
   if (p.mixed != 0 && p.mixed != 2) return false;
   if (p.mixed == 2 ? !m->has32 : !m->has64) return false;
-  if (p.dense_below > 0 && m->n < p.dense_below) return false;
+  if (dense_route(p, m->n)) return false;
   if (p.lanczos_tight || p.lanczos_slow) return false;
   if (p.lanczos_block_step > 0 && p.lanczos_block_step < p.lanczos_max_step) return false;
   return p.lanczos_max_step > p.lanczos_min_step;

@@ -10,6 +10,16 @@
 
 namespace dg {
 
+// The dense route (the reference's dense diagonalisation of systems below dense_below states) is
+// the FP64 form's.  The mixed form's answer comes from its FP64 refinement, which reaches FP64
+// accuracy at any size, so from 64 states up it runs its own Lanczos and refinement there too
+// (and small instances can join a lock-step batch); below 64 the Krylov space is exhausted in a
+// few steps either way.
+inline bool dense_route(const dg_solver_params &p, long n) {
+  return p.dense_below > 0 && n < p.dense_below && (p.mixed == 0 || n < 64);
+}
+
+
 // Operator launcher over a device CRS: FP64 values for FP64 input vectors, FP32 values for
 // FP32 input vectors (mixed-precision form).
 struct CrsLauncher {
@@ -98,7 +108,7 @@ SolveOut solve_ground_state(const Opl &op, const dg_solver_params &p, const doub
                             bool shifted_check = true) {
   const int n = op.n();
   DG_REQUIRE(n > 0, DG_ERR_ARG, "operator dimension must be positive");
-  DG_REQUIRE(p.lanczos_max_step > p.lanczos_min_step || (p.dense_below > 0 && n < p.dense_below), DG_ERR_ARG, "max_step=%d must exceed min_step=%d", p.lanczos_max_step,
+  DG_REQUIRE(p.lanczos_max_step > p.lanczos_min_step || dense_route(p, n), DG_ERR_ARG, "max_step=%d must exceed min_step=%d", p.lanczos_max_step,
              p.lanczos_min_step);
   cudaStream_t st = stream();
   Workspace ws(n, op.grid(), st);
@@ -120,7 +130,7 @@ SolveOut solve_ground_state(const Opl &op, const dg_solver_params &p, const doub
   DG_CUDA(cudaEventCreate(&e2));
   DG_CUDA(cudaEventRecord(e0, st));
   LanczosCfg cfg = lanczos_cfg_from(p);
-  if (p.dense_below > 0 && n < p.dense_below) {
+  if (dense_route(p, n)) {
     // Small problems: the reference diagonalises densely (sml/LANCZOS_SYM.c:37-56).  Here a
     // fully reorthogonalised Lanczos runs until the lowest Ritz pair is exact to rounding
     // (|last Ritz component| < 1e-15) or the Krylov space spans the whole matrix.

@@ -246,7 +246,8 @@ typedef struct {
    int lanczos_block_step;  /* BOX_LAN.max_block_step (restart length)       */
    int lanczos_tight;       /* 1 = "Tight", 0 = "Normal"                     */
    int lanczos_slow;        /* 1 = LANCZOS_SLOW semantics (re-formed vector) */
-   int dense_below;         /* solve n < dense_below to machine precision (reference: 1000) */
+   int dense_below;         /* solve n < dense_below to machine precision (reference: 1000);
+                               the FP64 form's route: the mixed form uses it below 64 only */
    double ii_acc;           /* BOX_II.ii_acc                                 */
    double ii_diag_add;      /* BOX_II.ii_diag_add                            */
    int ii_max_step;         /* BOX_II.ii_max_step; < 0 skips inverse iteration */

@@ -1,7 +1,8 @@
 """The batched form: dg_batch_ground_state (the Lanczos phases of many ED instances in lock-step,
 one launch of each kernel per step over all of them) against the one-at-a-time dg_ground_state on
 the same matrices, FP64 and mixed (mixed = 2), with instances of uneven size, one below the dense
-threshold (solved by the single path), and the FP64 energies against the oracle."""
+threshold (in FP64 solved by the single path's dense route; the mixed form batches it too), and the
+FP64 energies against the oracle."""
 import numpy as np
 import pytest
 
@@ -46,7 +47,7 @@ def test_batch_fp64_energies_match_oracle(gpu, oracle):
 
 def test_batch_repeated_and_empty(gpu):
     """Two batches in a row on the same matrices give the same energies; an empty batch is a no-op."""
-    inst = _instances(gpu)[0:4]        # the first is below the dense threshold (single path)
+    inst = _instances(gpu)[0:4]        # the first is below the dense threshold (batched in the mixed form)
     mats = [m for _, _, m in inst]
     _, a = gpu.batch_ground_state(mats, gpu.default_params(seed=5, mixed=2), want_vectors=False)
     _, b = gpu.batch_ground_state(mats, gpu.default_params(seed=5, mixed=2), want_vectors=False)

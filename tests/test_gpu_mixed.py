@@ -86,3 +86,19 @@ def test_mixed_needs_fp32_values(gpu):
     m = gpu.DeviceMatrix(low, gpu.DG_STORE_LOWER_DIAG_LAST)          # FP64 values only
     with pytest.raises(gpu.DgError):
         gpu.ground_state(m, _mixed_params(gpu))
+
+
+@pytest.mark.gpu
+def test_mixed_below_dense_threshold(gpu):
+    """Below dense_below (1000 states) the FP64 form takes the reference's dense route; the mixed
+    form runs its own Lanczos and FP64 refinement from 64 states up and still reaches the FP64
+    energy; below 64 states it takes the dense route as well."""
+    from dmrg_c_gb300 import ed_models
+    for L, dense_mixed in ((12, 0), (6, 1)):
+        ed = gpu.EDSystem(ed_models.xxz_chain(L, Jxy=1.0, Jz=0.8, hz=0.2))
+        m = ed.matrix(gpu.DG_VALUES_BOTH)
+        v0, i0 = gpu.ground_state(m, gpu.default_params(seed=4))
+        v2, i2 = gpu.ground_state(m, gpu.default_params(seed=4, mixed=2))
+        assert i0.dense == 1 and i2.dense == dense_mixed, (m.n, i0.dense, i2.dense)
+        assert abs(i2.eig_val - i0.eig_val) <= 1e-10 * abs(i0.eig_val), (m.n, i2.eig_val, i0.eig_val)
+        assert abs(v0 @ v2) >= 1 - 1e-9
