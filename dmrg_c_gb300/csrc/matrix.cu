@@ -308,6 +308,10 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   m->nnz_sell = total;
   m->s_col.alloc(total);
   m->s_val.alloc(total);
+  if (!m->s_err.get()) {
+    m->s_err.alloc(1);
+    DG_CUDA(cudaMemsetAsync(m->s_err.get(), 0, sizeof(int), st));
+  }
   const int g = vector_grid((long)nslots);
   k_sell_fill<double><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
                                               m->s_off.get(), nslices, m->s_col.get(), m->s_val.get()); ::dg::count_launch();
@@ -700,6 +704,17 @@ int dg_matrix_set_sell_window(dg_matrix *m, int window) {
     m->sell_ws = ws;
     m->sell_variant = var;
     m->format = DG_FORMAT_SELL;
+  });
+}
+
+int dg_matrix_sell_error(const dg_matrix *m, int *err) {
+  return guarded([&] {
+    DG_REQUIRE(m && err, DG_ERR_ARG, "null argument");
+    *err = 0;
+    if (!m->s_err.get()) return;
+    cudaStream_t st = stream();
+    DG_CUDA(cudaMemcpyAsync(err, m->s_err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
   });
 }
 

@@ -1,9 +1,12 @@
 // matrix.cuh -- device-resident full CRS operator (struct dg_matrix).
 #pragma once
 
+#include <atomic>
+
 #include "apply.cuh"
 #include "common.cuh"
 #include "sell.cuh"
+#include "sell_tma.cuh"
 
 struct dg_matrix {
   int n = 0;
@@ -29,11 +32,12 @@ struct dg_matrix {
   dg::DevBuf<int> s_width, s_perm, s_col;
   dg::DevBuf<double> s_val;
   dg::DevBuf<float> s_val32;
+  dg::DevBuf<int> s_err;           // V_TMA stage-wait failures (0: none)
 
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }
   dg::CrsOp<float> op32() const { return dg::CrsOp<float>{row.get(), col.get(), val32.get()}; }
-  dg::SellOp<double> sell64() const { return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant}; }
-  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant32}; }
+  dg::SellOp<double> sell64() const { return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant, s_err.get()}; }
+  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant32, s_err.get()}; }
 };
 
 namespace dg {
@@ -68,9 +72,32 @@ void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, Scale sc, doubl
   }
 }
 
+// The streamed form: one warp per slice, tma_block_bytes<VT>() of dynamic shared memory (the
+// opt-in above 48 KB is set once per device and instantiation).
+template <class VT, class XT, class Epi>
+void launch_sell_tma(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi,
+                     RedSlot slot, cudaStream_t st) {
+  auto kern = k_apply_sell_tma<VT, XT, Epi>;
+  static std::atomic<unsigned long long> ready{0};
+  int dev = 0;
+  DG_CUDA(cudaGetDevice(&dev));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(ready.load() & bit)) {
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_block_bytes<VT>()));
+    ready.fetch_or(bit);
+  }
+  launch_pdl_smem(kern, dim3(grid), dim3(kThreads), (size_t)tma_block_bytes<VT>(), st, op, x, sc, sigma, gate, epi, slot);
+}
+
 template <class VT, class XT, class Epi>
 void launch_sell(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma,
                  const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
+  // the bulk copies need 16-byte aligned arrays (pool allocations are 256-byte aligned)
+  if (op.variant == V_TMA && op.ws == 1 && ((uintptr_t)op.col % 16) == 0 && ((uintptr_t)op.val % 16) == 0) {
+    launch_sell_tma(op, grid, x, sc, sigma, gate, epi, slot, st);
+    DG_CUDA(cudaGetLastError());
+    return;
+  }
   switch (op.ws) {
     case 1: launch_sell_ws<1>(op, grid, x, sc, sigma, gate, epi, slot, st); break;
     case 2: launch_sell_ws<2>(op, grid, x, sc, sigma, gate, epi, slot, st); break;

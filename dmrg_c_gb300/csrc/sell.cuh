@@ -39,6 +39,7 @@ struct SellOp {
   int nslices;
   int ws;                            // warps per slice (1, 2, 4 or 8)
   int variant;                       // SellVariant
+  int *err;                          // V_TMA: set to 1 when a stage wait ran out (may be null)
 };
 
 // Kernel variants (chosen per matrix by the autotuner, dg_matrix_autotune).  Each issues
@@ -46,9 +47,11 @@ struct SellOp {
 // per warp hide the dependent col -> x load chain:
 //   V_U4 / V_U8 / V_U16  groups of 4 / 8 / 16 elements;
 //   V_PIPE8              U=8 with the next group's columns/values loaded before the current
-//                        group's multiply-adds (software pipelining).
+//                        group's multiply-adds (software pipelining);
+//   V_TMA                one warp per slice, the slice streamed into shared memory by bulk
+//                        copies several stages ahead (sell_tma.cuh); other warp counts run V_U8.
 // Measured on GB300 (FP64, 57M-element superblock): U=4 1.6 TB/s, U=8 4.5 TB/s.
-enum SellVariant : int { V_U4 = 0, V_U8 = 1, V_U16 = 2, V_PIPE8 = 3, V_COUNT = 4 };
+enum SellVariant : int { V_U4 = 0, V_U8 = 1, V_U16 = 2, V_PIPE8 = 3, V_TMA = 4, V_COUNT = 5 };
 
 template <bool STREAM, class T>
 __device__ __forceinline__ T ld_mat(const T *p) {

@@ -106,6 +106,7 @@ SIGNATURES = {
     "dg_matrix_set_format": (C.c_int, [vp, C.c_int]),
     "dg_matrix_set_sell_shape": (C.c_int, [vp, C.c_int, C.c_int]),
     "dg_matrix_set_sell_variant": (C.c_int, [vp, C.c_int]),
+    "dg_matrix_sell_error": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "dg_matrix_set_sell_window": (C.c_int, [vp, C.c_int]),
     "dg_matrix_autotune": (C.c_int, [vp, C.c_int, P(abi.dg_tune_result)]),
     "dg_matrix_format": (C.c_int, [vp, ip, lp]),
@@ -248,6 +249,11 @@ class DeviceMatrix:
 
     def set_sell_variant(self, variant: int):
         check(load().dg_matrix_set_sell_variant(self.h, variant))
+
+    def sell_error(self) -> int:
+        e = C.c_int(0)
+        check(load().dg_matrix_sell_error(self.h, C.byref(e)))
+        return e.value
 
     def set_sell_window(self, window: int):
         check(load().dg_matrix_set_sell_window(self.h, window))

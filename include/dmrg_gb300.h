@@ -193,9 +193,14 @@ int dg_matrix_set_format(dg_matrix *m, int format);
 /* Use the sliced-ELL kernel with warps_per_slice (1, 2, 4, 8) warps sharing a 32-row slice. */
 int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid);
 /* Sliced-ELL kernel variant: element groups of 0: 4, 1: 8, 2: 16, 3: 8 with
- * software-pipelined loads.  The FP64 product's default follows the warps per slice (3 for
- * 1-2 warps, 2 for 4-8), the FP32 (mixed) product's is 1; this call sets both. */
+ * software-pipelined loads; 4: one warp per slice with the slice streamed into shared memory
+ * by bulk copies (with more warps per slice it runs variant 1).  The FP64 product's default
+ * follows the warps per slice (3 for 1-2 warps, 2 for 4-8), the FP32 (mixed) product's is 1;
+ * this call sets both. */
 int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
+/* *err = 1 if a streamed (variant 4) product of this matrix ever gave up waiting for a stage
+ * of its copies (the product is then incomplete), else 0. */
+int dg_matrix_sell_error(const dg_matrix *m, int *err);
 /* Rebuild the sliced-ELL copy sorting rows by length within windows of `window` rows
  * (1..2048; <= 32 keeps the original row order). */
 int dg_matrix_set_sell_window(dg_matrix *m, int window);
