@@ -7,6 +7,7 @@
 // summation order (bitwise reproducible) and no atomics.
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 
 #include <type_traits>
 
@@ -190,13 +191,19 @@ __global__ void k_to_f32(const double *__restrict__ a, long n, float *__restrict
 // last row.
 constexpr int kSortThreads = kSellWindow / 2;   // one compare-exchange per thread and stage
 
-__global__ void __launch_bounds__(kSortThreads) k_sell_window_sort(const int64_t *__restrict__ row, int n, int window, int *perm) {
+// Row length as laid out: the CRS length, or blen (with the delta stream's bridges) when given.
+__device__ __forceinline__ long long laid_len(const int64_t *__restrict__ row, const int *__restrict__ blen, int r) {
+  return blen ? (long long)blen[r] : (long long)(row[r + 1] - row[r]);
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sell_window_sort(const int64_t *__restrict__ row, const int *__restrict__ blen, int n,
+                                                                   int window, int *perm) {
   __shared__ unsigned long long key[kSellWindow];
   const int base = blockIdx.x * kSellWindow;
   for (int t = threadIdx.x; t < kSellWindow; t += kSortThreads) {
     const int r = base + t;
     if (r < n) {
-      const unsigned long long len = (unsigned long long)(row[r + 1] - row[r]);
+      const unsigned long long len = (unsigned long long)laid_len(row, blen, r);
       key[t] = ((0x7fffffffull - len) << 32) | (unsigned)r;
     } else {
       key[t] = ~0ull;
@@ -226,13 +233,13 @@ __global__ void __launch_bounds__(kSortThreads) k_sell_window_sort(const int64_t
 }
 
 // width[s] = longest row of slice s; cnt[s] = 32 * width[s].
-__global__ void __launch_bounds__(kThreads) k_sell_widths(const int64_t *__restrict__ row, const int *__restrict__ perm, int nslices,
-                                                         int *width, long long *cnt) {
+__global__ void __launch_bounds__(kThreads) k_sell_widths(const int64_t *__restrict__ row, const int *__restrict__ blen,
+                                                         const int *__restrict__ perm, int nslices, int *width, long long *cnt) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int sl = warp; sl < nslices; sl += nw) {
     const int r = perm[sl * kSellC + lane];
-    const int w = (int)__reduce_max_sync(0xffffffffu, r >= 0 ? (unsigned)(row[r + 1] - row[r]) : 0u);
+    const int w = (int)__reduce_max_sync(0xffffffffu, r >= 0 ? (unsigned)laid_len(row, blen, r) : 0u);
     if (lane == 0) {
       width[sl] = w;
       cnt[sl] = (long long)w * kSellC;
@@ -280,6 +287,107 @@ __global__ void k_sell_fill(const int64_t *__restrict__ row, const int *__restri
   }
 }
 
+// Bridges each row needs for the 16-bit delta stream: (gap - 1) / 65,535 zero elements for a gap
+// between neighbouring columns; blen[r] = length + bridges.  A warp per row.  stats[0] counts
+// rows whose columns decrease (then there is no delta stream) or whose laid-out length would
+// overflow an int; stats[1] sums the bridges (one atomic per block).
+__global__ void __launch_bounds__(kThreads) k_row_bridges(const int64_t *__restrict__ row, const int *__restrict__ col, int n,
+                                                         int *blen, unsigned long long *stats) {
+  __shared__ unsigned long long s_br[kWarps], s_bad[kWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long br_w = 0, bad_w = 0;
+  for (int r = warp; r < n; r += nw) {
+    const int64_t b = row[r], len = row[r + 1] - b;
+    unsigned long long br = 0;
+    bool dec = false;
+    for (int64_t k = 1 + lane; k < len; k += 32) {
+      const long long gap = (long long)col[b + k] - col[b + k - 1];
+      if (gap < 0)
+        dec = true;
+      else if (gap > 0)
+        br += (unsigned long long)((gap - 1) / kSellBridge);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) br += __shfl_xor_sync(0xffffffffu, br, o);
+    dec = __any_sync(0xffffffffu, dec);
+    const unsigned long long laid = (unsigned long long)len + br;
+    if (lane == 0) {
+      blen[r] = laid > 0x7fffffffull ? 0x7fffffff : (int)laid;
+      br_w += br;
+      bad_w += (dec || laid > 0x7fffffffull) ? 1 : 0;
+    }
+  }
+  if (lane == 0) {
+    s_br[wib] = br_w;
+    s_bad[wib] = bad_w;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long a = 0, c = 0;
+    for (int i = 0; i < kWarps; ++i) {
+      a += s_br[i];
+      c += s_bad[i];
+    }
+    if (c) atomicAdd(stats, c);
+    if (a) atomicAdd(stats + 1, a);
+  }
+}
+
+// cnt[s] = checkpoint slots of slice s (32 per chunk of kSellChunk elements).
+__global__ void k_sell_chunks(const int *__restrict__ width, int nslices, long long *cnt) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nslices; s += gridDim.x * blockDim.x)
+    cnt[s] = (long long)((width[s] + kSellChunk - 1) / kSellChunk) * kSellC;
+}
+
+// Column-major fill of the bridged layout with both column streams, a thread per slot (the
+// row's elements are walked in order; neighbouring threads write neighbouring addresses).  A
+// bridge before an element whose column is more than 65,535 past the previous one sits 65,535
+// further on, with value 0; padding repeats the row's last column (the slot's own row for an
+// empty row, 0 for a slot without a row).  At every kSellChunk-th position the delta is 0 and
+// the checkpoint holds the column.
+__global__ void __launch_bounds__(kThreads) k_sell_fill_d16(const int64_t *__restrict__ row, const int *__restrict__ col,
+                                                           const double *__restrict__ val, const int *__restrict__ perm,
+                                                           const int *__restrict__ width, const int64_t *__restrict__ off,
+                                                           const int64_t *__restrict__ choff, int nslices, int *scol, double *sval,
+                                                           float *sval32, uint16_t *sd16, int *schk) {
+  const long slots = (long)nslices * kSellC;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < slots; t += (long)gridDim.x * blockDim.x) {
+    const int sl = (int)(t / kSellC), l = (int)(t % kSellC);
+    const int r = perm[t];
+    const int w = width[sl];
+    const int64_t b = (r >= 0) ? row[r] : 0;
+    const int64_t len = (r >= 0) ? row[r + 1] - b : 0;
+    const int64_t o = off[sl] + l, ch = choff[sl] + l;
+    int pos = 0;
+    int prev = r >= 0 ? r : 0;
+    auto put = [&](int c, double v, int d) {
+      const int64_t e = o + (int64_t)pos * kSellC;
+      scol[e] = c;
+      sval[e] = v;
+      if (sval32) sval32[e] = (float)v;
+      if (pos % kSellChunk == 0) {
+        schk[ch + (int64_t)(pos / kSellChunk) * kSellC] = c;
+        d = 0;
+      }
+      sd16[e] = (uint16_t)d;
+      prev = c;
+      ++pos;
+    };
+    for (int64_t i = 0; i < len; ++i) {
+      const int c = col[b + i];
+      const double v = val[b + i];
+      if (i == 0) {
+        put(c, v, 0);
+        continue;
+      }
+      while (c - prev > kSellBridge) put(prev + kSellBridge, 0.0, kSellBridge);
+      put(c, v, c - prev);
+    }
+    while (pos < w) put(prev, 0.0, 0);
+  }
+}
+
 }  // namespace
 
 void launch_validate(const int64_t *row, const int *col, int n, long nnz, int lower, int *bad, cudaStream_t st) {
@@ -299,8 +407,29 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   int w = kSellC;
   while (w < window && w < kSellWindow) w <<= 1;
   m->sell_window = w;
-  k_sell_window_sort<<<nwin, kSortThreads, 0, st>>>(m->row.get(), n, w, m->s_perm.get()); ::dg::count_launch();
-  k_sell_widths<<<warp_grid(nslices), kThreads, 0, st>>>(m->row.get(), m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
+  // The 16-bit delta stream: for matrices of at least kSellDeltaMin stored elements (smaller ones
+  // stay in L2, where fewer bytes buy nothing, and skip the check and its host synchronisation),
+  // rows sorted by column (every full CRS this library expands from a lower triangle is) and at
+  // most 1 bridge per 32 stored elements.  DG_SELL_DELTAS=0 turns it off, =1 tries it at any size.
+  constexpr long kSellDeltaMin = 1L << 22;
+  const char *env_d16 = std::getenv("DG_SELL_DELTAS");
+  bool d16 = env_d16 ? (env_d16[0] != '0' && m->nnz > 0) : (m->nnz >= kSellDeltaMin);
+  DevBuf<int> blen;
+  m->sell_bridges = 0;
+  if (d16) {
+    blen.alloc(n);
+    DevBuf<unsigned long long> stats(2);
+    DG_CUDA(cudaMemsetAsync(stats.get(), 0, 2 * sizeof(unsigned long long), st));
+    k_row_bridges<<<warp_grid(n), kThreads, 0, st>>>(m->row.get(), m->col.get(), n, blen.get(), stats.get()); ::dg::count_launch();
+    unsigned long long h[2] = {0, 0};
+    DG_CUDA(cudaMemcpyAsync(h, stats.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    d16 = h[0] == 0 && h[1] <= (unsigned long long)m->nnz / 32;
+    if (d16) m->sell_bridges = (long)h[1];
+  }
+  const int *bl = d16 ? blen.get() : nullptr;
+  k_sell_window_sort<<<nwin, kSortThreads, 0, st>>>(m->row.get(), bl, n, w, m->s_perm.get()); ::dg::count_launch();
+  k_sell_widths<<<warp_grid(nslices), kThreads, 0, st>>>(m->row.get(), bl, m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
   exclusive_scan(cnt.get(), nslices, m->s_off.get(), tmp.get(), st);
   int64_t total = 0;
   DG_CUDA(cudaMemcpyAsync(&total, m->s_off.get() + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -313,12 +442,29 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
     DG_CUDA(cudaMemsetAsync(m->s_err.get(), 0, sizeof(int), st));
   }
   const int g = vector_grid((long)nslots);
-  k_sell_fill<double><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
-                                              m->s_off.get(), nslices, m->s_col.get(), m->s_val.get()); ::dg::count_launch();
-  if (m->has32) {
-    m->s_val32.alloc(total);
-    k_sell_fill<float><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
-                                               m->s_off.get(), nslices, m->s_col.get(), m->s_val32.get()); ::dg::count_launch();
+  if (m->has32) m->s_val32.alloc(total);
+  if (d16) {
+    k_sell_chunks<<<vector_grid(nslices), kThreads, 0, st>>>(m->s_width.get(), nslices, cnt.get()); ::dg::count_launch();
+    m->s_choff.alloc(nslices + 1);
+    exclusive_scan(cnt.get(), nslices, m->s_choff.get(), tmp.get(), st);
+    // checkpoints: 32 per started chunk of a slice <= total / kSellChunk + 32 per slice
+    m->s_chk.alloc((size_t)total / kSellChunk + (size_t)nslices * kSellC);
+    m->s_d16.alloc(total);
+    k_sell_fill_d16<<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
+                                            m->s_off.get(), m->s_choff.get(), nslices, m->s_col.get(), m->s_val.get(),
+                                            m->has32 ? m->s_val32.get() : nullptr, m->s_d16.get(), m->s_chk.get()); ::dg::count_launch();
+  } else {
+    m->s_d16.release();
+    m->s_chk.release();
+    m->s_choff.release();
+    k_sell_fill<double><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
+                                                m->s_off.get(), nslices, m->s_col.get(), m->s_val.get()); ::dg::count_launch();
+    if (m->has32) {
+      k_sell_fill<float><<<g, kThreads, 0, st>>>(m->row.get(), m->col.get(), m->val.get(), m->s_perm.get(), m->s_width.get(),
+                                                 m->s_off.get(), nslices, m->s_col.get(), m->s_val32.get()); ::dg::count_launch();
+    }
+    if (sell_uses_deltas(m->sell_variant)) m->sell_variant = V_U8;
+    if (sell_uses_deltas(m->sell_variant32)) m->sell_variant32 = V_U8;
   }
   DG_CUDA(cudaGetLastError());
   choose_sell_shape(nslices, total, &m->sell_ws, &m->sell_grid);
@@ -329,6 +475,7 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   // pipelined form, which has no second group to overlap, is the slowest (12-14 % behind).
   const double per_row = (double)total / ((double)nslices * kSellC);
   m->sell_variant = (m->sell_ws >= 4 || per_row < 24.0) ? V_U16 : V_PIPE8;
+  m->sell_ws32 = m->sell_ws;
   DG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -511,6 +658,7 @@ int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid) {
                "warps_per_slice must be 1, 2, 4 or 8");
     DG_REQUIRE(grid >= 1 && grid <= (1 << 20), DG_ERR_ARG, "grid out of range");
     m->sell_ws = warps_per_slice;
+    m->sell_ws32 = warps_per_slice;
     m->sell_grid = grid;
     m->format = DG_FORMAT_SELL;
   });
@@ -699,10 +847,13 @@ int dg_matrix_set_sell_window(dg_matrix *m, int window) {
   return guarded([&] {
     DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
     DG_REQUIRE(window >= 1 && window <= kSellWindow, DG_ERR_ARG, "window must be in [1, %d]", kSellWindow);
-    const int ws = m->sell_ws, var = m->sell_variant;
+    const int ws = m->sell_ws, var = m->sell_variant, ws32 = m->sell_ws32, var32 = m->sell_variant32;
     build_sell(m, stream(), window);
     m->sell_ws = ws;
-    m->sell_variant = var;
+    m->sell_ws32 = ws32;
+    // a rebuilt layout without the delta stream falls back to 8-element groups
+    m->sell_variant = (sell_uses_deltas(var) && !m->has_d16()) ? V_U8 : var;
+    m->sell_variant32 = (sell_uses_deltas(var32) && !m->has_d16()) ? V_U8 : var32;
     m->format = DG_FORMAT_SELL;
   });
 }
@@ -722,8 +873,31 @@ int dg_matrix_set_sell_variant(dg_matrix *m, int variant) {
   return guarded([&] {
     DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
     DG_REQUIRE(variant >= 0 && variant < V_COUNT, DG_ERR_ARG, "unknown variant %d", variant);
+    DG_REQUIRE(!sell_uses_deltas(variant) || m->has_d16(), DG_ERR_ARG,
+               "variant %d needs the 16-bit column stream, which this matrix does not have", variant);
     m->sell_variant = variant;
     m->sell_variant32 = variant;
+  });
+}
+
+int dg_matrix_set_sell_mixed(dg_matrix *m, int warps_per_slice, int variant) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    DG_REQUIRE(warps_per_slice == 1 || warps_per_slice == 2 || warps_per_slice == 4 || warps_per_slice == 8, DG_ERR_ARG,
+               "warps_per_slice must be 1, 2, 4 or 8");
+    DG_REQUIRE(variant >= 0 && variant < V_COUNT, DG_ERR_ARG, "unknown variant %d", variant);
+    DG_REQUIRE(!sell_uses_deltas(variant) || m->has_d16(), DG_ERR_ARG,
+               "variant %d needs the 16-bit column stream, which this matrix does not have", variant);
+    m->sell_ws32 = warps_per_slice;
+    m->sell_variant32 = variant;
+  });
+}
+
+int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    if (present) *present = m->has_d16() ? 1 : 0;
+    if (bridges) *bridges = m->sell_bridges;
   });
 }
 
@@ -766,6 +940,7 @@ int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out) {
       if (m->sell_window != windows[wi]) build_sell(m, st, windows[wi]);
       for (int ws = 1; ws <= 8; ws <<= 1) {
         for (int var = 0; var < V_COUNT; ++var) {
+          if (sell_uses_deltas(var) && !m->has_d16()) continue;
           for (int bps : bps_list) {
             const int groups = kWarps / ws;
             const long need = (m->nslices + groups - 1) / groups;
@@ -799,8 +974,10 @@ int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out) {
       if (m->sell_window != best.window) build_sell(m, st, best.window);
       m->format = DG_FORMAT_SELL;
       m->sell_ws = best.shape;
+      m->sell_ws32 = best.shape;
       m->sell_variant = best.variant;
       m->sell_grid = best.grid;
+      if (sell_uses_deltas(m->sell_variant32) && !m->has_d16()) m->sell_variant32 = V_U8;
     } else {
       m->format = DG_FORMAT_CSR;
       m->lanes = best.shape;

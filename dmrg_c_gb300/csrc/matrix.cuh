@@ -24,6 +24,7 @@ struct dg_matrix {
   long nnz_sell = 0;               // stored elements including padding
   int sell_grid = 1;
   int sell_ws = 1;                 // warps per slice
+  int sell_ws32 = 1;               // warps per slice of the FP32 (mixed) product (same grid)
   int sell_variant = 1;            // SellVariant of the FP64 product (V_U8)
   int sell_variant32 = 1;          // SellVariant of the FP32 (mixed) product: 8-element groups
                                    // measured fastest there at every warps-per-slice count
@@ -33,11 +34,23 @@ struct dg_matrix {
   dg::DevBuf<double> s_val;
   dg::DevBuf<float> s_val32;
   dg::DevBuf<int> s_err;           // V_TMA stage-wait failures (0: none)
+  // 16-bit column deltas (sell.cuh), present when every row is sorted and gaps are rare
+  dg::DevBuf<uint16_t> s_d16;
+  dg::DevBuf<int> s_chk;
+  dg::DevBuf<int64_t> s_choff;
+  long sell_bridges = 0;           // zero elements bridging column gaps >= 65,536
 
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }
   dg::CrsOp<float> op32() const { return dg::CrsOp<float>{row.get(), col.get(), val32.get()}; }
-  dg::SellOp<double> sell64() const { return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant, s_err.get()}; }
-  dg::SellOp<float> sell32() const { return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws, sell_variant32, s_err.get()}; }
+  bool has_d16() const { return s_d16.get() != nullptr; }
+  dg::SellOp<double> sell64() const {
+    return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant,
+                              s_err.get(), s_d16.get(), s_chk.get(), s_choff.get()};
+  }
+  dg::SellOp<float> sell32() const {
+    return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws32, sell_variant32,
+                             s_err.get(), s_d16.get(), s_chk.get(), s_choff.get()};
+  }
 };
 
 namespace dg {
@@ -68,33 +81,43 @@ void launch_sell_ws(const SellOp<VT> &op, int grid, const XT *x, Scale sc, doubl
     case V_U4: launch_pdl(k_apply_sell<WS, V_U4, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
     case V_U16: launch_pdl(k_apply_sell<WS, V_U16, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
     case V_PIPE8: launch_pdl(k_apply_sell<WS, V_PIPE8, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
+    case V_D8:
+    case V_TMA16: launch_pdl(k_apply_sell<WS, V_D8, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
     default: launch_pdl(k_apply_sell<WS, V_U8, VT, XT, Epi>, grid, kThreads, st, op, x, sc, sigma, gate, epi, slot); break;
   }
 }
 
-// The streamed form: one warp per slice, tma_block_bytes<VT>() of dynamic shared memory (the
-// opt-in above 48 KB is set once per device and instantiation).
-template <class VT, class XT, class Epi>
+// The streamed form: one warp per slice, tma_block_bytes<VT, CT>() of dynamic shared memory
+// (the opt-in above 48 KB is set once per device and instantiation).
+template <bool D16, class VT, class XT, class Epi>
 void launch_sell_tma(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma, const int *gate, const Epi &epi,
                      RedSlot slot, cudaStream_t st) {
-  auto kern = k_apply_sell_tma<VT, XT, Epi>;
+  using CT = typename std::conditional<D16, uint16_t, int>::type;
+  auto kern = k_apply_sell_tma<D16, VT, XT, Epi>;
   static std::atomic<unsigned long long> ready{0};
   int dev = 0;
   DG_CUDA(cudaGetDevice(&dev));
   const unsigned long long bit = 1ull << (dev & 63);
   if (!(ready.load() & bit)) {
-    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_block_bytes<VT>()));
+    DG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_block_bytes<VT, CT>()));
     ready.fetch_or(bit);
   }
-  launch_pdl_smem(kern, dim3(grid), dim3(kThreads), (size_t)tma_block_bytes<VT>(), st, op, x, sc, sigma, gate, epi, slot);
+  launch_pdl_smem(kern, dim3(grid), dim3(kThreads), (size_t)tma_block_bytes<VT, CT>(), st, op, x, sc, sigma, gate, epi, slot);
 }
 
 template <class VT, class XT, class Epi>
 void launch_sell(const SellOp<VT> &op, int grid, const XT *x, Scale sc, double sigma,
                  const int *gate, const Epi &epi, RedSlot slot, cudaStream_t st) {
+  DG_REQUIRE(!sell_uses_deltas(op.variant) || (op.d16 && op.chk && op.choff), DG_ERR_INTERNAL,
+             "sliced-ELL variant %d needs the column delta stream", op.variant);
   // the bulk copies need 16-byte aligned arrays (pool allocations are 256-byte aligned)
   if (op.variant == V_TMA && op.ws == 1 && ((uintptr_t)op.col % 16) == 0 && ((uintptr_t)op.val % 16) == 0) {
-    launch_sell_tma(op, grid, x, sc, sigma, gate, epi, slot, st);
+    launch_sell_tma<false>(op, grid, x, sc, sigma, gate, epi, slot, st);
+    DG_CUDA(cudaGetLastError());
+    return;
+  }
+  if (op.variant == V_TMA16 && op.ws == 1 && ((uintptr_t)op.d16 % 16) == 0 && ((uintptr_t)op.val % 16) == 0) {
+    launch_sell_tma<true>(op, grid, x, sc, sigma, gate, epi, slot, st);
     DG_CUDA(cudaGetLastError());
     return;
   }

@@ -13,13 +13,23 @@
 //  * consecutive groups of 32 permuted rows form a slice, stored column-major and padded to
 //    the slice's longest row: element k of lane l sits at off[s] + 32 k + l, so the 32 lanes
 //    of a warp read 256 contiguous bytes of values and 128 of columns per step;
-//  * padding entries have value 0 and point at the row itself (an always-valid x index).
+//  * padding entries have value 0 and point at the row itself (an always-valid x index);
+//  * optionally (rows sorted by column, few long column gaps) a second column stream of 16-bit
+//    deltas: element k of a row holds col[k] - col[k-1], and at every kSellChunk-th element a
+//    32-bit checkpoint (op.chk) holds the column itself.  A gap of 65,536 or more between two
+//    neighbouring columns of a row is bridged by zero-valued elements placed 65,535 apart, so
+//    every delta fits 16 bits; the bridges add exact zeros and are part of the layout for every
+//    variant.  The FP32 product then streams 6 bytes an element instead of 8, the FP64 one 10
+//    instead of 12.
 //
 // With one warp per slice each row's elements are accumulated in their CRS order; with WS
-// warps per slice each warp sums every WS-th element and the partials are added in warp
-// order.  Either way the order is fixed, so the product is bitwise reproducible.
+// warps per slice each warp sums every WS-th element (the delta variants: every WS-th chunk of
+// kSellChunk elements, since a delta chain runs through a chunk) and the partials are added in
+// warp order.  Either way the order is fixed, so the product is bitwise reproducible, and with
+// one warp per slice every variant adds the same elements in the same order.
 #pragma once
 
+#include <cstdint>
 #include <type_traits>
 
 #include "apply.cuh"
@@ -28,6 +38,8 @@ namespace dg {
 
 constexpr int kSellC = 32;
 constexpr int kSellWindow = 2048;   // largest row-sorting window (shared-memory sort)
+constexpr int kSellChunk = 32;      // elements of a row between two column checkpoints
+constexpr int kSellBridge = 65535;  // largest column delta (a 16-bit field)
 
 template <class VT>
 struct SellOp {
@@ -40,6 +52,9 @@ struct SellOp {
   int ws;                            // warps per slice (1, 2, 4 or 8)
   int variant;                       // SellVariant
   int *err;                          // V_TMA: set to 1 when a stage wait ran out (may be null)
+  const uint16_t *__restrict__ d16;  // column deltas, laid out as col (null: no delta stream)
+  const int *__restrict__ chk;       // column of element k = kSellChunk j of each row: chk[choff[s] + 32 j + l]
+  const int64_t *__restrict__ choff; // nslices: first checkpoint of each slice
 };
 
 // Kernel variants (chosen per matrix by the autotuner, dg_matrix_autotune).  Each issues
@@ -49,9 +64,13 @@ struct SellOp {
 //   V_PIPE8              U=8 with the next group's columns/values loaded before the current
 //                        group's multiply-adds (software pipelining);
 //   V_TMA                one warp per slice, the slice streamed into shared memory by bulk
-//                        copies several stages ahead (sell_tma.cuh); other warp counts run V_U8.
+//                        copies several stages ahead (sell_tma.cuh); other warp counts run V_U8;
+//   V_D8                 the 16-bit delta stream, U=8 with the next group's loads issued before
+//                        the current group's multiply-adds; warps of a slice take whole chunks;
+//   V_TMA16              V_TMA on the delta stream; other warp counts run V_D8.
 // Measured on GB300 (FP64, 57M-element superblock): U=4 1.6 TB/s, U=8 4.5 TB/s.
-enum SellVariant : int { V_U4 = 0, V_U8 = 1, V_U16 = 2, V_PIPE8 = 3, V_TMA = 4, V_COUNT = 5 };
+enum SellVariant : int { V_U4 = 0, V_U8 = 1, V_U16 = 2, V_PIPE8 = 3, V_TMA = 4, V_D8 = 5, V_TMA16 = 6, V_COUNT = 7 };
+__host__ __device__ constexpr bool sell_uses_deltas(int variant) { return variant == V_D8 || variant == V_TMA16; }
 
 template <bool STREAM, class T>
 __device__ __forceinline__ T ld_mat(const T *p) {
@@ -151,15 +170,96 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
   return sell_row_acc<WS, U, PIPE, STREAM, VT, XT>(op, base, w, sub, x).get();
 }
 
+// The same on the delta stream.  A slice's chunks (kSellChunk elements of every row) are dealt
+// to its WS warps in turn; warp `sub` walks groups of 8 elements of its chunks in order,
+// restarting its running column at each chunk's checkpoint, with the next group's deltas,
+// values (and checkpoint) loaded before the current group's gathers and multiply-adds.  The
+// last chunk of the slice may be partial: its groups of 8, then single elements.
+template <int WS, class VT, class XT>
+__device__ __forceinline__ typename AccFor<VT, XT>::type sell_row_acc_d16(const SellOp<VT> &op, int sl, int lane, int sub,
+                                                                         const XT *__restrict__ x) {
+  constexpr int U = 8, GPC = kSellChunk / U;   // groups per full chunk
+  const int64_t base = op.off[sl] + lane;
+  const int w = op.width[sl];
+  const int nch = (w + kSellChunk - 1) / kSellChunk;
+  const int *const chk = op.chk + op.choff[sl] + lane;
+  // this warp's chunks: sub, sub + WS, ...; every one full except possibly the slice's last
+  const int mine = (nch > sub) ? (nch - sub + WS - 1) / WS : 0;
+  const int last = nch - 1, tail = w - last * kSellChunk;   // elements of the last chunk
+  const bool owns_last = mine > 0 && (last - sub) % WS == 0;
+  const int Q = (owns_last ? (mine - 1) * GPC + tail / U : mine * GPC);   // full groups of this warp
+  typename AccFor<VT, XT>::type acc;
+  auto kpos = [&](int q) { return (sub + (q / GPC) * WS) * kSellChunk + (q % GPC) * U; };
+  uint16_t d[U];
+  VT v[U];
+  int cnext = 0;
+  if (Q > 0) {
+    const int64_t p = base + (int64_t)kpos(0) * kSellC;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      d[u] = op.d16[p + u * kSellC];
+      v[u] = op.val[p + u * kSellC];
+    }
+    cnext = chk[(int64_t)sub * kSellC];
+  }
+  int c = 0;
+  for (int q = 0; q < Q; ++q) {
+    if (q % GPC == 0) c = cnext;   // chunk start: the delta there is 0
+    int cc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      c += d[u];
+      cc[u] = c;
+    }
+    VT vc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) vc[u] = v[u];
+    XT xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = x[cc[u]];
+    if (q + 1 < Q) {
+      const int kn = kpos(q + 1);
+      const int64_t p = base + (int64_t)kn * kSellC;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        d[u] = op.d16[p + u * kSellC];
+        v[u] = op.val[p + u * kSellC];
+      }
+      if ((q + 1) % GPC == 0) cnext = chk[(int64_t)(kn / kSellChunk) * kSellC];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc.add(vc[u], xv[u]);
+  }
+  if (owns_last && tail % U) {
+    int k = last * kSellChunk + (tail / U) * U;
+    if (tail < U) c = chk[(int64_t)last * kSellC];   // no full group of this chunk ran
+    for (; k < w; ++k) {
+      const int64_t p = base + (int64_t)k * kSellC;
+      c += op.d16[p];
+      acc.add(op.val[p], x[c]);
+    }
+  }
+  return acc;
+}
+
+// Row partial of slot `lane` of slice sl for warp `sub` of WS, in the variant's form.
+template <int WS, int VAR, class VT, class XT>
+__device__ __forceinline__ typename AccFor<VT, XT>::type slice_row_acc(const SellOp<VT> &op, int sl, int lane, int sub,
+                                                                      const XT *__restrict__ x) {
+  if constexpr (VAR == V_D8) {
+    return sell_row_acc_d16<WS, VT, XT>(op, sl, lane, sub, x);
+  } else {
+    constexpr int U = (VAR == V_U4) ? 4 : (VAR == V_U16) ? 16 : 8;
+    return sell_row_acc<WS, U, VAR == V_PIPE8, false, VT, XT>(op, op.off[sl] + lane, op.width[sl], sub, x);
+  }
+}
+
 template <int WS, int VAR, class VT, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
 k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, const int *gate,
              Epi epi, RedSlot slot) {
   pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
-  constexpr int U = (VAR == V_U4) ? 4 : (VAR == V_U16) ? 16 : 8;
-  constexpr bool PIPE = (VAR == V_PIPE8);
-  constexpr bool STREAM = false;
   const double s = begin_scale(sc, epi);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;          // warp in block
@@ -182,7 +282,7 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, co
     const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
     for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
       const int row = op.perm[sl * kSellC + lane];
-      const AccDot2 r = sell_row_acc<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x);
+      const AccDot2 r = slice_row_acc<1, VAR>(op, sl, lane, 0, x);
       float sum = __fadd_rn(r.p, r.c);
       if (sf != 1.0f) sum = __fmul_rn(sum, sf);
       if (row >= 0) {
@@ -196,7 +296,7 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, co
     const int warp_global = blockIdx.x * kWarps + wib, nwarps = gridDim.x * kWarps;
     for (int sl = warp_global; sl < op.nslices; sl += nwarps) {
       const int row = op.perm[sl * kSellC + lane];
-      double sum = sell_row_sum<1, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], 0, x);
+      double sum = slice_row_acc<1, VAR>(op, sl, lane, 0, x).get();
       if (s != 1.0) sum *= s;   // s (H x)_i: one multiply per row instead of one per element
       if (row >= 0) {
         const double xi = (s == 1.0) ? to_d(x[row]) : to_d(x[row]) * s;
@@ -208,7 +308,7 @@ k_apply_sell(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, co
     for (int sl0 = blockIdx.x * GROUPS; sl0 < op.nslices; sl0 += gridDim.x * GROUPS) {
       const int sl = sl0 + group;
       const bool live = sl < op.nslices;
-      double sum = live ? sell_row_sum<WS, U, PIPE, STREAM>(op, op.off[sl] + lane, op.width[sl], sub, x) : 0.0;
+      double sum = live ? slice_row_acc<WS, VAR>(op, sl, lane, sub, x).get() : 0.0;
       part[WS > 1 ? wib : 0][lane] = sum;
       __syncthreads();
       if (sub == 0) {

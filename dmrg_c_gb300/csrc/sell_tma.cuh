@@ -12,6 +12,10 @@
 // its gathers.  Element order per row, accumulation and epilogues are those of the one-warp-a-
 // slice kernel, so the results are bitwise the same.
 //
+// On the delta stream (V_TMA16) the stages carry 16-bit column deltas instead of 32-bit
+// columns and each lane keeps its running column, restarted from the checkpoint at every
+// kSellChunk-th element (loaded one chunk ahead).
+//
 // Every wait on an mbarrier is bounded: after kTmaSpinLimit polls (the decision taken by the
 // whole warp) the warp records the failure in op.err (read by dg_matrix_sell_error), stops
 // issuing copies, waits (again bounded) for every copy it has in flight and leaves the slice
@@ -19,6 +23,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 
 #include "sell.cuh"
 
@@ -27,14 +32,16 @@ namespace dg {
 constexpr int kTmaStages = 4;   // stages in flight per warp
 constexpr int kTmaK = 8;        // elements of every row per stage
 constexpr unsigned kTmaSpinLimit = 1u << 22;   // polls of a stage's mbarrier before giving up
+static_assert(kSellChunk % kTmaK == 0, "a stage never straddles a column checkpoint");
 
-template <class VT>
+// CT: the column element of a stage (int, or uint16_t deltas)
+template <class VT, class CT>
 constexpr int tma_warp_bytes() {
-  return kTmaStages * kTmaK * kSellC * (int)(sizeof(int) + sizeof(VT));
+  return kTmaStages * kTmaK * kSellC * (int)(sizeof(CT) + sizeof(VT));
 }
-template <class VT>
+template <class VT, class CT>
 constexpr int tma_block_bytes() {
-  return kWarps * tma_warp_bytes<VT>() + kWarps * kTmaStages * 8;   // stages, then the mbarriers
+  return kWarps * tma_warp_bytes<VT, CT>() + kWarps * kTmaStages * 8;   // stages, then the mbarriers
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -63,7 +70,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
 }
 // One stage: both copies complete on bar, which expects their bytes.  Sizes and addresses are
 // multiples of 16 bytes (slices start at multiples of 32 elements; a stage is k * 32 elements).
-__device__ __forceinline__ void tma_stage(uint64_t *bar, int *scol, const int *gcol, void *sval, const void *gval, unsigned bcol,
+__device__ __forceinline__ void tma_stage(uint64_t *bar, void *scol, const void *gcol, void *sval, const void *gval, unsigned bcol,
                                           unsigned bval) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the lanes' reads of the reused stage come first
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bcol + bval) : "memory");
@@ -76,18 +83,21 @@ __device__ __forceinline__ void tma_stage(uint64_t *bar, int *scol, const int *g
 }
 
 // y = ((H + sigma) s x) through the epilogue, one warp per slice (WS = 1), the slice streamed
-// through the warp's stage ring.  Dynamic shared memory: tma_block_bytes<VT>().
-template <class VT, class XT, class Epi>
+// through the warp's stage ring; D16: the column deltas instead of the columns.  Dynamic shared
+// memory: tma_block_bytes<VT, CT>().
+template <bool D16, class VT, class XT, class Epi>
 __global__ void __launch_bounds__(kThreads)
 k_apply_sell_tma(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma, const int *gate, Epi epi, RedSlot slot) {
+  using CT = typename std::conditional<D16, uint16_t, int>::type;
   pdl_wait();
   if (gate && *((volatile const int *)gate)) return;
   const double s = begin_scale(sc, epi);
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   extern __shared__ __align__(128) unsigned char tma_smem[];
-  int *const scol = reinterpret_cast<int *>(tma_smem + (size_t)wib * tma_warp_bytes<VT>());
+  CT *const scol = reinterpret_cast<CT *>(tma_smem + (size_t)wib * tma_warp_bytes<VT, CT>());
   VT *const sval = reinterpret_cast<VT *>(scol + kTmaStages * kTmaK * kSellC);
-  uint64_t *const bar = reinterpret_cast<uint64_t *>(tma_smem + (size_t)kWarps * tma_warp_bytes<VT>()) + wib * kTmaStages;
+  uint64_t *const bar = reinterpret_cast<uint64_t *>(tma_smem + (size_t)kWarps * tma_warp_bytes<VT, CT>()) + wib * kTmaStages;
+  const CT *const gcol = D16 ? reinterpret_cast<const CT *>(op.d16) : reinterpret_cast<const CT *>(op.col);
   if (lane == 0) {
     for (int t = 0; t < kTmaStages; ++t) mbar_init(bar + t);
     mbar_fence_init();
@@ -113,9 +123,14 @@ k_apply_sell_tma(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma
       const int k0 = t * kTmaK, kk = min(kTmaK, width - k0);
       const int slot_i = t % kTmaStages;
       const int64_t g = base + (int64_t)k0 * kSellC;
-      tma_stage(bar + slot_i, scol + slot_i * kTmaK * kSellC, op.col + g, sval + slot_i * kTmaK * kSellC, op.val + g,
-                (unsigned)(kk * kSellC * sizeof(int)), (unsigned)(kk * kSellC * sizeof(VT)));
+      tma_stage(bar + slot_i, scol + slot_i * kTmaK * kSellC, gcol + g, sval + slot_i * kTmaK * kSellC, op.val + g,
+                (unsigned)(kk * kSellC * sizeof(CT)), (unsigned)(kk * kSellC * sizeof(VT)));
     };
+    // delta stream: the running column and the checkpoint of the next chunk
+    const int *const chk = D16 ? op.chk + op.choff[sl] + lane : nullptr;
+    int c = 0, cnext = 0;
+    if constexpr (D16)
+      if (width > 0) cnext = chk[0];
     if (lane == 0)
       for (int t = 0; t < min(kTmaStages, nst); ++t) issue(t);
     Acc r;
@@ -128,17 +143,32 @@ k_apply_sell_tma(SellOp<VT> op, const XT *__restrict__ x, Scale sc, double sigma
       }
       parity ^= 1u << slot_i;
       const int kk = min(kTmaK, width - t * kTmaK);
-      const int *c = scol + slot_i * kTmaK * kSellC + lane;
+      const CT *sc_ = scol + slot_i * kTmaK * kSellC + lane;
       const VT *v = sval + slot_i * kTmaK * kSellC + lane;
       int cc[kTmaK];
       VT vv[kTmaK];
       XT xv[kTmaK];
-#pragma unroll
-      for (int u = 0; u < kTmaK; ++u)
-        if (u < kk) {
-          cc[u] = c[u * kSellC];
-          vv[u] = v[u * kSellC];
+      if constexpr (D16) {
+        const int k0 = t * kTmaK;
+        if (k0 % kSellChunk == 0) {   // chunk start (its delta is 0): restart from the checkpoint
+          c = cnext;
+          if (k0 + kSellChunk < width) cnext = chk[(int64_t)(k0 / kSellChunk + 1) * kSellC];
         }
+#pragma unroll
+        for (int u = 0; u < kTmaK; ++u)
+          if (u < kk) {
+            c += sc_[u * kSellC];
+            cc[u] = c;
+            vv[u] = v[u * kSellC];
+          }
+      } else {
+#pragma unroll
+        for (int u = 0; u < kTmaK; ++u)
+          if (u < kk) {
+            cc[u] = sc_[u * kSellC];
+            vv[u] = v[u * kSellC];
+          }
+      }
 #pragma unroll
       for (int u = 0; u < kTmaK; ++u)
         if (u < kk) xv[u] = x[cc[u]];

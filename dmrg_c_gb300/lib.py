@@ -107,6 +107,8 @@ SIGNATURES = {
     "dg_matrix_set_sell_shape": (C.c_int, [vp, C.c_int, C.c_int]),
     "dg_matrix_set_sell_variant": (C.c_int, [vp, C.c_int]),
     "dg_matrix_sell_error": (C.c_int, [vp, C.POINTER(C.c_int)]),
+    "dg_matrix_set_sell_mixed": (C.c_int, [vp, C.c_int, C.c_int]),
+    "dg_matrix_sell_deltas": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_long)]),
     "dg_matrix_set_sell_window": (C.c_int, [vp, C.c_int]),
     "dg_matrix_autotune": (C.c_int, [vp, C.c_int, P(abi.dg_tune_result)]),
     "dg_matrix_format": (C.c_int, [vp, ip, lp]),
@@ -249,6 +251,16 @@ class DeviceMatrix:
 
     def set_sell_variant(self, variant: int):
         check(load().dg_matrix_set_sell_variant(self.h, variant))
+
+    def set_sell_mixed(self, warps_per_slice: int, variant: int):
+        """Warps per slice and variant of the FP32 (mixed-precision) product alone."""
+        check(load().dg_matrix_set_sell_mixed(self.h, warps_per_slice, variant))
+
+    def sell_deltas(self) -> tuple[bool, int]:
+        """(whether the 16-bit column-delta stream exists, its zero bridge elements)."""
+        present, bridges = C.c_int(0), C.c_long(0)
+        check(load().dg_matrix_sell_deltas(self.h, C.byref(present), C.byref(bridges)))
+        return bool(present.value), bridges.value
 
     def sell_error(self) -> int:
         e = C.c_int(0)

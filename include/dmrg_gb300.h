@@ -194,12 +194,23 @@ int dg_matrix_set_format(dg_matrix *m, int format);
 int dg_matrix_set_sell_shape(dg_matrix *m, int warps_per_slice, int grid);
 /* Sliced-ELL kernel variant: element groups of 0: 4, 1: 8, 2: 16, 3: 8 with
  * software-pipelined loads; 4: one warp per slice with the slice streamed into shared memory
- * by bulk copies (with more warps per slice it runs variant 1).  The FP64 product's default
- * follows the warps per slice (3 for 1-2 warps, 2 for 4-8), the FP32 (mixed) product's is 1;
- * this call sets both. */
+ * by bulk copies (with more warps per slice it runs variant 1); 5: groups of 8 on the 16-bit
+ * column-delta stream (warps of a slice take whole 32-element chunks); 6: variant 4 on the
+ * delta stream (with more warps per slice it runs variant 5).  Variants 5 and 6 need the delta
+ * stream (dg_matrix_sell_deltas; DG_ERR_ARG otherwise).  The FP64 product's default follows
+ * the warps per slice (3 for 1-2 warps, 2 for 4-8), the FP32 (mixed) product's is 1; this call
+ * sets both. */
 int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
-/* *err = 1 if a streamed (variant 4) product of this matrix ever gave up waiting for a stage
- * of its copies (the product is then incomplete), else 0. */
+/* Warps per slice and variant of the FP32 (mixed-precision) product alone; it keeps the grid
+ * of dg_matrix_set_sell_shape. */
+int dg_matrix_set_sell_mixed(dg_matrix *m, int warps_per_slice, int variant);
+/* *present = 1 if the sliced-ELL copy carries the 16-bit column-delta stream (built for
+ * matrices of at least 4M stored elements whose rows are sorted by column and need at most one
+ * zero bridge element per 32 stored ones for gaps of 65,536 columns or more), and the number
+ * of bridge elements. */
+int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges);
+/* *err = 1 if a streamed (variant 4 or 6) product of this matrix ever gave up waiting for a
+ * stage of its copies (the product is then incomplete), else 0. */
 int dg_matrix_sell_error(const dg_matrix *m, int *err);
 /* Rebuild the sliced-ELL copy sorting rows by length within windows of `window` rows
  * (1..2048; <= 32 keeps the original row order). */

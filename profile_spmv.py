@@ -6,6 +6,8 @@
                                                              # a few launches, for an ncu capture
     python profile_spmv.py --case hubbard_m512 --mixed --launches 3
                                                              # the mixed-precision product
+    python profile_spmv.py --case dmrg_hubbard_m512 --mixed --launches 3 --ws 2 --variant 5
+                                                             # a given shape and kernel variant
     python profile_spmv.py --sweep --cases xxz_ed22 hubbard_ed12
                                                              # the ED Hamiltonians
     python profile_spmv.py --build ed_hubbard12 # device ED build (basis + CRS)
@@ -111,7 +113,9 @@ def survey(names, sweep, iters, out, mixed=False):
             for window in (2048, 32):
                 m.set_sell_window(window)
                 for ws in (1, 2, 4, 8):
-                    for var in range(4):
+                    for var in range(7):
+                        if (var in (5, 6) and not m.sell_deltas()[0]) or (var in (4, 6) and ws > 1):
+                            continue   # no delta stream / the streamed forms run one warp a slice
                         m.set_sell_shape(ws, _sell_grid(n, ws, sms))
                         m.set_sell_variant(var)
                         c, w = _rate(m, x, y, iters)
@@ -138,13 +142,23 @@ def survey(names, sweep, iters, out, mixed=False):
             json.dump(rows, f, indent=1)
 
 
-def launches(name, fmt, count, mixed=False):
-    """`count` launches of one kernel on one matrix (nothing else on the device after setup)."""
+def launches(name, fmt, count, mixed=False, ws=None, grid=None, variant=None, window=None):
+    """`count` launches of one kernel on one matrix (nothing else on the device after setup);
+    ws / grid / variant / window override the sliced-ELL shape the library chose."""
     import torch
     m = _matrix(name, L.DG_VALUES_BOTH if mixed else L.DG_VALUES_F64)
     x = torch.randn(m.n, dtype=torch.float64, device="cuda")
     if fmt == "csr":
         m.set_shape(8, _csr_grid(m.n, 8, torch.cuda.get_device_properties(x.device).multi_processor_count))
+    else:
+        if window is not None:
+            m.set_sell_window(window)
+        if ws is not None or grid is not None:
+            sms = torch.cuda.get_device_properties(x.device).multi_processor_count
+            w = ws if ws is not None else 1
+            m.set_sell_shape(w, grid if grid is not None else _sell_grid(m.n, w, sms))
+        if variant is not None:
+            m.set_sell_variant(variant)
     y = torch.empty_like(x)
     if mixed:
         t = m.profile_spmv_mixed(x.float(), y, iters=count)
@@ -481,6 +495,10 @@ def main(argv=None):
     ap.add_argument("--format", choices=["sell", "csr"], default="sell")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--mixed", action="store_true")
+    ap.add_argument("--ws", type=int, default=None, help="warps per slice (with --case)")
+    ap.add_argument("--grid", type=int, default=None, help="blocks (with --case)")
+    ap.add_argument("--variant", type=int, default=None, help="sliced-ELL kernel variant (with --case)")
+    ap.add_argument("--window", type=int, default=None, help="row-sorting window (with --case)")
     ap.add_argument("--build", choices=BUILDS, default=None)
     ap.add_argument("--obc", choices=list(CASES), default=None, help="matrix-free vs explicit Lanczos on a superblock")
     ap.add_argument("--vm", action="store_true", help="EXACT_V_M_Q0 on the Hubbard L=12 basis")
@@ -505,7 +523,7 @@ def main(argv=None):
     elif a.build:
         build(a.build)
     elif a.case:
-        launches(a.case, a.format, a.launches, a.mixed)
+        launches(a.case, a.format, a.launches, a.mixed, a.ws, a.grid, a.variant, a.window)
     else:
         survey(a.cases, a.sweep, a.iters, a.json, a.mixed)
     return 0
