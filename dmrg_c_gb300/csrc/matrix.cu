@@ -427,6 +427,9 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
     d16 = h[0] == 0 && h[1] <= (unsigned long long)m->nnz / 32;
     if (d16) m->sell_bridges = (long)h[1];
   }
+  // chunks a warp of the delta kernel prefetches into L2 ahead of its loads: DG_SELL_PREFETCH=0..4
+  const char *env_pf = std::getenv("DG_SELL_PREFETCH");
+  m->sell_pf = (env_pf && env_pf[0] >= '0' && env_pf[0] <= '4' && !env_pf[1]) ? env_pf[0] - '0' : 1;
   const int *bl = d16 ? blen.get() : nullptr;
   k_sell_window_sort<<<nwin, kSortThreads, 0, st>>>(m->row.get(), bl, n, w, m->s_perm.get()); ::dg::count_launch();
   k_sell_widths<<<warp_grid(nslices), kThreads, 0, st>>>(m->row.get(), bl, m->s_perm.get(), nslices, m->s_width.get(), cnt.get()); ::dg::count_launch();
@@ -475,7 +478,18 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   // pipelined form, which has no second group to overlap, is the slowest (12-14 % behind).
   const double per_row = (double)total / ((double)nslices * kSellC);
   m->sell_variant = (m->sell_ws >= 4 || per_row < 24.0) ? V_U16 : V_PIPE8;
-  m->sell_ws32 = m->sell_ws;
+  // The FP32 product on the delta stream (6 bytes an element instead of 8): on the config-5
+  // superblock (238 k rows of 236) 8-element groups with the next chunk prefetched into L2 took
+  // 79 us at one warp per slice and 81 at two, against 92 us for the 32-bit columns.  One warp a
+  // slice needs enough slices to fill the GPU (24 a SM); the FP64 product, bound by FP64 issue,
+  // gains nothing from the deltas and keeps its variant.
+  if (m->has_d16()) {
+    m->sell_variant32 = V_D8;
+    m->sell_ws32 = (m->sell_ws <= 2 && (long)nslices >= 24L * sm_count()) ? 1 : m->sell_ws;
+  } else {
+    if (sell_uses_deltas(m->sell_variant32)) m->sell_variant32 = V_U8;
+    m->sell_ws32 = m->sell_ws;
+  }
   DG_CUDA(cudaStreamSynchronize(st));
 }
 

@@ -39,17 +39,18 @@ struct dg_matrix {
   dg::DevBuf<int> s_chk;
   dg::DevBuf<int64_t> s_choff;
   long sell_bridges = 0;           // zero elements bridging column gaps >= 65,536
+  int sell_pf = 1;                 // V_D8 L2 prefetch distance in chunks (DG_SELL_PREFETCH)
 
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }
   dg::CrsOp<float> op32() const { return dg::CrsOp<float>{row.get(), col.get(), val32.get()}; }
   bool has_d16() const { return s_d16.get() != nullptr; }
   dg::SellOp<double> sell64() const {
     return dg::SellOp<double>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val.get(), nslices, sell_ws, sell_variant,
-                              s_err.get(), s_d16.get(), s_chk.get(), s_choff.get()};
+                              s_err.get(), s_d16.get(), s_chk.get(), s_choff.get(), sell_pf};
   }
   dg::SellOp<float> sell32() const {
     return dg::SellOp<float>{s_off.get(), s_width.get(), s_perm.get(), s_col.get(), s_val32.get(), nslices, sell_ws32, sell_variant32,
-                             s_err.get(), s_d16.get(), s_chk.get(), s_choff.get()};
+                             s_err.get(), s_d16.get(), s_chk.get(), s_choff.get(), sell_pf};
   }
 };
 

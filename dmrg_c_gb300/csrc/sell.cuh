@@ -55,7 +55,15 @@ struct SellOp {
   const uint16_t *__restrict__ d16;  // column deltas, laid out as col (null: no delta stream)
   const int *__restrict__ chk;       // column of element k = kSellChunk j of each row: chk[choff[s] + 32 j + l]
   const int64_t *__restrict__ choff; // nslices: first checkpoint of each slice
+  int pf;                            // V_D8: chunks of its own a warp prefetches into L2 ahead (0: none)
 };
+
+// Bulk prefetch of [p, p + bytes) into L2 by the copy engine (16-byte aligned address and size);
+// no completion to wait for and no registers held, so a warp keeps more of its matrix stream in
+// flight than its load registers allow.
+__device__ __forceinline__ void l2_prefetch_bulk(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 
 // Kernel variants (chosen per matrix by the autotuner, dg_matrix_autotune).  Each issues
 // U column/value loads, then U gathers of x, then U DFMAs per group; more groups in flight
@@ -173,7 +181,8 @@ __device__ __forceinline__ double sell_row_sum(const SellOp<VT> &op, int64_t bas
 // The same on the delta stream.  A slice's chunks (kSellChunk elements of every row) are dealt
 // to its WS warps in turn; warp `sub` walks groups of 8 elements of its chunks in order,
 // restarting its running column at each chunk's checkpoint, with the next group's deltas,
-// values (and checkpoint) loaded before the current group's gathers and multiply-adds.  The
+// values (and checkpoint) loaded before the current group's gathers and multiply-adds, and
+// (op.pf > 0) its chunk op.pf turns ahead prefetched into L2 by lane 0 at every chunk start.  The
 // last chunk of the slice may be partial: its groups of 8, then single elements.
 template <int WS, class VT, class XT>
 __device__ __forceinline__ typename AccFor<VT, XT>::type sell_row_acc_d16(const SellOp<VT> &op, int sl, int lane, int sub,
@@ -190,6 +199,19 @@ __device__ __forceinline__ typename AccFor<VT, XT>::type sell_row_acc_d16(const 
   const int Q = (owns_last ? (mine - 1) * GPC + tail / U : mine * GPC);   // full groups of this warp
   typename AccFor<VT, XT>::type acc;
   auto kpos = [&](int q) { return (sub + (q / GPC) * WS) * kSellChunk + (q % GPC) * U; };
+  // chunk jn of the slice: its deltas, values and checkpoints, into L2 (slices start at
+  // multiples of 32 elements and chunks at multiples of kSellChunk: every address and size is
+  // a multiple of 64 bytes)
+  auto prefetch_chunk = [&](int jn) {
+    const int64_t e = base - lane + (int64_t)jn * kSellChunk * kSellC;
+    const unsigned cnt = (unsigned)min(kSellChunk, w - jn * kSellChunk) * kSellC;
+    l2_prefetch_bulk(op.d16 + e, cnt * (unsigned)sizeof(uint16_t));
+    l2_prefetch_bulk(op.val + e, cnt * (unsigned)sizeof(VT));
+    l2_prefetch_bulk(chk - lane + (int64_t)jn * kSellC, kSellC * (unsigned)sizeof(int));
+  };
+  if (op.pf > 0 && lane == 0)
+    for (int a = 1; a < op.pf; ++a)
+      if (sub + a * WS < nch) prefetch_chunk(sub + a * WS);
   uint16_t d[U];
   VT v[U];
   int cnext = 0;
@@ -204,7 +226,11 @@ __device__ __forceinline__ typename AccFor<VT, XT>::type sell_row_acc_d16(const 
   }
   int c = 0;
   for (int q = 0; q < Q; ++q) {
-    if (q % GPC == 0) c = cnext;   // chunk start: the delta there is 0
+    if (q % GPC == 0) {
+      c = cnext;   // chunk start: the delta there is 0
+      const int jn = sub + (q / GPC + op.pf) * WS;
+      if (op.pf > 0 && lane == 0 && jn < nch) prefetch_chunk(jn);
+    }
     int cc[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
