@@ -24,7 +24,9 @@ One step = one ground-state solve as DMRG_DIAGONALIZE_SUPERBLOCK_SYM does it: La
 * ``sweeps``: every recorded sweep superblock of klm_vf and hubbard_vf solved FP64 and in both
   mixed forms: |dE|/|E| against the reference's gs_val per sweep.
 * ``roofline``: the fused FP64 product kernel on the workload, CUDA-event timed, algorithmic bytes
-  nnz_full*12 + (n+1)*4 + 2*n*8 per launch; ``roofline_mixed`` the FP32-value product.
+  nnz_full*12 + (n+1)*4 + 2*n*8 per launch; ``roofline_mixed`` the FP32-value product, with the
+  bytes of the layout it reads (the 16-bit column-delta stream when the matrix has one) and the
+  CRS-equivalent rate beside them.
 * ``cpu_baseline``: the oracle's OpenMP restatement of the same solve on all host cores.
 
 ``--impl reference`` times the CPU path (the oracle port of the reference's LANCZOS_SYM +
@@ -212,6 +214,23 @@ def peaks():
 
 def spmv_bytes(n, nnz_full, s_val=8, s_vec=8):
     return nnz_full * (s_val + 4) + (n + 1) * 4 + 2 * n * s_vec
+
+
+def sell_mixed_bytes(m, n, nnz_full):
+    """Bytes one FP32 (mixed) product must move in the layout it runs on.  With the 16-bit delta
+    stream: every stored slot's delta (2 B) and FP32 value (4 B), the 32-bit checkpoints, the slot
+    row map, the per-slice offsets / widths / checkpoint offsets, x (FP32) and y (FP64); else the
+    CRS footprint nnz_full*8 + (n+1)*4 + 2*n*4."""
+    from dmrg_c_gb300 import lib as L
+    cfg = m.sell_config()
+    present, _bridges = m.sell_deltas()
+    fmt, stored = m.format()
+    if fmt != L.DG_FORMAT_SELL or not present or cfg["variant32"] not in (5, 6):
+        return spmv_bytes(n, nnz_full, 4, 4), "CRS footprint: nnz_full*8 + (n+1)*4 + 2*n*4"
+    nslices = -(-n // 2048) * 2048 // 32
+    b = stored * 6 + m.sell_checkpoints() * 4 + nslices * 32 * 4 + nslices * 20 + n * 4 + n * 8
+    return b, ("delta layout: stored slots*(2+4) + checkpoints*4 + slot rows*4 + slices*20 + n*4 (x) "
+               "+ n*8 (y)")
 
 
 def traffic_from_profile(name, mixed=False):
@@ -530,7 +549,9 @@ def run_gb300(args, ws, rank, local_rank):
     spmv_ms = m.profile_spmv(x, y, iters=30, flush_bytes=FLUSH_BYTES)
     spmv_warm_ms = m.profile_spmv(x, y, iters=30, flush_bytes=0)
     spmv32_ms = m.profile_spmv_mixed(x.float(), y, iters=30, flush_bytes=FLUSH_BYTES)
-    B, B32 = spmv_bytes(n, nnz_full), spmv_bytes(n, nnz_full, 4, 4)
+    B = spmv_bytes(n, nnz_full)
+    B32, B32_basis = sell_mixed_bytes(m, n, nnz_full)
+    B32_crs = spmv_bytes(n, nnz_full, 4, 4)
     peak, peak_kind = peaks()
     achieved, achieved32 = B / (spmv_ms * 1e-3) / 1e9, B32 / (spmv32_ms * 1e-3) / 1e9
 
@@ -596,7 +617,9 @@ def run_gb300(args, ws, rank, local_rank):
         "roofline_mixed": {"bound": "hbm", "achieved": achieved32, "peak": peak, "unit": "GB/s", "frac": achieved32 / peak,
                            "traffic": traffic_from_profile(args.workload, mixed=True), "peak_source": peak_kind,
                            "kernel": "k_apply_sell<float> (FP32 values and x, compensated FP32 sums)",
-                           "ms_per_launch": spmv32_ms, "bytes_per_launch": B32},
+                           "sell_config": m.sell_config(), "ms_per_launch": spmv32_ms, "bytes_per_launch": B32,
+                           "bytes_basis": B32_basis, "crs_bytes_per_launch": B32_crs,
+                           "crs_equivalent_gbs": B32_crs / (spmv32_ms * 1e-3) / 1e9},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "mixed": mixed,

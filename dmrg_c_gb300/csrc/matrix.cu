@@ -446,10 +446,12 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   }
   const int g = vector_grid((long)nslots);
   if (m->has32) m->s_val32.alloc(total);
+  int64_t nchk = 0;
   if (d16) {
     k_sell_chunks<<<vector_grid(nslices), kThreads, 0, st>>>(m->s_width.get(), nslices, cnt.get()); ::dg::count_launch();
     m->s_choff.alloc(nslices + 1);
     exclusive_scan(cnt.get(), nslices, m->s_choff.get(), tmp.get(), st);
+    DG_CUDA(cudaMemcpyAsync(&nchk, m->s_choff.get() + nslices, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     // checkpoints: 32 per started chunk of a slice <= total / kSellChunk + 32 per slice
     m->s_chk.alloc((size_t)total / kSellChunk + (size_t)nslices * kSellC);
     m->s_d16.alloc(total);
@@ -491,6 +493,7 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
     m->sell_ws32 = m->sell_ws;
   }
   DG_CUDA(cudaStreamSynchronize(st));
+  m->sell_checkpoints = (long)nchk;
 }
 
 void choose_sell_shape(int nslices, long stored, int *ws, int *grid) {
@@ -907,11 +910,23 @@ int dg_matrix_set_sell_mixed(dg_matrix *m, int warps_per_slice, int variant) {
   });
 }
 
-int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges) {
+int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges, long *checkpoints) {
   return guarded([&] {
     DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
     if (present) *present = m->has_d16() ? 1 : 0;
-    if (bridges) *bridges = m->sell_bridges;
+    if (bridges) *bridges = m->has_d16() ? m->sell_bridges : 0;
+    if (checkpoints) *checkpoints = m->has_d16() ? m->sell_checkpoints : 0;
+  });
+}
+
+int dg_matrix_sell_config(const dg_matrix *m, int *warps_per_slice, int *grid, int *variant, int *warps_per_slice32, int *variant32) {
+  return guarded([&] {
+    DG_REQUIRE(m, DG_ERR_ARG, "null matrix");
+    if (warps_per_slice) *warps_per_slice = m->sell_ws;
+    if (grid) *grid = m->sell_grid;
+    if (variant) *variant = m->sell_variant;
+    if (warps_per_slice32) *warps_per_slice32 = m->sell_ws32;
+    if (variant32) *variant32 = m->sell_variant32;
   });
 }
 

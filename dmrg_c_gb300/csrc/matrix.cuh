@@ -39,6 +39,7 @@ struct dg_matrix {
   dg::DevBuf<int> s_chk;
   dg::DevBuf<int64_t> s_choff;
   long sell_bridges = 0;           // zero elements bridging column gaps >= 65,536
+  long sell_checkpoints = 0;       // 32-bit column checkpoints of the delta stream
   int sell_pf = 1;                 // V_D8 L2 prefetch distance in chunks (DG_SELL_PREFETCH)
 
   dg::CrsOp<double> op64() const { return dg::CrsOp<double>{row.get(), col.get(), val.get()}; }

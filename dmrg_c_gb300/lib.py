@@ -108,7 +108,8 @@ SIGNATURES = {
     "dg_matrix_set_sell_variant": (C.c_int, [vp, C.c_int]),
     "dg_matrix_sell_error": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "dg_matrix_set_sell_mixed": (C.c_int, [vp, C.c_int, C.c_int]),
-    "dg_matrix_sell_deltas": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_long)]),
+    "dg_matrix_sell_deltas": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long)]),
+    "dg_matrix_sell_config": (C.c_int, [vp, ip, ip, ip, ip, ip]),
     "dg_matrix_set_sell_window": (C.c_int, [vp, C.c_int]),
     "dg_matrix_autotune": (C.c_int, [vp, C.c_int, P(abi.dg_tune_result)]),
     "dg_matrix_format": (C.c_int, [vp, ip, lp]),
@@ -259,8 +260,20 @@ class DeviceMatrix:
     def sell_deltas(self) -> tuple[bool, int]:
         """(whether the 16-bit column-delta stream exists, its zero bridge elements)."""
         present, bridges = C.c_int(0), C.c_long(0)
-        check(load().dg_matrix_sell_deltas(self.h, C.byref(present), C.byref(bridges)))
+        check(load().dg_matrix_sell_deltas(self.h, C.byref(present), C.byref(bridges), None))
         return bool(present.value), bridges.value
+
+    def sell_checkpoints(self) -> int:
+        """32-bit column checkpoints of the delta stream (0 without one)."""
+        k = C.c_long(0)
+        check(load().dg_matrix_sell_deltas(self.h, None, None, C.byref(k)))
+        return k.value
+
+    def sell_config(self) -> dict:
+        """The sliced-ELL launch configuration in use (FP64 and FP32 products)."""
+        v = [C.c_int(0) for _ in range(5)]
+        check(load().dg_matrix_sell_config(self.h, *(C.byref(a) for a in v)))
+        return dict(ws=v[0].value, grid=v[1].value, variant=v[2].value, ws32=v[3].value, variant32=v[4].value)
 
     def sell_error(self) -> int:
         e = C.c_int(0)

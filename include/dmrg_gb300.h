@@ -206,9 +206,14 @@ int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
 int dg_matrix_set_sell_mixed(dg_matrix *m, int warps_per_slice, int variant);
 /* *present = 1 if the sliced-ELL copy carries the 16-bit column-delta stream (built for
  * matrices of at least 4M stored elements whose rows are sorted by column and need at most one
- * zero bridge element per 32 stored ones for gaps of 65,536 columns or more), and the number
- * of bridge elements. */
-int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges);
+ * zero bridge element per 32 stored ones for gaps of 65,536 columns or more), the number of
+ * bridge elements and of 32-bit column checkpoints (one per 32 elements of a row).  Any output
+ * may be NULL. */
+int dg_matrix_sell_deltas(const dg_matrix *m, int *present, long *bridges, long *checkpoints);
+/* The sliced-ELL launch configuration in use: warps per slice, grid and variant of the FP64
+ * product, warps per slice and variant of the FP32 (mixed) product.  Any output may be NULL. */
+int dg_matrix_sell_config(const dg_matrix *m, int *warps_per_slice, int *grid, int *variant, int *warps_per_slice32,
+                          int *variant32);
 /* *err = 1 if a streamed (variant 4 or 6) product of this matrix ever gave up waiting for a
  * stage of its copies (the product is then incomplete), else 0. */
 int dg_matrix_sell_error(const dg_matrix *m, int *err);
