@@ -331,7 +331,7 @@ class dg_sb_basis_spec(C.Structure):
 
 class dg_engine_config(C.Structure):
     """include/dmrg_gb300_ed.h: dg_engine_config"""
-    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t), ("lanczos_batch", C.c_int)]
+    _fields_ = [("workers", C.c_int), ("hbm_budget", C.c_size_t), ("lanczos_batch", C.c_int), ("tune_shapes", C.c_int)]
 
 
 class dg_job_result(C.Structure):

@@ -15,6 +15,10 @@
 // iteration or refinement on its own stream and posts the result.  Jobs join and leave the
 // lock-step batch at any step, so requests that arrive while others iterate start at once.
 //
+// With tune_shapes, each job's matrix takes the launch shape tuned for its size class
+// (dg_shape_cache_apply): rows per warp (warps per slice), kernel variant and grid, timed on the
+// first job of the class, which is then solved with it.
+//
 // Admission: a job starts only when a worker is idle and its device-memory estimate fits the
 // engine's budget next to the jobs already running (a job larger than the whole budget runs
 // alone).  Jobs start in submission order.  Every job's result is the same as when it runs
@@ -205,6 +209,7 @@ struct dg_engine {
       dg_ed_free(ed);
       ed = nullptr;
     }
+    if (rc == DG_OK && cfg.tune_shapes) rc = dg_shape_cache_apply(mat, 1, 3, nullptr);
     r.t_built_ms = now_ms();
     if (rc == DG_OK && cfg.lanczos_batch && dg::batch_eligible(mat, j.params)) {
       // park the job; its Lanczos phase joins the lock-step batch

@@ -8,6 +8,9 @@
 #include <algorithm>
 #include <climits>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <set>
 
 #include <type_traits>
 
@@ -407,13 +410,15 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   int w = kSellC;
   while (w < window && w < kSellWindow) w <<= 1;
   m->sell_window = w;
-  // The 16-bit delta stream: for matrices of at least kSellDeltaMin stored elements (smaller ones
-  // stay in L2, where fewer bytes buy nothing, and skip the check and its host synchronisation),
-  // rows sorted by column (every full CRS this library expands from a lower triangle is) and at
-  // most 1 bridge per 32 stored elements.  DG_SELL_DELTAS=0 turns it off, =1 tries it at any size.
+  // The 16-bit delta stream: for matrices with FP32 values (the FP32 product is the one that reads
+  // it by default; the FP64 product, bound by FP64 issue, does not gain) of at least kSellDeltaMin
+  // stored elements (smaller ones stay in L2, where fewer bytes buy nothing, and skip the check and
+  // its host synchronisation), rows sorted by column (every full CRS this library expands from a
+  // lower triangle is) and at most 1 bridge per 32 stored elements.  DG_SELL_DELTAS=0 turns it off,
+  // =1 tries it for every matrix.
   constexpr long kSellDeltaMin = 1L << 22;
   const char *env_d16 = std::getenv("DG_SELL_DELTAS");
-  bool d16 = env_d16 ? (env_d16[0] != '0' && m->nnz > 0) : (m->nnz >= kSellDeltaMin);
+  bool d16 = env_d16 ? (env_d16[0] != '0' && m->nnz > 0) : (m->has32 && m->nnz >= kSellDeltaMin);
   DevBuf<int> blen;
   m->sell_bridges = 0;
   if (d16) {
@@ -848,6 +853,138 @@ void profile_apply(dg_matrix *m, const XT *x_dev, double *y_dev, int iters, size
   cudaEventDestroy(e1);
   *ms_per_launch = (float)(total / iters);
 }
+
+// ---- Sliced-ELL shapes tuned per size class (the engine's autotuner).
+//
+// Matrices of one class (the same floor(log2 n), stored elements a row rounded, FP32 values or
+// not) share a launch shape.  The first matrix of a class is timed over every sliced-ELL
+// configuration: warps per slice x variant x grid for the FP64 product, then warps per slice x
+// variant of the FP32 product at that grid (the consumers of the products' reduction partials
+// count one per block, so both products keep one grid).  Only sliced-ELL shapes are candidates:
+// the lock-step batch runs on that layout.  The timings run next to whatever else the device is
+// doing (the engine's other jobs), so each candidate takes the better of two rounds and replaces
+// the build heuristic's shape only when at least 5 % faster.  The result is kept for the process.
+struct ShapeClass {
+  int logn, per_row, has32;
+  bool operator<(const ShapeClass &o) const {
+    return logn != o.logn ? logn < o.logn : per_row != o.per_row ? per_row < o.per_row : has32 < o.has32;
+  }
+};
+struct TunedShape {
+  int ws, variant, ws32, variant32;
+  int bps;   // the grid is min(blocks the slices need, bps blocks a SM)
+};
+std::mutex g_shape_mu;
+std::map<ShapeClass, TunedShape> g_shapes;
+std::set<ShapeClass> g_shape_busy;   // classes a thread is tuning now
+
+ShapeClass shape_class(const dg_matrix *m) {
+  int logn = 0;
+  while ((2L << logn) <= (long)m->n) ++logn;
+  const long per = (m->nnz + m->n / 2) / std::max(1, m->n);
+  return ShapeClass{logn, (int)std::min(per, 1L << 20), m->has32 ? 1 : 0};
+}
+
+int sell_grid_for(const dg_matrix *m, int ws, int bps) {
+  const int groups = kWarps / ws;
+  const long need = (m->nslices + groups - 1) / groups;
+  return (int)std::max(1L, std::min(need, (long)sm_count() * bps));
+}
+
+// A variant this matrix can run: the delta variants fall back to the same kernel on 32-bit
+// columns when a matrix of the class has no delta stream.
+int runnable_variant(const dg_matrix *m, int v) {
+  if (sell_uses_deltas(v) && !m->has_d16()) return v == V_TMA16 ? V_TMA : V_U8;
+  return v;
+}
+
+void apply_shape(dg_matrix *m, const TunedShape &t) {
+  m->format = DG_FORMAT_SELL;
+  m->sell_ws = t.ws;
+  m->sell_variant = runnable_variant(m, t.variant);
+  m->sell_grid = sell_grid_for(m, t.ws, t.bps);
+  m->sell_ws32 = t.ws32;
+  m->sell_variant32 = runnable_variant(m, t.variant32);
+}
+
+TunedShape tune_sell(dg_matrix *m, int iters) {
+  cudaStream_t st = stream();
+  const int sms = sm_count();
+  DevBuf<double> x(m->n), y(m->n), out1(1), partials((size_t)sms * 16 + 64);
+  DevBuf<float> x32(m->has32 ? (size_t)m->n : 1);
+  DevBuf<unsigned> ticket(1);
+  DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), st));
+  DG_CUDA(cudaMemsetAsync(x.get(), 0, sizeof(double) * m->n, st));
+  if (m->has32) DG_CUDA(cudaMemsetAsync(x32.get(), 0, sizeof(float) * m->n, st));
+  cudaEvent_t e0, e1;
+  DG_CUDA(cudaEventCreate(&e0));
+  DG_CUDA(cudaEventCreate(&e1));
+  auto time_it = [&](bool f32) -> float {
+    const RedSlot slot{partials.get(), ticket.get()};
+    const EpiDot<double> epi{y.get(), out1.get()};
+    float best_round = 1e30f;
+    for (int round = 0; round < 2; ++round) {
+      for (int i = -1; i < iters; ++i) {   // i = -1: untimed
+        if (i == 0) DG_CUDA(cudaEventRecord(e0, st));
+        if (f32)
+          matrix_apply32(m, x32.get(), Scale{}, 0.0, (const int *)nullptr, epi, slot, st);
+        else
+          matrix_apply64(m, x.get(), Scale{}, 0.0, (const int *)nullptr, epi, slot, st);
+      }
+      DG_CUDA(cudaEventRecord(e1, st));
+      DG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      DG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best_round = std::min(best_round, ms / iters);
+    }
+    return best_round;
+  };
+  constexpr float kGain = 0.95f;   // a candidate must beat the best so far by 5 %
+  auto candidate = [&](int ws, int v) {   // the streamed variants run one warp a slice
+    return (!sell_uses_deltas(v) || m->has_d16()) && !((v == V_TMA || v == V_TMA16) && ws > 1);
+  };
+  // the build heuristic's shape first: its grid is one of the two candidates' (16 blocks a SM)
+  m->format = DG_FORMAT_SELL;
+  TunedShape best{m->sell_ws, m->sell_variant, m->sell_ws32, m->sell_variant32, 16};
+  m->sell_grid = sell_grid_for(m, best.ws, best.bps);
+  float best_ms = time_it(false);
+  for (int ws = 1; ws <= 8; ws <<= 1)
+    for (int v = 0; v < V_COUNT; ++v) {
+      if (!candidate(ws, v)) continue;
+      for (int bps : {8, 16}) {
+        m->sell_ws = ws;
+        m->sell_variant = v;
+        m->sell_grid = sell_grid_for(m, ws, bps);
+        const float t = time_it(false);
+        if (t < kGain * best_ms) {
+          best_ms = t;
+          best.ws = ws;
+          best.variant = v;
+          best.bps = bps;
+        }
+      }
+    }
+  apply_shape(m, best);
+  if (m->has32) {
+    best_ms = time_it(true);
+    for (int ws = 1; ws <= 8; ws <<= 1)
+      for (int v = 0; v < V_COUNT; ++v) {
+        if (!candidate(ws, v)) continue;
+        m->sell_ws32 = ws;
+        m->sell_variant32 = v;
+        const float t = time_it(true);
+        if (t < kGain * best_ms) {
+          best_ms = t;
+          best.ws32 = ws;
+          best.variant32 = v;
+        }
+      }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  apply_shape(m, best);
+  return best;
+}
 }  // namespace
 
 extern "C" {
@@ -1014,6 +1151,55 @@ int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out) {
     }
     best.candidates = tried;
     if (out) *out = best;
+  });
+}
+
+
+int dg_shape_cache_apply(dg_matrix *m, int tune, int iters, int *how) {
+  return guarded([&] {
+    require_device();
+    DG_REQUIRE(m && iters > 0, DG_ERR_ARG, "bad argument");
+    const ShapeClass k = shape_class(m);
+    int h = 0;
+    {
+      std::unique_lock<std::mutex> lk(g_shape_mu);
+      auto it = g_shapes.find(k);
+      if (it != g_shapes.end()) {
+        apply_shape(m, it->second);
+        h = 1;
+      } else if (tune && !g_shape_busy.count(k)) {
+        g_shape_busy.insert(k);
+        h = 2;
+      }
+    }
+    if (h == 2) {
+      struct Done {   // the class leaves the busy set on every exit
+        ShapeClass k;
+        ~Done() {
+          std::lock_guard<std::mutex> lk(g_shape_mu);
+          g_shape_busy.erase(k);
+        }
+      } done{k};
+      const TunedShape t = tune_sell(m, iters);
+      std::lock_guard<std::mutex> lk(g_shape_mu);
+      g_shapes[k] = t;
+    }
+    if (how) *how = h;
+  });
+}
+
+int dg_shape_cache_clear(void) {
+  return guarded([&] {
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_shapes.clear();
+  });
+}
+
+int dg_shape_cache_size(int *count) {
+  return guarded([&] {
+    DG_REQUIRE(count, DG_ERR_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    *count = (int)g_shapes.size();
   });
 }
 

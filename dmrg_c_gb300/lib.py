@@ -108,6 +108,9 @@ SIGNATURES = {
     "dg_matrix_set_sell_variant": (C.c_int, [vp, C.c_int]),
     "dg_matrix_sell_error": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "dg_matrix_set_sell_mixed": (C.c_int, [vp, C.c_int, C.c_int]),
+    "dg_shape_cache_apply": (C.c_int, [vp, C.c_int, C.c_int, ip]),
+    "dg_shape_cache_clear": (C.c_int, []),
+    "dg_shape_cache_size": (C.c_int, [ip]),
     "dg_matrix_sell_deltas": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_long)]),
     "dg_matrix_sell_config": (C.c_int, [vp, ip, ip, ip, ip, ip]),
     "dg_matrix_set_sell_window": (C.c_int, [vp, C.c_int]),
@@ -274,6 +277,13 @@ class DeviceMatrix:
         v = [C.c_int(0) for _ in range(5)]
         check(load().dg_matrix_sell_config(self.h, *(C.byref(a) for a in v)))
         return dict(ws=v[0].value, grid=v[1].value, variant=v[2].value, ws32=v[3].value, variant32=v[4].value)
+
+    def shape_cache_apply(self, tune: bool = True, iters: int = 3) -> int:
+        """Take the tuned sliced-ELL shape of this matrix's size class (1), tune and record it
+        (2), or keep the current shape (0)."""
+        how = C.c_int(0)
+        check(load().dg_shape_cache_apply(self.h, int(tune), iters, C.byref(how)))
+        return how.value
 
     def sell_error(self) -> int:
         e = C.c_int(0)
@@ -537,11 +547,23 @@ class SuperblockCRS:
         return DeviceMatrix(None, handle=h)
 
 
+def shape_cache_clear():
+    """Forget every tuned size class (dg_shape_cache_clear)."""
+    check(load().dg_shape_cache_clear())
+
+
+def shape_cache_size() -> int:
+    k = C.c_int(0)
+    check(load().dg_shape_cache_size(C.byref(k)))
+    return k.value
+
+
 class Engine:
     """Concurrent ED ground-state engine (dg_engine): submit models, poll results."""
 
-    def __init__(self, workers: int = 0, hbm_budget: int = 0, lanczos_batch: bool = False):
-        cfg = abi.dg_engine_config(workers=workers, hbm_budget=hbm_budget, lanczos_batch=int(lanczos_batch))
+    def __init__(self, workers: int = 0, hbm_budget: int = 0, lanczos_batch: bool = False, tune_shapes: bool = False):
+        cfg = abi.dg_engine_config(workers=workers, hbm_budget=hbm_budget, lanczos_batch=int(lanczos_batch),
+                                   tune_shapes=int(tune_shapes))
         h = C.c_void_p()
         check(load().dg_engine_create(C.byref(cfg), C.byref(h)))
         self.h = h

@@ -205,7 +205,8 @@ int dg_matrix_set_sell_variant(dg_matrix *m, int variant);
  * of dg_matrix_set_sell_shape. */
 int dg_matrix_set_sell_mixed(dg_matrix *m, int warps_per_slice, int variant);
 /* *present = 1 if the sliced-ELL copy carries the 16-bit column-delta stream (built for
- * matrices of at least 4M stored elements whose rows are sorted by column and need at most one
+ * matrices with FP32 values (DG_VALUES_F32 / DG_VALUES_BOTH) of at least 4M stored elements
+ * whose rows are sorted by column and need at most one
  * zero bridge element per 32 stored ones for gaps of 65,536 columns or more), the number of
  * bridge elements and of 32-bit column checkpoints (one per 32 elements of a row).  Any output
  * may be NULL. */
@@ -235,6 +236,20 @@ typedef struct {
 /* Time the candidate configurations of the fused product on this matrix (iters launches
  * each) and keep the fastest for all later products. */
 int dg_matrix_autotune(dg_matrix *m, int iters, dg_tune_result *out);
+/* Sliced-ELL launch shapes tuned per size class, kept for the process (the engine's
+ * autotuner).  A class is floor(log2 n), the stored elements a row rounded, and whether the
+ * matrix has FP32 values.  If m's class has a tuned shape it is applied to m (*how = 1).  Else,
+ * with tune != 0 and no other thread tuning the class, m is timed over every sliced-ELL
+ * configuration (warps per slice x variant x grid of 8 or 16 blocks a SM for the FP64 product,
+ * then warps per slice x variant of the FP32 product at that grid; iters launches each), the
+ * fastest is applied and recorded for the class (*how = 2).  Otherwise m keeps its shape
+ * (*how = 0).  The timings run on the calling thread's stream and see whatever else the device
+ * is doing. */
+int dg_shape_cache_apply(dg_matrix *m, int tune, int iters, int *how);
+/* Forget every tuned class. */
+int dg_shape_cache_clear(void);
+/* Number of tuned classes. */
+int dg_shape_cache_size(int *count);
 /* Current layout and, for DG_FORMAT_SELL, the stored elements including slice padding. */
 int dg_matrix_format(const dg_matrix *m, int *format, long *stored);
 /* Download the device full CRS (row: n+1, col/val: nnz_full). */

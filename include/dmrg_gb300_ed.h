@@ -97,6 +97,9 @@ typedef struct {
    int lanczos_batch;      /* 1: the Lanczos phases of eligible jobs (mixed = 0 or 2) run
                               in the engine's lock-step batch (one launch of each kernel a
                               step over all of them); 0: every job solves on its worker   */
+   int tune_shapes;        /* 1: every job's matrix takes the tuned sliced-ELL shape of its
+                              size class (dg_shape_cache_apply); the first job of a class
+                              not yet tuned is timed on its worker; 0: the build heuristic */
 } dg_engine_config;
 
 typedef struct {
