@@ -485,8 +485,8 @@ void build_sell(dg_matrix *m, cudaStream_t st, int window) {
   // pipelined form, which has no second group to overlap, is the slowest (12-14 % behind).
   const double per_row = (double)total / ((double)nslices * kSellC);
   m->sell_variant = (m->sell_ws >= 4 || per_row < 24.0) ? V_U16 : V_PIPE8;
-  // The FP32 product on the delta stream (6 bytes an element instead of 8): on the config-5
-  // superblock (238 k rows of 236) 8-element groups with the next chunk prefetched into L2 took
+  // The FP32 product on the delta stream (6 bytes an element instead of 8): on the Hubbard m=512
+  // superblock of a DMRG sweep (238 k rows of 236 stored elements) 8-element groups with the next chunk prefetched into L2 took
   // 79 us at one warp per slice and 81 at two, against 92 us for the 32-bit columns.  One warp a
   // slice needs enough slices to fill the GPU (24 a SM); the FP64 product, bound by FP64 issue,
   // gains nothing from the deltas and keeps its variant.

@@ -158,13 +158,13 @@ def test_small_matrices_skip_the_stream_by_default(gpu, monkeypatch):
 
 @pytest.mark.parametrize("mixed", [0, 2], ids=["fp64", "mixed2"])
 def test_delta_solve_is_bitwise_the_register_form(gpu, mixed):
-    """Lanczos + inverse iteration / refinement on the config-5 superblock of the reference's own
+    """Lanczos + inverse iteration / refinement on the Hubbard m=512 superblock (L=64, U=4, 4th sweep) of the reference's own
     Hubbard run (n = 238,462, 236 elements a row; the stream is built by default at this size):
     with one warp per slice the same energy and vector bit for bit as variant 1."""
     from dmrg_c_gb300 import sb_models
     path = GOLDEN / "dmrg_hubbard_vf_sweep4.npz"
     if not path.exists():
-        pytest.skip("no config-5 fixture")
+        pytest.skip("no Hubbard m=512 superblock fixture")
     sb = sb_models.load_dmrg_superblock(path)
     s = gpu.SuperblockCRS(sb.model)
     res = {}
