@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi_cluster(const EigBlk *__res
     if (threadIdx.x == 0) s_rot = 0;   // each CTA flags the rotations it computes (all CTAs compute all)
     __syncthreads();
     for (int r = 0; r < m - 1; ++r) {
-      // 1. the rotations of this round (every CTA computes all of them)
+      // 1. the rotations of Jacobi round r (every CTA computes all of them)
       for (int k = threadIdx.x; k < half; k += blockDim.x) {
         int p, q;
         if (k == 0) {
