@@ -162,8 +162,7 @@ __global__ void __launch_bounds__(kThreads) k_mr_update(int n, const double *__r
 // ---- mixed-precision Lanczos ----------------------------------------------------------
 
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
-                                                    int n, int nchunk, float2 *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket) {
+                                                    int n, int nchunk, float2 *__restrict__ partials) {
   pdl_wait();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int j = blockIdx.y * kWarps + warp;
@@ -174,15 +173,15 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
     const float *vj = V + (long)j * ldv;
     AccDot2 acc;
     long i = r0 + lane;
-    for (; i + 96 < r1; i += 128) {   // four loads in flight per lane
-      float a[4], b[4];
+    for (; i + 224 < r1; i += 256) {   // eight loads of each vector in flight per lane
+      float a[8], b[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < 8; ++u) {
         a[u] = vj[i + 32 * u];
         b[u] = y[i + 32 * u];
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc.add(a[u], b[u]);
+      for (int u = 0; u < 8; ++u) acc.add(a[u], b[u]);
     }
     for (; i < r1; i += 32) acc.add(vj[i], y[i]);
 #pragma unroll
@@ -194,19 +193,14 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
     if (lane == 0) partials[(long)j * nchunk + chunk] = make_float2(acc.p, acc.c);
   }
   pdl_trigger();
-  // The last block sums the chunk partials of every vector (one warp per vector, fixed
-  // order) into the subtraction coefficients coef_j = -sig_j^2 <V_j, y>.
-  __shared__ bool s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned nblocks = gridDim.x * gridDim.y;
-    s_last = atomicAdd(ticket, 1u) == nblocks - 1;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  for (int jj = warp; jj < nvec; jj += kWarps) {
+}
+
+__global__ void __launch_bounds__(kThreads) k_mx_coef(const float2 *__restrict__ partials, int nvec, int nchunk,
+                                                     const double *__restrict__ sig, float *__restrict__ coef) {
+  pdl_wait();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int jj = blockIdx.x * kWarps + warp;
+  if (jj < nvec) {
     AccDot2 c;
     for (int ch = lane; ch < nchunk; ch += 32) {
       const float2 v = __ldcg(partials + (long)jj * nchunk + ch);
@@ -220,7 +214,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V
     }
     if (lane == 0) coef[jj] = (float)(-c.get() * sig[jj] * sig[jj]);
   }
-  if (threadIdx.x == 0) *ticket = 0u;
+  pdl_trigger();
 }
 
 __global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nvec, const float *__restrict__ coef_g,
@@ -235,12 +229,19 @@ __global__ void __launch_bounds__(kThreads) k_mx_sub(float *V, long ldv, int nve
     AccDot2 a;
     a.p = y[i];
     int j = 0;
-    for (; j + 8 <= nvec; j += 8) {   // eight loads in flight per thread
-      float v[8];
+    for (; j + 16 <= nvec; j += 16) {   // sixteen loads in flight per thread
+      float v[16];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = __ldg(V + (long)(j + u) * ldv + i);   // V_j, j < nvec: read-only here
+      for (int u = 0; u < 16; ++u) v[u] = __ldg(V + (long)(j + u) * ldv + i);   // V_j, j < nvec: read-only here
 #pragma unroll
-      for (int u = 0; u < 8; ++u) a.add(coef[j + u], v[u]);
+      for (int u = 0; u < 16; ++u) a.add(coef[j + u], v[u]);
+    }
+    for (; j + 4 <= nvec; j += 4) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldg(V + (long)(j + u) * ldv + i);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a.add(coef[j + u], v[u]);
     }
     for (; j < nvec; ++j) a.add(coef[j], __ldg(V + (long)j * ldv + i));
     const float w = __fadd_rn(a.p, a.c);

@@ -303,18 +303,21 @@ __global__ void __launch_bounds__(kThreads) k_ritz(const VT *__restrict__ V, lon
 // three-term recurrence.  Dots and the subtraction use compensated FP32 arithmetic (Dot2),
 // the recurrence scalars and norms FP64.
 
-// Rows per dot-product chunk (one warp each): four rounds of four loads per lane.  Measured on
+// Rows per dot-product chunk (one warp each): two rounds of eight loads per lane.  Measured on
 // the KLM m=128 benchmark (mixed=1 solves/s): 1024 rows 290, 512 rows 312, 256 rows 304 (more
 // chunks: more FP64 warp sums of the chunk partials).
 constexpr int kMxChunk = 512;
 
-// partials[j * nchunk + chunk] = <V_j, y> over the chunk's rows, one warp per vector; the
-// last block reduces them (fixed order) to coef_j = -sig_j^2 <V_j, y> = -c_j sig_j with
-// coef_j = -sig_j^2 <v_j, y> for j < nvec: per-chunk pair partials, summed by the last block.
-// ticket: zero between uses.
+// partials[j * nchunk + chunk] = <V_j, y> over the chunk's rows as compensated pairs, one warp
+// per (vector, chunk).
 __global__ void __launch_bounds__(kThreads) k_mx_dot(const float *__restrict__ V, long ldv, int nvec, const float *__restrict__ y,
-                                                    int n, int nchunk, float2 *__restrict__ partials, const double *__restrict__ sig,
-                                                    float *__restrict__ coef, unsigned *ticket);
+                                                    int n, int nchunk, float2 *__restrict__ partials);
+// coef_j = -sig_j^2 <V_j, y> for j < nvec: one warp per vector sums its nchunk partials in a
+// fixed order (lanes over the chunks, then a shuffle tree).  Its own launch, in parallel over the
+// vectors: summed by the dot kernel's last block, the vectors waited on one another (~6 of them
+// a warp at 44 vectors) after the rest of the grid had finished.
+__global__ void __launch_bounds__(kThreads) k_mx_coef(const float2 *__restrict__ partials, int nvec, int nchunk,
+                                                     const double *__restrict__ sig, float *__restrict__ coef);
 // Three-term recurrence of the mixed form: w = y - D[b] sig_b V_b - O[b] sig_{b-1} V_{b-1} in
 // compensated FP32 with the scalars as float pairs; V[b+1] = w.  D[b] summed from the
 // product's pcount pair partials, or, with pcount 0, as its last block recorded it; <w,w> into
@@ -603,14 +606,12 @@ struct LzStepsMixed {
   double *w;             // FP64 start / restart vector
   DevBuf<float> y, coef, rcoef;
   DevBuf<double> sig, partials;
-  DevBuf<unsigned> ticket;
   KrylovBasis<float> B;
   int nchunk;
   LzStepsMixed(const Opl &o, const LanczosCfg &cf, Workspace &w_, LzState &z_, double *w_dev)
-      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), coef(z_.cap_max + 1), sig(z_.cap_max + 1), ticket(1), B(z_.n, w_.st) {
+      : op(o), cfg(cf), ws(w_), z(z_), w(w_dev), y(z_.n), coef(z_.cap_max + 1), sig(z_.cap_max + 1), B(z_.n, w_.st) {
     nchunk = (int)((z_.n + kMxChunk - 1) / kMxChunk);
     partials.alloc((size_t)(z_.cap_max + 1) * nchunk);
-    DG_CUDA(cudaMemsetAsync(ticket.get(), 0, sizeof(unsigned), w_.st));
   }
   // V[0] = fl32(w) (unnormalised); S->r2 already holds <w,w>.
   void begin_cycle() {
@@ -656,7 +657,9 @@ struct LzStepsMixed {
     const int nvec = b + 1;
     const float *w3 = B.vec(b + 1);
     launch_pdl(k_mx_dot, dim3(nchunk, (nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float *)B.V, (long)n, nvec, w3, n,
-               nchunk, reinterpret_cast<float2 *>(partials.get()), (const double *)sig.get(), coef.get(), ticket.get());
+               nchunk, reinterpret_cast<float2 *>(partials.get()));
+    launch_pdl(k_mx_coef, dim3((nvec + kWarps - 1) / kWarps), dim3(kThreads), st, (const float2 *)partials.get(), nvec, nchunk,
+               (const double *)sig.get(), coef.get());
     launch_pdl_smem(k_mx_sub, dim3(ws.vgrid), dim3(kThreads), sizeof(float) * nvec, st, B.V, (long)n, nvec,
                     (const float *)coef.get(), w3, n, r2slot, r2);
   }
