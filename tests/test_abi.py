@@ -53,11 +53,16 @@ STRUCTS = ["CRS1", "BOX_CG", "BOX_II", "BOX_LAN", "DMRG_PARAMETER", "DMRG_TIME",
            "DMRG_SYSTEM_INFO"]
 
 
-def c_layout(tmp_path: Path, include_dirs, header):
+# the library's own structs (include/dmrg_gb300*.h)
+OWN_STRUCTS = ["dg_solver_params", "dg_solve_info", "dg_tune_result", "dg_sb_term", "dg_sb_model", "dg_sb_expect_term",
+               "dg_sb_basis_spec", "dg_engine_config", "dg_job_result", "dg_ed_term", "dg_ed_model"]
+
+
+def c_layout(tmp_path: Path, include_dirs, header, structs=None):
     """sizeof and field offsets of every struct, from the C compiler."""
     from dmrg_c_gb300 import abi
     lines = [f'#include "{header}"', "#include <stdio.h>", "#include <stddef.h>", "int main(void) {"]
-    for s in STRUCTS:
+    for s in structs or STRUCTS:
         cls = getattr(abi, s)
         lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
         for f, _ in cls._fields_:
@@ -71,12 +76,12 @@ def c_layout(tmp_path: Path, include_dirs, header):
     return dict(line.split() for line in out.splitlines())
 
 
-def ctypes_layout():
+def ctypes_layout(structs=None):
     import ctypes as C
 
     from dmrg_c_gb300 import abi
     out = {}
-    for s in STRUCTS:
+    for s in structs or STRUCTS:
         cls = getattr(abi, s)
         out[s] = str(C.sizeof(cls))
         for f, _ in cls._fields_:
@@ -86,6 +91,14 @@ def ctypes_layout():
 
 def test_struct_layouts_match_our_header(tmp_path):
     assert c_layout(tmp_path, [ROOT / "include"], "dmrg_gb300.h") == ctypes_layout()
+
+
+def test_own_struct_layouts_match_our_headers(tmp_path):
+    """The ctypes mirrors of the library's own structs (solver parameters, engine configuration,
+    ED and superblock models) have the C layouts."""
+    hdr = tmp_path / "own.h"
+    hdr.write_text("".join(f'#include "{h.name}"\n' for h in HEADERS))
+    assert c_layout(tmp_path, [ROOT / "include", tmp_path], "own.h", OWN_STRUCTS) == ctypes_layout(OWN_STRUCTS)
 
 
 def test_struct_layouts_match_reference_headers(tmp_path):
