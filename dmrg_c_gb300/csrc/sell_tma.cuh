@@ -16,10 +16,10 @@
 // columns and each lane keeps its running column, restarted from the checkpoint at every
 // kSellChunk-th element (loaded one chunk ahead).
 //
-// Every wait on an mbarrier is bounded: after kTmaSpinLimit polls (the decision taken by the
-// whole warp) the warp records the failure in op.err (read by dg_matrix_sell_error), stops
-// issuing copies, waits (again bounded) for every copy it has in flight and leaves the slice
-// loop.
+// Every wait on an mbarrier is bounded: after 0.5 s or kTmaSpinLimit polls, whichever comes
+// first (the decision taken by the whole warp), the warp records the failure in op.err (read by
+// dg_matrix_sell_error), stops issuing copies, waits (again bounded) for every copy it has in
+// flight and leaves the slice loop.
 #pragma once
 
 #include <cstdint>
@@ -32,6 +32,7 @@ namespace dg {
 constexpr int kTmaStages = 4;   // stages in flight per warp
 constexpr int kTmaK = 8;        // elements of every row per stage
 constexpr unsigned kTmaSpinLimit = 1u << 22;   // polls of a stage's mbarrier before giving up
+constexpr unsigned long long kTmaWaitNs = 500000000ull;   // and at most 0.5 s of waiting
 static_assert(kSellChunk % kTmaK == 0, "a stage never straddles a column checkpoint");
 
 // CT: the column element of a stage (int, or uint16_t deltas)
@@ -62,10 +63,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase with the given parity; false when the limit ran out.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for the phase with the given parity; false when the limit ran out.  try_wait may
+// suspend the thread for a hardware-dependent time before it returns false, so the poll count
+// alone does not bound the time: the global timer does (read every 256 polls).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-  for (unsigned i = 0; i < kTmaSpinLimit; ++i)
+  unsigned long long t0 = 0;
+  for (unsigned i = 0; i < kTmaSpinLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u) {
+      const unsigned long long t = global_ns();
+      if (t0 == 0)
+        t0 = t;
+      else if (t - t0 > kTmaWaitNs)
+        return false;
+    }
+  }
   return false;
 }
 // One stage: both copies complete on bar, which expects their bytes.  Sizes and addresses are
