@@ -76,3 +76,35 @@ def test_clock_summary_keeps_the_timed_window():
     clk.window(2.98, 2.985)
     s = clk.summary()
     assert s["samples"] == 1 and s["sm_mhz"] == 1400 and s["reasons"] == ["sw_thermal_slowdown"]
+
+
+def test_mixed_roofline_counts_the_layout_it_reads():
+    """roofline_mixed's bytes: with the 16-bit delta stream in use, 2 + 4 bytes a stored slot plus
+    the checkpoints, slot rows, slice words and the two vectors; without it, the CRS footprint."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class M:
+        def __init__(self, deltas, variant32):
+            self.d, self.v = deltas, variant32
+
+        def sell_config(self):
+            return dict(ws=2, grid=1872, variant=3, ws32=1, variant32=self.v)
+
+        def sell_deltas(self):
+            return (self.d, 42080 if self.d else 0)
+
+        def format(self):
+            return (1, 56362528)
+
+        def sell_checkpoints(self):
+            return 1881984 if self.d else 0
+
+    n, nnz = 238462, 56222276
+    b, basis = bench.sell_mixed_bytes(M(True, 5), n, nnz)
+    nslices = -(-n // 2048) * 2048 // 32
+    assert b == 56362528 * 6 + 1881984 * 4 + nslices * 32 * 4 + nslices * 20 + n * 4 + n * 8 == 349672872
+    assert basis.startswith("delta layout")
+    for m in (M(False, 1), M(True, 1)):          # no stream, or the FP32 product not on it
+        b, basis = bench.sell_mixed_bytes(m, n, nnz)
+        assert b == bench.spmv_bytes(n, nnz, 4, 4) and basis.startswith("CRS")
